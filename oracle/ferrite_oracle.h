@@ -1,0 +1,104 @@
+/*
+ * ferrite_oracle.h -- CPU FP64 restatement of Ferrite.jl's assembly path.
+ *
+ * TEST INFRASTRUCTURE ONLY. This library is the parity checker for the CUDA engine in
+ * ferrite.jl_gb300/: only tests, __graft_entry__.smoke() and bench.py's CPU baseline leg
+ * may load it. The product path never calls into it.
+ *
+ * It restates, in plain C++ with FP64 arithmetic, the Julia code of Ferrite.jl v1.6.0:
+ *   grid generation      src/Grid/grid_generators.jl:78-112, 159-257, 474-559
+ *   dof distribution     src/Dofs/DofHandler.jl:493-794, 829-1057
+ *   sparsity pattern     src/Dofs/sparsity_pattern.jl:223-253, 549, 1136-1249
+ *   quadrature           src/Quadrature/quadrature.jl:83-154, generate_quadrature.jl:93-112,
+ *                        gaussquad_tet_table.jl (Jinyun/Keast), gaussquad_prism_table.jl:6-366
+ *   shape functions      src/interpolations.jl:640-661, 891-913, 1038-1164, 1258-1280
+ *   CellValues reinit!   src/FEValues/CellValues.jl:110-140, GeometryMapping.jl:124-130,
+ *                        FunctionValues.jl:163, 186-192
+ *   element kernels      docs/src/literate-tutorials/heat_equation.jl:143-164,
+ *                        docs/src/literate-howto/threaded_assembly.jl:105-132,
+ *                        docs/src/literate-tutorials/hyperelasticity.jl:157-276,
+ *                        docs/src/literate-gallery/topology_optimization.jl:347-383
+ *   CSC assembler        src/assembler.jl:287-291, 322-457, 513-576; src/arrayutils.jl:100-152
+ *   greedy coloring      src/Grid/coloring.jl:47-143
+ *
+ * Conventions follow Ferrite's memory layout: node coordinates AoS [n_nodes][dim],
+ * connectivity, cell_dofs, cell_dofs_offset, colptr and rowval are 1-based Int64, nzval is
+ * Float64 column-major CSC.
+ */
+#ifndef FERRITE_ORACLE_H
+#define FERRITE_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* cell types (Ferrite: Triangle, Quadrilateral, Tetrahedron, Hexahedron, Wedge) */
+enum { OR_TRIANGLE = 1, OR_QUADRILATERAL = 2, OR_TETRAHEDRON = 3, OR_HEXAHEDRON = 4, OR_WEDGE = 5 };
+/* physics (element routines of the tutorials) */
+enum { OR_HEAT = 1, OR_LINEAR_ELASTIC = 2, OR_NEO_HOOKE = 3 };
+/* status codes, same meaning as the library's FE_* codes */
+enum { OR_OK = 0, OR_ERR_ARG = 1, OR_ERR_BOUNDS = 2, OR_ERR_DETJ = 3, OR_ERR_PATTERN_MISSING = 4,
+       OR_ERR_UNSUPPORTED = 5 };
+
+typedef struct {
+    int32_t dim;
+    int64_t n_nodes;
+    const double* nodes;              /* [n_nodes][dim] */
+    int64_t n_cells;
+    const int32_t* cell_types;        /* [n_cells] */
+    const int64_t* cell_nodes_offset; /* [n_cells+1], 0-based into cell_nodes */
+    const int64_t* cell_nodes;        /* 1-based node ids */
+    int32_t n_sdh;                    /* SubDofHandlers, visited in this order */
+    const int32_t* sdh_ip_order;      /* Lagrange order per sdh */
+    const int32_t* sdh_ncomp;         /* 1 = scalar field, dim = ip^dim */
+    const int32_t* sdh_qr_order;      /* QuadratureRule order per sdh */
+    const int64_t* sdh_cellset_offset;/* [n_sdh+1] */
+    const int64_t* sdh_cellset;       /* 1-based cell ids, ascending */
+    int64_t ndofs;
+    const int64_t* cell_dofs;         /* flat */
+    const int64_t* cell_dofs_offset;  /* [n_cells], 1-based */
+    const int64_t* colptr;            /* [ndofs+1], 1-based */
+    const int64_t* rowval;            /* [nnz], 1-based */
+} or_problem;
+
+typedef struct {
+    int32_t physics;
+    double p0, p1;       /* heat: k, source; elastic: E, nu; neo-hooke: mu, lambda */
+    double body[3];      /* body force (elastic, neo-hooke) */
+    const double* cell_scale; /* optional per-cell factor on the material (E_e or rho^p); NULL = 1 */
+    const double* u;     /* neo-hooke: current displacement [ndofs] */
+} or_physics;
+
+typedef struct {
+    int32_t code;
+    int64_t cell;        /* 1-based */
+    double detJ;
+    int64_t row, col;    /* 1-based, pattern miss */
+} or_error;
+
+int or_grid_counts(int32_t cell_type, const int64_t* nel, int64_t* n_nodes, int64_t* n_cells,
+                   int32_t* nodes_per_cell, int32_t* dim);
+int or_generate_grid(int32_t cell_type, const int64_t* nel, const double* left, const double* right,
+                     double* nodes, int64_t* cells);
+
+int or_nbase(int32_t cell_type, int32_t ip_order);
+int or_close_dofhandler(const or_problem* p, int64_t* cell_dofs, int64_t* cell_dofs_offset,
+                        int64_t* ndofs);
+int or_sparsity_pattern(const or_problem* p, int64_t* colptr, int64_t* rowval, int64_t* nnz);
+
+int or_quadrature(int32_t cell_type, int32_t order, int32_t* n_qp, double* weights, double* points);
+int or_shape_tables(int32_t cell_type, int32_t ip_order, int32_t n_qp, const double* points,
+                    double* N, double* dN);
+
+int or_assemble(const or_problem* p, const or_physics* phys, int32_t nthreads, int32_t fillzero,
+                double* nzval, double* f, or_error* err);
+int or_element_matrix(const or_problem* p, const or_physics* phys, int64_t cell, double* Ke,
+                      double* fe, or_error* err);
+int or_index_map(const or_problem* p, int64_t cell, int64_t* positions);
+int or_greedy_coloring(const or_problem* p, int32_t* cell_color, int32_t* n_colors);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

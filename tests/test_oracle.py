@@ -1,0 +1,288 @@
+"""The CPU oracle pinned against Ferrite.jl's own known answers and test identities.
+
+These run without a GPU. They check the oracle (a restatement of the reference's assembly
+path, oracle/ferrite_oracle.cpp) before anything is compared against it:
+  * the two golden values the reference's tutorials assert (tests/golden/known_answers.json);
+  * quadrature exactness (test/test_quadrules.jl:22-38);
+  * CellValues identities: volume, linear-field reproduction (test/test_cellvalues.jl:51-161);
+  * Q2 dof sharing consistency (test/test_dofs.jl:1156-1235, restated as a nodal
+    interpolation check);
+  * assembler semantics: zero skipping, pattern-miss errors (test/test_assemble.jl:4-214);
+  * colored threaded determinism (docs/src/literate-howto/threaded_assembly.jl:397-410).
+"""
+import itertools
+import json
+import os
+
+import numpy as np
+import pytest
+import scipy.sparse.linalg as spla
+
+GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "known_answers.json")))
+
+
+def node_to_dofs(prob, ncomp):
+    """Map node id (0-based) -> its ncomp dofs (0-based), for vertex-only fields."""
+    x = prob.nodes
+    out = np.full((len(x), ncomp), -1, np.int64)
+    for c in range(prob.n_cells):
+        nodes = prob.cells_of(c) - 1
+        d = prob.celldofs(c) - 1
+        out[nodes] = d[: len(nodes) * ncomp].reshape(len(nodes), ncomp)
+    return out
+
+
+def test_heat_equation_golden(oracle):
+    O = oracle
+    p = O.box_problem(O.QUADRILATERAL, (20, 20), qr_order=2)
+    nz, f = p.assemble(O.HEAT, 1.0, 1.0)
+    K = p.to_scipy(nz)
+    x = p.nodes
+    n2d = node_to_dofs(p, 1)[:, 0]
+    bnd = np.where((np.abs(np.abs(x[:, 0]) - 1) < 1e-12) | (np.abs(np.abs(x[:, 1]) - 1) < 1e-12))[0]
+    free = np.setdiff1d(np.arange(p.ndofs), n2d[bnd])
+    u = np.zeros(p.ndofs)
+    u[free] = spla.spsolve(K[free][:, free].tocsc(), f[free])
+    g = GOLDEN["heat_equation_norm_u"]
+    assert np.linalg.norm(u) == pytest.approx(g["value"], rel=g["rtol"])
+
+
+def test_hyperelasticity_golden(oracle):
+    O = oracle
+    N, L = 10, 1.0
+    p = O.box_problem(O.TETRAHEDRON, (N, N, N), [0, 0, 0], [L, L, L], ip_order=1, ncomp=3, qr_order=1)
+    E, nu = 10.0, 0.3
+    lam, mu = O.lame(E, nu)
+    x = p.nodes
+    n2d = node_to_dofs(p, 3)
+    right = np.where(np.abs(x[:, 0] - L) < 1e-12)[0]
+    left = np.where(np.abs(x[:, 0]) < 1e-12)[0]
+    th, t = np.pi / 3, 0.5
+    un = np.zeros(p.ndofs)
+    for n in left:  # rotation(X, t), hyperelasticity.jl:352-362
+        X, Y, Z = x[n]
+        un[n2d[n]] = t * np.array([0.0, L / 2 - Y + (Y - L / 2) * np.cos(th) - (Z - L / 2) * np.sin(th),
+                                   L / 2 - Z + (Y - L / 2) * np.sin(th) + (Z - L / 2) * np.cos(th)])
+    cons = np.concatenate([n2d[right].ravel(), n2d[left].ravel()])
+    # dead traction 0.1*n on top/bottom/front/back with a 1-point facet rule
+    # (hyperelasticity.jl:262-275): each facet node receives -t * area / 3
+    faces = [(0, 2, 1), (0, 1, 3), (1, 2, 3), (0, 3, 2)]
+    gt = np.zeros(p.ndofs)
+    for c in range(p.n_cells):
+        cn = p.cells_of(c) - 1
+        for fc in faces:
+            nd = cn[list(fc)]
+            P = x[nd]
+            for ax, val, nrm in [(2, L, (0, 0, 1)), (2, 0, (0, 0, -1)), (1, 0, (0, -1, 0)), (1, L, (0, 1, 0))]:
+                if np.all(np.abs(P[:, ax] - val) < 1e-12):
+                    area = 0.5 * np.linalg.norm(np.cross(P[1] - P[0], P[2] - P[0]))
+                    for n in nd:
+                        gt[n2d[n]] -= 0.1 * np.array(nrm) * area / 3
+    du = np.zeros(p.ndofs)
+    free = np.setdiff1d(np.arange(p.ndofs), cons)
+    for _ in range(30):
+        u = un + du
+        nz, g = p.assemble(O.NEO_HOOKE, mu, lam, body=[0, -0.5, 0], u=u)
+        g = g + gt
+        g[cons] = 0.0  # apply_zero!
+        if np.linalg.norm(g) < 1e-8:
+            break
+        K = p.to_scipy(nz)
+        d = np.zeros(p.ndofs)
+        d[free] = spla.spsolve(K[free][:, free].tocsc(), g[free])
+        du -= d
+    gold = GOLDEN["hyperelasticity_norm_u"]
+    assert np.linalg.norm(u) == pytest.approx(gold["value"], rel=gold["rtol"])
+
+
+@pytest.mark.parametrize("ct,orders,vol", [(2, [1, 2, 3, 4], 4.0), (4, [1, 2, 3, 4], 8.0),
+                                           (3, [1, 2, 3], 1 / 6), (5, [1, 2], 0.5)])
+def test_quadrature_exactness(oracle, ct, orders, vol):
+    O = oracle
+    for order in orders:
+        w, pts = O.quadrature(ct, order)
+        assert w.sum() == pytest.approx(vol, abs=1e-14)
+        if ct in (O.QUADRILATERAL, O.HEXAHEDRON):
+            deg = 2 * order - 1
+            d = pts.shape[1]
+            for exps in itertools.product(range(deg + 1), repeat=d):
+                exact = np.prod([(1 - (-1) ** (e + 1)) / (e + 1) for e in exps])
+                num = np.sum(w * np.prod(pts ** np.array(exps), axis=1))
+                assert num == pytest.approx(exact, abs=1e-13)
+
+
+@pytest.mark.parametrize("ct,nel,ip,nc", [(2, (3, 4), 1, 1), (4, (3, 2, 2), 1, 3), (4, (2, 2, 2), 2, 3),
+                                          (3, (2, 2, 2), 1, 3), (5, (2, 2, 3), 1, 3)])
+def test_volume_and_linear_field(oracle, ct, nel, ip, nc):
+    """sum(detJdV) = |box| on a perturbed grid; the FE gradient of an interpolated linear
+    field is exact (test_cellvalues.jl:51-161)."""
+    O = oracle
+    d = O.ref_dim(ct)
+    left, right = -np.ones(d), np.ones(d) * 2
+    qo = 2 if ct != O.TETRAHEDRON else 2
+    p = O.box_problem(ct, nel, left, right, ip_order=ip, ncomp=nc, qr_order=qo, perturb=0.15, seed=3,
+                      pattern=True)
+    # volume via heat f with unit source: sum(f) = integral of sum_i N_i = |Omega|
+    nz, f = p.assemble(O.HEAT if nc == 1 else O.LINEAR_ELASTIC, 1.0, 1.0 if nc == 1 else 0.3,
+                       body=[1.0, 0.0, 0.0])
+    total = f.sum()
+    assert total == pytest.approx(np.prod(right - left), rel=1e-12)
+    # linear field: K * u_lin for heat has zero row sums at interior nodes
+    if nc == 1:
+        K = p.to_scipy(nz)
+        assert np.allclose(K @ np.ones(p.ndofs), 0.0, atol=1e-12)
+
+
+def test_rigid_body_modes_elastic(oracle):
+    """K annihilates rigid translations and infinitesimal rotations."""
+    O = oracle
+    p = O.box_problem(O.HEXAHEDRON, (3, 3, 2), ip_order=1, ncomp=3, perturb=0.2, seed=7)
+    nz, _ = p.assemble(O.LINEAR_ELASTIC, 200e3, 0.3)
+    K = p.to_scipy(nz)
+    n2d = node_to_dofs(p, 3)
+    x = p.nodes
+    for mode in range(6):
+        u = np.zeros(p.ndofs)
+        for n in range(len(x)):
+            if mode < 3:
+                v = np.eye(3)[mode]
+            else:
+                w = np.eye(3)[mode - 3]
+                v = np.cross(w, x[n])
+            u[n2d[n]] = v
+        assert np.abs(K @ u).max() < 1e-9 * np.abs(nz).max()
+
+
+def test_elastic_equals_neo_hooke_tangent_at_rest(oracle):
+    """At u = 0 the Neo-Hooke tangent equals the small-strain isotropic stiffness."""
+    O = oracle
+    p = O.box_problem(O.HEXAHEDRON, (2, 3, 2), ip_order=1, ncomp=3, perturb=0.2, seed=5)
+    E, nu = 10.0, 0.3
+    lam, mu = O.lame(E, nu)
+    k1, _ = p.assemble(O.LINEAR_ELASTIC, E, nu)
+    k2, _ = p.assemble(O.NEO_HOOKE, mu, lam, u=np.zeros(p.ndofs))
+    assert np.allclose(k1, k2, rtol=1e-12, atol=1e-12 * np.abs(k1).max())
+
+
+def test_neo_hooke_tangent_matches_fd(oracle):
+    O = oracle
+    p = O.box_problem(O.WEDGE, (2, 2, 1), ip_order=1, ncomp=3, qr_order=2, perturb=0.1, seed=1)
+    rng = np.random.default_rng(0)
+    u = 0.05 * rng.uniform(-1, 1, p.ndofs)
+    nz, g = p.assemble(O.NEO_HOOKE, 1.0, 10.0, u=u)
+    K = p.to_scipy(nz)
+    v = rng.standard_normal(p.ndofs)
+    h = 1e-6
+    _, gp = p.assemble(O.NEO_HOOKE, 1.0, 10.0, u=u + h * v)
+    _, gm = p.assemble(O.NEO_HOOKE, 1.0, 10.0, u=u - h * v)
+    fd = (gp - gm) / (2 * h)
+    assert np.allclose(K @ v, fd, rtol=1e-6, atol=1e-7 * np.abs(fd).max())
+
+
+def test_q2_dof_sharing_consistent(oracle):
+    """Every Q2 hexahedron dof gets one value from the nodal interpolation of a quadratic
+    field, and each cell then reproduces the field exactly: shared edge/face dofs are
+    shared, not duplicated (restates test_dofs.jl:1156-1235's consistency goal)."""
+    O = oracle
+    nel = (2, 3, 2)
+    p = O.box_problem(O.HEXAHEDRON, nel, [0, 0, 0], [2, 3, 1], ip_order=2, ncomp=1, qr_order=3)
+    nv, ne = np.prod(np.array(nel) + 1), 0
+    nx, ny, nz = nel
+    ne = nx * (ny + 1) * (nz + 1) + ny * (nx + 1) * (nz + 1) + nz * (nx + 1) * (ny + 1)
+    nf = nx * ny * (nz + 1) + nx * nz * (ny + 1) + ny * nz * (nx + 1)
+    assert p.ndofs == nv + ne + nf + nx * ny * nz
+    lattice = np.array(list(itertools.product([-1.0, 0.0, 1.0], repeat=3)))[:, ::-1]
+    N27, _ = O.shape_tables(O.HEXAHEDRON, 2, lattice)
+    refc = lattice[np.argmax(N27, axis=0)]  # reference coordinate of each base function
+    M8, _ = O.shape_tables(O.HEXAHEDRON, 1, refc)
+    ufun = lambda X: 1 + X[..., 0] + 2 * X[..., 1] ** 2 + 3 * X[..., 0] * X[..., 2] - X[..., 1] * X[..., 2]
+    val = np.full(p.ndofs, np.nan)
+    for c in range(p.n_cells):
+        xg = p.nodes[p.cells_of(c) - 1]
+        pos = M8 @ xg
+        d = p.celldofs(c) - 1
+        v = ufun(pos)
+        seen = ~np.isnan(val[d])
+        assert np.allclose(val[d][seen], v[seen], atol=1e-12)
+        val[d] = v
+    w, qp = O.quadrature(O.HEXAHEDRON, 3)
+    Nq, _ = O.shape_tables(O.HEXAHEDRON, 2, qp)
+    Mq, _ = O.shape_tables(O.HEXAHEDRON, 1, qp)
+    for c in range(p.n_cells):
+        xg = p.nodes[p.cells_of(c) - 1]
+        assert np.allclose(Nq @ val[p.celldofs(c) - 1], ufun(Mq @ xg), atol=1e-12)
+
+
+def test_pattern_structure(oracle):
+    O = oracle
+    p = O.box_problem(O.HEXAHEDRON, (3, 2, 2), ip_order=1, ncomp=3)
+    K = p.to_scipy(np.ones(p.nnz))
+    assert (abs(K - K.T)).nnz == 0
+    assert np.all(K.diagonal() == 1)
+    for c in range(p.ndofs):
+        rows = p.rowval[p.colptr[c] - 1:p.colptr[c + 1] - 1]
+        assert np.all(np.diff(rows) > 0)
+    # entries = dof pairs sharing a cell (plus diagonal)
+    pairs = set()
+    for c in range(p.n_cells):
+        d = p.celldofs(c)
+        pairs.update((int(a), int(b)) for a in d for b in d)
+    assert len(pairs) == p.nnz
+
+
+def test_zero_skipping_and_pattern_miss(oracle):
+    """Exact zeros are never added (entries that only receive zeros stay +0.0), and a
+    non-zero value without a pattern entry raises (assembler.jl:413-467)."""
+    O = oracle
+    p = O.box_problem(O.QUADRILATERAL, (3, 3), qr_order=2)
+    nz, f = p.assemble(O.HEAT, 0.0, 1.0)  # k = 0: every Ke entry is exactly 0
+    assert np.all(nz == 0) and not np.any(np.signbit(nz))
+    # drop one off-diagonal entry from the pattern: assembling must now fail
+    col = 5
+    a, b = p.colptr[col] - 1, p.colptr[col + 1] - 1
+    rows = p.rowval[a:b]
+    drop = a + int(np.where(rows != col + 1)[0][0])
+    rowval = np.delete(p.rowval, drop)
+    colptr = p.colptr.copy()
+    colptr[col + 1:] -= 1
+    p.rowval, p.colptr = rowval, colptr
+    with pytest.raises(O.OracleError) as ei:
+        p.assemble(O.HEAT, 1.0, 1.0)
+    assert ei.value.name == "PATTERN_MISSING" and ei.value.col == col + 1
+    # zero contributions to the missing entry are allowed
+    p.assemble(O.HEAT, 0.0, 1.0)
+
+
+def test_detj_error(oracle):
+    O = oracle
+    nodes, cells = O.generate_grid(O.QUADRILATERAL, (2, 2))
+    cells[3] = cells[3][[1, 0, 3, 2]]  # mirrored cell -> detJ < 0
+    p = O.Problem.single(O.QUADRILATERAL, nodes, cells).close().allocate_matrix()
+    with pytest.raises(O.OracleError) as ei:
+        p.assemble(O.HEAT, 1.0, 1.0)
+    assert ei.value.name == "DETJ" and ei.value.cell == 4 and ei.value.detJ < 0
+
+
+def test_colored_threaded_determinism(oracle):
+    """Colored threaded assembly is bitwise identical for 1, 2 and 4 threads and equal to
+    the sequential loop up to summation order (threaded_assembly.jl:397-410)."""
+    O = oracle
+    p = O.box_problem(O.HEXAHEDRON, (10, 5, 5), [0, 0, 0], [10, 5, 5], ip_order=1, ncomp=3)
+    runs = [p.assemble(O.LINEAR_ELASTIC, 200e9, 0.3, body=[0, 0, -1], nthreads=t) for t in (1, 2, 4)]
+    for nz, f in runs[1:]:
+        assert np.array_equal(nz, runs[0][0]) and np.array_equal(f, runs[0][1])
+    nz0, f0 = p.assemble(O.LINEAR_ELASTIC, 200e9, 0.3, body=[0, 0, -1])
+    assert np.allclose(runs[0][0], nz0, rtol=1e-13, atol=1e-13 * np.abs(nz0).max())
+    assert np.allclose(runs[0][1], f0, rtol=1e-13)
+
+
+def test_index_map_matches_binary_search(oracle):
+    O = oracle
+    p = O.box_problem(O.HEXAHEDRON, (2, 2, 2), ip_order=2, ncomp=3, qr_order=3)
+    for c in (0, 5, 7):
+        pos = p.index_map(c)
+        d = p.celldofs(c)
+        for J in range(len(d)):
+            a, b = p.colptr[d[J] - 1] - 1, p.colptr[d[J]] - 1
+            expect = a + np.searchsorted(p.rowval[a:b], d) + 1
+            assert np.array_equal(pos[:, J], expect)
