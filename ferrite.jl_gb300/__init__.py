@@ -1,0 +1,366 @@
+"""ferrite_gb300 -- Python host binding of libferrite_gb300.so, the GB300 (sm_103a)
+finite-element assembly engine that replaces Ferrite.jl's assembly hot path.
+
+The C ABI (include/ferrite_gb300.h) is the product; this module mirrors the Ferrite-level
+interface on top of it so a Python caller (and the parity tests) reads like Ferrite code:
+
+    handle = Handle(grid_nodes, [Subdomain(...)], dh_cell_dofs, dh_cell_dofs_offset, ndofs,
+                    K_colptr, K_rowval, n_cells)            # allocate_matrix + CellValues data
+    asm = start_assemble(handle, K_nzval, f)                 # src/assembler.jl:287-291
+    assemble(asm, LinearElasticity(E, nu, body))             # the whole cell loop, one call
+    K_nzval, f = finish_assemble(asm)                        # src/assembler.jl:299-301
+
+nzval / f / u / cell_scale may be numpy arrays (host; staged through device buffers) or
+torch CUDA tensors (device, written in place). Errors raise ``FEError`` carrying the same
+information as Ferrite's exceptions (cell id and detJ, or the missing (row, col)).
+
+There is no CPU fallback: if the shared library is missing or no GPU is present, calls fail.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass, field
+from typing import Optional, Sequence
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libferrite_gb300.so")
+
+# constants of include/ferrite_gb300.h
+FE_OK, FE_ERR_ARG, FE_ERR_BOUNDS, FE_ERR_DETJ, FE_ERR_PATTERN_MISSING = 0, 1, 2, 3, 4
+FE_ERR_UNSUPPORTED, FE_ERR_CUDA, FE_ERR_OOM, FE_ERR_STATE = 5, 6, 7, 8
+ERROR_NAMES = {0: "OK", 1: "ARG", 2: "BOUNDS", 3: "DETJ", 4: "PATTERN_MISSING", 5: "UNSUPPORTED",
+               6: "CUDA", 7: "OOM", 8: "STATE"}
+TRIANGLE, QUADRILATERAL, TETRAHEDRON, HEXAHEDRON, WEDGE = 1, 2, 3, 4, 5
+HEAT, LINEAR_ELASTIC, NEO_HOOKE = 1, 2, 3
+PREC_MIXED, PREC_FP64 = 0, 1
+FILLZERO, NO_K, NO_F, ASYNC = 1, 2, 4, 8
+
+EXPORTED = ["fe_abi_version", "fe_create", "fe_assemble", "fe_sync", "fe_last_error", "fe_get_info",
+            "fe_get_index_map", "fe_plan_dry_run", "fe_destroy"]
+
+i64p = ctypes.POINTER(ctypes.c_int64)
+f64p = ctypes.POINTER(ctypes.c_double)
+
+
+class GridDesc(ctypes.Structure):
+    _fields_ = [("dim", ctypes.c_int32), ("n_nodes", ctypes.c_int64), ("nodes", f64p), ("n_cells", ctypes.c_int64)]
+
+
+class SubdomainDesc(ctypes.Structure):
+    _fields_ = [("cell_type", ctypes.c_int32), ("ip_order", ctypes.c_int32), ("n_components", ctypes.c_int32),
+                ("n_qp", ctypes.c_int32), ("qr_weights", f64p), ("N", f64p), ("dNdxi", f64p), ("M", f64p),
+                ("dMdxi", f64p), ("n_cells", ctypes.c_int64), ("cellset", i64p), ("cell_nodes", i64p)]
+
+
+class DofDesc(ctypes.Structure):
+    _fields_ = [("ndofs", ctypes.c_int64), ("cell_dofs", i64p), ("cell_dofs_offset", i64p)]
+
+
+class CscDesc(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("nnz", ctypes.c_int64), ("colptr", i64p), ("rowval", i64p)]
+
+
+class AssembleParams(ctypes.Structure):
+    _fields_ = [("physics", ctypes.c_int32), ("precision", ctypes.c_int32), ("flags", ctypes.c_uint32),
+                ("p0", ctypes.c_double), ("p1", ctypes.c_double), ("body", ctypes.c_double * 3),
+                ("cell_scale", ctypes.c_void_p), ("u", ctypes.c_void_p), ("cond_threshold", ctypes.c_double),
+                ("stream", ctypes.c_void_p)]
+
+
+class ErrorInfo(ctypes.Structure):
+    _fields_ = [("code", ctypes.c_int32), ("cell", ctypes.c_int64), ("detJ", ctypes.c_double),
+                ("row", ctypes.c_int64), ("col", ctypes.c_int64), ("message", ctypes.c_char * 256)]
+
+
+class Info(ctypes.Structure):
+    _fields_ = [("n_cells", ctypes.c_int64), ("ndofs", ctypes.c_int64), ("nnz", ctypes.c_int64),
+                ("n_tiles", ctypes.c_int64), ("n_cell_visits", ctypes.c_int64), ("n_items", ctypes.c_int64),
+                ("flagged_cells", ctypes.c_int64), ("device_bytes", ctypes.c_int64),
+                ("create_seconds", ctypes.c_double)]
+
+
+_lib = None
+
+
+def build(verbose: bool = False, force: bool = False) -> str:
+    """Compile the CUDA library for sm_103a (ferrite.jl_gb300/build.py)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_fe_build", os.path.join(PKG, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(verbose=verbose, force=force)
+
+
+def lib():
+    """Load libferrite_gb300.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run ferrite_gb300.build() (nvcc, sm_103a) first")
+        L = ctypes.CDLL(LIB_PATH)
+        L.fe_abi_version.restype = ctypes.c_int
+        L.fe_create.argtypes = [ctypes.POINTER(GridDesc), ctypes.c_int32, ctypes.POINTER(SubdomainDesc),
+                                ctypes.POINTER(DofDesc), ctypes.POINTER(CscDesc), ctypes.POINTER(ctypes.c_void_p)]
+        L.fe_assemble.argtypes = [ctypes.c_void_p, ctypes.POINTER(AssembleParams), ctypes.c_void_p, ctypes.c_void_p]
+        L.fe_sync.argtypes = [ctypes.c_void_p]
+        L.fe_last_error.argtypes = [ctypes.c_void_p, ctypes.POINTER(ErrorInfo)]
+        L.fe_get_info.argtypes = [ctypes.c_void_p, ctypes.POINTER(Info)]
+        L.fe_get_index_map.argtypes = [ctypes.c_void_p, ctypes.c_int64, i64p]
+        L.fe_plan_dry_run.argtypes = [ctypes.POINTER(GridDesc), ctypes.c_int32, ctypes.POINTER(SubdomainDesc),
+                                      ctypes.POINTER(DofDesc), ctypes.POINTER(CscDesc), ctypes.POINTER(Info)]
+        L.fe_destroy.argtypes = [ctypes.c_void_p]
+        L.fe_destroy.restype = None
+        _lib = L
+    return _lib
+
+
+class FEError(RuntimeError):
+    """An FE_* status from the library, with Ferrite's exception details."""
+
+    def __init__(self, code: int, info: Optional[ErrorInfo] = None):
+        self.code = code
+        self.name = ERROR_NAMES.get(code, str(code))
+        self.cell = info.cell if info else 0
+        self.detJ = info.detJ if info else 0.0
+        self.row = info.row if info else 0
+        self.col = info.col if info else 0
+        msg = info.message.decode(errors="replace") if info else ""
+        super().__init__(f"FE_ERR_{self.name}: {msg}")
+
+
+def _as_i64(a):
+    return np.ascontiguousarray(a, dtype=np.int64)
+
+
+def _as_f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _ptr(x):
+    """Raw address of a numpy array or a torch tensor (None -> NULL)."""
+    if x is None:
+        return None
+    if isinstance(x, np.ndarray):
+        if not x.flags.c_contiguous:
+            raise ValueError("array must be contiguous")
+        return x.ctypes.data
+    if hasattr(x, "data_ptr"):
+        if not x.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return x.data_ptr()
+    raise TypeError(f"unsupported buffer type {type(x)}")
+
+
+@dataclass
+class Subdomain:
+    """One SubDofHandler + its CellValues data (the arrays a Julia caller extracts from
+    ``dh.subdofhandlers[k]``, ``cv.fun_values`` and ``cv.geo_mapping``)."""
+    cell_type: int
+    ip_order: int
+    n_components: int
+    qr_weights: np.ndarray
+    N: np.ndarray        # [nq, nb]
+    dNdxi: np.ndarray    # [nq, nb, rdim]
+    M: np.ndarray        # [nq, ng]
+    dMdxi: np.ndarray    # [nq, ng, rdim]
+    cellset: np.ndarray  # [n] 1-based
+    cell_nodes: np.ndarray  # [n, ng] 1-based
+    _keep: list = field(default_factory=list, repr=False)
+
+    def desc(self) -> SubdomainDesc:
+        arrs = [_as_f64(self.qr_weights), _as_f64(self.N), _as_f64(self.dNdxi), _as_f64(self.M),
+                _as_f64(self.dMdxi), _as_i64(self.cellset), _as_i64(self.cell_nodes)]
+        self._keep = arrs
+        d = SubdomainDesc()
+        d.cell_type, d.ip_order, d.n_components = self.cell_type, self.ip_order, self.n_components
+        d.n_qp = len(arrs[0])
+        d.qr_weights, d.N, d.dNdxi, d.M, d.dMdxi = [a.ctypes.data_as(f64p) for a in arrs[:5]]
+        d.n_cells = len(arrs[5])
+        d.cellset = arrs[5].ctypes.data_as(i64p)
+        d.cell_nodes = arrs[6].ctypes.data_as(i64p)
+        return d
+
+
+def _descs(nodes, subdomains, cell_dofs, cell_dofs_offset, ndofs, colptr, rowval, n_cells):
+    nodes = _as_f64(nodes)
+    g = GridDesc(nodes.shape[1], nodes.shape[0], nodes.ctypes.data_as(f64p), int(n_cells))
+    subs = (SubdomainDesc * len(subdomains))(*[s.desc() for s in subdomains])
+    cd, co = _as_i64(cell_dofs), _as_i64(cell_dofs_offset)
+    dd = DofDesc(int(ndofs), cd.ctypes.data_as(i64p), co.ctypes.data_as(i64p))
+    cp, rv = _as_i64(colptr), _as_i64(rowval)
+    pd = CscDesc(int(ndofs), int(len(rv)), cp.ctypes.data_as(i64p), rv.ctypes.data_as(i64p))
+    return (g, subs, dd, pd), (nodes, cd, co, cp, rv)
+
+
+def plan_dry_run(nodes, subdomains, cell_dofs, cell_dofs_offset, ndofs, colptr, rowval, n_cells) -> dict:
+    """fe_plan_dry_run: validate the arrays and build the index map and owner tiles on the
+    host only (no GPU needed)."""
+    (g, subs, dd, pd), _keep = _descs(nodes, subdomains, cell_dofs, cell_dofs_offset, ndofs, colptr, rowval, n_cells)
+    info = Info()
+    L = lib()
+    rc = L.fe_plan_dry_run(ctypes.byref(g), len(subdomains), subs, ctypes.byref(dd), ctypes.byref(pd), ctypes.byref(info))
+    if rc != FE_OK:
+        e = ErrorInfo()
+        L.fe_last_error(None, ctypes.byref(e))
+        raise FEError(rc, e)
+    return {k: getattr(info, k) for k, _ in Info._fields_}
+
+
+class Handle:
+    """fe_create/fe_destroy: the device-resident problem (grid, dofs, pattern, index map,
+    owner tiles)."""
+
+    def __init__(self, nodes, subdomains: Sequence[Subdomain], cell_dofs, cell_dofs_offset, ndofs: int,
+                 colptr, rowval, n_cells: int):
+        L = lib()
+        nodes = _as_f64(nodes)
+        g = GridDesc(nodes.shape[1], nodes.shape[0], nodes.ctypes.data_as(f64p), int(n_cells))
+        subs = (SubdomainDesc * len(subdomains))(*[s.desc() for s in subdomains])
+        cd, co = _as_i64(cell_dofs), _as_i64(cell_dofs_offset)
+        dd = DofDesc(int(ndofs), cd.ctypes.data_as(i64p), co.ctypes.data_as(i64p))
+        cp, rv = _as_i64(colptr), _as_i64(rowval)
+        pd = CscDesc(int(ndofs), int(len(rv)), cp.ctypes.data_as(i64p), rv.ctypes.data_as(i64p))
+        h = ctypes.c_void_p()
+        rc = L.fe_create(ctypes.byref(g), len(subdomains), subs, ctypes.byref(dd), ctypes.byref(pd), ctypes.byref(h))
+        if rc != FE_OK:
+            info = ErrorInfo()
+            L.fe_last_error(None, ctypes.byref(info))
+            raise FEError(rc, info)
+        self._h = h
+        self.ndofs = int(ndofs)
+        self.nnz = int(len(rv))
+        self.n_cells = int(n_cells)
+        self.ndofs_per_cell = {}
+        self._subdomains = list(subdomains)
+
+    @property
+    def ptr(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fe_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _raise(self, rc):
+        info = ErrorInfo()
+        lib().fe_last_error(self._h, ctypes.byref(info))
+        raise FEError(rc, info)
+
+    def assemble(self, nzval, f, physics: int, p0: float, p1: float, body=(0.0, 0.0, 0.0), cell_scale=None, u=None,
+                 precision: int = PREC_MIXED, fillzero: bool = True, stream=None, sync: bool = True,
+                 cond_threshold: float = 0.0):
+        """One fe_assemble call. ``stream`` is a torch.cuda.Stream, a raw handle or None."""
+        p = AssembleParams()
+        p.physics, p.precision = physics, precision
+        flags = FILLZERO if fillzero else 0
+        if nzval is None:
+            flags |= NO_K
+        if f is None:
+            flags |= NO_F
+        if not sync:
+            flags |= ASYNC
+        p.flags = flags
+        p.p0, p.p1 = float(p0), float(p1)
+        for k in range(3):
+            p.body[k] = float(body[k]) if k < len(body) else 0.0
+        p.cell_scale = _ptr(cell_scale)
+        p.u = _ptr(u)
+        p.cond_threshold = float(cond_threshold)
+        if stream is not None and hasattr(stream, "cuda_stream"):
+            stream = stream.cuda_stream
+        p.stream = stream
+        rc = lib().fe_assemble(self._h, ctypes.byref(p), _ptr(nzval), _ptr(f))
+        if rc != FE_OK:
+            self._raise(rc)
+        return nzval, f
+
+    def sync(self):
+        rc = lib().fe_sync(self._h)
+        if rc != FE_OK:
+            self._raise(rc)
+
+    def info(self) -> dict:
+        i = Info()
+        lib().fe_get_info(self._h, ctypes.byref(i))
+        return {k: getattr(i, k) for k, _ in Info._fields_}
+
+    def index_map(self, cell: int, ld: int):
+        """1-based nzval positions of Ke entries of a (1-based) cell: array [ld, ld], Ke[I, J]."""
+        out = np.zeros((ld, ld), np.int64, order="F")
+        rc = lib().fe_get_index_map(self._h, int(cell), out.ctypes.data_as(i64p))
+        if rc != FE_OK:
+            self._raise(rc)
+        return out
+
+
+# ---------------------------------------------------------------------------------------
+# Ferrite-style front end
+# ---------------------------------------------------------------------------------------
+@dataclass
+class Heat:
+    """heat_equation.jl:143-164: Ke += k gradN_i.gradN_j dOmega, fe += source N_i dOmega."""
+    k: float = 1.0
+    source: float = 1.0
+    cell_scale: object = None
+
+    def args(self):
+        return dict(physics=HEAT, p0=self.k, p1=self.source, cell_scale=self.cell_scale)
+
+
+@dataclass
+class LinearElasticity:
+    """threaded_assembly.jl:105-132 (isotropic C from E, nu); cell_scale multiplies E per cell
+    (SIMP, topology_optimization.jl:347-383)."""
+    E: float
+    nu: float
+    body: tuple = (0.0, 0.0, 0.0)
+    cell_scale: object = None
+
+    def args(self):
+        return dict(physics=LINEAR_ELASTIC, p0=self.E, p1=self.nu, body=self.body, cell_scale=self.cell_scale)
+
+
+@dataclass
+class NeoHooke:
+    """hyperelasticity.jl:157-276 (cell part): tangent K and residual g at displacement u."""
+    mu: float
+    lam: float
+    u: object = None
+    body: tuple = (0.0, 0.0, 0.0)
+
+    def args(self):
+        return dict(physics=NEO_HOOKE, p0=self.mu, p1=self.lam, body=self.body, u=self.u)
+
+
+class GPUAssembler:
+    """What ``start_assemble(K, f)`` returns (src/assembler.jl:287-291), for the device engine."""
+
+    def __init__(self, handle: Handle, nzval, f, fillzero: bool = True, precision: int = PREC_MIXED, stream=None):
+        self.handle, self.nzval, self.f = handle, nzval, f
+        self.fillzero, self.precision, self.stream = fillzero, precision, stream
+
+
+def start_assemble(handle: Handle, nzval, f=None, fillzero: bool = True, precision: int = PREC_MIXED, stream=None):
+    return GPUAssembler(handle, nzval, f, fillzero, precision, stream)
+
+
+def assemble(asm: GPUAssembler, element, sync: bool = True):
+    """The whole ``for cell in CellIterator(dh); reinit!; element!; assemble!; end`` loop."""
+    asm.handle.assemble(asm.nzval, asm.f, precision=asm.precision, fillzero=asm.fillzero, stream=asm.stream,
+                        sync=sync, **element.args())
+    asm.fillzero = False  # later calls accumulate, like a second loop over the same assembler
+    return asm
+
+
+def finish_assemble(asm: GPUAssembler):
+    return asm.nzval, asm.f

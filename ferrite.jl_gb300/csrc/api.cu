@@ -1,0 +1,544 @@
+// api.cu -- the extern "C" entry points declared in include/ferrite_gb300.h.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "ferrite_gb300.h"
+#include "plan.h"
+#include "registry.h"
+#include "tile_kernel.cuh"
+
+using namespace fe;
+
+namespace {
+
+const std::vector<KernelEntry>& registry() {
+    static std::vector<KernelEntry> reg;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        register_heat(reg);
+        register_elastic(reg);
+        register_neo(reg);
+    });
+    return reg;
+}
+
+__global__ void to_float_kernel(const double* __restrict__ in, float* __restrict__ out, int64_t n) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        out[k] = (float)in[k];
+}
+
+bool is_device_ptr(const void* p) {
+    if (!p) return false;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+
+struct fe_handle {
+    HostProblem hp;
+    Plan plan;
+    std::vector<void*> allocs;
+    int64_t device_bytes = 0;
+    KernelArgs base{};
+    // staged reference tables (one block per subdomain), float and double
+    float* shape_f = nullptr;
+    double* shape_d = nullptr;
+    int shape_bytes[2] = {0, 0}, shape_off1[2] = {0, 0}, shape_off2[2] = {0, 0};
+    DevStatus* status_d = nullptr;
+    DevStatus* status_h = nullptr;  // pinned
+    // staging buffers for host-pointer calls
+    double* nz_stage = nullptr;
+    double* f_stage = nullptr;
+    double* u_stage = nullptr;
+    double* scale_stage = nullptr;
+    float* u_f = nullptr;
+    float* scale_f = nullptr;
+    cudaStream_t last_stream = 0;
+    int pending = 0;  // an FE_ASYNC assembly whose status has not been read
+    fe_error_info last{};
+    int64_t flagged = 0;
+    double create_seconds = 0;
+    int device = 0;
+
+    template <typename T>
+    cudaError_t alloc(T** p, size_t count) {
+        if (count == 0) count = 1;
+        cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+        if (e == cudaSuccess) {
+            allocs.push_back((void*)*p);
+            device_bytes += (int64_t)(count * sizeof(T));
+        }
+        return e;
+    }
+    template <typename T>
+    cudaError_t upload(T** p, const T* src, size_t count) {
+        cudaError_t e = alloc(p, count);
+        if (e != cudaSuccess) return e;
+        if (count) e = cudaMemcpy(*p, src, count * sizeof(T), cudaMemcpyHostToDevice);
+        return e;
+    }
+    ~fe_handle() {
+        for (void* p : allocs) cudaFree(p);
+        if (status_h) cudaFreeHost(status_h);
+    }
+};
+
+namespace {
+
+thread_local fe_error_info g_create_error{};
+
+int set_error(fe_handle* h, int code, const std::string& msg, int64_t cell = 0, double detJ = 0, int64_t row = 0,
+              int64_t col = 0) {
+    if (!h) return code;
+    h->last.code = code;
+    h->last.cell = cell;
+    h->last.detJ = detJ;
+    h->last.row = row;
+    h->last.col = col;
+    std::snprintf(h->last.message, sizeof(h->last.message), "%s", msg.c_str());
+    return code;
+}
+
+int cuda_fail(fe_handle* h, cudaError_t e, const char* what) {
+    const int code = (e == cudaErrorMemoryAllocation) ? FE_ERR_OOM : FE_ERR_CUDA;
+    return set_error(h, code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Read the device status of the last assembly and translate it into an FE_* code.
+int finish_status(fe_handle* h) {
+    const DevStatus& st = *h->status_h;
+    h->flagged = st.flagged;
+    h->pending = 0;
+    if (st.timeout) return set_error(h, FE_ERR_CUDA, "a tile timed out waiting for its reference-table copy");
+    if (st.detj_key != ~0ull) {
+        const int64_t cell = (int64_t)(st.detj_key >> 32) + 1;
+        uint32_t bits = (uint32_t)(st.detj_key & 0xFFFFFFFFu);
+        float dj;
+        std::memcpy(&dj, &bits, 4);
+        char buf[160];
+        std::snprintf(buf, sizeof buf, "det(J) is not positive: det(J) = %g in cell %lld", (double)dj, (long long)cell);
+        return set_error(h, FE_ERR_DETJ, buf, cell, dj);
+    }
+    if (st.miss_key != ~0ull) {
+        const int64_t cell = (int64_t)(st.miss_key >> 32) + 1;
+        const int I = (int)((st.miss_key >> 16) & 0xFFFF), J = (int)(st.miss_key & 0xFFFF);
+        const int64_t* cd = h->hp.cell_dofs.data() + h->hp.cell_dofs_off[cell - 1] - 1;
+        const int64_t row = cd[I], col = cd[J];
+        char buf[200];
+        std::snprintf(buf, sizeof buf, "You are trying to assemble values in to K[%lld, %lld], but K[%lld, %lld] is missing in the sparsity pattern.",
+                      (long long)row, (long long)col, (long long)row, (long long)col);
+        return set_error(h, FE_ERR_PATTERN_MISSING, buf, cell, 0, row, col);
+    }
+    h->last = fe_error_info{};
+    return FE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fe_abi_version(void) { return FE_ABI_VERSION; }
+
+int fe_create(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain_desc* subdomains, const fe_dof_desc* dofs,
+              const fe_csc_desc* pattern, fe_handle** out) {
+    if (!out) return FE_ERR_ARG;
+    *out = nullptr;
+    const auto t0 = std::chrono::steady_clock::now();
+    fe_handle* h = new (std::nothrow) fe_handle();
+    if (!h) return FE_ERR_OOM;
+    Error err;
+    CreateInput in{grid, n_subdomains, subdomains, dofs, pattern};
+    int rc = build_problem(in, h->hp, err);
+    if (rc == FE_OK) {
+        PlanOptions opt;
+        if (const char* s = std::getenv("FE_GB300_ACC_CAP")) opt.acc_cap = std::atoi(s);
+        rc = build_plan(h->hp, opt, h->plan, err);
+        if (rc == FE_OK) rc = check_plan(h->hp, h->plan, err);
+    }
+    if (rc != FE_OK) {
+        g_create_error = fe_error_info{};
+        g_create_error.code = rc;
+        g_create_error.cell = err.cell;
+        g_create_error.row = err.row;
+        g_create_error.col = err.col;
+        std::snprintf(g_create_error.message, sizeof(g_create_error.message), "%s", err.msg.c_str());
+        delete h;
+        return rc;
+    }
+    const HostProblem& hp = h->hp;
+    const Plan& pl = h->plan;
+    cudaError_t e = cudaGetDevice(&h->device);
+#define CK(x)                                   \
+    do {                                        \
+        e = (x);                                \
+        if (e != cudaSuccess) {                 \
+            int c_ = cuda_fail(h, e, #x);       \
+            g_create_error = h->last;           \
+            delete h;                           \
+            return c_;                          \
+        }                                       \
+    } while (0)
+    CK(e);
+    KernelArgs& A = h->base;
+    A.nc = hp.nc;
+    A.dim = hp.dim;
+    A.n_sub = (int32_t)hp.subs.size();
+    A.n_tiles = (int32_t)pl.tiles.size();
+    // node coordinates: FP64 AoS and float hi/lo SoA
+    {
+        double* xd;
+        CK(h->upload(&xd, hp.nodes.data(), hp.nodes.size()));
+        A.xd = xd;
+        std::vector<float> hi(hp.n_nodes), lo(hp.n_nodes);
+        for (int x = 0; x < 3; ++x) {
+            if (x >= hp.dim) {
+                A.xh[x] = A.xl[x] = nullptr;
+                continue;
+            }
+            for (int64_t n = 0; n < hp.n_nodes; ++n) {
+                const double v = hp.nodes[n * hp.dim + x];
+                hi[n] = (float)v;
+                lo[n] = (float)(v - (double)hi[n]);
+            }
+            float *ph, *pl_;
+            CK(h->upload(&ph, hi.data(), hi.size()));
+            CK(h->upload(&pl_, lo.data(), lo.size()));
+            A.xh[x] = ph;
+            A.xl[x] = pl_;
+        }
+    }
+    int64_t* colptr_d;
+    CK(h->upload(&colptr_d, hp.colptr.data(), hp.colptr.size()));
+    A.colptr = colptr_d;
+    // subdomains
+    std::vector<float> shf;
+    std::vector<double> shd;
+    int offs_f[MAX_SUB] = {0, 0, 0}, offs_d[MAX_SUB] = {0, 0, 0};
+    for (size_t s = 0; s < hp.subs.size(); ++s) {
+        const HostSub& hs = hp.subs[s];
+        SubDev& sd = A.sub[s];
+        sd.kind = hs.kind; sd.nb = hs.nb; sd.ng = hs.ng; sd.nq = hs.nq; sd.dim = hs.dim; sd.nc = hs.nc;
+        sd.n_cells = hs.n_cells;
+        int32_t *cid, *conn, *ents;
+        CK(h->upload(&cid, hs.cellid.data(), hs.cellid.size()));
+        CK(h->upload(&conn, hs.conn.data(), hs.conn.size()));
+        CK(h->upload(&ents, hs.ents.data(), hs.ents.size()));
+        sd.cellid = cid; sd.conn = conn; sd.ents = ents;
+        sd.rank8 = nullptr; sd.rank16 = nullptr;
+        if (hs.wide_rank) {
+            uint16_t* r;
+            CK(h->upload(&r, hs.rank16.data(), hs.rank16.size()));
+            sd.rank16 = r;
+        } else {
+            uint8_t* r;
+            CK(h->upload(&r, hs.rank8.data(), hs.rank8.size()));
+            sd.rank8 = r;
+        }
+        // reference tables: w, N, dN (physical layout [q][i][c]), dM; padded blocks
+        auto push_block = [&](auto& vec, const std::vector<double>& src) {
+            using T = typename std::remove_reference<decltype(vec)>::type::value_type;
+            const size_t start = vec.size();
+            for (double v : src) vec.push_back((T)v);
+            while (((vec.size() - start) * sizeof(T)) % 16) vec.push_back((T)0);
+        };
+        offs_f[s] = (int)(shf.size() * sizeof(float));
+        offs_d[s] = (int)(shd.size() * sizeof(double));
+        for (auto* src : {&hs.w, &hs.N, &hs.dN, &hs.dM}) {
+            push_block(shf, *src);
+            push_block(shd, *src);
+        }
+        float *wf, *Nf, *dNf, *dMf;
+        double *wd, *Nd, *dNd, *dMd;
+        std::vector<float> tmp;
+        auto upf = [&](float** p, const std::vector<double>& v) {
+            tmp.assign(v.begin(), v.end());
+            return h->upload(p, tmp.data(), tmp.size());
+        };
+        CK(upf(&wf, hs.w)); CK(upf(&Nf, hs.N)); CK(upf(&dNf, hs.dN)); CK(upf(&dMf, hs.dM));
+        CK(h->upload(&wd, hs.w.data(), hs.w.size()));
+        CK(h->upload(&Nd, hs.N.data(), hs.N.size()));
+        CK(h->upload(&dNd, hs.dN.data(), hs.dN.size()));
+        CK(h->upload(&dMd, hs.dM.data(), hs.dM.size()));
+        sd.w_f = wf; sd.N_f = Nf; sd.dN_f = dNf; sd.dM_f = dMf;
+        sd.w_d = wd; sd.N_d = Nd; sd.dN_d = dNd; sd.dM_d = dMd;
+    }
+    CK(h->upload(&h->shape_f, shf.data(), shf.size()));
+    CK(h->upload(&h->shape_d, shd.data(), shd.size()));
+    h->shape_bytes[0] = (int)(shf.size() * sizeof(float));
+    h->shape_bytes[1] = (int)(shd.size() * sizeof(double));
+    h->shape_off1[0] = offs_f[1]; h->shape_off2[0] = offs_f[2];
+    h->shape_off1[1] = offs_d[1]; h->shape_off2[1] = offs_d[2];
+    // plan
+    TileDesc* tiles; RangeDesc* ranges; WaveDesc* waves; int32_t *wc, *wci; uint32_t* items;
+    CK(h->upload(&tiles, pl.tiles.data(), pl.tiles.size()));
+    CK(h->upload(&ranges, pl.ranges.data(), pl.ranges.size()));
+    CK(h->upload(&waves, pl.waves.data(), pl.waves.size()));
+    CK(h->upload(&wc, pl.wave_cells.data(), pl.wave_cells.size()));
+    CK(h->upload(&wci, pl.wave_cell_items.data(), pl.wave_cell_items.size()));
+    CK(h->upload(&items, pl.items.data(), pl.items.size()));
+    A.tiles = tiles; A.ranges = ranges; A.waves = waves;
+    A.wave_cells = wc; A.wave_cell_items = wci; A.items = items;
+    A.acc_cap = std::max(pl.max_acc, 1);
+    A.ent_cap = std::max(pl.max_ent, 1);
+    CK(h->alloc(&h->status_d, 1));
+    CK(cudaMallocHost((void**)&h->status_h, sizeof(DevStatus)));
+#undef CK
+    h->create_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    *out = h;
+    return FE_OK;
+}
+
+int fe_plan_dry_run(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain_desc* subdomains,
+                    const fe_dof_desc* dofs, const fe_csc_desc* pattern, fe_info* out) {
+    if (!out) return FE_ERR_ARG;
+    const auto t0 = std::chrono::steady_clock::now();
+    HostProblem hp;
+    Plan pl;
+    Error err;
+    CreateInput in{grid, n_subdomains, subdomains, dofs, pattern};
+    int rc = build_problem(in, hp, err);
+    PlanOptions opt;
+    if (const char* s = std::getenv("FE_GB300_ACC_CAP")) opt.acc_cap = std::atoi(s);
+    if (rc == FE_OK) rc = build_plan(hp, opt, pl, err);
+    if (rc == FE_OK) rc = check_plan(hp, pl, err);
+    if (rc != FE_OK) {
+        g_create_error = fe_error_info{};
+        g_create_error.code = rc;
+        g_create_error.cell = err.cell;
+        g_create_error.row = err.row;
+        g_create_error.col = err.col;
+        std::snprintf(g_create_error.message, sizeof(g_create_error.message), "%s", err.msg.c_str());
+        return rc;
+    }
+    *out = fe_info{};
+    out->n_cells = hp.n_cells;
+    out->ndofs = hp.ndofs;
+    out->nnz = hp.nnz;
+    out->n_tiles = (int64_t)pl.tiles.size();
+    out->n_cell_visits = pl.visits;
+    out->n_items = (int64_t)pl.items.size();
+    out->create_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return FE_OK;
+}
+
+void fe_destroy(fe_handle* h) {
+    if (!h) return;
+    if (h->pending) cudaStreamSynchronize(h->last_stream);
+    delete h;
+}
+
+int fe_sync(fe_handle* h) {
+    if (!h) return FE_ERR_ARG;
+    if (!h->pending) return h->last.code;
+    cudaError_t e = cudaStreamSynchronize(h->last_stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamSynchronize");
+    return finish_status(h);
+}
+
+int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double* f) {
+    if (!h || !p) return FE_ERR_ARG;
+    const HostProblem& hp = h->hp;
+    const int nc = hp.nc;
+    int phys = 0;
+    switch (p->physics) {
+        case FE_HEAT:
+            if (nc != 1) return set_error(h, FE_ERR_ARG, "FE_HEAT needs a scalar field");
+            phys = PHYS_HEAT;
+            break;
+        case FE_LINEAR_ELASTIC:
+            if (nc != hp.dim) return set_error(h, FE_ERR_ARG, "FE_LINEAR_ELASTIC needs a dim-component field");
+            phys = PHYS_ELASTIC;
+            break;
+        case FE_NEO_HOOKE:
+            if (nc != 3 || hp.dim != 3) return set_error(h, FE_ERR_ARG, "FE_NEO_HOOKE needs a 3-component field in 3D");
+            if (!p->u) return set_error(h, FE_ERR_ARG, "FE_NEO_HOOKE needs u");
+            phys = PHYS_NEO;
+            break;
+        default:
+            return set_error(h, FE_ERR_ARG, "unknown physics");
+    }
+    if (p->precision != FE_PREC_MIXED && p->precision != FE_PREC_FP64) return set_error(h, FE_ERR_ARG, "unknown precision");
+    const bool fp64 = p->precision == FE_PREC_FP64;
+    const bool do_k = !(p->flags & FE_NO_K), do_f = !(p->flags & FE_NO_F);
+    if (do_k && !nzval) return set_error(h, FE_ERR_ARG, "nzval is NULL");
+    if (do_f && !f) return set_error(h, FE_ERR_ARG, "f is NULL");
+    if (h->pending) {
+        int rc = fe_sync(h);
+        (void)rc;
+    }
+    // pick the kernel
+    const KernelEntry* ke = nullptr;
+    for (const KernelEntry& e : registry()) {
+        if (e.phys != phys || e.fp64 != (int)fp64) continue;
+        bool ok = true;
+        for (int s = 0; s < MAX_SUB; ++s) {
+            if (s < (int)hp.subs.size()) {
+                if (e.kind[s] != hp.subs[s].kind || e.nq[s] != hp.subs[s].nq) ok = false;
+            } else if (e.kind[s] >= 0) {
+                ok = false;
+            }
+        }
+        if (ok) { ke = &e; break; }
+    }
+    if (!ke) return set_error(h, FE_ERR_UNSUPPORTED, "no kernel compiled for this element / quadrature / physics combination");
+    cudaStream_t st = (cudaStream_t)p->stream;
+    cudaError_t e;
+    KernelArgs A = h->base;
+    // outputs: device pointers are written in place, host pointers are staged
+    const bool nz_dev = do_k && is_device_ptr(nzval);
+    const bool f_dev = do_f && is_device_ptr(f);
+    const bool fill = (p->flags & FE_FILLZERO) != 0;
+    if (do_k && !nz_dev) {
+        if (!h->nz_stage && (e = h->alloc(&h->nz_stage, hp.nnz)) != cudaSuccess) return cuda_fail(h, e, "alloc nzval");
+        if (!fill && (e = cudaMemcpyAsync(h->nz_stage, nzval, hp.nnz * 8, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+            return cuda_fail(h, e, "copy nzval");
+    }
+    if (do_f && !f_dev) {
+        if (!h->f_stage && (e = h->alloc(&h->f_stage, hp.ndofs)) != cudaSuccess) return cuda_fail(h, e, "alloc f");
+        if (!fill && (e = cudaMemcpyAsync(h->f_stage, f, hp.ndofs * 8, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+            return cuda_fail(h, e, "copy f");
+    }
+    A.nzval = do_k ? (nz_dev ? nzval : h->nz_stage) : nullptr;
+    A.f = do_f ? (f_dev ? f : h->f_stage) : nullptr;
+    A.do_k = do_k;
+    A.do_f = do_f;
+    A.fillzero = fill;
+    // inputs
+    Physics& ph = A.phys;
+    ph = Physics{};
+    ph.kind = p->physics;
+    ph.p0 = p->p0;
+    ph.p1 = p->p1;
+    for (int x = 0; x < 3; ++x) ph.body[x] = p->body[x];
+    if (p->physics == FE_LINEAR_ELASTIC) {
+        const double E = p->p0, nu = p->p1;
+        ph.lam = E * nu / ((1 + nu) * (1 - 2 * nu));
+        ph.mu = E / (2 * (1 + nu));
+    }
+    ph.cond_threshold = p->cond_threshold > 0 ? (float)p->cond_threshold : 64.0f;
+    auto stage_input = [&](const double* src, int64_t n, double** stage, float** stage_f, const double** out_d,
+                           const float** out_f) -> int {
+        const double* dsrc = src;
+        if (!is_device_ptr(src)) {
+            if (!*stage && (e = h->alloc(stage, n)) != cudaSuccess) return cuda_fail(h, e, "alloc input");
+            if ((e = cudaMemcpyAsync(*stage, src, n * 8, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+                return cuda_fail(h, e, "copy input");
+            dsrc = *stage;
+        }
+        *out_d = dsrc;
+        if (!fp64) {
+            if (!*stage_f && (e = h->alloc(stage_f, n)) != cudaSuccess) return cuda_fail(h, e, "alloc input");
+            to_float_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, st>>>(dsrc, *stage_f, n);
+            *out_f = *stage_f;
+        }
+        return FE_OK;
+    };
+    if (p->cell_scale) {
+        int rc = stage_input(p->cell_scale, hp.n_cells, &h->scale_stage, &h->scale_f, &ph.scale_d, &ph.scale_f);
+        if (rc) return rc;
+        if (fp64) ph.scale_f = (const float*)ph.scale_d;  // non-null marker; the FP64 kernel reads scale_d
+    }
+    if (p->physics == FE_NEO_HOOKE) {
+        int rc = stage_input(p->u, hp.ndofs, &h->u_stage, &h->u_f, &ph.u_d, &ph.u_f);
+        if (rc) return rc;
+    }
+    // shared memory: shape tables + accumulators + entity table + chunk tables
+    const int pi = fp64 ? 1 : 0;
+    const int acc_elem = 8;
+    const int fixed = pad16(h->shape_bytes[pi]) + pad16(A.acc_cap * acc_elem) + pad16(A.ent_cap * nc * acc_elem) + A.ent_cap * 16;
+    int tb = 0;
+    for (int s = 0; s < MAX_SUB; ++s) tb = std::max(tb, ke->table_bytes[s]);
+    int max_smem = 0;
+    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+    const int budget = max_smem - 1024;  // static shared (mbarrier) headroom
+    int chunk = std::min(64, std::max(1, (budget - fixed) / std::max(tb, 1)));
+    if (const char* s = std::getenv("FE_GB300_CHUNK")) chunk = std::max(1, std::min(chunk, std::atoi(s)));
+    if (fixed + tb > budget) return set_error(h, FE_ERR_UNSUPPORTED, "tile does not fit in shared memory");
+    chunk = std::min(chunk, std::max(1, h->plan.max_wave_cells));
+    A.chunk_cells = chunk;
+    const int smem = fixed + chunk * tb;
+    if ((e = cudaFuncSetAttribute(ke->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
+        return cuda_fail(h, e, "cudaFuncSetAttribute");
+    // status
+    DevStatus init{~0ull, ~0ull, 0u, 0u};
+    *h->status_h = init;
+    if ((e = cudaMemcpyAsync(h->status_d, h->status_h, sizeof(DevStatus), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return cuda_fail(h, e, "status reset");
+    A.status = h->status_d;
+    const void* shp = fp64 ? (const void*)h->shape_d : (const void*)h->shape_f;
+    int sb = h->shape_bytes[pi], o1 = h->shape_off1[pi], o2 = h->shape_off2[pi];
+    void* args[] = {(void*)&A, (void*)&shp, (void*)&sb, (void*)&o1, (void*)&o2};
+    if (A.n_tiles > 0) {
+        e = cudaLaunchKernel(ke->fn, dim3((unsigned)A.n_tiles), dim3(THREADS), args, (size_t)smem, st);
+        if (e != cudaSuccess) return cuda_fail(h, e, "tile kernel launch");
+    }
+    if ((e = cudaMemcpyAsync(h->status_h, h->status_d, sizeof(DevStatus), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return cuda_fail(h, e, "status read");
+    if (do_k && !nz_dev && (e = cudaMemcpyAsync(nzval, h->nz_stage, hp.nnz * 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return cuda_fail(h, e, "copy nzval back");
+    if (do_f && !f_dev && (e = cudaMemcpyAsync(f, h->f_stage, hp.ndofs * 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return cuda_fail(h, e, "copy f back");
+    h->last_stream = st;
+    h->pending = 1;
+    const bool host_out = (do_k && !nz_dev) || (do_f && !f_dev);
+    if ((p->flags & FE_ASYNC) && !host_out) return FE_OK;
+    return fe_sync(h);
+}
+
+int fe_last_error(const fe_handle* h, fe_error_info* out) {
+    if (!out) return FE_ERR_ARG;
+    *out = h ? h->last : g_create_error;
+    return FE_OK;
+}
+
+int fe_get_info(const fe_handle* h, fe_info* out) {
+    if (!h || !out) return FE_ERR_ARG;
+    out->n_cells = h->hp.n_cells;
+    out->ndofs = h->hp.ndofs;
+    out->nnz = h->hp.nnz;
+    out->n_tiles = (int64_t)h->plan.tiles.size();
+    out->n_cell_visits = h->plan.visits;
+    out->n_items = (int64_t)h->plan.items.size();
+    out->flagged_cells = h->flagged;
+    out->device_bytes = h->device_bytes;
+    out->create_seconds = h->create_seconds;
+    return FE_OK;
+}
+
+int fe_get_index_map(const fe_handle* h, int64_t cell, int64_t* positions) {
+    if (!h || !positions) return FE_ERR_ARG;
+    const HostProblem& hp = h->hp;
+    if (cell < 1 || cell > hp.n_cells) return FE_ERR_BOUNDS;
+    const int s = hp.cell_sub[cell - 1];
+    if (s < 0) return FE_ERR_ARG;
+    const HostSub& hs = hp.subs[s];
+    const int64_t k = hp.cell_local[cell - 1];
+    const int nc = hp.nc, nb = hs.nb, ld = nb * nc;
+    for (int j = 0; j < nb; ++j) {
+        const int64_t n = hs.ents[k * nb + j];
+        const int64_t c0 = hp.colptr[nc * n] - 1;
+        const int64_t L = hp.colptr[nc * n + 1] - hp.colptr[nc * n];
+        for (int i = 0; i < nb; ++i) {
+            const size_t t = ((size_t)k * nb + j) * nb + i;
+            const int r = hs.wide_rank ? (hs.rank16[t] == 0xFFFF ? -1 : hs.rank16[t]) : (hs.rank8[t] == 255 ? -1 : hs.rank8[t]);
+            for (int b = 0; b < nc; ++b)
+                for (int a = 0; a < nc; ++a)
+                    positions[(int64_t)(j * nc + b) * ld + (i * nc + a)] = r < 0 ? 0 : c0 + b * L + (int64_t)nc * r + a + 1;
+        }
+    }
+    return FE_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,34 @@
+// instantiate.cuh -- helpers to list tile-kernel instantiations in the registry.
+#pragma once
+#include <type_traits>
+
+#include "registry.h"
+#include "tile_kernel.cuh"
+
+namespace fe {
+
+template <int K, int Q, int PH, typename R>
+constexpr int table_bytes_or0() {
+    if constexpr (K < 0) return 0;
+    else return cell_table_bytes<K, Q, PH, R>();
+}
+
+template <int K0, int Q0, int K1, int Q1, int K2, int Q2, int PH, typename R>
+KernelEntry make_entry() {
+    KernelEntry e;
+    e.kind[0] = K0; e.kind[1] = K1; e.kind[2] = K2;
+    e.nq[0] = Q0; e.nq[1] = Q1; e.nq[2] = Q2;
+    e.phys = PH;
+    e.fp64 = std::is_same<R, double>::value ? 1 : 0;
+    e.fn = (const void*)&tile_kernel<K0, Q0, K1, Q1, K2, Q2, PH, R>;
+    e.table_bytes[0] = table_bytes_or0<K0, Q0, PH, R>();
+    e.table_bytes[1] = table_bytes_or0<K1, Q1, PH, R>();
+    e.table_bytes[2] = table_bytes_or0<K2, Q2, PH, R>();
+    return e;
+}
+
+#define FE_ONE(K, Q, PH)                                                  \
+    out.push_back(make_entry<K, Q, -1, 0, -1, 0, PH, float>());           \
+    out.push_back(make_entry<K, Q, -1, 0, -1, 0, PH, double>());
+
+}  // namespace fe

@@ -1,0 +1,14 @@
+// kernels_elastic.cu -- small-strain isotropic elasticity instantiations,
+// threaded_assembly.jl:105-132 (per-cell modulus: topology_optimization.jl:347-383).
+#include "instantiate.cuh"
+
+namespace fe {
+void register_elastic(std::vector<KernelEntry>& out) {
+    FE_ONE(KIND_HEX8, 8, PHYS_ELASTIC)
+    FE_ONE(KIND_HEX27, 27, PHYS_ELASTIC)
+    FE_ONE(KIND_TET4, 1, PHYS_ELASTIC)
+    FE_ONE(KIND_TET4, 4, PHYS_ELASTIC)
+    FE_ONE(KIND_WEDGE6, 5, PHYS_ELASTIC)
+    FE_ONE(KIND_QUAD4, 4, PHYS_ELASTIC)
+}
+}  // namespace fe

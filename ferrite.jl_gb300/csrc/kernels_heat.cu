@@ -1,0 +1,16 @@
+// kernels_heat.cu -- scalar heat (Poisson) instantiations, heat_equation.jl:143-164.
+#include "instantiate.cuh"
+
+namespace fe {
+void register_heat(std::vector<KernelEntry>& out) {
+    FE_ONE(KIND_QUAD4, 4, PHYS_HEAT)
+    FE_ONE(KIND_QUAD4, 1, PHYS_HEAT)
+    FE_ONE(KIND_TRI3, 1, PHYS_HEAT)
+    FE_ONE(KIND_TRI3, 3, PHYS_HEAT)
+    FE_ONE(KIND_QUAD9, 9, PHYS_HEAT)
+    FE_ONE(KIND_HEX8, 8, PHYS_HEAT)
+    FE_ONE(KIND_TET4, 1, PHYS_HEAT)
+    FE_ONE(KIND_TET4, 4, PHYS_HEAT)
+    FE_ONE(KIND_HEX27, 27, PHYS_HEAT)
+}
+}  // namespace fe

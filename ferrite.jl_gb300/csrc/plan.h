@@ -1,0 +1,79 @@
+// plan.h -- host-side set-up of a handle: validation of the Ferrite arrays, the compact
+// element-to-nzval index map, and the owner-tile plan the kernels execute.
+#pragma once
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "common.h"
+#include "ferrite_gb300.h"
+
+namespace fe {
+
+struct HostSub {
+    int32_t cell_type = 0, ip_order = 0, kind = 0;
+    int32_t nb = 0, ng = 0, nq = 0, dim = 0, nc = 0;
+    int64_t n_cells = 0;
+    std::vector<int32_t> cellid;   // 0-based Ferrite cell ids
+    std::vector<int32_t> conn;     // [n][ng] 0-based node ids
+    std::vector<int32_t> ents;     // [n][nb] entity ids
+    std::vector<uint8_t> rank8;    // [n][nb][nb] (j-major), 255 = missing
+    std::vector<uint16_t> rank16;  // used when a rank exceeds 254; 65535 = missing
+    bool wide_rank = false;
+    std::vector<double> w, N, dN, dM;  // reference tables (row-major, as passed)
+};
+
+struct HostProblem {
+    int32_t dim = 0;
+    int64_t n_nodes = 0, n_cells = 0, ndofs = 0, nnz = 0;
+    int32_t nc = 0;            // components per entity
+    int64_t n_ent = 0;         // ndofs / nc
+    std::vector<double> nodes; // [n_nodes][dim]
+    std::vector<HostSub> subs;
+    std::vector<int64_t> colptr;          // 1-based copy
+    std::vector<int64_t> cell_dofs_off;   // per Ferrite cell: 1-based offset (for index-map queries)
+    std::vector<int32_t> cell_sub;        // per Ferrite cell: subdomain or -1
+    std::vector<int32_t> cell_local;      // per Ferrite cell: index within its subdomain
+    std::vector<int64_t> cell_dofs;       // copy of dh.cell_dofs (for index-map queries / errors)
+};
+
+struct PlanOptions {
+    int32_t acc_cap = 12288;  // accumulator entries per tile (8 bytes each)
+    int32_t ent_cap = 4096;   // entities per tile
+    double fill = 0.70;       // target mean accumulator fill of a tile
+};
+
+struct Plan {
+    std::vector<TileDesc> tiles;
+    std::vector<RangeDesc> ranges;
+    std::vector<WaveDesc> waves;
+    std::vector<int32_t> wave_cells;
+    std::vector<int32_t> wave_cell_items;
+    std::vector<uint32_t> items;
+    int32_t max_acc = 0, max_ent = 0, max_wave_cells = 0;
+    int64_t visits = 0;
+};
+
+struct Error {
+    int code = 0;
+    std::string msg;
+    int64_t cell = 0, row = 0, col = 0;
+};
+
+int kind_of(int32_t cell_type, int32_t ip_order, int32_t& nb, int32_t& ng, int32_t& rdim);
+
+// Fill HostProblem from the C-ABI descriptors; validates sizes, bounds and the dof layout,
+// builds the entity ranks (the index map). Returns an FE_* code.
+struct CreateInput {
+    const fe_grid_desc* grid;
+    int32_t n_sub;
+    const fe_subdomain_desc* subs;
+    const fe_dof_desc* dofs;
+    const fe_csc_desc* pattern;
+};
+int build_problem(const CreateInput& in, HostProblem& hp, Error& err);
+int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error& err);
+int check_plan(const HostProblem& hp, const Plan& plan, Error& err);
+
+}  // namespace fe

@@ -1,0 +1,22 @@
+// registry.h -- the compiled tile-kernel instantiations and how the host picks one.
+#pragma once
+#include <vector>
+
+#include "common.h"
+
+namespace fe {
+
+struct KernelEntry {
+    int kind[MAX_SUB];   // -1 = unused slot
+    int nq[MAX_SUB];
+    int phys;            // 1 heat, 2 elastic, 3 neo-hooke
+    int fp64;            // 0 = mixed precision, 1 = FP64
+    const void* fn;      // __global__ tile_kernel<...>
+    int table_bytes[MAX_SUB];  // chunk-table bytes per cell of each slot
+};
+
+void register_heat(std::vector<KernelEntry>& out);
+void register_elastic(std::vector<KernelEntry>& out);
+void register_neo(std::vector<KernelEntry>& out);
+
+}  // namespace fe

@@ -1,0 +1,193 @@
+/*
+ * ferrite_gb300.h -- C ABI of the GB300 (sm_103a) finite-element assembly engine.
+ *
+ * One call replaces Ferrite.jl's assembly hot path
+ *
+ *     assembler = start_assemble(K, f)                     # src/assembler.jl:287-291
+ *     for cell in CellIterator(dh)                         # src/iterators.jl:248-274, 389-396
+ *         reinit!(cellvalues, cell)                        # src/FEValues/CellValues.jl:122-140
+ *         element_routine!(Ke, fe, cellvalues, ...)        # user code (tutorials)
+ *         assemble!(assembler, celldofs(cell), Ke, fe)     # src/assembler.jl:322-457
+ *     end
+ *
+ * with fe_assemble(), which fills the nzval of the same SparseMatrixCSC (pattern from
+ * allocate_matrix(dh), src/Dofs/sparsity_pattern.jl:628-645) and the right-hand side f.
+ * Everything a caller passes is plain memory in Ferrite's own layout: node coordinates as
+ * Vector{Node{dim,Float64}} (AoS), connectivity / cell_dofs / cell_dofs_offset / colptr /
+ * rowval as 1-based Int64, nzval and f as Float64. A Julia binding is in
+ * ferrite.jl_gb300/julia/FerriteGB300.jl.
+ *
+ * Every function returns an int status (FE_OK = 0). Device-side failures never trap: the
+ * kernels record the first failure in a status word and fe_assemble() returns its code;
+ * fe_last_error() gives the details (cell id, detJ, row/col), mirroring the exceptions of
+ * the reference (throw_detJ_not_pos, src/FEValues/common_values.jl:5; the missing pattern
+ * entry error, src/assembler.jl:459-467; BoundsError / ArgumentError for bad input).
+ *
+ * Threading: like Ferrite's assemblers (src/assembler.jl:273-276) a handle is not
+ * re-entrant; concurrent assemblies need separate handles. Work is queued on the stream
+ * passed in fe_assemble_params.
+ */
+#ifndef FERRITE_GB300_H
+#define FERRITE_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FE_ABI_VERSION 1
+
+/* status codes */
+#define FE_OK 0
+#define FE_ERR_ARG 1             /* inconsistent sizes / bad argument (ArgumentError, DimensionMismatch) */
+#define FE_ERR_BOUNDS 2          /* node / dof / cell index out of range (BoundsError) */
+#define FE_ERR_DETJ 3            /* detJ <= 0 in some cell (throw_detJ_not_pos) */
+#define FE_ERR_PATTERN_MISSING 4 /* a non-zero value has no entry in the pattern (assembler.jl:459-467) */
+#define FE_ERR_UNSUPPORTED 5     /* element / dof layout this engine does not implement */
+#define FE_ERR_CUDA 6            /* CUDA runtime error */
+#define FE_ERR_OOM 7             /* device memory exhausted */
+#define FE_ERR_STATE 8           /* call out of order (e.g. replay without capture) */
+
+/* cell types (Ferrite: Triangle, Quadrilateral, Tetrahedron, Hexahedron, Wedge) */
+#define FE_TRIANGLE 1
+#define FE_QUADRILATERAL 2
+#define FE_TETRAHEDRON 3
+#define FE_HEXAHEDRON 4
+#define FE_WEDGE 5
+
+/* element routines: the ones of Ferrite's tutorials */
+#define FE_HEAT 1           /* Ke += k (gradN_i . gradN_j) dOmega, fe += s N_i dOmega (heat_equation.jl:143-164) */
+#define FE_LINEAR_ELASTIC 2 /* Ke += (eps_i : C : eps_j) dOmega, fe += (N_i . b) dOmega (threaded_assembly.jl:105-132) */
+#define FE_NEO_HOOKE 3      /* tangent and residual of hyperelasticity.jl:157-276 (cell part) */
+
+/* precision */
+#define FE_PREC_MIXED 0 /* FP32 element math, FP64 Jacobians for flagged cells, FP64-class accumulation */
+#define FE_PREC_FP64 1  /* the plain FP64 drop-in: all math and accumulation in FP64 */
+
+/* fe_assemble flags */
+#define FE_FILLZERO 1u /* zero K and f first, as start_assemble(K, f; fillzero=true) */
+#define FE_NO_K 2u     /* skip K (nzval may be NULL) */
+#define FE_NO_F 4u     /* skip f (f may be NULL) */
+#define FE_ASYNC 8u    /* do not wait for the kernels; read the status later with fe_sync() */
+
+typedef struct fe_handle fe_handle;
+
+typedef struct {
+    int32_t dim;          /* spatial dimension, 2 or 3 */
+    int64_t n_nodes;
+    const double* nodes;  /* [n_nodes][dim]: the memory of grid.nodes */
+    int64_t n_cells;      /* getncells(grid) */
+} fe_grid_desc;
+
+/* One SubDofHandler with its CellValues (dh.subdofhandlers[k], src/Dofs/DofHandler.jl:15-26). */
+typedef struct {
+    int32_t cell_type;    /* FE_* cell type of every cell in the set */
+    int32_t ip_order;     /* Lagrange order of the field interpolation (1 or 2) */
+    int32_t n_components; /* 1 = scalar field, dim = vectorized ip^dim (interleaved dofs) */
+    int32_t n_qp;         /* quadrature points of the CellValues' QuadratureRule */
+    const double* qr_weights; /* [n_qp] getweights(qr) */
+    const double* N;      /* [n_qp][n_base] reference shape values (FunctionValues.Nxi of the scalar ip) */
+    const double* dNdxi;  /* [n_qp][n_base][rdim] reference gradients (FunctionValues.dNdxi) */
+    const double* M;      /* [n_qp][n_geo] geometric shape values (GeometryMapping.M) */
+    const double* dMdxi;  /* [n_qp][n_geo][rdim] (GeometryMapping.dMdxi) */
+    int64_t n_cells;
+    const int64_t* cellset;    /* [n_cells] 1-based cell ids, ascending (sdh.cellset) */
+    const int64_t* cell_nodes; /* [n_cells][n_geo] 1-based node ids of those cells (grid.cells[cellset]) */
+} fe_subdomain_desc;
+
+typedef struct {
+    int64_t ndofs;
+    const int64_t* cell_dofs;        /* dh.cell_dofs */
+    const int64_t* cell_dofs_offset; /* [n_cells] 1-based, dh.cell_dofs_offset */
+} fe_dof_desc;
+
+typedef struct {
+    int64_t n;             /* number of columns (= ndofs) */
+    int64_t nnz;
+    const int64_t* colptr; /* [n+1] 1-based (K.colptr) */
+    const int64_t* rowval; /* [nnz] 1-based (K.rowval); read during fe_create only */
+} fe_csc_desc;
+
+typedef struct {
+    int32_t physics;       /* FE_HEAT, FE_LINEAR_ELASTIC, FE_NEO_HOOKE */
+    int32_t precision;     /* FE_PREC_MIXED or FE_PREC_FP64 */
+    uint32_t flags;        /* FE_FILLZERO | FE_NO_K | FE_NO_F | FE_ASYNC */
+    double p0, p1;         /* heat: k, source; elastic: E, nu; neo-hooke: mu, lambda */
+    double body[3];        /* body force b (elastic, neo-hooke) */
+    const double* cell_scale; /* optional [n_cells]: per-cell factor on the material (E_e/E, rho^p), by cell id - 1 */
+    const double* u;       /* neo-hooke: current solution [ndofs] */
+    double cond_threshold; /* mixed precision: cells whose Jacobian condition number exceeds this
+                              are recomputed in FP64 (<= 0: default 64) */
+    void* stream;          /* cudaStream_t; NULL = legacy default stream */
+} fe_assemble_params;
+
+typedef struct {
+    int32_t code;
+    int64_t cell;          /* 1-based cell id (DETJ, PATTERN_MISSING) */
+    double detJ;           /* DETJ */
+    int64_t row, col;      /* PATTERN_MISSING, 1-based */
+    char message[256];
+} fe_error_info;
+
+typedef struct {
+    int64_t n_cells, ndofs, nnz;
+    int64_t n_tiles;        /* owner tiles the nzval is partitioned into */
+    int64_t n_cell_visits;  /* (cell, tile) pairs: geometry evaluations per assembly */
+    int64_t n_items;        /* (cell, owned base function) work items per assembly */
+    int64_t flagged_cells;  /* cells recomputed with FP64 Jacobians in the last mixed assembly */
+    int64_t device_bytes;   /* device memory held by the handle */
+    double create_seconds;  /* host time spent in fe_create */
+} fe_info;
+
+/*
+ * fe_create: validate and upload the problem, build the element-to-nzval index map
+ * (bit-exact with Ferrite's assembler, src/assembler.jl:376-457) and the owner tiles.
+ * Replaces the host side of start_assemble(K, f) (src/assembler.jl:287-291) together with
+ * the device adaptation of grid/dh (ext/FerriteKAExt/adapt_core.jl:6-31,
+ * ext/FerriteCudaExt.jl:44-48, 95-101). rowval is only read here.
+ */
+int fe_create(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain_desc* subdomains,
+              const fe_dof_desc* dofs, const fe_csc_desc* pattern, fe_handle** out);
+
+/*
+ * fe_assemble: the whole `start_assemble` + `for cell in CellIterator(dh) ... assemble!`
+ * loop (docs/src/literate-tutorials/heat_equation.jl:186-206,
+ * docs/src/literate-howto/threaded_assembly.jl:232-265, ext/FerriteCudaExt.jl:50-93).
+ * nzval [nnz] and f [ndofs] may be device or host pointers (host: staged through the
+ * handle's device buffers). Same for params->u and params->cell_scale.
+ */
+int fe_assemble(fe_handle* h, const fe_assemble_params* params, double* nzval, double* f);
+
+/* Wait for queued work of the handle and return the status of the last assembly. */
+int fe_sync(fe_handle* h);
+
+/* Details of the last failure (src/FEValues/common_values.jl:5, src/assembler.jl:459-467).
+ * h == NULL: the last failed fe_create() of the calling thread. */
+int fe_last_error(const fe_handle* h, fe_error_info* out);
+
+int fe_get_info(const fe_handle* h, fe_info* out);
+
+/*
+ * fe_get_index_map: 1-based nzval positions of the element entries of one cell, in the
+ * layout of Ke (positions[J*ld + I] for Ke[I, J], ld = ndofs_per_cell); 0 where the
+ * pattern has no entry. Equals the positions Ferrite's merge walk
+ * (src/assembler.jl:376-457) visits for celldofs(cell).
+ */
+int fe_get_index_map(const fe_handle* h, int64_t cell, int64_t* positions);
+
+/*
+ * fe_plan_dry_run: everything fe_create does on the host (validation, index map, owner
+ * tiles and their bounds check) without touching a device; fills n_tiles, n_cell_visits,
+ * n_items. Lets a caller check its arrays, or size a problem, on a machine without a GPU.
+ */
+int fe_plan_dry_run(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain_desc* subdomains,
+                    const fe_dof_desc* dofs, const fe_csc_desc* pattern, fe_info* out);
+
+void fe_destroy(fe_handle* h);
+
+int fe_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,52 @@
+"""CPU unit test of the compensated-pair -> FP64 rounding used by the kernels' write-out
+(ferrite.jl_gb300/csrc/dfloat.h): bitwise equal to the correctly rounded double sum."""
+import os
+import subprocess
+import tempfile
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+SRC = r'''
+#include "dfloat.h"
+#include <cstdio>
+#include <cmath>
+#include <random>
+#include <cstring>
+int main() {
+    std::mt19937_64 g(12345);
+    std::uniform_real_distribution<double> U(-1.0, 1.0);
+    long bad = 0, n = 0;
+    for (int it = 0; it < 2000000; ++it) {
+        const int ex = (int)(g() % 60) - 30;
+        float hi = (float)std::ldexp(U(g), ex);
+        if (it % 7 == 0) hi = std::ldexp(1.0f, ex) * ((it & 8) ? -1.f : 1.f);  // powers of two
+        const int k = (int)(g() % 40);
+        float lo = (float)std::ldexp(U(g), ex - 24 - k);
+        if (it % 11 == 0) lo = 0.0f;
+        if (it % 13 == 0) lo = std::ldexp(std::nextafter(std::ldexp(hi, 0), 2 * hi) - hi, -1);  // exact half ulp
+        const double want = (double)hi + (double)lo;
+        const double got = fe::pair_to_double(hi, lo);
+        uint64_t a, b;
+        std::memcpy(&a, &want, 8);
+        std::memcpy(&b, &got, 8);
+        ++n;
+        if (a != b) {
+            if (bad < 5) std::printf("hi=%a lo=%a want=%a got=%a\n", hi, lo, want, got);
+            ++bad;
+        }
+    }
+    std::printf("%ld %ld\n", bad, n);
+    return bad != 0;
+}
+'''
+
+
+def test_pair_to_double_bitwise():
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "t.cpp")
+        exe = os.path.join(d, "t")
+        open(src, "w").write(SRC)
+        subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "ferrite.jl_gb300", "csrc"), src, "-o", exe],
+                       check=True)
+        r = subprocess.run([exe], capture_output=True, text=True)
+        assert r.returncode == 0, r.stdout + r.stderr

@@ -1,0 +1,209 @@
+"""GPU parity: the CUDA engine (through the C ABI) against the CPU oracle.
+
+Tolerances (relative Frobenius norm of nzval and f against the FP64 oracle):
+  * FE_PREC_FP64 (the plain FP64 drop-in):      <= 1e-12
+  * FE_PREC_MIXED (FP32 element math, FP64-class accumulation): <= 1e-6
+Sparsity structure and index maps are bit-exact. Runs are bitwise reproducible.
+"""
+import numpy as np
+import pytest
+
+from helpers import make_handle, rel_fro
+
+pytestmark = pytest.mark.gpu
+
+TOL_FP64 = 1e-12
+TOL_MIXED = 1e-6
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+@pytest.fixture(scope="module")
+def built(fg, torch_cuda):
+    fg.build()
+    return fg
+
+
+def check(fg, O, prob, element_args, oracle_args, precisions=(0, 1), tol=None):
+    h = make_handle(fg, O, prob)
+    nz_ref, f_ref = prob.assemble(**oracle_args)
+    out = {}
+    for prec in precisions:
+        nz = np.full(prob.nnz, np.nan)
+        f = np.full(prob.ndofs, np.nan)
+        h.assemble(nz, f, precision=prec, **element_args)
+        t = (tol or {}).get(prec, TOL_FP64 if prec == 1 else TOL_MIXED)
+        assert rel_fro(nz, nz_ref) <= t, (prec, rel_fro(nz, nz_ref))
+        assert rel_fro(f, f_ref) <= t, (prec, rel_fro(f, f_ref))
+        out[prec] = (nz, f)
+    return h, out
+
+
+def test_heat_quad_100x100(built, oracle):
+    """2D Poisson as in the heat tutorial, 100x100 Q1, 2x2 Gauss (10,201 dofs)."""
+    fg, O = built, oracle
+    prob = O.box_problem(O.QUADRILATERAL, (100, 100), qr_order=2)
+    check(fg, O, prob, dict(physics=fg.HEAT, p0=1.0, p1=1.0), dict(physics=O.HEAT, p0=1.0, p1=1.0))
+
+
+def test_elastic_hex_q1_perturbed(built, oracle):
+    fg, O = built, oracle
+    prob = O.box_problem(O.HEXAHEDRON, (9, 7, 6), [0, 0, 0], [1, 1, 1], ip_order=1, ncomp=3, qr_order=2,
+                         perturb=0.2, seed=11)
+    E, nu, b = 200e3, 0.3, (0.0, 0.0, -1.0)
+    check(fg, O, prob, dict(physics=fg.LINEAR_ELASTIC, p0=E, p1=nu, body=b),
+          dict(physics=O.LINEAR_ELASTIC, p0=E, p1=nu, body=b))
+
+
+def test_elastic_hex_q2_cell_modulus(built, oracle):
+    fg, O = built, oracle
+    prob = O.box_problem(O.HEXAHEDRON, (4, 3, 3), [0, 0, 0], [1, 1, 1], ip_order=2, ncomp=3, qr_order=3,
+                         perturb=0.2, seed=12)
+    rng = np.random.default_rng(5)
+    scale = rng.lognormal(0.0, 0.5, prob.n_cells)
+    E, nu = 200e3, 0.3
+    check(fg, O, prob, dict(physics=fg.LINEAR_ELASTIC, p0=E, p1=nu, cell_scale=scale),
+          dict(physics=O.LINEAR_ELASTIC, p0=E, p1=nu, cell_scale=scale))
+
+
+@pytest.mark.parametrize("ct,qo", [(3, 1), (5, 2), (4, 2)])
+def test_neo_hooke_single_type(built, oracle, ct, qo):
+    fg, O = built, oracle
+    prob = O.box_problem(ct, (4, 3, 3), [0, 0, 0], [1, 1, 1], ip_order=1, ncomp=3, qr_order=qo, perturb=0.15, seed=3)
+    rng = np.random.default_rng(1)
+    u = 0.05 * rng.uniform(-1, 1, prob.ndofs)
+    check(fg, O, prob, dict(physics=fg.NEO_HOOKE, p0=1.0, p1=10.0, u=u, body=(0, -0.5, 0)),
+          dict(physics=O.NEO_HOOKE, p0=1.0, p1=10.0, u=u, body=(0, -0.5, 0)), tol={0: 2e-6})
+
+
+def mixed_problem(O, nel=(6, 3, 3), seed=4):
+    """Three x-slabs over one node grid: hexahedra, then tetrahedra (6 per cube), then
+    wedges (2 per cube), one SubDofHandler each, dofs shared through the vertex dict."""
+    nodes, hexes = O.generate_grid(O.HEXAHEDRON, nel, [0, 0, 0], [2, 1, 1])
+    nodes = O.perturb_interior(nodes, nel, 0.15, seed, [0, 0, 0], [2, 1, 1])
+    nx = nel[0]
+    i = (np.arange(len(hexes)) % nx)
+    third = nx // 3
+    T = [[1, 2, 4, 8], [1, 5, 2, 8], [2, 3, 4, 8], [2, 7, 3, 8], [2, 5, 6, 8], [2, 6, 7, 8]]
+    W = [[1, 2, 4, 5, 6, 8], [2, 3, 4, 6, 7, 8]]
+    cells, types = [], []
+    for c in np.where(i < third)[0]:
+        cells.append(hexes[c]); types.append(O.HEXAHEDRON)
+    for c in np.where((i >= third) & (i < 2 * third))[0]:
+        for t in T:
+            cells.append(hexes[c][np.array(t) - 1]); types.append(O.TETRAHEDRON)
+    for c in np.where(i >= 2 * third)[0]:
+        for t in W:
+            cells.append(hexes[c][np.array(t) - 1]); types.append(O.WEDGE)
+    types = np.array(types, np.int32)
+    off = np.zeros(len(cells) + 1, np.int64)
+    off[1:] = np.cumsum([len(c) for c in cells])
+    flat = np.concatenate(cells).astype(np.int64)
+    subs = []
+    for ct, qo in [(O.HEXAHEDRON, 2), (O.TETRAHEDRON, 1), (O.WEDGE, 2)]:
+        subs.append(O.Subdomain(np.where(types == ct)[0] + 1, 1, 3, qo))
+    prob = O.Problem(nodes, types, off, flat, subs).close().allocate_matrix()
+    return prob
+
+
+def test_neo_hooke_mixed_cells(built, oracle):
+    fg, O = built, oracle
+    prob = mixed_problem(O)
+    rng = np.random.default_rng(2)
+    u = 0.05 * rng.uniform(-1, 1, prob.ndofs)
+    check(fg, O, prob, dict(physics=fg.NEO_HOOKE, p0=1.0, p1=10.0, u=u),
+          dict(physics=O.NEO_HOOKE, p0=1.0, p1=10.0, u=u), tol={0: 2e-6})
+
+
+def test_index_map_bit_exact(built, oracle):
+    fg, O = built, oracle
+    for ct, ip, nc, nel in [(4, 1, 3, (3, 3, 2)), (4, 2, 3, (2, 2, 2)), (2, 1, 1, (4, 3)), (3, 1, 3, (2, 2, 1))]:
+        prob = O.box_problem(ct, nel, ip_order=ip, ncomp=nc, qr_order=2)
+        h = make_handle(fg, O, prob)
+        for c in range(prob.n_cells):
+            ld = prob.ndofs_per_cell(0)
+            assert np.array_equal(h.index_map(c + 1, ld), prob.index_map(c))
+
+
+def test_bitwise_reproducible_and_device_pointers(built, oracle, torch_cuda):
+    fg, O, torch = built, oracle, torch_cuda
+    prob = O.box_problem(O.HEXAHEDRON, (8, 8, 8), [0, 0, 0], [1, 1, 1], ip_order=1, ncomp=3, perturb=0.2, seed=9)
+    h = make_handle(fg, O, prob)
+    args = dict(physics=fg.LINEAR_ELASTIC, p0=200e3, p1=0.3, body=(0, 0, -1))
+    a = [np.zeros(prob.nnz), np.zeros(prob.ndofs)]
+    b = [np.zeros(prob.nnz), np.zeros(prob.ndofs)]
+    h.assemble(*a, **args)
+    h.assemble(*b, **args)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    nz_d = torch.zeros(prob.nnz, dtype=torch.float64, device="cuda")
+    f_d = torch.zeros(prob.ndofs, dtype=torch.float64, device="cuda")
+    h.assemble(nz_d, f_d, stream=torch.cuda.current_stream(), **args)
+    torch.cuda.synchronize()
+    assert np.array_equal(nz_d.cpu().numpy(), a[0]) and np.array_equal(f_d.cpu().numpy(), a[1])
+
+
+def test_fillzero_false_accumulates(built, oracle):
+    fg, O = built, oracle
+    prob = O.box_problem(O.QUADRILATERAL, (7, 5), qr_order=2)
+    h = make_handle(fg, O, prob)
+    nz1, f1 = np.zeros(prob.nnz), np.zeros(prob.ndofs)
+    h.assemble(nz1, f1, physics=fg.HEAT, p0=1.0, p1=1.0, precision=fg.PREC_FP64)
+    nz2, f2 = nz1.copy(), f1.copy()
+    h.assemble(nz2, f2, physics=fg.HEAT, p0=1.0, p1=1.0, precision=fg.PREC_FP64, fillzero=False)
+    assert np.allclose(nz2, 2 * nz1, rtol=1e-14, atol=0) and np.allclose(f2, 2 * f1, rtol=1e-14)
+
+
+def test_detj_error(built, oracle):
+    fg, O = built, oracle
+    nodes, cells = O.generate_grid(O.QUADRILATERAL, (3, 3))
+    cells[4] = cells[4][[1, 0, 3, 2]]
+    prob = O.Problem.single(O.QUADRILATERAL, nodes, cells).close().allocate_matrix()
+    h = make_handle(fg, O, prob)
+    for prec in (0, 1):
+        with pytest.raises(fg.FEError) as ei:
+            h.assemble(np.zeros(prob.nnz), np.zeros(prob.ndofs), physics=fg.HEAT, p0=1.0, p1=1.0, precision=prec)
+        assert ei.value.name == "DETJ" and ei.value.cell == 5 and ei.value.detJ < 0
+
+
+def test_pattern_missing_error(built, oracle):
+    fg, O = built, oracle
+    prob = O.box_problem(O.QUADRILATERAL, (3, 3), qr_order=2)
+    col = 5
+    a, b = prob.colptr[col] - 1, prob.colptr[col + 1] - 1
+    rows = prob.rowval[a:b]
+    drop = a + int(np.where(rows != col + 1)[0][0])
+    dropped_row = int(prob.rowval[drop])
+    prob.rowval = np.delete(prob.rowval, drop)
+    prob.colptr = prob.colptr.copy()
+    prob.colptr[col + 1:] -= 1
+    h = make_handle(fg, O, prob)
+    with pytest.raises(fg.FEError) as ei:
+        h.assemble(np.zeros(prob.nnz), np.zeros(prob.ndofs), physics=fg.HEAT, p0=1.0, p1=1.0)
+    assert ei.value.name == "PATTERN_MISSING"
+    assert (ei.value.row, ei.value.col) in [(dropped_row, col + 1)]
+    # zero contributions to the missing entry are fine (k = 0)
+    h.assemble(np.zeros(prob.nnz), np.zeros(prob.ndofs), physics=fg.HEAT, p0=0.0, p1=1.0)
+
+
+def test_distorted_cells_use_fp64_jacobians(built, oracle):
+    """A layer of thin cells (aspect ratio ~2500, detJ > 0, Jacobian condition number far
+    above the threshold) is recomputed with FP64 Jacobians; the mixed result stays within
+    tolerance."""
+    fg, O = built, oracle
+    nel = (4, 4, 4)
+    nodes, cells = O.generate_grid(O.HEXAHEDRON, nel, [0, 0, 0], [1, 1, 1])
+    nodes = nodes.copy()
+    nodes[np.abs(nodes[:, 2] - 0.25) < 1e-12, 2] = 1e-4
+    prob = O.Problem.single(O.HEXAHEDRON, nodes, cells, 1, 3, 2).close().allocate_matrix()
+    h = make_handle(fg, O, prob)
+    nz_ref, f_ref = prob.assemble(O.LINEAR_ELASTIC, 200e3, 0.3, body=[0, 0, -1])
+    nz, f = np.zeros(prob.nnz), np.zeros(prob.ndofs)
+    h.assemble(nz, f, physics=fg.LINEAR_ELASTIC, p0=200e3, p1=0.3, body=(0, 0, -1), cond_threshold=16.0)
+    assert h.info()["flagged_cells"] == 16
+    assert rel_fro(nz, nz_ref) <= TOL_MIXED and rel_fro(f, f_ref) <= TOL_MIXED

@@ -1,0 +1,57 @@
+"""Host-side set-up on the CPU (no GPU): input validation, the index map and the owner-tile
+plan with its bounds check, through fe_plan_dry_run."""
+import numpy as np
+import pytest
+
+from helpers import subdomain_specs
+
+
+def dry(fg, O, prob):
+    return fg.plan_dry_run(prob.nodes, subdomain_specs(fg, O, prob), prob.cell_dofs, prob.cell_dofs_offset,
+                           prob.ndofs, prob.colptr, prob.rowval, prob.n_cells)
+
+
+@pytest.mark.parametrize("ct,nel,ip,nc,qo", [(2, (13, 9), 1, 1, 2), (2, (6, 5), 1, 2, 2), (4, (7, 6, 5), 1, 3, 2),
+                                             (4, (4, 3, 3), 2, 3, 3), (3, (4, 4, 3), 1, 3, 1), (5, (4, 3, 3), 1, 3, 2),
+                                             (1, (5, 4), 1, 1, 1)])
+def test_dry_run_plans(fg, oracle, ct, nel, ip, nc, qo):
+    fg.build()
+    O = oracle
+    prob = O.box_problem(ct, nel, ip_order=ip, ncomp=nc, qr_order=qo, perturb=0.1, seed=1)
+    info = dry(fg, O, prob)
+    assert info["ndofs"] == prob.ndofs and info["nnz"] == prob.nnz
+    assert info["n_items"] == prob.n_cells * O.nbase(ct, ip)
+    assert info["n_cell_visits"] >= prob.n_cells and info["n_tiles"] >= 1
+
+
+def test_dry_run_mixed(fg, oracle):
+    from test_gpu_parity import mixed_problem
+    fg.build()
+    prob = mixed_problem(oracle)
+    info = dry(fg, oracle, prob)
+    assert info["n_cells"] == prob.n_cells
+
+
+def test_rejects_bad_input(fg, oracle):
+    fg.build()
+    O = oracle
+    prob = O.box_problem(O.HEXAHEDRON, (2, 2, 2), ip_order=1, ncomp=3)
+    cells = prob.cell_nodes.copy()
+    prob.cell_nodes = cells
+    bad = prob.cell_nodes.copy()
+    bad[5] = prob.nodes.shape[0] + 7
+    prob.cell_nodes = bad
+    with pytest.raises(fg.FEError) as ei:
+        dry(fg, O, prob)
+    assert ei.value.name == "BOUNDS"
+    prob.cell_nodes = cells
+    # a pattern that does not couple all components of an entity is not supported
+    rowval = prob.rowval.copy()
+    colptr = prob.colptr.copy()
+    drop = int(colptr[0] - 1) + 1  # second row entry of column 1 (same entity, component 2)
+    prob.rowval = np.delete(rowval, drop)
+    prob.colptr = colptr.copy()
+    prob.colptr[1:] -= 1
+    with pytest.raises(fg.FEError) as ei:
+        dry(fg, O, prob)
+    assert ei.value.name == "UNSUPPORTED"
