@@ -36,10 +36,10 @@ ERROR_NAMES = {0: "OK", 1: "ARG", 2: "BOUNDS", 3: "DETJ", 4: "PATTERN_MISSING", 
 TRIANGLE, QUADRILATERAL, TETRAHEDRON, HEXAHEDRON, WEDGE = 1, 2, 3, 4, 5
 HEAT, LINEAR_ELASTIC, NEO_HOOKE = 1, 2, 3
 PREC_MIXED, PREC_FP64 = 0, 1
-FILLZERO, NO_K, NO_F, ASYNC = 1, 2, 4, 8
+FILLZERO, NO_K, NO_F, ASYNC, PROFILE = 1, 2, 4, 8, 16
 
 EXPORTED = ["fe_abi_version", "fe_create", "fe_assemble", "fe_sync", "fe_last_error", "fe_get_info",
-            "fe_get_index_map", "fe_plan_dry_run", "fe_destroy"]
+            "fe_get_index_map", "fe_plan_dry_run", "fe_distribute_dofs", "fe_sparsity_pattern", "fe_kernel_time", "fe_destroy"]
 
 i64p = ctypes.POINTER(ctypes.c_int64)
 f64p = ctypes.POINTER(ctypes.c_double)
@@ -111,6 +111,11 @@ def lib():
         L.fe_get_index_map.argtypes = [ctypes.c_void_p, ctypes.c_int64, i64p]
         L.fe_plan_dry_run.argtypes = [ctypes.POINTER(GridDesc), ctypes.c_int32, ctypes.POINTER(SubdomainDesc),
                                       ctypes.POINTER(DofDesc), ctypes.POINTER(CscDesc), ctypes.POINTER(Info)]
+        L.fe_distribute_dofs.argtypes = [ctypes.POINTER(GridDesc), ctypes.c_int32, ctypes.POINTER(SubdomainDesc),
+                                         i64p, i64p, i64p]
+        L.fe_sparsity_pattern.argtypes = [ctypes.POINTER(GridDesc), ctypes.c_int32, ctypes.POINTER(SubdomainDesc),
+                                          ctypes.POINTER(DofDesc), i64p, i64p, i64p]
+        L.fe_kernel_time.argtypes = [ctypes.c_void_p, f64p, i64p]
         L.fe_destroy.argtypes = [ctypes.c_void_p]
         L.fe_destroy.restype = None
         _lib = L
@@ -258,7 +263,7 @@ class Handle:
 
     def assemble(self, nzval, f, physics: int, p0: float, p1: float, body=(0.0, 0.0, 0.0), cell_scale=None, u=None,
                  precision: int = PREC_MIXED, fillzero: bool = True, stream=None, sync: bool = True,
-                 cond_threshold: float = 0.0):
+                 cond_threshold: float = 0.0, profile: bool = False):
         """One fe_assemble call. ``stream`` is a torch.cuda.Stream, a raw handle or None."""
         p = AssembleParams()
         p.physics, p.precision = physics, precision
@@ -269,6 +274,8 @@ class Handle:
             flags |= NO_F
         if not sync:
             flags |= ASYNC
+        if profile:
+            flags |= PROFILE
         p.flags = flags
         p.p0, p.p1 = float(p0), float(p1)
         for k in range(3):
@@ -288,6 +295,14 @@ class Handle:
         rc = lib().fe_sync(self._h)
         if rc != FE_OK:
             self._raise(rc)
+
+    def kernel_time(self):
+        """(total ms, launches) of the FE_PROFILE launches since the last call."""
+        ms, n = ctypes.c_double(), ctypes.c_int64()
+        rc = lib().fe_kernel_time(self._h, ctypes.byref(ms), ctypes.byref(n))
+        if rc != FE_OK:
+            self._raise(rc)
+        return ms.value, n.value
 
     def info(self) -> dict:
         i = Info()

@@ -68,6 +68,8 @@ struct fe_handle {
     cudaStream_t last_stream = 0;
     int pending = 0;  // an FE_ASYNC assembly whose status has not been read
     fe_error_info last{};
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_events;  // recorded, unread
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_pool;    // free for reuse
     int64_t flagged = 0;
     double create_seconds = 0;
     int device = 0;
@@ -90,6 +92,8 @@ struct fe_handle {
         return e;
     }
     ~fe_handle() {
+        for (auto& e : prof_events) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+        for (auto& e : prof_pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
         for (void* p : allocs) cudaFree(p);
         if (status_h) cudaFreeHost(status_h);
     }
@@ -480,9 +484,24 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
     const void* shp = fp64 ? (const void*)h->shape_d : (const void*)h->shape_f;
     int sb = h->shape_bytes[pi], o1 = h->shape_off1[pi], o2 = h->shape_off2[pi];
     void* args[] = {(void*)&A, (void*)&shp, (void*)&sb, (void*)&o1, (void*)&o2};
+    std::pair<cudaEvent_t, cudaEvent_t> ev{nullptr, nullptr};
+    const bool prof = (p->flags & FE_PROFILE) != 0;
+    if (prof) {
+        if (!h->prof_pool.empty()) {
+            ev = h->prof_pool.back();
+            h->prof_pool.pop_back();
+        } else if ((e = cudaEventCreate(&ev.first)) != cudaSuccess || (e = cudaEventCreate(&ev.second)) != cudaSuccess) {
+            return cuda_fail(h, e, "cudaEventCreate");
+        }
+        cudaEventRecord(ev.first, st);
+    }
     if (A.n_tiles > 0) {
         e = cudaLaunchKernel(ke->fn, dim3((unsigned)A.n_tiles), dim3(THREADS), args, (size_t)smem, st);
         if (e != cudaSuccess) return cuda_fail(h, e, "tile kernel launch");
+    }
+    if (prof) {
+        cudaEventRecord(ev.second, st);
+        h->prof_events.push_back(ev);
     }
     if ((e = cudaMemcpyAsync(h->status_h, h->status_d, sizeof(DevStatus), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
         return cuda_fail(h, e, "status read");
@@ -495,6 +514,23 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
     const bool host_out = (do_k && !nz_dev) || (do_f && !f_dev);
     if ((p->flags & FE_ASYNC) && !host_out) return FE_OK;
     return fe_sync(h);
+}
+
+int fe_kernel_time(fe_handle* h, double* total_ms, int64_t* launches) {
+    if (!h || !total_ms || !launches) return FE_ERR_ARG;
+    double sum = 0;
+    for (auto& ev : h->prof_events) {
+        cudaError_t e = cudaEventSynchronize(ev.second);
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaEventSynchronize");
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ev.first, ev.second);
+        sum += ms;
+        h->prof_pool.push_back(ev);
+    }
+    *launches = (int64_t)h->prof_events.size();
+    *total_ms = sum;
+    h->prof_events.clear();
+    return FE_OK;
 }
 
 int fe_last_error(const fe_handle* h, fe_error_info* out) {

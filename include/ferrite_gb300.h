@@ -69,6 +69,7 @@ extern "C" {
 #define FE_NO_K 2u     /* skip K (nzval may be NULL) */
 #define FE_NO_F 4u     /* skip f (f may be NULL) */
 #define FE_ASYNC 8u    /* do not wait for the kernels; read the status later with fe_sync() */
+#define FE_PROFILE 16u /* bracket the assembly kernel with CUDA events; read with fe_kernel_time() */
 
 typedef struct fe_handle fe_handle;
 
@@ -182,6 +183,26 @@ int fe_get_index_map(const fe_handle* h, int64_t cell, int64_t* positions);
  */
 int fe_plan_dry_run(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain_desc* subdomains,
                     const fe_dof_desc* dofs, const fe_csc_desc* pattern, fe_info* out);
+
+/*
+ * Host-side set-up in Ferrite's numbering, for callers that do not hold Ferrite objects.
+ * Only cell_type, ip_order, n_components, n_cells, cellset and cell_nodes of the subdomain
+ * descriptors are read (the reference tables may be NULL).
+ *
+ * fe_distribute_dofs: close!(dh) for one field (src/Dofs/DofHandler.jl:493-794). cell_dofs
+ * must hold sum(n_cells * n_base * n_components) entries; cell_dofs_offset [grid->n_cells]
+ * receives 1-based offsets (0 for cells in no subdomain).
+ * fe_sparsity_pattern: allocate_matrix(dh) (src/Dofs/sparsity_pattern.jl:223-253, 549):
+ * call with rowval == NULL to get colptr [ndofs+1] and nnz, then again with rowval [nnz].
+ */
+int fe_distribute_dofs(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain_desc* subdomains,
+                       int64_t* cell_dofs, int64_t* cell_dofs_offset, int64_t* ndofs);
+int fe_sparsity_pattern(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain_desc* subdomains,
+                        const fe_dof_desc* dofs, int64_t* colptr, int64_t* rowval, int64_t* nnz);
+
+/* Device time of the assembly kernels launched with FE_PROFILE since the last call: waits
+ * for them, returns the summed milliseconds and the number of launches, then resets. */
+int fe_kernel_time(fe_handle* h, double* total_ms, int64_t* launches);
 
 void fe_destroy(fe_handle* h);
 

@@ -1,0 +1,62 @@
+"""The library's own host-side set-up (numpy grids, native dof distribution and pattern,
+reference tables) against the oracle's restatement of Ferrite: bit-exact dofs and patterns."""
+import importlib
+
+import numpy as np
+import pytest
+
+
+@pytest.fixture(scope="module")
+def host(fg):
+    fg.build()
+    return importlib.import_module("ferrite_gb300.host")
+
+
+CASES = [(2, (7, 5), 1, 1), (2, (4, 3), 2, 1), (1, (5, 4), 1, 1), (4, (5, 4, 3), 1, 3), (4, (3, 3, 2), 2, 3),
+         (3, (3, 2, 2), 1, 3), (5, (3, 3, 2), 1, 3), (4, (4, 4, 4), 1, 1)]
+
+
+@pytest.mark.parametrize("ct,nel,ip,nc", CASES)
+def test_grid_dofs_pattern_match_oracle(host, oracle, ct, nel, ip, nc):
+    O = oracle
+    d = len(nel)
+    left, right = np.zeros(d), np.arange(1, d + 1, dtype=float)
+    g = host.generate_grid(ct, nel, left, right)
+    nodes, cells = O.generate_grid(ct, nel, left, right)
+    assert np.array_equal(g.nodes, nodes)
+    assert np.array_equal(g.cells, cells)
+    dh = host.DofHandler.from_grid(g, ip, nc).close()
+    prob = O.Problem.single(ct, nodes, cells, ip, nc, 2).close().allocate_matrix()
+    assert dh.ndofs == prob.ndofs
+    assert np.array_equal(dh.cell_dofs, prob.cell_dofs)
+    assert np.array_equal(dh.cell_dofs_offset, prob.cell_dofs_offset)
+    colptr, rowval = dh.allocate_matrix()
+    assert np.array_equal(colptr, prob.colptr) and np.array_equal(rowval, prob.rowval)
+
+
+def test_mixed_subdomains_match_oracle(host, oracle):
+    from test_gpu_parity import mixed_problem
+    prob = mixed_problem(oracle)
+    dh = host.DofHandler(prob.nodes, prob.n_cells)
+    for sd in prob.subdomains:
+        ct = int(prob.cell_types[sd.cellset[0] - 1])
+        ng = oracle.nbase(ct, 1)
+        cn = prob.cell_nodes[prob.cell_nodes_offset[sd.cellset - 1][:, None] + np.arange(ng)[None, :]]
+        dh.add(ct, cn, sd.cellset, 1, 3)
+    dh.close()
+    assert np.array_equal(dh.cell_dofs, prob.cell_dofs)
+    colptr, rowval = dh.allocate_matrix()
+    assert np.array_equal(colptr, prob.colptr) and np.array_equal(rowval, prob.rowval)
+
+
+@pytest.mark.parametrize("ct,orders", [(2, [1, 2, 3]), (4, [1, 2, 3]), (3, [1, 2]), (5, [1, 2]), (1, [1, 2])])
+def test_tables_match_oracle(host, oracle, ct, orders):
+    for qo in orders:
+        w, p = host.quadrature_rule(ct, qo)
+        w2, p2 = oracle.quadrature(ct, qo)
+        assert np.allclose(w, w2, rtol=0, atol=2e-16) and np.allclose(p, p2, rtol=0, atol=2e-16)
+        ips = [1, 2] if ct in (2, 4) else [1]
+        for ip in ips:
+            N, dN = host.shape_tables(ct, ip, p2)
+            N2, dN2 = oracle.shape_tables(ct, ip, p2)
+            assert np.allclose(N, N2, atol=1e-15) and np.allclose(dN, dN2, atol=1e-15)
