@@ -125,7 +125,7 @@ int finish_status(fe_handle* h) {
     const DevStatus& st = *h->status_h;
     h->flagged = st.flagged;
     h->pending = 0;
-    if (st.timeout) return set_error(h, FE_ERR_CUDA, "a tile timed out waiting for its reference-table copy");
+    if (st.timeout) return set_error(h, FE_ERR_CUDA, "a tile gave up: table copy timed out or shared memory too small");
     if (st.detj_key != ~0ull) {
         const int64_t cell = (int64_t)(st.detj_key >> 32) + 1;
         uint32_t bits = (uint32_t)(st.detj_key & 0xFFFFFFFFu);
@@ -167,7 +167,7 @@ int fe_create(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain
     int rc = build_problem(in, h->hp, err);
     if (rc == FE_OK) {
         PlanOptions opt;
-        if (const char* s = std::getenv("FE_GB300_ACC_CAP")) opt.acc_cap = std::atoi(s);
+        if (const char* s = std::getenv("FE_GB300_STAGE_CAP")) opt.stage_cap = std::atoi(s);
         rc = build_plan(h->hp, opt, h->plan, err);
         if (rc == FE_OK) rc = check_plan(h->hp, h->plan, err);
     }
@@ -241,13 +241,26 @@ int fe_create(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain
         CK(h->upload(&ents, hs.ents.data(), hs.ents.size()));
         sd.cellid = cid; sd.conn = conn; sd.ents = ents;
         sd.rank8 = nullptr; sd.rank16 = nullptr;
+        // device layout: one row per (cell, row function i), the ranks of all column functions
+        // j, padded to 8 bytes, so a lane fetches its row with 8-byte loads
+        const int nbq = hs.nb;
         if (hs.wide_rank) {
+            const int rs = 4 * ((nbq + 3) / 4);
+            std::vector<uint16_t> t((size_t)hs.n_cells * nbq * rs, 0xFFFF);
+            for (int64_t k = 0; k < hs.n_cells; ++k)
+                for (int j = 0; j < nbq; ++j)
+                    for (int i = 0; i < nbq; ++i) t[((size_t)k * nbq + i) * rs + j] = hs.rank16[((size_t)k * nbq + j) * nbq + i];
             uint16_t* r;
-            CK(h->upload(&r, hs.rank16.data(), hs.rank16.size()));
+            CK(h->upload(&r, t.data(), t.size()));
             sd.rank16 = r;
         } else {
+            const int rs = 8 * ((nbq + 7) / 8);
+            std::vector<uint8_t> t((size_t)hs.n_cells * nbq * rs, 0xFF);
+            for (int64_t k = 0; k < hs.n_cells; ++k)
+                for (int j = 0; j < nbq; ++j)
+                    for (int i = 0; i < nbq; ++i) t[((size_t)k * nbq + i) * rs + j] = hs.rank8[((size_t)k * nbq + j) * nbq + i];
             uint8_t* r;
-            CK(h->upload(&r, hs.rank8.data(), hs.rank8.size()));
+            CK(h->upload(&r, t.data(), t.size()));
             sd.rank8 = r;
         }
         // reference tables: w, N, dN (physical layout [q][i][c]), dM; padded blocks
@@ -285,17 +298,30 @@ int fe_create(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain
     h->shape_off1[0] = offs_f[1]; h->shape_off2[0] = offs_f[2];
     h->shape_off1[1] = offs_d[1]; h->shape_off2[1] = offs_d[2];
     // plan
-    TileDesc* tiles; RangeDesc* ranges; WaveDesc* waves; int32_t *wc, *wci; uint32_t* items;
+    TileDesc* tiles; RangeDesc* ranges; SegDesc* segs; EntMeta* emeta; int32_t *eids, *tc, *ci; uint32_t* items;
     CK(h->upload(&tiles, pl.tiles.data(), pl.tiles.size()));
     CK(h->upload(&ranges, pl.ranges.data(), pl.ranges.size()));
-    CK(h->upload(&waves, pl.waves.data(), pl.waves.size()));
-    CK(h->upload(&wc, pl.wave_cells.data(), pl.wave_cells.size()));
-    CK(h->upload(&wci, pl.wave_cell_items.data(), pl.wave_cell_items.size()));
+    CK(h->upload(&segs, pl.segs.data(), pl.segs.size()));
+    CK(h->upload(&emeta, pl.emeta.data(), pl.emeta.size()));
+    CK(h->upload(&eids, pl.eids.data(), pl.eids.size()));
+    CK(h->upload(&tc, pl.tile_cells.data(), pl.tile_cells.size()));
+    CK(h->upload(&ci, pl.cell_items.data(), pl.cell_items.size()));
     CK(h->upload(&items, pl.items.data(), pl.items.size()));
-    A.tiles = tiles; A.ranges = ranges; A.waves = waves;
-    A.wave_cells = wc; A.wave_cell_items = wci; A.items = items;
-    A.acc_cap = std::max(pl.max_acc, 1);
+    uint32_t* red;
+    CK(h->upload(&red, pl.red_list.data(), pl.red_list.size()));
+    A.red_list = red;
+    A.tiles = tiles; A.ranges = ranges; A.segs = segs; A.emeta = emeta; A.eids = eids;
+    A.tile_cells = tc; A.cell_items = ci; A.items = items;
+    A.nb_max = pl.nb_max;
+    A.bs = (hp.nc * hp.nc + 1) & ~1;
+    A.stage_cap = std::max(pl.max_stage, 1);
+    A.map_cap = std::max(pl.max_map, 16);
     A.ent_cap = std::max(pl.max_ent, 1);
+    A.red_cap = std::max(pl.max_red, 1);
+    A.cells_cap = std::max(pl.max_cells, 1);
+    A.items_cap = std::max(pl.max_items, 1);
+    A.ng_max = 1;
+    for (const HostSub& hs2 : hp.subs) A.ng_max = std::max(A.ng_max, hs2.ng);
     CK(h->alloc(&h->status_d, 1));
     CK(cudaMallocHost((void**)&h->status_h, sizeof(DevStatus)));
 #undef CK
@@ -314,7 +340,7 @@ int fe_plan_dry_run(const fe_grid_desc* grid, int32_t n_subdomains, const fe_sub
     CreateInput in{grid, n_subdomains, subdomains, dofs, pattern};
     int rc = build_problem(in, hp, err);
     PlanOptions opt;
-    if (const char* s = std::getenv("FE_GB300_ACC_CAP")) opt.acc_cap = std::atoi(s);
+    if (const char* s = std::getenv("FE_GB300_STAGE_CAP")) opt.stage_cap = std::atoi(s);
     if (rc == FE_OK) rc = build_plan(hp, opt, pl, err);
     if (rc == FE_OK) rc = check_plan(hp, pl, err);
     if (rc != FE_OK) {
@@ -458,21 +484,25 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
         int rc = stage_input(p->u, hp.ndofs, &h->u_stage, &h->u_f, &ph.u_d, &ph.u_f);
         if (rc) return rc;
     }
-    // shared memory: shape tables + accumulators + entity table + chunk tables
+    // shared memory: shape tables + staging + map + entity table + chunk tables
     const int pi = fp64 ? 1 : 0;
-    const int acc_elem = 8;
-    const int fixed = pad16(h->shape_bytes[pi]) + pad16(A.acc_cap * acc_elem) + pad16(A.ent_cap * nc * acc_elem) + A.ent_cap * 16;
-    int tb = 0;
-    for (int s = 0; s < MAX_SUB; ++s) tb = std::max(tb, ke->table_bytes[s]);
+    const int real = fp64 ? 8 : 4;
+    const int fixed = smem_layout(A, h->shape_bytes[pi], real).chunk;
     int max_smem = 0;
     cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
     const int budget = max_smem - 1024;  // static shared (mbarrier) headroom
-    int chunk = std::min(64, std::max(1, (budget - fixed) / std::max(tb, 1)));
-    if (const char* s = std::getenv("FE_GB300_CHUNK")) chunk = std::max(1, std::min(chunk, std::atoi(s)));
+    // cell-table buffers: one per lane group; fewer groups when the tables are large
+    int tb = 0;
+    for (int s = 0; s < MAX_SUB; ++s) {
+        A.groups[s] = 0;
+        if (ke->kind[s] < 0) continue;
+        const int room = (budget - fixed) / std::max(ke->table_bytes[s], 1);
+        A.groups[s] = std::max(1, std::min(ke->groups[s], room));
+        tb = std::max(tb, ke->table_bytes[s] * A.groups[s]);
+    }
     if (fixed + tb > budget) return set_error(h, FE_ERR_UNSUPPORTED, "tile does not fit in shared memory");
-    chunk = std::min(chunk, std::max(1, h->plan.max_wave_cells));
-    A.chunk_cells = chunk;
-    const int smem = fixed + chunk * tb;
+    A.chunk_bytes = tb;
+    const int smem = fixed + tb;
     if ((e = cudaFuncSetAttribute(ke->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
         return cuda_fail(h, e, "cudaFuncSetAttribute");
     // status

@@ -2,6 +2,7 @@
 // rounding to FP64 with integer operations (GB300's FP64 pipe is a small fraction of its
 // FP32 rate, so the write-out path avoids it). Host+device so it is unit-tested on the CPU.
 #pragma once
+#include <math.h>
 #include <stdint.h>
 #include <string.h>
 
@@ -69,6 +70,56 @@ __host__ __device__ __forceinline__ double pair_to_double(float hi, float lo) {
     }
     D = same ? D + delta : D - delta;
     return u2d(D);
+}
+
+__host__ __device__ __forceinline__ float u2f(uint32_t u) {
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(u);
+#else
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+#endif
+}
+__host__ __device__ __forceinline__ int f2i_rn(float x) {
+#ifdef __CUDA_ARCH__
+    return __float2int_rn(x);
+#else
+    return (int)lrintf(x);
+#endif
+}
+
+// Same result as pair_to_double, fewer operations: the low word, scaled by a power of two
+// to units of the double's last place, is rounded to an integer (ties to even) and added to
+// the bit pattern of double(s). |e| <= ulp_f(s)/2 keeps that integer within +-2^28.
+__host__ __device__ __forceinline__ double pair_to_double_fast(float hi, float lo) {
+    const float s = hi + lo;
+    const float e = lo - (s - hi);
+    const uint32_t bs = f2u(s);
+    const uint32_t mag = bs & 0x7FFFFFFFu;
+    const uint32_t es = mag >> 23;
+    if (es < 60u || es == 0xFFu) return pair_to_double(hi, lo);  // tiny / subnormal / inf: rare
+    // double(s): same sign, exponent rebased by 1023-127, mantissa shifted up by 29
+    const uint32_t dhi = (bs & 0x80000000u) | ((mag >> 3) + (896u << 20));
+    const uint32_t dlo = mag << 29;
+    // e in units of ulp(double(s)) = 2^(es-127-52); one more bit if s is a power of two and
+    // e points into the binade below
+    const bool down = ((bs ^ f2u(e)) & 0x80000000u) && (mag & 0x7FFFFFu) == 0u;
+    const uint32_t sc = (uint32_t)(306 - (int)es + (down ? 1 : 0)) << 23;
+    const int d = f2i_rn(e * u2f(sc));
+    const uint64_t D = (((uint64_t)dhi << 32) | dlo) + (uint64_t)(int64_t)((bs & 0x80000000u) ? -d : d);
+    return u2d(D);
+}
+
+// Exact FP32 -> FP64 with integer operations (no FP64 pipe) for normal numbers.
+__host__ __device__ __forceinline__ double float_to_double(float v) {
+    const uint32_t b = f2u(v);
+    const uint32_t mag = b & 0x7FFFFFFFu;
+    const uint32_t ex = mag >> 23;
+    if (mag == 0u) return (b >> 31) ? -0.0 : 0.0;
+    if (ex == 0u || ex == 0xFFu) return (double)v;
+    const uint32_t dhi = (b & 0x80000000u) | ((mag >> 3) + (896u << 20));
+    return u2d(((uint64_t)dhi << 32) | (uint64_t)(mag << 29));
 }
 
 }  // namespace fe

@@ -12,6 +12,11 @@ constexpr int table_bytes_or0() {
     if constexpr (K < 0) return 0;
     else return cell_table_bytes<K, Q, PH, R>();
 }
+template <int K>
+constexpr int groups_or0() {
+    if constexpr (K < 0) return 0;
+    else return THREADS / ElemT<K>::GS;
+}
 
 template <int K0, int Q0, int K1, int Q1, int K2, int Q2, int PH, typename R>
 KernelEntry make_entry() {
@@ -24,6 +29,9 @@ KernelEntry make_entry() {
     e.table_bytes[0] = table_bytes_or0<K0, Q0, PH, R>();
     e.table_bytes[1] = table_bytes_or0<K1, Q1, PH, R>();
     e.table_bytes[2] = table_bytes_or0<K2, Q2, PH, R>();
+    e.groups[0] = groups_or0<K0>();
+    e.groups[1] = groups_or0<K1>();
+    e.groups[2] = groups_or0<K2>();
     return e;
 }
 

@@ -218,15 +218,24 @@ int build_problem(const CreateInput& in, HostProblem& hp, Error& err) {
 
 // ---------------------------------------------------------------------------------------
 // Owner tiles
+//
+// Entities are bucketed by position into compact tiles (a handful of contiguous id runs
+// each). A tile lists every cell touching one of its entities; for every (cell, owned base
+// function j) an item carries k, the position of the cell among the cells of entity(j) in
+// cell order. The kernel writes each contribution to its own staging slot (entity, k, i) and
+// the reduce step sums the slots of an entry in k order: the reference's cell order.
 // ---------------------------------------------------------------------------------------
 int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error& err) {
     const int nc = hp.nc;
     const int64_t n_ent = hp.n_ent;
     const int dim = hp.dim;
     const int64_t* cp = hp.colptr.data();
-    // entity "positions": mean of the centroids of the cells that carry the entity
+    int nb_max = 0;
+    for (const HostSub& hs : hp.subs) nb_max = std::max(nb_max, hs.nb);
+    plan.nb_max = nb_max;
+    // entity "positions" (mean of incident cell centroids) and incident cell counts
     std::vector<double> pos(n_ent * 3, 0.0);
-    std::vector<int32_t> cnt(n_ent, 0);
+    std::vector<int32_t> kcount(n_ent, 0);
     for (const HostSub& hs : hp.subs) {
         for (int64_t k = 0; k < hs.n_cells; ++k) {
             double cen[3] = {0, 0, 0};
@@ -236,21 +245,33 @@ int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error&
             for (int i = 0; i < hs.nb; ++i) {
                 const int64_t n = hs.ents[k * hs.nb + i];
                 for (int x = 0; x < dim; ++x) pos[n * 3 + x] += cen[x];
-                cnt[n]++;
+                kcount[n]++;
             }
         }
     }
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
     for (int64_t n = 0; n < n_ent; ++n) {
-        if (!cnt[n]) continue;
+        if (kcount[n] > MAX_ENT_CELLS) return fail(err, FE_ERR_UNSUPPORTED, "a dof entity belongs to more than 63 cells");
+        if (!kcount[n]) continue;
         for (int x = 0; x < dim; ++x) {
-            pos[n * 3 + x] /= cnt[n];
+            pos[n * 3 + x] /= kcount[n];
             lo[x] = std::min(lo[x], pos[n * 3 + x]);
             hi[x] = std::max(hi[x], pos[n * 3 + x]);
         }
     }
-    const double avg_entries = (double)hp.nnz / (double)n_ent;
-    const double target_ent = std::max(1.0, opt.acc_cap * opt.fill / avg_entries);
+    auto nnb_of = [&](int64_t n) { return (int64_t)((cp[nc * n + 1] - cp[nc * n]) / nc); };
+    const int bs = (nc * nc + 1) & ~1;
+    auto stage_of = [&](int64_t n) { return ((int64_t)kcount[n] * (nb_max * bs + nc) + 1) & ~1ll; };
+    auto map_of = [&](int64_t n) { return nnb_of(n) * kcount[n]; };
+    // target entities per tile from the staging capacity
+    double avg_stage = 0;
+    for (int64_t n = 0; n < n_ent; ++n) avg_stage += (double)stage_of(n);
+    avg_stage = std::max(1.0, avg_stage / (double)n_ent);
+    double avg_nnb = 0;
+    for (int64_t n = 0; n < n_ent; ++n) avg_nnb += (double)nnb_of(n);
+    avg_nnb = std::max(1.0, avg_nnb / (double)n_ent);
+    const double target_ent = std::max(1.0, std::min({0.85 * opt.stage_cap / avg_stage, 0.85 * opt.ent_cap,
+                                                       0.85 * opt.red_cap / avg_nnb}));
     const double n_tiles_target = std::max(1.0, (double)n_ent / target_ent);
     double ext[3] = {1, 1, 1}, vol = 1;
     for (int x = 0; x < dim; ++x) {
@@ -261,12 +282,11 @@ int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error&
     int64_t nt[3] = {1, 1, 1};
     for (int x = 0; x < dim; ++x) nt[x] = std::max<int64_t>(1, (int64_t)std::llround(ext[x] / side));
     const int64_t nbk = nt[0] * nt[1] * nt[2];
-    // bucket per entity; entities with no cell go to bucket 0
     std::vector<int64_t> bstart(nbk + 1, 0);
     std::vector<int64_t> bucket(n_ent);
     for (int64_t n = 0; n < n_ent; ++n) {
         int64_t id[3] = {0, 0, 0};
-        if (cnt[n])
+        if (kcount[n])
             for (int x = 0; x < dim; ++x) {
                 int64_t t = (int64_t)((pos[n * 3 + x] - lo[x]) / ext[x] * nt[x]);
                 id[x] = std::min(std::max<int64_t>(t, 0), nt[x] - 1);
@@ -280,26 +300,31 @@ int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error&
         std::vector<int64_t> cur(bstart.begin(), bstart.end() - 1);
         for (int64_t n = 0; n < n_ent; ++n) order[cur[bucket[n]]++] = (int32_t)n;
     }
-    // tiles: split buckets by accumulator / entity capacity, then runs of consecutive ids
+    // tiles: split buckets by capacity; runs of consecutive ids become ranges
     std::vector<int32_t> tile_of(n_ent), tile_local(n_ent);
     plan.tiles.clear();
     plan.ranges.clear();
-    auto ent_nz = [&](int64_t n) { return (int64_t)(cp[nc * n + nc] - cp[nc * n]); };
+    plan.emeta.clear();
+    plan.eids.clear();
     for (int64_t b = 0; b < nbk; ++b) {
         int64_t k = bstart[b];
         while (k < bstart[b + 1]) {
             TileDesc t{};
             t.range_begin = (int32_t)plan.ranges.size();
-            int64_t acc = 0;
+            t.ent_begin = (int32_t)plan.emeta.size();
+            int64_t stage = 0, map = 0, red = 0;
             int32_t ne = 0;
             const int32_t tid = (int32_t)plan.tiles.size();
             while (k < bstart[b + 1]) {
                 const int64_t n = order[k];
-                const int64_t z = ent_nz(n);
-                if (z > opt.acc_cap) return fail(err, FE_ERR_UNSUPPORTED, "a dof entity's columns exceed the tile accumulator");
-                if (ne && (acc + z > opt.acc_cap || ne + 1 > opt.ent_cap || ne + 1 > MAX_TILE_ENTS)) break;
-                if (!plan.ranges.empty() && (int32_t)plan.ranges.size() > t.range_begin &&
-                    plan.ranges.back().ent0 + plan.ranges.back().n_ent == n) {
+                const int64_t st = stage_of(n), mp = (map_of(n) + 3) & ~3ll;
+                if (st > opt.stage_cap || mp > opt.map_cap)
+                    return fail(err, FE_ERR_UNSUPPORTED, "a dof entity's contributions exceed the tile staging capacity");
+                if (ne && (stage + st > opt.stage_cap || map + mp > opt.map_cap || ne + 1 > opt.ent_cap ||
+                           ne + 1 > MAX_TILE_ENTS || red + nnb_of(n) > opt.red_cap))
+                    break;
+                const int64_t z = (int64_t)(cp[nc * n + nc] - cp[nc * n]);
+                if ((int32_t)plan.ranges.size() > t.range_begin && plan.ranges.back().ent0 + plan.ranges.back().n_ent == n) {
                     plan.ranges.back().n_ent++;
                     plan.ranges.back().nz_len += (int32_t)z;
                 } else {
@@ -307,22 +332,34 @@ int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error&
                     r.nz0 = cp[nc * n] - 1;
                     r.ent0 = (int32_t)n;
                     r.n_ent = 1;
-                    r.acc_base = (int32_t)acc;
                     r.nz_len = (int32_t)z;
                     plan.ranges.push_back(r);
                 }
+                EntMeta m;
+                m.x = (int32_t)stage;
+                m.y = (int32_t)map;
+                m.z = (int32_t)red;
+                m.w = kcount[n] | (int32_t)(nnb_of(n) << 8);
+                plan.emeta.push_back(m);
+                plan.eids.push_back((int32_t)n);
                 tile_of[n] = tid;
                 tile_local[n] = ne;
-                acc += z;
+                stage += st;
+                map += mp;
+                red += nnb_of(n);
                 ++ne;
                 ++k;
             }
             t.range_end = (int32_t)plan.ranges.size();
             t.n_ent = ne;
-            t.acc_len = (int32_t)acc;
+            t.n_red = (int32_t)red;
+            t.stage_vals = (int32_t)stage;
+            t.map_bytes = (int32_t)map;
             plan.tiles.push_back(t);
-            plan.max_acc = std::max(plan.max_acc, t.acc_len);
+            plan.max_stage = std::max(plan.max_stage, t.stage_vals);
+            plan.max_map = std::max(plan.max_map, t.map_bytes);
             plan.max_ent = std::max(plan.max_ent, ne);
+            plan.max_red = std::max(plan.max_red, t.n_red);
         }
     }
     const int64_t n_tiles = (int64_t)plan.tiles.size();
@@ -343,189 +380,216 @@ int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error&
                 }
         }
     }
-    // per tile: cells, greedy coloring on owned entities, waves, items
     struct TileOut {
-        std::vector<WaveDesc> waves;
+        std::vector<SegDesc> segs;
         std::vector<int32_t> cells, cell_items;
-        std::vector<uint32_t> items;
-        int64_t visits = 0;
-        int32_t max_wave = 0;
+        std::vector<uint32_t> items, red;
         int status = 0;
     };
     std::vector<TileOut> outs(n_tiles);
-    int status = FE_OK;
 #pragma omp parallel
     {
-        std::vector<uint64_t> emask;
-        std::vector<int32_t> ccolor;
-        std::vector<int64_t> cfirst;  // first triple of each distinct cell
+        std::vector<int32_t> kc;
 #pragma omp for schedule(dynamic, 16)
         for (int64_t t = 0; t < n_tiles; ++t) {
             TileOut& o = outs[t];
-            const int64_t a = tstart[t], b = tstart[t + 1];
-            emask.assign(plan.tiles[t].n_ent, 0);
-            cfirst.clear();
-            for (int64_t k = a; k < b; ++k)
-                if (k == a || (trip[k] >> 8) != (trip[k - 1] >> 8)) cfirst.push_back(k);
-            const int64_t ncell = (int64_t)cfirst.size();
-            cfirst.push_back(b);
-            o.visits = ncell;
-            ccolor.assign(ncell, 0);
-            int max_color = 0;
-            for (int64_t c = 0; c < ncell; ++c) {
-                uint64_t used = 0;
-                for (int64_t k = cfirst[c]; k < cfirst[c + 1]; ++k) {
-                    const int s = (int)(trip[k] >> 40);
-                    const int64_t cell = (int64_t)((trip[k] >> 8) & 0xFFFFFFFFull);
-                    const int j = (int)(trip[k] & 0xFF);
-                    const HostSub& hs = hp.subs[s];
-                    used |= emask[tile_local[hs.ents[cell * hs.nb + j]]];
-                }
-                if (~used == 0) { o.status = FE_ERR_UNSUPPORTED; break; }
-                const int col = __builtin_ctzll(~used);
-                ccolor[c] = col;
-                max_color = std::max(max_color, col + 1);
-                for (int64_t k = cfirst[c]; k < cfirst[c + 1]; ++k) {
-                    const int s = (int)(trip[k] >> 40);
-                    const int64_t cell = (int64_t)((trip[k] >> 8) & 0xFFFFFFFFull);
-                    const int j = (int)(trip[k] & 0xFF);
-                    const HostSub& hs = hp.subs[s];
-                    emask[tile_local[hs.ents[cell * hs.nb + j]]] |= 1ull << col;
-                }
-            }
-            if (o.status) continue;
-            // waves: by color, then by subdomain; at most MAX_WAVE_CELLS cells each
-            for (int col = 0; col < max_color; ++col)
-                for (size_t s = 0; s < hp.subs.size(); ++s) {
-                    WaveDesc w{};
-                    bool open = false;
-                    for (int64_t c = 0; c < ncell; ++c) {
-                        if (ccolor[c] != col || (int)(trip[cfirst[c]] >> 40) != (int)s) continue;
-                        if (open && w.n_cells == MAX_WAVE_CELLS) {
-                            o.waves.push_back(w);
-                            open = false;
-                        }
-                        if (!open) {
-                            w = WaveDesc{};
-                            w.sub = (int32_t)s;
-                            w.cell_begin = (int32_t)o.cells.size();
-                            w.item_begin = (int32_t)o.items.size();
-                            open = true;
-                        }
-                        const int64_t cell = (int64_t)((trip[cfirst[c]] >> 8) & 0xFFFFFFFFull);
-                        const HostSub& hs = hp.subs[s];
-                        const uint32_t slot = (uint32_t)w.n_cells;
-                        o.cells.push_back((int32_t)cell);
-                        o.cell_items.push_back((int32_t)o.items.size());
-                        for (int64_t k = cfirst[c]; k < cfirst[c + 1]; ++k) {
-                            const int j = (int)(trip[k] & 0xFF);
-                            const uint32_t te = (uint32_t)tile_local[hs.ents[cell * hs.nb + j]];
-                            o.items.push_back(pack_item(slot, (uint32_t)j, te));
-                            w.n_items++;
-                        }
-                        w.n_cells++;
-                        o.max_wave = std::max(o.max_wave, w.n_cells);
+            kc.assign(plan.tiles[t].n_ent, 0);
+            for (int64_t q = tstart[t]; q < tstart[t + 1]; ++q) {
+                const int s = (int)(trip[q] >> 40);
+                const int64_t cell = (int64_t)((trip[q] >> 8) & 0xFFFFFFFFull);
+                const int j = (int)(trip[q] & 0xFF);
+                const bool new_cell = q == tstart[t] || (trip[q] >> 8) != (trip[q - 1] >> 8);
+                if (new_cell) {
+                    if (o.segs.empty() || o.segs.back().sub != s) {
+                        if (!o.segs.empty()) o.segs.back().item_end = (int32_t)o.items.size();
+                        SegDesc g{};
+                        g.sub = s;
+                        g.cell_begin = (int32_t)o.cells.size();
+                        o.segs.push_back(g);
                     }
-                    if (open) o.waves.push_back(w);
+                    o.cells.push_back((int32_t)cell);
+                    o.cell_items.push_back((int32_t)o.items.size());
+                    o.segs.back().n_cells++;
                 }
+                const HostSub& hs = hp.subs[s];
+                const int32_t te = tile_local[hs.ents[cell * hs.nb + j]];
+                o.items.push_back(pack_item((uint32_t)j, (uint32_t)te, (uint32_t)kc[te]));
+                kc[te]++;
+            }
+            if (!o.segs.empty()) o.segs.back().item_end = (int32_t)o.items.size();
+            // reduce order: owned blocks by contribution count, most first (stable in (entity, r))
+            {
+                const TileDesc& T = plan.tiles[t];
+                std::vector<int32_t> cnt(T.n_red, 0);
+                for (int64_t q = tstart[t]; q < tstart[t + 1]; ++q) {
+                    const int s = (int)(trip[q] >> 40);
+                    const int64_t cell = (int64_t)((trip[q] >> 8) & 0xFFFFFFFFull);
+                    const int j = (int)(trip[q] & 0xFF);
+                    const HostSub& hs = hp.subs[s];
+                    const int32_t te = tile_local[hs.ents[cell * hs.nb + j]];
+                    const int32_t z = plan.emeta[T.ent_begin + te].z;
+                    for (int i = 0; i < hs.nb; ++i) {
+                        const size_t rq = ((size_t)cell * hs.nb + j) * hs.nb + i;
+                        const int r = hs.wide_rank ? (hs.rank16[rq] == 0xFFFF ? -1 : hs.rank16[rq]) : (hs.rank8[rq] == 255 ? -1 : hs.rank8[rq]);
+                        if (r >= 0) cnt[z + r]++;
+                    }
+                }
+                std::vector<uint32_t> keys(T.n_red);
+                for (int32_t te = 0; te < T.n_ent; ++te) {
+                    const EntMeta m = plan.emeta[T.ent_begin + te];
+                    for (int32_t r = 0; r < (m.w >> 8); ++r) keys[m.z + r] = ((uint32_t)te << 22) | (uint32_t)r;
+                }
+                std::vector<int32_t> ord(T.n_red);
+                for (int32_t q = 0; q < T.n_red; ++q) ord[q] = q;
+                std::stable_sort(ord.begin(), ord.end(), [&](int32_t x, int32_t y) { return cnt[x] > cnt[y]; });
+                o.red.resize(T.n_red);
+                for (int32_t q = 0; q < T.n_red; ++q) o.red[q] = keys[ord[q]];
+            }
+            // within a segment, cells with more owned base functions first: the lane groups of
+            // one warp then run loops of similar length
+            for (SegDesc& g : o.segs) {
+                const int32_t c0 = g.cell_begin, c1 = g.cell_begin + g.n_cells;
+                std::vector<int32_t> idx(g.n_cells);
+                for (int32_t c = 0; c < g.n_cells; ++c) idx[c] = c0 + c;
+                auto cnt = [&](int32_t c) { return (c + 1 < c1 ? o.cell_items[c + 1] : g.item_end) - o.cell_items[c]; };
+                std::stable_sort(idx.begin(), idx.end(), [&](int32_t x, int32_t y) { return cnt(x) > cnt(y); });
+                std::vector<int32_t> cells2, ci2;
+                std::vector<uint32_t> items2;
+                const int32_t ib = o.cell_items[c0];
+                for (int32_t c : idx) {
+                    cells2.push_back(o.cells[c]);
+                    ci2.push_back(ib + (int32_t)items2.size());
+                    const int32_t e0 = o.cell_items[c], e1 = c + 1 < c1 ? o.cell_items[c + 1] : g.item_end;
+                    items2.insert(items2.end(), o.items.begin() + e0, o.items.begin() + e1);
+                }
+                std::copy(cells2.begin(), cells2.end(), o.cells.begin() + c0);
+                std::copy(ci2.begin(), ci2.end(), o.cell_items.begin() + c0);
+                std::copy(items2.begin(), items2.end(), o.items.begin() + ib);
+            }
+            for (int32_t te = 0; te < plan.tiles[t].n_ent; ++te)
+                if (kc[te] != (plan.emeta[plan.tiles[t].ent_begin + te].w & 0xFF)) o.status = 1;
         }
     }
-    // concatenate
-    plan.waves.clear();
-    plan.wave_cells.clear();
-    plan.wave_cell_items.clear();
+    plan.segs.clear();
+    plan.tile_cells.clear();
+    plan.cell_items.clear();
     plan.items.clear();
+    plan.red_list.clear();
     plan.visits = 0;
-    size_t nw = 0, ncl = 0, nit = 0;
+    size_t ncl = 0, nit = 0;
     for (auto& o : outs) {
-        if (o.status) status = o.status;
-        nw += o.waves.size();
+        if (o.status) return fail(err, FE_ERR_ARG, "internal: incident cell count mismatch");
         ncl += o.cells.size();
         nit += o.items.size();
     }
-    if (status) return fail(err, status, "more than 64 colors needed inside one tile");
     if (nit >= (size_t)INT32_MAX || ncl >= (size_t)INT32_MAX) return fail(err, FE_ERR_UNSUPPORTED, "plan too large");
-    plan.waves.reserve(nw);
-    plan.wave_cells.reserve(ncl);
-    plan.wave_cell_items.reserve(ncl);
+    plan.tile_cells.reserve(ncl);
+    plan.cell_items.reserve(ncl);
     plan.items.reserve(nit);
     for (int64_t t = 0; t < n_tiles; ++t) {
         TileOut& o = outs[t];
-        const int32_t cb = (int32_t)plan.wave_cells.size(), ib = (int32_t)plan.items.size();
-        plan.tiles[t].wave_begin = (int32_t)plan.waves.size();
-        for (WaveDesc w : o.waves) {
-            w.cell_begin += cb;
-            w.item_begin += ib;
-            plan.waves.push_back(w);
+        const int32_t cb = (int32_t)plan.tile_cells.size(), ib = (int32_t)plan.items.size();
+        plan.tiles[t].seg_begin = (int32_t)plan.segs.size();
+        for (SegDesc g : o.segs) {
+            g.cell_begin += cb;
+            g.item_end += ib;
+            plan.segs.push_back(g);
         }
-        plan.tiles[t].wave_end = (int32_t)plan.waves.size();
+        plan.tiles[t].seg_end = (int32_t)plan.segs.size();
         for (size_t c = 0; c < o.cells.size(); ++c) {
-            plan.wave_cells.push_back(o.cells[c]);
-            plan.wave_cell_items.push_back(o.cell_items[c] + ib);
+            plan.tile_cells.push_back(o.cells[c]);
+            plan.cell_items.push_back(o.cell_items[c] + ib);
         }
         plan.items.insert(plan.items.end(), o.items.begin(), o.items.end());
-        plan.visits += o.visits;
-        plan.max_wave_cells = std::max(plan.max_wave_cells, o.max_wave);
-        std::vector<WaveDesc>().swap(o.waves);
+        plan.tiles[t].cell_begin = cb;
+        plan.tiles[t].n_cells = (int32_t)o.cells.size();
+        plan.tiles[t].item_begin = ib;
+        plan.tiles[t].n_items = (int32_t)o.items.size();
+        plan.max_items = std::max(plan.max_items, (int32_t)o.items.size());
+        plan.tiles[t].red_begin = (int32_t)plan.red_list.size();
+        plan.red_list.insert(plan.red_list.end(), o.red.begin(), o.red.end());
+        plan.visits += (int64_t)o.cells.size();
+        plan.max_cells = std::max(plan.max_cells, (int32_t)o.cells.size());
+        std::vector<uint32_t>().swap(o.items);
     }
     return FE_OK;
 }
 
-}  // namespace fe
-
-namespace fe {
-
 // Every index the kernel derives from the plan stays inside the buffers it addresses: the
-// tile accumulator (acc_len entries), the entity table, the chunk tables (slot < wave size),
-// the per-cell rank rows. Run once per fe_create; O(items).
+// tile staging (stage_vals), the contribution map (map_bytes), the entity table, the cell
+// tables and the per-cell rank rows. Run once per fe_create; O(items * n_base).
 int check_plan(const HostProblem& hp, const Plan& pl, Error& err) {
     const int nc = hp.nc;
     const int64_t* cp = hp.colptr.data();
+    const int nbm = pl.nb_max;
+    const int bs = (nc * nc + 1) & ~1;
     int bad = 0;
 #pragma omp parallel for schedule(dynamic, 64) reduction(| : bad)
     for (int64_t t = 0; t < (int64_t)pl.tiles.size(); ++t) {
         const TileDesc& T = pl.tiles[t];
-        std::vector<int64_t> ent_of;  // tile-local entity -> global id
-        std::vector<int32_t> colbase_off;
-        int64_t acc = 0;
+        int64_t stage = 0, map = 0, red = 0;
+        int32_t e = 0;
         for (int r = T.range_begin; r < T.range_end && !bad; ++r) {
             const RangeDesc& R = pl.ranges[r];
-            if (R.acc_base != acc || R.nz0 != cp[(int64_t)nc * R.ent0] - 1 ||
-                R.nz_len != cp[(int64_t)nc * (R.ent0 + R.n_ent)] - cp[(int64_t)nc * R.ent0])
+            if (R.nz0 != cp[(int64_t)nc * R.ent0] - 1 || R.nz_len != cp[(int64_t)nc * (R.ent0 + R.n_ent)] - cp[(int64_t)nc * R.ent0])
                 bad = 1;
-            for (int k = 0; k < R.n_ent; ++k) {
-                ent_of.push_back(R.ent0 + k);
-                colbase_off.push_back((int32_t)(R.acc_base + (cp[(int64_t)nc * (R.ent0 + k)] - 1 - R.nz0)));
+            for (int q = 0; q < R.n_ent && !bad; ++q, ++e) {
+                const EntMeta m = pl.emeta[T.ent_begin + e];
+                const int64_t n = R.ent0 + q;
+                const int kcnt = m.w & 0xFF, nnb = m.w >> 8;
+                if (pl.eids[T.ent_begin + e] != n || m.x != stage || m.y != map || m.z != red ||
+                    nnb != (cp[nc * n + 1] - cp[nc * n]) / nc)
+                    bad = 1;
+                stage += ((int64_t)kcnt * (nbm * bs + nc) + 1) & ~1ll;
+                map += ((int64_t)nnb * kcnt + 3) & ~3ll;
+                red += nnb;
             }
-            acc += R.nz_len;
         }
-        if (bad || acc != T.acc_len || (int64_t)ent_of.size() != T.n_ent) { bad = 1; continue; }
-        for (int wi = T.wave_begin; wi < T.wave_end && !bad; ++wi) {
-            const WaveDesc& W = pl.waves[wi];
-            if (W.sub < 0 || W.sub >= (int)hp.subs.size() || W.n_cells < 1 || W.n_cells > MAX_WAVE_CELLS) { bad = 1; break; }
-            const HostSub& hs = hp.subs[W.sub];
-            if (pl.wave_cell_items[W.cell_begin] != W.item_begin) { bad = 1; break; }
-            for (int s = 0; s < W.n_cells && !bad; ++s) {
-                const int32_t cell = pl.wave_cells[W.cell_begin + s];
+        if (bad || e != T.n_ent || stage != T.stage_vals || map != T.map_bytes || red != T.n_red) { bad = 1; continue; }
+        {
+            std::vector<char> seen(T.n_red, 0);
+            for (int32_t q = 0; q < T.n_red && !bad; ++q) {
+                const uint32_t key = pl.red_list[T.red_begin + q];
+                const int te = (int)(key >> 22), r = (int)(key & ((1u << 22) - 1));
+                if (te >= T.n_ent) { bad = 1; break; }
+                const EntMeta m = pl.emeta[T.ent_begin + te];
+                if (r >= (m.w >> 8) || seen[m.z + r]) { bad = 1; break; }
+                seen[m.z + r] = 1;
+            }
+        }
+        if (T.seg_end > T.seg_begin) {
+            const SegDesc& G0 = pl.segs[T.seg_begin];
+            const SegDesc& G1 = pl.segs[T.seg_end - 1];
+            if (G0.cell_begin != T.cell_begin || G1.cell_begin + G1.n_cells != T.cell_begin + T.n_cells ||
+                pl.cell_items[T.cell_begin] != T.item_begin || G1.item_end != T.item_begin + T.n_items)
+                bad = 1;
+        }
+        for (int g = T.seg_begin; g < T.seg_end && !bad; ++g) {
+            const SegDesc& G = pl.segs[g];
+            if (G.sub < 0 || G.sub >= (int)hp.subs.size() || G.n_cells < 1) { bad = 1; break; }
+            const HostSub& hs = hp.subs[G.sub];
+            for (int c = 0; c < G.n_cells && !bad; ++c) {
+                const int32_t cell = pl.tile_cells[G.cell_begin + c];
                 if (cell < 0 || cell >= hs.n_cells) { bad = 1; break; }
-                const int32_t i0 = pl.wave_cell_items[W.cell_begin + s];
-                const int32_t i1 = s + 1 < W.n_cells ? pl.wave_cell_items[W.cell_begin + s + 1] : W.item_begin + W.n_items;
-                if (i1 < i0 || i0 < W.item_begin || i1 > W.item_begin + W.n_items) { bad = 1; break; }
+                const int32_t i0 = pl.cell_items[G.cell_begin + c];
+                const int32_t i1 = c + 1 < G.n_cells ? pl.cell_items[G.cell_begin + c + 1] : G.item_end;
+                if (i1 < i0) { bad = 1; break; }
                 for (int32_t it = i0; it < i1; ++it) {
                     const uint32_t w = pl.items[it];
-                    const int slot = (int)(w >> (ITEM_J_BITS + ITEM_ENT_BITS));
-                    const int j = (int)((w >> ITEM_ENT_BITS) & ((1u << ITEM_J_BITS) - 1));
-                    const int te = (int)(w & ((1u << ITEM_ENT_BITS) - 1));
-                    if (slot != s || j >= hs.nb || te >= T.n_ent || ent_of[te] != hs.ents[(int64_t)cell * hs.nb + j]) { bad = 1; break; }
-                    const int64_t n = ent_of[te];
-                    const int64_t L = cp[nc * n + 1] - cp[nc * n];
+                    const int j = (int)(w & ((1u << ITEM_J_BITS) - 1));
+                    const int te = (int)((w >> ITEM_J_BITS) & ((1u << ITEM_ENT_BITS) - 1));
+                    const int k = (int)(w >> (ITEM_J_BITS + ITEM_ENT_BITS));
+                    if (j >= hs.nb || te >= T.n_ent || pl.eids[T.ent_begin + te] != hs.ents[(int64_t)cell * hs.nb + j]) { bad = 1; break; }
+                    const EntMeta m = pl.emeta[T.ent_begin + te];
+                    const int kcnt = m.w & 0xFF, nnb = m.w >> 8;
+                    if (k >= kcnt) { bad = 1; break; }
                     for (int i = 0; i < hs.nb; ++i) {
-                        const size_t k = ((size_t)cell * hs.nb + j) * hs.nb + i;
-                        const int r = hs.wide_rank ? (hs.rank16[k] == 0xFFFF ? -1 : hs.rank16[k]) : (hs.rank8[k] == 255 ? -1 : hs.rank8[k]);
-                        if (r < 0) continue;
-                        const int64_t last = colbase_off[te] + (int64_t)(nc - 1) * L + (int64_t)nc * r + (nc - 1);
-                        if ((int64_t)nc * r + nc > L || last >= T.acc_len) { bad = 1; break; }
+                        const size_t q = ((size_t)cell * hs.nb + j) * hs.nb + i;
+                        const int r = hs.wide_rank ? (hs.rank16[q] == 0xFFFF ? -1 : hs.rank16[q]) : (hs.rank8[q] == 255 ? -1 : hs.rank8[q]);
+                        if (r >= nnb || m.y + (int64_t)r * kcnt + k >= T.map_bytes) { bad = 1; break; }
                     }
+                    if ((int64_t)m.x + ((int64_t)k * nbm + hs.nb) * bs > T.stage_vals ||
+                        (int64_t)m.x + (int64_t)kcnt * nbm * bs + (int64_t)(k + 1) * nc > T.stage_vals) { bad = 1; break; }
                 }
             }
         }

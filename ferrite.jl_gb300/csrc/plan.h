@@ -39,19 +39,24 @@ struct HostProblem {
 };
 
 struct PlanOptions {
-    int32_t acc_cap = 12288;  // accumulator entries per tile (8 bytes each)
-    int32_t ent_cap = 4096;   // entities per tile
-    double fill = 0.70;       // target mean accumulator fill of a tile
+    int32_t stage_cap = 12288;  // staging values per tile (4 bytes each in mixed precision)
+    int32_t map_cap = 16384;    // contribution-map bytes per tile
+    int32_t ent_cap = MAX_TILE_ENTS;
+    int32_t red_cap = 2048;     // owned blocks (reduce lanes) per tile
 };
 
 struct Plan {
     std::vector<TileDesc> tiles;
     std::vector<RangeDesc> ranges;
-    std::vector<WaveDesc> waves;
-    std::vector<int32_t> wave_cells;
-    std::vector<int32_t> wave_cell_items;
+    std::vector<SegDesc> segs;
+    std::vector<EntMeta> emeta;
+    std::vector<int32_t> eids;
+    std::vector<int32_t> tile_cells;
+    std::vector<int32_t> cell_items;
     std::vector<uint32_t> items;
-    int32_t max_acc = 0, max_ent = 0, max_wave_cells = 0;
+    std::vector<uint32_t> red_list;
+    int32_t nb_max = 0;
+    int32_t max_stage = 0, max_map = 0, max_ent = 0, max_cells = 0, max_red = 0, max_items = 0;
     int64_t visits = 0;
 };
 

@@ -12,7 +12,8 @@ struct KernelEntry {
     int phys;            // 1 heat, 2 elastic, 3 neo-hooke
     int fp64;            // 0 = mixed precision, 1 = FP64
     const void* fn;      // __global__ tile_kernel<...>
-    int table_bytes[MAX_SUB];  // chunk-table bytes per cell of each slot
+    int table_bytes[MAX_SUB];  // cell-table bytes per lane group of each slot
+    int groups[MAX_SUB];       // lane groups per CTA of each slot
 };
 
 void register_heat(std::vector<KernelEntry>& out);

@@ -135,7 +135,8 @@ typedef struct {
     int64_t n_tiles;        /* owner tiles the nzval is partitioned into */
     int64_t n_cell_visits;  /* (cell, tile) pairs: geometry evaluations per assembly */
     int64_t n_items;        /* (cell, owned base function) work items per assembly */
-    int64_t flagged_cells;  /* cells recomputed with FP64 Jacobians in the last mixed assembly */
+    int64_t flagged_cells;  /* cell evaluations redone with FP64 Jacobians in the last mixed assembly
+                               (a cell is evaluated once per owner tile it touches) */
     int64_t device_bytes;   /* device memory held by the handle */
     double create_seconds;  /* host time spent in fe_create */
 } fe_info;

@@ -17,7 +17,7 @@ int main() {
     std::uniform_real_distribution<double> U(-1.0, 1.0);
     long bad = 0, n = 0;
     for (int it = 0; it < 2000000; ++it) {
-        const int ex = (int)(g() % 60) - 30;
+        const int ex = (int)(g() % 120) - 60;
         float hi = (float)std::ldexp(U(g), ex);
         if (it % 7 == 0) hi = std::ldexp(1.0f, ex) * ((it & 8) ? -1.f : 1.f);  // powers of two
         const int k = (int)(g() % 40);
@@ -26,14 +26,22 @@ int main() {
         if (it % 13 == 0) lo = std::ldexp(std::nextafter(std::ldexp(hi, 0), 2 * hi) - hi, -1);  // exact half ulp
         const double want = (double)hi + (double)lo;
         const double got = fe::pair_to_double(hi, lo);
+        const double got2 = fe::pair_to_double_fast(hi, lo);
+        uint64_t c2;
+        std::memcpy(&c2, &got2, 8);
         uint64_t a, b;
         std::memcpy(&a, &want, 8);
         std::memcpy(&b, &got, 8);
         ++n;
-        if (a != b) {
-            if (bad < 5) std::printf("hi=%a lo=%a want=%a got=%a\n", hi, lo, want, got);
+        if (a != b || a != c2) {
+            if (bad < 5) std::printf("hi=%a lo=%a want=%a got=%a fast=%a\n", hi, lo, want, got, got2);
             ++bad;
         }
+    }
+    for (int it = 0; it < 1000000; ++it) {
+        const float v = (float)std::ldexp(U(g), (int)(g() % 200) - 100);
+        const double w = (double)v, z = fe::float_to_double(v);
+        if (std::memcmp(&w, &z, 8) != 0) { ++bad; if (bad < 5) std::printf("f2d %a\n", v); }
     }
     std::printf("%ld %ld\n", bad, n);
     return bad != 0;
