@@ -1,0 +1,161 @@
+# FerriteGB300.jl -- Julia binding of libferrite_gb300 (the C ABI in include/ferrite_gb300.h).
+#
+# Replaces Ferrite's assembly loop
+#     assembler = start_assemble(K, f); for cell in CellIterator(dh) ... assemble!(...) end
+# with one ccall that fills K.nzval and f. Everything is passed as Ferrite's own memory.
+# (Julia is not available where this repository is built and tested; the same entry points are
+# exercised from Python through ctypes with byte-identical arrays.)
+module FerriteGB300
+
+using Ferrite, SparseArrays
+
+const LIB = get(ENV, "FERRITE_GB300_LIB", joinpath(@__DIR__, "..", "lib", "libferrite_gb300.so"))
+
+const FE_HEAT, FE_LINEAR_ELASTIC, FE_NEO_HOOKE = Int32(1), Int32(2), Int32(3)
+const FE_PREC_MIXED, FE_PREC_FP64 = Int32(0), Int32(1)
+const FE_FILLZERO = UInt32(1)
+
+struct GridDesc
+    dim::Int32
+    n_nodes::Int64
+    nodes::Ptr{Float64}
+    n_cells::Int64
+end
+
+struct SubdomainDesc
+    cell_type::Int32
+    ip_order::Int32
+    n_components::Int32
+    n_qp::Int32
+    qr_weights::Ptr{Float64}
+    N::Ptr{Float64}
+    dNdxi::Ptr{Float64}
+    M::Ptr{Float64}
+    dMdxi::Ptr{Float64}
+    n_cells::Int64
+    cellset::Ptr{Int64}
+    cell_nodes::Ptr{Int64}
+end
+
+struct DofDesc
+    ndofs::Int64
+    cell_dofs::Ptr{Int64}
+    cell_dofs_offset::Ptr{Int64}
+end
+
+struct CscDesc
+    n::Int64
+    nnz::Int64
+    colptr::Ptr{Int64}
+    rowval::Ptr{Int64}
+end
+
+struct AssembleParams
+    physics::Int32
+    precision::Int32
+    flags::UInt32
+    p0::Float64
+    p1::Float64
+    body::NTuple{3,Float64}
+    cell_scale::Ptr{Float64}
+    u::Ptr{Float64}
+    cond_threshold::Float64
+    stream::Ptr{Cvoid}
+end
+
+struct ErrorInfo
+    code::Int32
+    cell::Int64
+    detJ::Float64
+    row::Int64
+    col::Int64
+    message::NTuple{256,UInt8}
+end
+
+celltype_code(::Type{Triangle}) = Int32(1)
+celltype_code(::Type{Quadrilateral}) = Int32(2)
+celltype_code(::Type{Tetrahedron}) = Int32(3)
+celltype_code(::Type{Hexahedron}) = Int32(4)
+celltype_code(::Type{Wedge}) = Int32(5)
+
+mutable struct Handle
+    ptr::Ptr{Cvoid}
+    keep::Vector{Any}
+end
+
+function check(rc, h)
+    rc == 0 && return
+    info = Ref{ErrorInfo}()
+    ccall((:fe_last_error, LIB), Cint, (Ptr{Cvoid}, Ptr{ErrorInfo}), h, info)
+    msg = String(filter(!=(0x00), collect(info[].message)))
+    rc == 3 && throw(ArgumentError("det(J) is not positive: det(J) = $(info[].detJ) (cell $(info[].cell))"))
+    rc == 4 && error(msg)
+    error("ferrite_gb300 error $rc: $msg")
+end
+
+"""
+    Handle(dh, cellvalues_per_sdh, K)
+
+fe_create for a closed DofHandler, one scalar-interpolation CellValues per SubDofHandler (the
+field is `ip^n_components`), and the pattern of `K = allocate_matrix(dh)`.
+"""
+function Handle(dh::DofHandler, cvs::Vector, K::SparseMatrixCSC{Float64,Int})
+    grid = Ferrite.get_grid(dh)
+    nodes = reinterpret(Float64, grid.nodes)            # AoS Vec{dim} memory
+    keep = Any[nodes]
+    subs = SubdomainDesc[]
+    for (sdh, cv) in zip(dh.subdofhandlers, cvs)
+        cells = sort!(collect(sdh.cellset))
+        ct = typeof(grid.cells[first(cells)])
+        conn = reduce(vcat, [collect(Int64, grid.cells[c].nodes) for c in cells])
+        fv, gm = cv.fun_values, cv.geo_mapping
+        N = Matrix{Float64}(fv.Nξ)                       # [n_base, n_qp] == C [n_qp][n_base]
+        dN = reinterpret(Float64, fv.dNdξ)               # Vec{rdim} per (base, qp)
+        M = Matrix{Float64}(gm.M)
+        dM = reinterpret(Float64, gm.dMdξ)
+        w = Vector{Float64}(getweights(cv.qr))
+        cs = Vector{Int64}(cells)
+        ip = Ferrite.getfieldinterpolation(sdh, first(sdh.field_names))
+        nc = ip isa VectorizedInterpolation ? ip.vdim : 1
+        order = Ferrite.getorder(Ferrite.get_base_interpolation(ip))
+        append!(keep, (conn, N, dN, M, dM, w, cs))
+        push!(subs, SubdomainDesc(celltype_code(ct), Int32(order), Int32(nc), Int32(length(w)),
+                                  pointer(w), pointer(N), pointer(dN), pointer(M), pointer(dM),
+                                  length(cs), pointer(cs), pointer(conn)))
+    end
+    offs = Vector{Int64}(dh.cell_dofs_offset)
+    cd = Vector{Int64}(dh.cell_dofs)
+    append!(keep, (offs, cd))
+    g = Ref(GridDesc(Int32(Ferrite.getspatialdim(grid)), length(grid.nodes), pointer(nodes), length(grid.cells)))
+    d = Ref(DofDesc(ndofs(dh), pointer(cd), pointer(offs)))
+    p = Ref(CscDesc(size(K, 2), nnz(K), pointer(K.colptr), pointer(K.rowval)))
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    rc = GC.@preserve keep subs ccall((:fe_create, LIB), Cint,
+        (Ptr{GridDesc}, Int32, Ptr{SubdomainDesc}, Ptr{DofDesc}, Ptr{CscDesc}, Ptr{Ptr{Cvoid}}),
+        g, Int32(length(subs)), subs, d, p, out)
+    check(rc, C_NULL)
+    h = Handle(out[], keep)
+    finalizer(x -> ccall((:fe_destroy, LIB), Cvoid, (Ptr{Cvoid},), x.ptr), h)
+    return h
+end
+
+"""
+    assemble_csc!(K, f, h; physics, p0, p1, body, cell_scale, u, precision, fillzero)
+
+The whole `start_assemble(K, f)` + cell loop + `assemble!` in one call. K.nzval and f may be
+host arrays or device arrays (CuArray pointers).
+"""
+function assemble_csc!(K::SparseMatrixCSC{Float64,Int}, f::Vector{Float64}, h::Handle;
+                       physics=FE_LINEAR_ELASTIC, p0=1.0, p1=0.3, body=(0.0, 0.0, 0.0),
+                       cell_scale=nothing, u=nothing, precision=FE_PREC_MIXED, fillzero=true)
+    cs = cell_scale === nothing ? Ptr{Float64}(C_NULL) : pointer(cell_scale)
+    up = u === nothing ? Ptr{Float64}(C_NULL) : pointer(u)
+    par = Ref(AssembleParams(physics, precision, fillzero ? FE_FILLZERO : UInt32(0), p0, p1,
+                             Tuple(Float64.(body)), cs, up, 0.0, C_NULL))
+    rc = GC.@preserve K f cell_scale u ccall((:fe_assemble, LIB), Cint,
+        (Ptr{Cvoid}, Ptr{AssembleParams}, Ptr{Float64}, Ptr{Float64}), h.ptr, par, K.nzval, f)
+    check(rc, h.ptr)
+    return K, f
+end
+
+end # module
