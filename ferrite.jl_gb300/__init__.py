@@ -39,7 +39,7 @@ PREC_MIXED, PREC_FP64 = 0, 1
 FILLZERO, NO_K, NO_F, ASYNC, PROFILE = 1, 2, 4, 8, 16
 
 EXPORTED = ["fe_abi_version", "fe_create", "fe_assemble", "fe_sync", "fe_last_error", "fe_get_info",
-            "fe_get_index_map", "fe_plan_dry_run", "fe_distribute_dofs", "fe_sparsity_pattern", "fe_kernel_time", "fe_destroy"]
+            "fe_get_index_map", "fe_plan_dry_run", "fe_distribute_dofs", "fe_sparsity_pattern", "fe_kernel_time", "fe_assemble_noalloc", "fe_destroy"]
 
 i64p = ctypes.POINTER(ctypes.c_int64)
 f64p = ctypes.POINTER(ctypes.c_double)
@@ -116,6 +116,7 @@ def lib():
         L.fe_sparsity_pattern.argtypes = [ctypes.POINTER(GridDesc), ctypes.c_int32, ctypes.POINTER(SubdomainDesc),
                                           ctypes.POINTER(DofDesc), i64p, i64p, i64p]
         L.fe_kernel_time.argtypes = [ctypes.c_void_p, f64p, i64p]
+        L.fe_assemble_noalloc.argtypes = [ctypes.c_void_p, ctypes.POINTER(AssembleParams), ctypes.c_void_p, ctypes.c_void_p]
         L.fe_destroy.argtypes = [ctypes.c_void_p]
         L.fe_destroy.restype = None
         _lib = L

@@ -608,3 +608,176 @@ int fe_get_index_map(const fe_handle* h, int64_t cell, int64_t* positions) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// fe_assemble_noalloc: the same assembly without any device allocation, for callers that
+// cannot allocate (see the declaration in include/ferrite_gb300.h). The FP32 copies of u and
+// of the per-cell factors live in one file-scope device array; its device address is looked
+// up once per device on the first call there.
+// ---------------------------------------------------------------------------------------
+namespace {
+
+constexpr int64_t NOALLOC_SCRATCH_FLOATS = (int64_t)1 << 22;  // 16 MiB per device
+static __device__ __align__(256) float g_noalloc_scratch[NOALLOC_SCRATCH_FLOATS];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mutex;
+float* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of g_noalloc_scratch on the current device (resolved once per device).
+cudaError_t noalloc_scratch(int device, float** out) {
+    if (device < 0 || device >= NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[device]) {
+        float* ptr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_ptr[device] = ptr;
+    }
+    *out = g_noalloc_ptr[device];
+    return cudaSuccess;
+}
+
+__global__ void noalloc_to_float(const double* __restrict__ in, float* __restrict__ out, int64_t n) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        out[k] = (float)in[k];
+}
+
+}  // namespace
+
+extern "C" int fe_assemble_noalloc(fe_handle* h, const fe_assemble_params* p, double* nzval, double* f) {
+    if (!h || !p) return FE_ERR_ARG;
+    const HostProblem& hp = h->hp;
+    const int nc = hp.nc;
+    int phys = 0;
+    switch (p->physics) {
+        case FE_HEAT:
+            if (nc != 1) return set_error(h, FE_ERR_ARG, "FE_HEAT needs a scalar field");
+            phys = PHYS_HEAT;
+            break;
+        case FE_LINEAR_ELASTIC:
+            if (nc != hp.dim) return set_error(h, FE_ERR_ARG, "FE_LINEAR_ELASTIC needs a dim-component field");
+            phys = PHYS_ELASTIC;
+            break;
+        case FE_NEO_HOOKE:
+            if (nc != 3 || hp.dim != 3) return set_error(h, FE_ERR_ARG, "FE_NEO_HOOKE needs a 3-component field in 3D");
+            if (!p->u) return set_error(h, FE_ERR_ARG, "FE_NEO_HOOKE needs u");
+            phys = PHYS_NEO;
+            break;
+        default:
+            return set_error(h, FE_ERR_ARG, "unknown physics");
+    }
+    if (p->precision != FE_PREC_MIXED && p->precision != FE_PREC_FP64) return set_error(h, FE_ERR_ARG, "unknown precision");
+    if (p->flags & FE_PROFILE) return set_error(h, FE_ERR_ARG, "fe_assemble_noalloc does not profile (events are resources)");
+    const bool fp64 = p->precision == FE_PREC_FP64;
+    const bool do_k = !(p->flags & FE_NO_K), do_f = !(p->flags & FE_NO_F);
+    // every buffer must already be device memory: host buffers would need staging copies
+    if (do_k && !is_device_ptr(nzval)) return set_error(h, FE_ERR_ARG, "fe_assemble_noalloc: nzval must be device memory");
+    if (do_f && !is_device_ptr(f)) return set_error(h, FE_ERR_ARG, "fe_assemble_noalloc: f must be device memory");
+    if (p->u && !is_device_ptr(p->u)) return set_error(h, FE_ERR_ARG, "fe_assemble_noalloc: u must be device memory");
+    if (p->cell_scale && !is_device_ptr(p->cell_scale))
+        return set_error(h, FE_ERR_ARG, "fe_assemble_noalloc: cell_scale must be device memory");
+    const int64_t need = (phys == PHYS_NEO ? hp.ndofs : 0) + (p->cell_scale ? hp.n_cells : 0);
+    if (!fp64 && need > NOALLOC_SCRATCH_FLOATS) {
+        char buf[200];
+        std::snprintf(buf, sizeof buf,
+                      "fe_assemble_noalloc: needs %lld scratch floats (u and cell factors in FP32), the static maximum is %lld",
+                      (long long)need, (long long)NOALLOC_SCRATCH_FLOATS);
+        return set_error(h, FE_ERR_ARG, buf);
+    }
+    if (h->pending) fe_sync(h);
+    const KernelEntry* ke = nullptr;
+    for (const KernelEntry& e : registry()) {
+        if (e.phys != phys || e.fp64 != (int)fp64) continue;
+        bool ok = true;
+        for (int s = 0; s < MAX_SUB; ++s) {
+            if (s < (int)hp.subs.size()) {
+                if (e.kind[s] != hp.subs[s].kind || e.nq[s] != hp.subs[s].nq) ok = false;
+            } else if (e.kind[s] >= 0) {
+                ok = false;
+            }
+        }
+        if (ok) { ke = &e; break; }
+    }
+    if (!ke) return set_error(h, FE_ERR_UNSUPPORTED, "no kernel compiled for this element / quadrature / physics combination");
+    cudaStream_t st = (cudaStream_t)p->stream;
+    cudaError_t e;
+    float* scratch = nullptr;
+    if ((e = noalloc_scratch(h->device, &scratch)) != cudaSuccess) return cuda_fail(h, e, "cudaGetSymbolAddress");
+    KernelArgs A = h->base;
+    A.nzval = do_k ? nzval : nullptr;
+    A.f = do_f ? f : nullptr;
+    A.do_k = do_k;
+    A.do_f = do_f;
+    A.fillzero = (p->flags & FE_FILLZERO) != 0;
+    Physics& ph = A.phys;
+    ph = Physics{};
+    ph.kind = p->physics;
+    ph.p0 = p->p0;
+    ph.p1 = p->p1;
+    for (int x = 0; x < 3; ++x) ph.body[x] = p->body[x];
+    if (p->physics == FE_LINEAR_ELASTIC) {
+        const double E = p->p0, nu = p->p1;
+        ph.lam = E * nu / ((1 + nu) * (1 - 2 * nu));
+        ph.mu = E / (2 * (1 + nu));
+    }
+    ph.cond_threshold = p->cond_threshold > 0 ? (float)p->cond_threshold : 64.0f;
+    // FP32 inputs in the static scratch: u first, then the per-cell factors. Both are fully
+    // overwritten here, so nothing needs clearing between calls.
+    int64_t off = 0;
+    if (phys == PHYS_NEO) {
+        ph.u_d = p->u;
+        if (!fp64) {
+            noalloc_to_float<<<(unsigned)std::min<int64_t>((hp.ndofs + 255) / 256, 4096), 256, 0, st>>>(p->u, scratch, hp.ndofs);
+            ph.u_f = scratch;
+            off += hp.ndofs;
+        }
+    }
+    if (p->cell_scale) {
+        ph.scale_d = p->cell_scale;
+        if (!fp64) {
+            noalloc_to_float<<<(unsigned)std::min<int64_t>((hp.n_cells + 255) / 256, 4096), 256, 0, st>>>(p->cell_scale, scratch + off,
+                                                                                                        hp.n_cells);
+            ph.scale_f = scratch + off;
+        } else {
+            ph.scale_f = (const float*)ph.scale_d;  // non-null marker; the FP64 kernel reads scale_d
+        }
+    }
+    const int pi = fp64 ? 1 : 0;
+    const int real = fp64 ? 8 : 4;
+    const int fixed = smem_layout(A, h->shape_bytes[pi], real).chunk;
+    int max_smem = 0;
+    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+    const int budget = max_smem - 1024;
+    int tb = 0;
+    for (int s = 0; s < MAX_SUB; ++s) {
+        A.groups[s] = 0;
+        if (ke->kind[s] < 0) continue;
+        const int room = (budget - fixed) / std::max(ke->table_bytes[s], 1);
+        A.groups[s] = std::max(1, std::min(ke->groups[s], room));
+        tb = std::max(tb, ke->table_bytes[s] * A.groups[s]);
+    }
+    if (fixed + tb > budget) return set_error(h, FE_ERR_UNSUPPORTED, "tile does not fit in shared memory");
+    A.chunk_bytes = tb;
+    const int smem = fixed + tb;
+    if ((e = cudaFuncSetAttribute(ke->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
+        return cuda_fail(h, e, "cudaFuncSetAttribute");
+    DevStatus init{~0ull, ~0ull, 0u, 0u};
+    *h->status_h = init;
+    if ((e = cudaMemcpyAsync(h->status_d, h->status_h, sizeof(DevStatus), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return cuda_fail(h, e, "status reset");
+    A.status = h->status_d;
+    const void* shp = fp64 ? (const void*)h->shape_d : (const void*)h->shape_f;
+    int sb = h->shape_bytes[pi], o1 = h->shape_off1[pi], o2 = h->shape_off2[pi];
+    void* args[] = {(void*)&A, (void*)&shp, (void*)&sb, (void*)&o1, (void*)&o2};
+    if (A.n_tiles > 0) {
+        e = cudaLaunchKernel(ke->fn, dim3((unsigned)A.n_tiles), dim3(THREADS), args, (size_t)smem, st);
+        if (e != cudaSuccess) return cuda_fail(h, e, "tile kernel launch");
+    }
+    if ((e = cudaMemcpyAsync(h->status_h, h->status_d, sizeof(DevStatus), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return cuda_fail(h, e, "status read");
+    h->last_stream = st;
+    h->pending = 1;
+    if (p->flags & FE_ASYNC) return FE_OK;
+    return fe_sync(h);
+}

@@ -205,6 +205,23 @@ int fe_sparsity_pattern(const fe_grid_desc* grid, int32_t n_subdomains, const fe
  * for them, returns the summed milliseconds and the number of launches, then resets. */
 int fe_kernel_time(fe_handle* h, double* total_ms, int64_t* launches);
 
+/*
+ * fe_assemble_noalloc: fe_assemble for callers that cannot allocate device memory -- for
+ * instance code running where cudaMalloc is forbidden or would synchronize the device, such
+ * as an allocator-less embedding of the solver loop. No counterpart in the reference (Ferrite
+ * has no device allocation concerns on this path).
+ * It allocates nothing: nzval, f, u and cell_scale must already be device memory (host
+ * buffers are rejected with FE_ERR_ARG, since they would need staging copies), and the FP32
+ * copies of u and of cell_scale that mixed precision uses live in one static device array of
+ * 4,194,304 floats (16 MiB) that every GPU loading this library holds until exit. Problems
+ * needing more (ndofs for FE_NEO_HOOKE plus n_cells when cell_scale is given) are rejected
+ * with FE_ERR_ARG. The first call on a device looks up that array's address
+ * (cudaGetSymbolAddress); make that first call before any stream capture. All calls share the
+ * array, which keeps the last call's values: calls that overlap on the GPU (other streams,
+ * other handles) race on it. FE_PROFILE is not supported here.
+ */
+int fe_assemble_noalloc(fe_handle* h, const fe_assemble_params* params, double* nzval, double* f);
+
 void fe_destroy(fe_handle* h);
 
 int fe_abi_version(void);
