@@ -149,6 +149,52 @@ int finish_status(fe_handle* h) {
     return FE_OK;
 }
 
+// Shared-memory sizing, status reset and the launch of one assembly: persistent CTAs, as
+// many as fit on the device at once (never more than there are tiles).
+int launch_assembly(fe_handle* h, const KernelEntry* ke, KernelArgs& A, bool fp64, cudaStream_t st,
+                    std::pair<cudaEvent_t, cudaEvent_t>* ev) {
+    cudaError_t e;
+    const int pi = fp64 ? 1 : 0;
+    const int fixed = smem_layout(A, h->shape_bytes[pi], fp64 ? 8 : 4).chunk;
+    int max_smem = 0, n_sm = 0;
+    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, h->device);
+    const int budget = max_smem - 1024;  // static shared (mbarriers) headroom
+    // cell-table buffers: one per lane group; fewer groups when the tables are large
+    int tb = 0;
+    for (int s = 0; s < MAX_SUB; ++s) {
+        A.groups[s] = 0;
+        if (ke->kind[s] < 0) continue;
+        const int room = (budget - fixed) / std::max(ke->table_bytes[s], 1);
+        A.groups[s] = std::max(1, std::min(ke->groups[s], room));
+        tb = std::max(tb, ke->table_bytes[s] * A.groups[s]);
+    }
+    if (fixed + tb > budget) return set_error(h, FE_ERR_UNSUPPORTED, "tile does not fit in shared memory");
+    A.chunk_bytes = tb;
+    const int smem = fixed + tb;
+    if ((e = cudaFuncSetAttribute(ke->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
+        return cuda_fail(h, e, "cudaFuncSetAttribute");
+    int per_sm = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ke->fn, THREADS, smem)) != cudaSuccess)
+        return cuda_fail(h, e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    const int64_t grid = std::min<int64_t>(A.n_tiles, (int64_t)std::max(per_sm, 1) * std::max(n_sm, 1));
+    DevStatus init{~0ull, ~0ull, 0u, 0u};
+    *h->status_h = init;
+    if ((e = cudaMemcpyAsync(h->status_d, h->status_h, sizeof(DevStatus), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return cuda_fail(h, e, "status reset");
+    A.status = h->status_d;
+    const void* shp = fp64 ? (const void*)h->shape_d : (const void*)h->shape_f;
+    int sb = h->shape_bytes[pi], o1 = h->shape_off1[pi], o2 = h->shape_off2[pi];
+    void* args[] = {(void*)&A, (void*)&shp, (void*)&sb, (void*)&o1, (void*)&o2};
+    if (ev) cudaEventRecord(ev->first, st);
+    if (grid > 0) {
+        e = cudaLaunchKernel(ke->fn, dim3((unsigned)grid), dim3(THREADS), args, (size_t)smem, st);
+        if (e != cudaSuccess) return cuda_fail(h, e, "tile kernel launch");
+    }
+    if (ev) cudaEventRecord(ev->second, st);
+    return FE_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -199,33 +245,29 @@ int fe_create(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain
     A.nc = hp.nc;
     A.dim = hp.dim;
     A.n_sub = (int32_t)hp.subs.size();
-    A.n_tiles = (int32_t)pl.tiles.size();
-    // node coordinates: FP64 AoS and float hi/lo SoA
+    // node coordinates: FP64 [n][dim], and 32 bytes per node for the gathers: float hi (x, y,
+    // z, 0) then float lo, or FP64 (x, y, z, 0)
     {
         double* xd;
         CK(h->upload(&xd, hp.nodes.data(), hp.nodes.size()));
         A.xd = xd;
-        std::vector<float> hi(hp.n_nodes), lo(hp.n_nodes);
-        for (int x = 0; x < 3; ++x) {
-            if (x >= hp.dim) {
-                A.xh[x] = A.xl[x] = nullptr;
-                continue;
-            }
-            for (int64_t n = 0; n < hp.n_nodes; ++n) {
+        std::vector<float> x8((size_t)hp.n_nodes * 8, 0.f);
+        std::vector<double> x4((size_t)hp.n_nodes * 4, 0.0);
+        for (int64_t n = 0; n < hp.n_nodes; ++n)
+            for (int x = 0; x < hp.dim; ++x) {
                 const double v = hp.nodes[n * hp.dim + x];
-                hi[n] = (float)v;
-                lo[n] = (float)(v - (double)hi[n]);
+                const float hi = (float)v;
+                x8[n * 8 + x] = hi;
+                x8[n * 8 + 4 + x] = (float)(v - (double)hi);
+                x4[n * 4 + x] = v;
             }
-            float *ph, *pl_;
-            CK(h->upload(&ph, hi.data(), hi.size()));
-            CK(h->upload(&pl_, lo.data(), lo.size()));
-            A.xh[x] = ph;
-            A.xl[x] = pl_;
-        }
+        float* xf8;
+        double* xd4;
+        CK(h->upload(&xf8, x8.data(), x8.size()));
+        CK(h->upload(&xd4, x4.data(), x4.size()));
+        A.xf8 = xf8;
+        A.xd4 = xd4;
     }
-    int64_t* colptr_d;
-    CK(h->upload(&colptr_d, hp.colptr.data(), hp.colptr.size()));
-    A.colptr = colptr_d;
     // subdomains
     std::vector<float> shf;
     std::vector<double> shd;
@@ -235,34 +277,10 @@ int fe_create(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain
         SubDev& sd = A.sub[s];
         sd.kind = hs.kind; sd.nb = hs.nb; sd.ng = hs.ng; sd.nq = hs.nq; sd.dim = hs.dim; sd.nc = hs.nc;
         sd.n_cells = hs.n_cells;
-        int32_t *cid, *conn, *ents;
+        int32_t *cid, *ents;
         CK(h->upload(&cid, hs.cellid.data(), hs.cellid.size()));
-        CK(h->upload(&conn, hs.conn.data(), hs.conn.size()));
         CK(h->upload(&ents, hs.ents.data(), hs.ents.size()));
-        sd.cellid = cid; sd.conn = conn; sd.ents = ents;
-        sd.rank8 = nullptr; sd.rank16 = nullptr;
-        // device layout: one row per (cell, row function i), the ranks of all column functions
-        // j, padded to 8 bytes, so a lane fetches its row with 8-byte loads
-        const int nbq = hs.nb;
-        if (hs.wide_rank) {
-            const int rs = 4 * ((nbq + 3) / 4);
-            std::vector<uint16_t> t((size_t)hs.n_cells * nbq * rs, 0xFFFF);
-            for (int64_t k = 0; k < hs.n_cells; ++k)
-                for (int j = 0; j < nbq; ++j)
-                    for (int i = 0; i < nbq; ++i) t[((size_t)k * nbq + i) * rs + j] = hs.rank16[((size_t)k * nbq + j) * nbq + i];
-            uint16_t* r;
-            CK(h->upload(&r, t.data(), t.size()));
-            sd.rank16 = r;
-        } else {
-            const int rs = 8 * ((nbq + 7) / 8);
-            std::vector<uint8_t> t((size_t)hs.n_cells * nbq * rs, 0xFF);
-            for (int64_t k = 0; k < hs.n_cells; ++k)
-                for (int j = 0; j < nbq; ++j)
-                    for (int i = 0; i < nbq; ++i) t[((size_t)k * nbq + i) * rs + j] = hs.rank8[((size_t)k * nbq + j) * nbq + i];
-            uint8_t* r;
-            CK(h->upload(&r, t.data(), t.size()));
-            sd.rank8 = r;
-        }
+        sd.cellid = cid; sd.ents = ents;
         // reference tables: w, N, dN (physical layout [q][i][c]), dM; padded blocks
         auto push_block = [&](auto& vec, const std::vector<double>& src) {
             using T = typename std::remove_reference<decltype(vec)>::type::value_type;
@@ -297,31 +315,27 @@ int fe_create(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain
     h->shape_bytes[1] = (int)(shd.size() * sizeof(double));
     h->shape_off1[0] = offs_f[1]; h->shape_off2[0] = offs_f[2];
     h->shape_off1[1] = offs_d[1]; h->shape_off2[1] = offs_d[2];
-    // plan
-    TileDesc* tiles; RangeDesc* ranges; SegDesc* segs; EntMeta* emeta; int32_t *eids, *tc, *ci; uint32_t* items;
-    CK(h->upload(&tiles, pl.tiles.data(), pl.tiles.size()));
-    CK(h->upload(&ranges, pl.ranges.data(), pl.ranges.size()));
-    CK(h->upload(&segs, pl.segs.data(), pl.segs.size()));
-    CK(h->upload(&emeta, pl.emeta.data(), pl.emeta.size()));
-    CK(h->upload(&eids, pl.eids.data(), pl.eids.size()));
-    CK(h->upload(&tc, pl.tile_cells.data(), pl.tile_cells.size()));
-    CK(h->upload(&ci, pl.cell_items.data(), pl.cell_items.size()));
-    CK(h->upload(&items, pl.items.data(), pl.items.size()));
-    uint32_t* red;
-    CK(h->upload(&red, pl.red_list.data(), pl.red_list.size()));
-    A.red_list = red;
-    A.tiles = tiles; A.ranges = ranges; A.segs = segs; A.emeta = emeta; A.eids = eids;
-    A.tile_cells = tc; A.cell_items = ci; A.items = items;
-    A.nb_max = pl.nb_max;
+    // tile records
+    {
+        char* rec;
+        int64_t* roff;
+        CK(h->upload(&rec, (const char*)pl.rec.data(), pl.rec.size()));
+        CK(h->upload(&roff, pl.rec_off.data(), pl.rec_off.size()));
+        A.rec = rec;
+        A.rec_off = roff;
+        std::vector<uint8_t>().swap(h->plan.rec);  // the device copy is the one in use
+    }
+    A.n_tiles = (int32_t)pl.n_tiles;
     A.bs = (hp.nc * hp.nc + 1) & ~1;
-    A.stage_cap = std::max(pl.max_stage, 1);
-    A.map_cap = std::max(pl.max_map, 16);
-    A.ent_cap = std::max(pl.max_ent, 1);
-    A.red_cap = std::max(pl.max_red, 1);
-    A.cells_cap = std::max(pl.max_cells, 1);
-    A.items_cap = std::max(pl.max_items, 1);
-    A.ng_max = 1;
-    for (const HostSub& hs2 : hp.subs) A.ng_max = std::max(A.ng_max, hs2.ng);
+    A.rec_cap = std::max(pl.max_rec, 64);
+    A.node_cap = std::max(pl.max_nodes, 1);
+    A.stage_cap = std::max(pl.max_stage, 2);
+    if (pl.n_tiles >= (int64_t)INT32_MAX) {
+        set_error(h, FE_ERR_UNSUPPORTED, "too many tiles");
+        g_create_error = h->last;
+        delete h;
+        return FE_ERR_UNSUPPORTED;
+    }
     CK(h->alloc(&h->status_d, 1));
     CK(cudaMallocHost((void**)&h->status_h, sizeof(DevStatus)));
 #undef CK
@@ -356,9 +370,9 @@ int fe_plan_dry_run(const fe_grid_desc* grid, int32_t n_subdomains, const fe_sub
     out->n_cells = hp.n_cells;
     out->ndofs = hp.ndofs;
     out->nnz = hp.nnz;
-    out->n_tiles = (int64_t)pl.tiles.size();
+    out->n_tiles = pl.n_tiles;
     out->n_cell_visits = pl.visits;
-    out->n_items = (int64_t)pl.items.size();
+    out->n_items = pl.items;
     out->create_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return FE_OK;
 }
@@ -484,36 +498,6 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
         int rc = stage_input(p->u, hp.ndofs, &h->u_stage, &h->u_f, &ph.u_d, &ph.u_f);
         if (rc) return rc;
     }
-    // shared memory: shape tables + staging + map + entity table + chunk tables
-    const int pi = fp64 ? 1 : 0;
-    const int real = fp64 ? 8 : 4;
-    const int fixed = smem_layout(A, h->shape_bytes[pi], real).chunk;
-    int max_smem = 0;
-    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
-    const int budget = max_smem - 1024;  // static shared (mbarrier) headroom
-    // cell-table buffers: one per lane group; fewer groups when the tables are large
-    int tb = 0;
-    for (int s = 0; s < MAX_SUB; ++s) {
-        A.groups[s] = 0;
-        if (ke->kind[s] < 0) continue;
-        const int room = (budget - fixed) / std::max(ke->table_bytes[s], 1);
-        A.groups[s] = std::max(1, std::min(ke->groups[s], room));
-        tb = std::max(tb, ke->table_bytes[s] * A.groups[s]);
-    }
-    if (fixed + tb > budget) return set_error(h, FE_ERR_UNSUPPORTED, "tile does not fit in shared memory");
-    A.chunk_bytes = tb;
-    const int smem = fixed + tb;
-    if ((e = cudaFuncSetAttribute(ke->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
-        return cuda_fail(h, e, "cudaFuncSetAttribute");
-    // status
-    DevStatus init{~0ull, ~0ull, 0u, 0u};
-    *h->status_h = init;
-    if ((e = cudaMemcpyAsync(h->status_d, h->status_h, sizeof(DevStatus), cudaMemcpyHostToDevice, st)) != cudaSuccess)
-        return cuda_fail(h, e, "status reset");
-    A.status = h->status_d;
-    const void* shp = fp64 ? (const void*)h->shape_d : (const void*)h->shape_f;
-    int sb = h->shape_bytes[pi], o1 = h->shape_off1[pi], o2 = h->shape_off2[pi];
-    void* args[] = {(void*)&A, (void*)&shp, (void*)&sb, (void*)&o1, (void*)&o2};
     std::pair<cudaEvent_t, cudaEvent_t> ev{nullptr, nullptr};
     const bool prof = (p->flags & FE_PROFILE) != 0;
     if (prof) {
@@ -523,15 +507,11 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
         } else if ((e = cudaEventCreate(&ev.first)) != cudaSuccess || (e = cudaEventCreate(&ev.second)) != cudaSuccess) {
             return cuda_fail(h, e, "cudaEventCreate");
         }
-        cudaEventRecord(ev.first, st);
     }
-    if (A.n_tiles > 0) {
-        e = cudaLaunchKernel(ke->fn, dim3((unsigned)A.n_tiles), dim3(THREADS), args, (size_t)smem, st);
-        if (e != cudaSuccess) return cuda_fail(h, e, "tile kernel launch");
-    }
-    if (prof) {
-        cudaEventRecord(ev.second, st);
-        h->prof_events.push_back(ev);
+    {
+        const int rc = launch_assembly(h, ke, A, fp64, st, prof ? &ev : nullptr);
+        if (prof) (rc == FE_OK ? h->prof_events : h->prof_pool).push_back(ev);
+        if (rc != FE_OK) return rc;
     }
     if ((e = cudaMemcpyAsync(h->status_h, h->status_d, sizeof(DevStatus), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
         return cuda_fail(h, e, "status read");
@@ -574,9 +554,9 @@ int fe_get_info(const fe_handle* h, fe_info* out) {
     out->n_cells = h->hp.n_cells;
     out->ndofs = h->hp.ndofs;
     out->nnz = h->hp.nnz;
-    out->n_tiles = (int64_t)h->plan.tiles.size();
+    out->n_tiles = h->plan.n_tiles;
     out->n_cell_visits = h->plan.visits;
-    out->n_items = (int64_t)h->plan.items.size();
+    out->n_items = h->plan.items;
     out->flagged_cells = h->flagged;
     out->device_bytes = h->device_bytes;
     out->create_seconds = h->create_seconds;
@@ -743,36 +723,9 @@ extern "C" int fe_assemble_noalloc(fe_handle* h, const fe_assemble_params* p, do
             ph.scale_f = (const float*)ph.scale_d;  // non-null marker; the FP64 kernel reads scale_d
         }
     }
-    const int pi = fp64 ? 1 : 0;
-    const int real = fp64 ? 8 : 4;
-    const int fixed = smem_layout(A, h->shape_bytes[pi], real).chunk;
-    int max_smem = 0;
-    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
-    const int budget = max_smem - 1024;
-    int tb = 0;
-    for (int s = 0; s < MAX_SUB; ++s) {
-        A.groups[s] = 0;
-        if (ke->kind[s] < 0) continue;
-        const int room = (budget - fixed) / std::max(ke->table_bytes[s], 1);
-        A.groups[s] = std::max(1, std::min(ke->groups[s], room));
-        tb = std::max(tb, ke->table_bytes[s] * A.groups[s]);
-    }
-    if (fixed + tb > budget) return set_error(h, FE_ERR_UNSUPPORTED, "tile does not fit in shared memory");
-    A.chunk_bytes = tb;
-    const int smem = fixed + tb;
-    if ((e = cudaFuncSetAttribute(ke->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
-        return cuda_fail(h, e, "cudaFuncSetAttribute");
-    DevStatus init{~0ull, ~0ull, 0u, 0u};
-    *h->status_h = init;
-    if ((e = cudaMemcpyAsync(h->status_d, h->status_h, sizeof(DevStatus), cudaMemcpyHostToDevice, st)) != cudaSuccess)
-        return cuda_fail(h, e, "status reset");
-    A.status = h->status_d;
-    const void* shp = fp64 ? (const void*)h->shape_d : (const void*)h->shape_f;
-    int sb = h->shape_bytes[pi], o1 = h->shape_off1[pi], o2 = h->shape_off2[pi];
-    void* args[] = {(void*)&A, (void*)&shp, (void*)&sb, (void*)&o1, (void*)&o2};
-    if (A.n_tiles > 0) {
-        e = cudaLaunchKernel(ke->fn, dim3((unsigned)A.n_tiles), dim3(THREADS), args, (size_t)smem, st);
-        if (e != cudaSuccess) return cuda_fail(h, e, "tile kernel launch");
+    {
+        const int rc = launch_assembly(h, ke, A, fp64, st, nullptr);
+        if (rc != FE_OK) return rc;
     }
     if ((e = cudaMemcpyAsync(h->status_h, h->status_d, sizeof(DevStatus), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
         return cuda_fail(h, e, "status read");

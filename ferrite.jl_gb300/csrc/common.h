@@ -36,63 +36,82 @@ constexpr int MAX_NG = 8;    // geometric nodes per cell
 constexpr int MAX_NQ = 27;   // quadrature points per cell
 constexpr int MAX_SUB = 3;   // subdomains one kernel handles
 
-// item word: local base function j (5 bits) | tile-local entity (10 bits) | k (6 bits), where
-// k is the position of the item's cell among the cells of that entity (cell order)
-constexpr int ITEM_J_BITS = 5, ITEM_ENT_BITS = 10, ITEM_K_BITS = 6;
-constexpr int MAX_TILE_ENTS = 1 << ITEM_ENT_BITS;
-constexpr int MAX_ENT_CELLS = (1 << ITEM_K_BITS) - 1;
-__host__ __device__ inline uint32_t pack_item(uint32_t j, uint32_t ent, uint32_t k) {
-    return j | (ent << ITEM_J_BITS) | (k << (ITEM_J_BITS + ITEM_ENT_BITS));
-}
+// ---------------------------------------------------------------------------------------
+// Tile record: everything the kernel needs to assemble one tile, in one contiguous block
+// of global memory that a CTA copies to shared memory with a single TMA bulk copy. All
+// section offsets are bytes from the record start, multiples of 16; the record size is a
+// multiple of 16. Sections:
+//   RecHead                                   80 bytes
+//   RecSeg[n_seg]                             the tile's cells, one segment per subdomain
+//   RecEnt[n_ent]       (off_ent)             owned entities: column base, length, id
+//   uint32 fk[n_ent]    (off_fk)              f staging: first f slot | cell count << 16
+//   uint32 red[n_red]   (off_red)             owned (entity, row entity) blocks: ent << 22 | rank,
+//                                             most contributions first
+//   RecRun runs[n_runs] (off_runs)            the blocks as runs of equal contribution count:
+//                                             block b of run u has its slots at
+//                                             base + (b - first) * count .. + count - 1, in cell order
+//   uint32 items[n_items] (off_items)         per (cell, owned base function j): j | f slot << 16
+//   RecCell[n_cells]    (off_cells)           sub-local cell index, its items
+//   uint16 conn[..]     (RecSeg::conn_off)    per segment: [cells][NG] tile-local node index
+//   uint16 slots[..]    (RecSeg::slot_off)    per segment: [items][NB] staging slot of row i,
+//                                             SLOT_MISS where the pattern has no entry
+//   int32 nodes[n_nodes] (off_nodes)          global node ids (coordinates are gathered)
+// Staging (shared memory, Real values): slot s holds one nc x nc block at s * BS
+// (BS = nc*nc rounded up to even, column-major); f slot q holds nc values at
+// n_slots * BS + q * nc.
+// ---------------------------------------------------------------------------------------
+constexpr uint16_t SLOT_MISS = 0xFFFF;
+constexpr int RED_RANK_BITS = 22;
+constexpr int MAX_TILE_ENTS = 1 << (32 - RED_RANK_BITS);
+constexpr int MAX_ENT_CELLS = 255;   // cells of one dof entity
+constexpr int MAX_TILE_SLOTS = 0xFFFF;
 
-struct TileDesc {
-    int32_t seg_begin, seg_end;      // into segs[]: the tile's cells, one segment per subdomain
-    int32_t range_begin, range_end;  // into ranges[]: the owned entities as runs of ids
-    int32_t ent_begin;               // into emeta[] / eids[]
-    int32_t n_ent;                   // owned entities
-    int32_t n_red;                   // owned (entity, row entity) blocks = reduce lanes
-    int32_t stage_vals;              // staging values (block contributions + f contributions)
-    int32_t map_bytes;               // contribution map bytes
-    int32_t red_begin;               // into red_list[]: the n_red blocks, most contributions first
-    int32_t cell_begin, n_cells;     // into tile_cells[] / cell_items[]: all cells of the tile
-    int32_t item_begin, n_items;     // into items[]: all items of the tile
+struct RecHead {
+    int32_t bytes;
+    int32_t n_seg, n_ent, n_cells;
+    int32_t n_items, n_red, n_nodes, n_slots;
+    int32_t n_fslots, off_ent, off_fk, off_red;
+    int32_t n_runs, off_runs, off_items, off_cells;
+    int32_t off_nodes, pad[3];
 };
+static_assert(sizeof(RecHead) == 80, "record head is 80 bytes");
 
-struct RangeDesc {
-    int64_t nz0;      // 0-based nzval index of the first owned entry
-    int32_t ent0;     // first entity id (0-based)
-    int32_t n_ent;    // entities in the run
-    int32_t nz_len;   // nzval entries in the run
+struct RecSeg {
+    int32_t sub;
+    int32_t cell_begin, cell_end;  // tile cells of the segment
+    int32_t item_begin, item_end;  // tile items of the segment
+    int32_t conn_off, slot_off;    // byte offsets of the segment's conn and slot rows
     int32_t pad;
 };
+static_assert(sizeof(RecSeg) == 32, "segment entry is 32 bytes");
 
-struct SegDesc {
-    int32_t sub;         // subdomain index
-    int32_t cell_begin;  // into tile_cells[] / cell_items[]
-    int32_t n_cells;
-    int32_t item_end;    // one past the last item of the segment's last cell
+struct RecEnt {
+    int64_t colbase;  // 0-based nzval index of the entity's first column
+    int32_t L;        // column length (entries)
+    int32_t id;       // entity id (0-based): f rows id*nc .. id*nc+nc-1
 };
+static_assert(sizeof(RecEnt) == 16, "entity entry is 16 bytes");
 
-// Per owned entity of a tile (in range order):
-//   x: staging offset (values): [kcount][NBmax][BS] block contributions (BS = nc*nc rounded up
-//      to even), then [kcount][nc] f
-//   y: map offset (bytes): [nnb][kcount], the row function i of each contribution or 0xFF
-//   z: first reduce lane of the entity
-//   w: kcount | nnb << 8  (cells of the entity, row entities of its columns)
-struct alignas(16) EntMeta {
-    int32_t x, y, z, w;
+struct RecRun {
+    int32_t first;  // first block (position in red[]) of the run
+    int32_t count;  // contributions (slots) of each block of the run
+    int32_t base;   // first slot of the run
+    int32_t pad;
 };
+static_assert(sizeof(RecRun) == 16, "run entry is 16 bytes");
+
+struct RecCell {
+    int32_t cell;                  // subdomain-local cell index
+    uint16_t item_begin, item_end; // tile items of the cell
+};
+static_assert(sizeof(RecCell) == 8, "cell entry is 8 bytes");
 
 // per-subdomain device data
 struct SubDev {
     int32_t kind, nb, ng, nq, dim, nc;
     int64_t n_cells;
     const int32_t* cellid;   // [n] 0-based Ferrite cell id
-    const int32_t* conn;     // [n][ng] 0-based node ids
     const int32_t* ents;     // [n][nb] entity ids
-    const uint8_t* rank8;    // [n][nb i][RS8] rank of entity i in the columns of entity j (byte j), or NULL;
-                             // rows padded to RS8 = 8 * ceil(nb / 8) bytes
-    const uint16_t* rank16;  // same with 16-bit ranks (some rank exceeds 254); rows of RS16 = 4 * ceil(nb / 4)
     // reference tables (float and double copies), row-major as in the C ABI
     const float* w_f;        // [nq]
     const float* N_f;        // [nq][nb]
@@ -128,35 +147,22 @@ struct KernelArgs {
     int32_t n_tiles;
     int32_t nc;              // components per entity (dofs per entity)
     int32_t n_sub;
-    int32_t nb_max;          // staging stride: max base functions over subdomains
     int32_t bs;              // staging values per block: nc*nc rounded up to even
     SubDev sub[MAX_SUB];
-    const TileDesc* tiles;
-    const RangeDesc* ranges;
-    const SegDesc* segs;
-    const EntMeta* emeta;
-    const int32_t* eids;             // global entity id of each owned entity
-    const int32_t* tile_cells;       // subdomain-local cell index
-    const int32_t* cell_items;       // first item of each tile cell
-    const uint32_t* items;
-    const uint32_t* red_list;        // per tile: owned blocks (entity << 22 | row entity), sorted
-    const int64_t* colptr;   // device copy, 1-based
-    const float* xh[3];      // node coordinates split into float hi + lo
-    const float* xl[3];
-    const double* xd;        // node coordinates [n_nodes][dim], FP64
+    const char* rec;         // tile records (16-byte aligned)
+    const int64_t* rec_off;  // [n_tiles + 1] byte offset of each record
+    const float* xf8;        // [n_nodes][8]: x, y, z, 0 as float hi, then the float lo parts
+    const double* xd4;       // [n_nodes][4]: x, y, z, 0 in FP64
+    const double* xd;        // [n_nodes][dim] FP64 (Jacobians recomputed in FP64)
     int32_t dim;
     double* nzval;
     double* f;
     int32_t do_k, do_f, fillzero;
     Physics phys;
     DevStatus* status;
-    int32_t stage_cap;       // staging values the plan guarantees per tile
-    int32_t map_cap;         // map bytes per tile
-    int32_t ent_cap;         // owned entities per tile, max
-    int32_t red_cap;         // reduce lanes (owned blocks) per tile, max
-    int32_t cells_cap;       // cells per tile, max
-    int32_t items_cap;       // items per tile, max
-    int32_t ng_max;          // geometric nodes per cell, max over subdomains
+    int32_t rec_cap;         // record bytes per ring buffer (max over tiles)
+    int32_t node_cap;        // nodes per tile, max
+    int32_t stage_cap;       // staging values per tile, max
     int32_t chunk_bytes;     // bytes of the per-group cell table buffers of the launched kernel
     int32_t groups[MAX_SUB]; // lane groups (cells in flight) per CTA, per subdomain
 };

@@ -219,12 +219,219 @@ int build_problem(const CreateInput& in, HostProblem& hp, Error& err) {
 // ---------------------------------------------------------------------------------------
 // Owner tiles
 //
-// Entities are bucketed by position into compact tiles (a handful of contiguous id runs
-// each). A tile lists every cell touching one of its entities; for every (cell, owned base
-// function j) an item carries k, the position of the cell among the cells of entity(j) in
-// cell order. The kernel writes each contribution to its own staging slot (entity, k, i) and
-// the reduce step sums the slots of an entry in k order: the reference's cell order.
+// Entities are bucketed by position into compact tiles. A tile lists every cell touching one
+// of its entities; for every (cell, owned base function j) an item, and for every row i of
+// an item the staging slot its nc x nc block goes to. The slots of one owned block
+// (entity n, row entity r) are consecutive and ordered by cell (k = position of the cell
+// among the cells of n), so the reduce step sums each entry in the reference's cell order.
+// The tile's data is emitted as one record (layout in common.h).
 // ---------------------------------------------------------------------------------------
+namespace {
+
+inline int32_t pad16(int64_t b) { return (int32_t)((b + 15) & ~15ll); }
+
+struct TileItem {
+    int32_t cell;  // tile cell index (before the per-segment reorder)
+    int32_t j, te, k;
+};
+
+// Build the record of one tile. ents: owned global entity ids; trip: the tile's (sub, cell,
+// j) triples in (sub, cell, j) order. Returns 0 or an error code (internal inconsistency).
+int build_record(const HostProblem& hp, const std::vector<int32_t>& kcount, const std::vector<int32_t>& tile_local,
+                 const int32_t* ents, int32_t n_ent, const uint64_t* trip, int64_t n_trip, std::vector<uint8_t>& out,
+                 int32_t& n_nodes_out, int32_t& stage_out, int32_t& n_cells_out, int32_t& n_items_out) {
+    const int nc = hp.nc;
+    const int bs = (nc * nc + 1) & ~1;
+    const int64_t* cp = hp.colptr.data();
+    // segments, cells, items (cell order)
+    struct Seg { int32_t sub, cell_begin, cell_end, item_begin, item_end; };
+    std::vector<Seg> segs;
+    std::vector<int32_t> cells;       // sub-local cell index
+    std::vector<int32_t> cell_item0;  // first item of each cell
+    std::vector<TileItem> items;
+    std::vector<int32_t> kc(n_ent, 0);
+    for (int64_t q = 0; q < n_trip; ++q) {
+        const int s = (int)(trip[q] >> 40);
+        const int32_t cell = (int32_t)((trip[q] >> 8) & 0xFFFFFFFFull);
+        const int j = (int)(trip[q] & 0xFF);
+        const bool new_cell = q == 0 || (trip[q] >> 8) != (trip[q - 1] >> 8);
+        if (new_cell) {
+            if (segs.empty() || segs.back().sub != s) {
+                if (!segs.empty()) { segs.back().cell_end = (int32_t)cells.size(); segs.back().item_end = (int32_t)items.size(); }
+                segs.push_back(Seg{s, (int32_t)cells.size(), 0, (int32_t)items.size(), 0});
+            }
+            cells.push_back(cell);
+            cell_item0.push_back((int32_t)items.size());
+        }
+        const HostSub& hs = hp.subs[s];
+        const int32_t te = tile_local[hs.ents[(int64_t)cell * hs.nb + j]];
+        items.push_back(TileItem{(int32_t)cells.size() - 1, j, te, kc[te]++});
+    }
+    if (!segs.empty()) { segs.back().cell_end = (int32_t)cells.size(); segs.back().item_end = (int32_t)items.size(); }
+    for (int32_t te = 0; te < n_ent; ++te)
+        if (kc[te] != kcount[ents[te]]) return 1;
+    // owned blocks: z[te] + r
+    std::vector<int32_t> z(n_ent + 1, 0);
+    for (int32_t te = 0; te < n_ent; ++te) {
+        const int64_t n = ents[te];
+        z[te + 1] = z[te] + (int32_t)((cp[nc * n + 1] - cp[nc * n]) / nc);
+    }
+    const int32_t n_red = z[n_ent];
+    std::vector<int32_t> cnt(n_red, 0);
+    // per (item, i): block index or -1
+    auto cell_sub = [&](int32_t c) {
+        int s = 0;
+        while (s + 1 < (int)segs.size() && c >= segs[s].cell_end) ++s;
+        return s;
+    };
+    std::vector<int32_t> item_nb(items.size());
+    std::vector<int64_t> item_row0(items.size() + 1, 0);
+    {
+        int sg = 0;
+        for (size_t it = 0; it < items.size(); ++it) {
+            while (sg + 1 < (int)segs.size() && (int32_t)it >= segs[sg].item_end) ++sg;
+            item_nb[it] = hp.subs[segs[sg].sub].nb;
+            item_row0[it + 1] = item_row0[it] + item_nb[it];
+        }
+    }
+    std::vector<int32_t> row_block(item_row0.back());
+    std::vector<int32_t> row_ord(item_row0.back());  // position among the block's contributions
+    for (size_t it = 0; it < items.size(); ++it) {
+        const TileItem& I = items[it];
+        const int sg = cell_sub(I.cell);
+        const HostSub& hs = hp.subs[segs[sg].sub];
+        const int32_t cell = cells[I.cell];
+        for (int i = 0; i < hs.nb; ++i) {
+            const int r = rank_of(hs, cell, I.j, i);
+            int32_t b = -1;
+            if (r >= 0) {
+                b = z[I.te] + r;
+                row_ord[item_row0[it] + i] = cnt[b]++;
+            }
+            row_block[item_row0[it] + i] = b;
+        }
+    }
+    for (int32_t b = 0; b < n_red; ++b)
+        if (cnt[b] > MAX_ENT_CELLS) return 2;
+    // reduce order: most contributions first (stable in (entity, rank)); slots follow it
+    std::vector<int32_t> ord(n_red);
+    for (int32_t b = 0; b < n_red; ++b) ord[b] = b;
+    std::stable_sort(ord.begin(), ord.end(), [&](int32_t x, int32_t y) { return cnt[x] > cnt[y]; });
+    std::vector<int32_t> base(n_red);
+    std::vector<RecRun> runs;
+    int32_t n_slots = 0;
+    for (int32_t q = 0; q < n_red; ++q) {
+        base[ord[q]] = n_slots;
+        if (runs.empty() || runs.back().count != cnt[ord[q]]) runs.push_back(RecRun{q, cnt[ord[q]], n_slots, 0});
+        n_slots += cnt[ord[q]];
+        if (n_slots > MAX_TILE_SLOTS - 1) return 3;
+    }
+    const int32_t n_runs = (int32_t)runs.size();
+    std::vector<uint32_t> red(n_red);
+    for (int32_t te = 0; te < n_ent; ++te)
+        for (int32_t r = 0; r < z[te + 1] - z[te]; ++r) red[z[te] + r] = ((uint32_t)te << RED_RANK_BITS) | (uint32_t)r;
+    std::vector<uint32_t> red_sorted(n_red);
+    for (int32_t q = 0; q < n_red; ++q) red_sorted[q] = red[ord[q]];
+    // f slots: per owned entity, one per cell in k order
+    std::vector<int32_t> fbase(n_ent + 1, 0);
+    for (int32_t te = 0; te < n_ent; ++te) fbase[te + 1] = fbase[te] + kc[te];
+    const int32_t n_fslots = fbase[n_ent];
+    if (n_fslots > 0xFFFF) return 3;
+    // within a segment, cells with more items first: the lane groups of one warp then run
+    // loops of similar length (the values do not depend on this order)
+    std::vector<int32_t> cell_order(cells.size());
+    for (size_t c = 0; c < cells.size(); ++c) cell_order[c] = (int32_t)c;
+    auto n_items_of = [&](int32_t c) {
+        const int32_t e = c + 1 < (int32_t)cells.size() ? cell_item0[c + 1] : (int32_t)items.size();
+        return e - cell_item0[c];
+    };
+    for (const Seg& g : segs)
+        std::stable_sort(cell_order.begin() + g.cell_begin, cell_order.begin() + g.cell_end,
+                         [&](int32_t x, int32_t y) { return n_items_of(x) > n_items_of(y); });
+    // nodes of the tile, ascending
+    std::vector<int32_t> nodes;
+    for (size_t c = 0; c < cells.size(); ++c) {
+        const HostSub& hs = hp.subs[segs[cell_sub((int32_t)c)].sub];
+        for (int a = 0; a < hs.ng; ++a) nodes.push_back(hs.conn[(int64_t)cells[c] * hs.ng + a]);
+    }
+    std::sort(nodes.begin(), nodes.end());
+    nodes.erase(std::unique(nodes.begin(), nodes.end()), nodes.end());
+    if (nodes.size() > 0xFFFF) return 3;
+    auto local_node = [&](int32_t g) { return (uint16_t)(std::lower_bound(nodes.begin(), nodes.end(), g) - nodes.begin()); };
+    // layout
+    const int32_t n_seg = (int32_t)segs.size(), n_cells = (int32_t)cells.size(), n_items = (int32_t)items.size();
+    RecHead H{};
+    H.n_seg = n_seg; H.n_ent = n_ent; H.n_cells = n_cells; H.n_items = n_items;
+    H.n_red = n_red; H.n_nodes = (int32_t)nodes.size(); H.n_slots = n_slots; H.n_fslots = n_fslots;
+    H.n_runs = n_runs;
+    int64_t o = (int64_t)sizeof(RecHead) + (int64_t)n_seg * 32;
+    H.off_ent = pad16(o); o = H.off_ent + (int64_t)n_ent * 16;
+    H.off_fk = pad16(o); o = H.off_fk + (int64_t)n_ent * 4;
+    H.off_red = pad16(o); o = H.off_red + (int64_t)n_red * 4;
+    H.off_runs = pad16(o); o = H.off_runs + (int64_t)n_runs * 16;
+    H.off_items = pad16(o); o = H.off_items + (int64_t)n_items * 4;
+    H.off_cells = pad16(o); o = H.off_cells + (int64_t)n_cells * 8;
+    std::vector<RecSeg> rsegs(n_seg);
+    for (int32_t g = 0; g < n_seg; ++g) {
+        const HostSub& hs = hp.subs[segs[g].sub];
+        RecSeg& R = rsegs[g];
+        R.sub = segs[g].sub;
+        R.cell_begin = segs[g].cell_begin; R.cell_end = segs[g].cell_end;
+        R.item_begin = segs[g].item_begin; R.item_end = segs[g].item_end;
+        R.conn_off = pad16(o); o = R.conn_off + (int64_t)(R.cell_end - R.cell_begin) * hs.ng * 2;
+        R.slot_off = pad16(o); o = R.slot_off + (int64_t)(R.item_end - R.item_begin) * hs.nb * 2;
+        R.pad = 0;
+    }
+    H.off_nodes = pad16(o); o = H.off_nodes + (int64_t)nodes.size() * 4;
+    H.bytes = pad16(o);
+    if (H.bytes > (1 << 20)) return 3;
+    out.assign(H.bytes, 0);
+    uint8_t* B = out.data();
+    std::memcpy(B, &H, sizeof(RecHead));
+    std::memcpy(B + sizeof(RecHead), rsegs.data(), (size_t)n_seg * 32);
+    for (int32_t te = 0; te < n_ent; ++te) {
+        const int64_t n = ents[te];
+        RecEnt E{cp[nc * n] - 1, (int32_t)(cp[nc * n + 1] - cp[nc * n]), (int32_t)n};
+        std::memcpy(B + H.off_ent + (int64_t)te * 16, &E, 16);
+        const uint32_t fk = (uint32_t)fbase[te] | ((uint32_t)kc[te] << 16);
+        std::memcpy(B + H.off_fk + (int64_t)te * 4, &fk, 4);
+    }
+    std::memcpy(B + H.off_red, red_sorted.data(), (size_t)n_red * 4);
+    std::memcpy(B + H.off_runs, runs.data(), (size_t)n_runs * 16);
+    // cells and items in the reordered cell order
+    int32_t it_out = 0;
+    for (int32_t g = 0; g < n_seg; ++g) {
+        const HostSub& hs = hp.subs[segs[g].sub];
+        const RecSeg& R = rsegs[g];
+        for (int32_t pc = R.cell_begin; pc < R.cell_end; ++pc) {
+            const int32_t c = cell_order[pc];
+            const int32_t i0 = cell_item0[c], i1 = c + 1 < n_cells ? cell_item0[c + 1] : n_items;
+            RecCell C{cells[c], (uint16_t)it_out, (uint16_t)(it_out + i1 - i0)};
+            std::memcpy(B + H.off_cells + (int64_t)pc * 8, &C, 8);
+            uint16_t* cn = (uint16_t*)(B + R.conn_off) + (int64_t)(pc - R.cell_begin) * hs.ng;
+            for (int a = 0; a < hs.ng; ++a) cn[a] = local_node(hs.conn[(int64_t)cells[c] * hs.ng + a]);
+            for (int32_t it = i0; it < i1; ++it, ++it_out) {
+                const TileItem& I = items[it];
+                const uint32_t w = (uint32_t)I.j | ((uint32_t)(fbase[I.te] + I.k) << 16);
+                std::memcpy(B + H.off_items + (int64_t)it_out * 4, &w, 4);
+                uint16_t* sl = (uint16_t*)(B + R.slot_off) + (int64_t)(it_out - R.item_begin) * hs.nb;
+                for (int i = 0; i < hs.nb; ++i) {
+                    const int32_t b = row_block[item_row0[it] + i];
+                    sl[i] = b < 0 ? SLOT_MISS : (uint16_t)(base[b] + row_ord[item_row0[it] + i]);
+                }
+            }
+        }
+    }
+    std::memcpy(B + H.off_nodes, nodes.data(), nodes.size() * 4);
+    n_nodes_out = (int32_t)nodes.size();
+    stage_out = n_slots * bs + n_fslots * nc;
+    n_cells_out = n_cells;
+    n_items_out = n_items;
+    return 0;
+}
+
+}  // namespace
+
 int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error& err) {
     const int nc = hp.nc;
     const int64_t n_ent = hp.n_ent;
@@ -232,7 +439,6 @@ int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error&
     const int64_t* cp = hp.colptr.data();
     int nb_max = 0;
     for (const HostSub& hs : hp.subs) nb_max = std::max(nb_max, hs.nb);
-    plan.nb_max = nb_max;
     // entity "positions" (mean of incident cell centroids) and incident cell counts
     std::vector<double> pos(n_ent * 3, 0.0);
     std::vector<int32_t> kcount(n_ent, 0);
@@ -251,7 +457,7 @@ int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error&
     }
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
     for (int64_t n = 0; n < n_ent; ++n) {
-        if (kcount[n] > MAX_ENT_CELLS) return fail(err, FE_ERR_UNSUPPORTED, "a dof entity belongs to more than 63 cells");
+        if (kcount[n] > MAX_ENT_CELLS) return fail(err, FE_ERR_UNSUPPORTED, "a dof entity belongs to more than 255 cells");
         if (!kcount[n]) continue;
         for (int x = 0; x < dim; ++x) {
             pos[n * 3 + x] /= kcount[n];
@@ -261,14 +467,15 @@ int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error&
     }
     auto nnb_of = [&](int64_t n) { return (int64_t)((cp[nc * n + 1] - cp[nc * n]) / nc); };
     const int bs = (nc * nc + 1) & ~1;
-    auto stage_of = [&](int64_t n) { return ((int64_t)kcount[n] * (nb_max * bs + nc) + 1) & ~1ll; };
-    auto map_of = [&](int64_t n) { return nnb_of(n) * kcount[n]; };
+    // staging values of an entity: an upper bound (every row of every cell gets a slot)
+    auto stage_of = [&](int64_t n) { return (int64_t)kcount[n] * (nb_max * bs + nc); };
     // target entities per tile from the staging capacity
-    double avg_stage = 0;
-    for (int64_t n = 0; n < n_ent; ++n) avg_stage += (double)stage_of(n);
+    double avg_stage = 0, avg_nnb = 0;
+    for (int64_t n = 0; n < n_ent; ++n) {
+        avg_stage += (double)stage_of(n);
+        avg_nnb += (double)nnb_of(n);
+    }
     avg_stage = std::max(1.0, avg_stage / (double)n_ent);
-    double avg_nnb = 0;
-    for (int64_t n = 0; n < n_ent; ++n) avg_nnb += (double)nnb_of(n);
     avg_nnb = std::max(1.0, avg_nnb / (double)n_ent);
     const double target_ent = std::max(1.0, std::min({0.85 * opt.stage_cap / avg_stage, 0.85 * opt.ent_cap,
                                                        0.85 * opt.red_cap / avg_nnb}));
@@ -300,69 +507,37 @@ int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error&
         std::vector<int64_t> cur(bstart.begin(), bstart.end() - 1);
         for (int64_t n = 0; n < n_ent; ++n) order[cur[bucket[n]]++] = (int32_t)n;
     }
-    // tiles: split buckets by capacity; runs of consecutive ids become ranges
+    // tiles: split buckets by capacity
     std::vector<int32_t> tile_of(n_ent), tile_local(n_ent);
-    plan.tiles.clear();
-    plan.ranges.clear();
-    plan.emeta.clear();
-    plan.eids.clear();
+    std::vector<int32_t> eids;              // owned entities, tile after tile
+    std::vector<int64_t> tent = {0};        // tile t owns eids[tent[t] .. tent[t+1])
+    eids.reserve(n_ent);
     for (int64_t b = 0; b < nbk; ++b) {
         int64_t k = bstart[b];
         while (k < bstart[b + 1]) {
-            TileDesc t{};
-            t.range_begin = (int32_t)plan.ranges.size();
-            t.ent_begin = (int32_t)plan.emeta.size();
-            int64_t stage = 0, map = 0, red = 0;
+            int64_t stage = 0, red = 0;
             int32_t ne = 0;
-            const int32_t tid = (int32_t)plan.tiles.size();
+            const int32_t tid = (int32_t)(tent.size() - 1);
             while (k < bstart[b + 1]) {
                 const int64_t n = order[k];
-                const int64_t st = stage_of(n), mp = (map_of(n) + 3) & ~3ll;
-                if (st > opt.stage_cap || mp > opt.map_cap)
+                const int64_t st = stage_of(n);
+                if (st > opt.stage_cap || nnb_of(n) > opt.red_cap)
                     return fail(err, FE_ERR_UNSUPPORTED, "a dof entity's contributions exceed the tile staging capacity");
-                if (ne && (stage + st > opt.stage_cap || map + mp > opt.map_cap || ne + 1 > opt.ent_cap ||
-                           ne + 1 > MAX_TILE_ENTS || red + nnb_of(n) > opt.red_cap))
+                if (ne && (stage + st > opt.stage_cap || ne + 1 > opt.ent_cap || ne + 1 > MAX_TILE_ENTS ||
+                           red + nnb_of(n) > opt.red_cap))
                     break;
-                const int64_t z = (int64_t)(cp[nc * n + nc] - cp[nc * n]);
-                if ((int32_t)plan.ranges.size() > t.range_begin && plan.ranges.back().ent0 + plan.ranges.back().n_ent == n) {
-                    plan.ranges.back().n_ent++;
-                    plan.ranges.back().nz_len += (int32_t)z;
-                } else {
-                    RangeDesc r{};
-                    r.nz0 = cp[nc * n] - 1;
-                    r.ent0 = (int32_t)n;
-                    r.n_ent = 1;
-                    r.nz_len = (int32_t)z;
-                    plan.ranges.push_back(r);
-                }
-                EntMeta m;
-                m.x = (int32_t)stage;
-                m.y = (int32_t)map;
-                m.z = (int32_t)red;
-                m.w = kcount[n] | (int32_t)(nnb_of(n) << 8);
-                plan.emeta.push_back(m);
-                plan.eids.push_back((int32_t)n);
+                eids.push_back((int32_t)n);
                 tile_of[n] = tid;
                 tile_local[n] = ne;
                 stage += st;
-                map += mp;
                 red += nnb_of(n);
                 ++ne;
                 ++k;
             }
-            t.range_end = (int32_t)plan.ranges.size();
-            t.n_ent = ne;
-            t.n_red = (int32_t)red;
-            t.stage_vals = (int32_t)stage;
-            t.map_bytes = (int32_t)map;
-            plan.tiles.push_back(t);
-            plan.max_stage = std::max(plan.max_stage, t.stage_vals);
-            plan.max_map = std::max(plan.max_map, t.map_bytes);
-            plan.max_ent = std::max(plan.max_ent, ne);
-            plan.max_red = std::max(plan.max_red, t.n_red);
+            tent.push_back((int64_t)eids.size());
         }
     }
-    const int64_t n_tiles = (int64_t)plan.tiles.size();
+    const int64_t n_tiles = (int64_t)tent.size() - 1;
     // (sub, cell, j) triples per tile, in (sub, cell, j) order
     std::vector<int64_t> tstart(n_tiles + 1, 0);
     for (const HostSub& hs : hp.subs)
@@ -380,219 +555,165 @@ int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error&
                 }
         }
     }
-    struct TileOut {
-        std::vector<SegDesc> segs;
-        std::vector<int32_t> cells, cell_items;
-        std::vector<uint32_t> items, red;
-        int status = 0;
-    };
-    std::vector<TileOut> outs(n_tiles);
-#pragma omp parallel
-    {
-        std::vector<int32_t> kc;
-#pragma omp for schedule(dynamic, 16)
-        for (int64_t t = 0; t < n_tiles; ++t) {
-            TileOut& o = outs[t];
-            kc.assign(plan.tiles[t].n_ent, 0);
-            for (int64_t q = tstart[t]; q < tstart[t + 1]; ++q) {
-                const int s = (int)(trip[q] >> 40);
-                const int64_t cell = (int64_t)((trip[q] >> 8) & 0xFFFFFFFFull);
-                const int j = (int)(trip[q] & 0xFF);
-                const bool new_cell = q == tstart[t] || (trip[q] >> 8) != (trip[q - 1] >> 8);
-                if (new_cell) {
-                    if (o.segs.empty() || o.segs.back().sub != s) {
-                        if (!o.segs.empty()) o.segs.back().item_end = (int32_t)o.items.size();
-                        SegDesc g{};
-                        g.sub = s;
-                        g.cell_begin = (int32_t)o.cells.size();
-                        o.segs.push_back(g);
-                    }
-                    o.cells.push_back((int32_t)cell);
-                    o.cell_items.push_back((int32_t)o.items.size());
-                    o.segs.back().n_cells++;
-                }
-                const HostSub& hs = hp.subs[s];
-                const int32_t te = tile_local[hs.ents[cell * hs.nb + j]];
-                o.items.push_back(pack_item((uint32_t)j, (uint32_t)te, (uint32_t)kc[te]));
-                kc[te]++;
-            }
-            if (!o.segs.empty()) o.segs.back().item_end = (int32_t)o.items.size();
-            // reduce order: owned blocks by contribution count, most first (stable in (entity, r))
-            {
-                const TileDesc& T = plan.tiles[t];
-                std::vector<int32_t> cnt(T.n_red, 0);
-                for (int64_t q = tstart[t]; q < tstart[t + 1]; ++q) {
-                    const int s = (int)(trip[q] >> 40);
-                    const int64_t cell = (int64_t)((trip[q] >> 8) & 0xFFFFFFFFull);
-                    const int j = (int)(trip[q] & 0xFF);
-                    const HostSub& hs = hp.subs[s];
-                    const int32_t te = tile_local[hs.ents[cell * hs.nb + j]];
-                    const int32_t z = plan.emeta[T.ent_begin + te].z;
-                    for (int i = 0; i < hs.nb; ++i) {
-                        const size_t rq = ((size_t)cell * hs.nb + j) * hs.nb + i;
-                        const int r = hs.wide_rank ? (hs.rank16[rq] == 0xFFFF ? -1 : hs.rank16[rq]) : (hs.rank8[rq] == 255 ? -1 : hs.rank8[rq]);
-                        if (r >= 0) cnt[z + r]++;
-                    }
-                }
-                std::vector<uint32_t> keys(T.n_red);
-                for (int32_t te = 0; te < T.n_ent; ++te) {
-                    const EntMeta m = plan.emeta[T.ent_begin + te];
-                    for (int32_t r = 0; r < (m.w >> 8); ++r) keys[m.z + r] = ((uint32_t)te << 22) | (uint32_t)r;
-                }
-                std::vector<int32_t> ord(T.n_red);
-                for (int32_t q = 0; q < T.n_red; ++q) ord[q] = q;
-                std::stable_sort(ord.begin(), ord.end(), [&](int32_t x, int32_t y) { return cnt[x] > cnt[y]; });
-                o.red.resize(T.n_red);
-                for (int32_t q = 0; q < T.n_red; ++q) o.red[q] = keys[ord[q]];
-            }
-            // within a segment, cells with more owned base functions first: the lane groups of
-            // one warp then run loops of similar length
-            for (SegDesc& g : o.segs) {
-                const int32_t c0 = g.cell_begin, c1 = g.cell_begin + g.n_cells;
-                std::vector<int32_t> idx(g.n_cells);
-                for (int32_t c = 0; c < g.n_cells; ++c) idx[c] = c0 + c;
-                auto cnt = [&](int32_t c) { return (c + 1 < c1 ? o.cell_items[c + 1] : g.item_end) - o.cell_items[c]; };
-                std::stable_sort(idx.begin(), idx.end(), [&](int32_t x, int32_t y) { return cnt(x) > cnt(y); });
-                std::vector<int32_t> cells2, ci2;
-                std::vector<uint32_t> items2;
-                const int32_t ib = o.cell_items[c0];
-                for (int32_t c : idx) {
-                    cells2.push_back(o.cells[c]);
-                    ci2.push_back(ib + (int32_t)items2.size());
-                    const int32_t e0 = o.cell_items[c], e1 = c + 1 < c1 ? o.cell_items[c + 1] : g.item_end;
-                    items2.insert(items2.end(), o.items.begin() + e0, o.items.begin() + e1);
-                }
-                std::copy(cells2.begin(), cells2.end(), o.cells.begin() + c0);
-                std::copy(ci2.begin(), ci2.end(), o.cell_items.begin() + c0);
-                std::copy(items2.begin(), items2.end(), o.items.begin() + ib);
-            }
-            for (int32_t te = 0; te < plan.tiles[t].n_ent; ++te)
-                if (kc[te] != (plan.emeta[plan.tiles[t].ent_begin + te].w & 0xFF)) o.status = 1;
-        }
-    }
-    plan.segs.clear();
-    plan.tile_cells.clear();
-    plan.cell_items.clear();
-    plan.items.clear();
-    plan.red_list.clear();
-    plan.visits = 0;
-    size_t ncl = 0, nit = 0;
-    for (auto& o : outs) {
-        if (o.status) return fail(err, FE_ERR_ARG, "internal: incident cell count mismatch");
-        ncl += o.cells.size();
-        nit += o.items.size();
-    }
-    if (nit >= (size_t)INT32_MAX || ncl >= (size_t)INT32_MAX) return fail(err, FE_ERR_UNSUPPORTED, "plan too large");
-    plan.tile_cells.reserve(ncl);
-    plan.cell_items.reserve(ncl);
-    plan.items.reserve(nit);
+    std::vector<std::vector<uint8_t>> recs(n_tiles);
+    std::vector<int32_t> rn(n_tiles), rs(n_tiles), rc(n_tiles), ri(n_tiles);
+    int status = 0;
+#pragma omp parallel for schedule(dynamic, 16) reduction(max : status)
     for (int64_t t = 0; t < n_tiles; ++t) {
-        TileOut& o = outs[t];
-        const int32_t cb = (int32_t)plan.tile_cells.size(), ib = (int32_t)plan.items.size();
-        plan.tiles[t].seg_begin = (int32_t)plan.segs.size();
-        for (SegDesc g : o.segs) {
-            g.cell_begin += cb;
-            g.item_end += ib;
-            plan.segs.push_back(g);
-        }
-        plan.tiles[t].seg_end = (int32_t)plan.segs.size();
-        for (size_t c = 0; c < o.cells.size(); ++c) {
-            plan.tile_cells.push_back(o.cells[c]);
-            plan.cell_items.push_back(o.cell_items[c] + ib);
-        }
-        plan.items.insert(plan.items.end(), o.items.begin(), o.items.end());
-        plan.tiles[t].cell_begin = cb;
-        plan.tiles[t].n_cells = (int32_t)o.cells.size();
-        plan.tiles[t].item_begin = ib;
-        plan.tiles[t].n_items = (int32_t)o.items.size();
-        plan.max_items = std::max(plan.max_items, (int32_t)o.items.size());
-        plan.tiles[t].red_begin = (int32_t)plan.red_list.size();
-        plan.red_list.insert(plan.red_list.end(), o.red.begin(), o.red.end());
-        plan.visits += (int64_t)o.cells.size();
-        plan.max_cells = std::max(plan.max_cells, (int32_t)o.cells.size());
-        std::vector<uint32_t>().swap(o.items);
+        const int st = build_record(hp, kcount, tile_local, eids.data() + tent[t], (int32_t)(tent[t + 1] - tent[t]),
+                                    trip.data() + tstart[t], tstart[t + 1] - tstart[t], recs[t], rn[t], rs[t], rc[t], ri[t]);
+        status = std::max(status, st);
+    }
+    if (status == 1) return fail(err, FE_ERR_ARG, "internal: incident cell count mismatch");
+    if (status == 2) return fail(err, FE_ERR_UNSUPPORTED, "an owned block has more than 255 contributions");
+    if (status) return fail(err, FE_ERR_UNSUPPORTED, "a tile record exceeds its limits");
+    plan.n_tiles = n_tiles;
+    plan.rec_off.assign(n_tiles + 1, 0);
+    plan.max_rec = plan.max_nodes = plan.max_stage = 0;
+    plan.visits = plan.items = 0;
+    for (int64_t t = 0; t < n_tiles; ++t) {
+        plan.rec_off[t + 1] = plan.rec_off[t] + (int64_t)recs[t].size();
+        plan.max_rec = std::max(plan.max_rec, (int32_t)recs[t].size());
+        plan.max_nodes = std::max(plan.max_nodes, rn[t]);
+        plan.max_stage = std::max(plan.max_stage, rs[t]);
+        plan.visits += rc[t];
+        plan.items += ri[t];
+    }
+    plan.rec.resize(plan.rec_off[n_tiles]);
+#pragma omp parallel for schedule(static)
+    for (int64_t t = 0; t < n_tiles; ++t) {
+        std::memcpy(plan.rec.data() + plan.rec_off[t], recs[t].data(), recs[t].size());
+        std::vector<uint8_t>().swap(recs[t]);
     }
     return FE_OK;
 }
 
-// Every index the kernel derives from the plan stays inside the buffers it addresses: the
-// tile staging (stage_vals), the contribution map (map_bytes), the entity table, the cell
-// tables and the per-cell rank rows. Run once per fe_create; O(items * n_base).
+// ---------------------------------------------------------------------------------------
+// Record check: parses every record the way the kernel does and verifies that each index
+// stays inside the buffer it addresses (record, staging, node list, nzval, f, subdomain
+// arrays) and that the slots are a bijection onto the owned blocks' contributions with
+// the right destinations. Run once per fe_create.
+// ---------------------------------------------------------------------------------------
 int check_plan(const HostProblem& hp, const Plan& pl, Error& err) {
     const int nc = hp.nc;
     const int64_t* cp = hp.colptr.data();
-    const int nbm = pl.nb_max;
-    const int bs = (nc * nc + 1) & ~1;
     int bad = 0;
 #pragma omp parallel for schedule(dynamic, 64) reduction(| : bad)
-    for (int64_t t = 0; t < (int64_t)pl.tiles.size(); ++t) {
-        const TileDesc& T = pl.tiles[t];
-        int64_t stage = 0, map = 0, red = 0;
-        int32_t e = 0;
-        for (int r = T.range_begin; r < T.range_end && !bad; ++r) {
-            const RangeDesc& R = pl.ranges[r];
-            if (R.nz0 != cp[(int64_t)nc * R.ent0] - 1 || R.nz_len != cp[(int64_t)nc * (R.ent0 + R.n_ent)] - cp[(int64_t)nc * R.ent0])
-                bad = 1;
-            for (int q = 0; q < R.n_ent && !bad; ++q, ++e) {
-                const EntMeta m = pl.emeta[T.ent_begin + e];
-                const int64_t n = R.ent0 + q;
-                const int kcnt = m.w & 0xFF, nnb = m.w >> 8;
-                if (pl.eids[T.ent_begin + e] != n || m.x != stage || m.y != map || m.z != red ||
-                    nnb != (cp[nc * n + 1] - cp[nc * n]) / nc)
-                    bad = 1;
-                stage += ((int64_t)kcnt * (nbm * bs + nc) + 1) & ~1ll;
-                map += ((int64_t)nnb * kcnt + 3) & ~3ll;
-                red += nnb;
-            }
+    for (int64_t t = 0; t < pl.n_tiles; ++t) {
+        const int64_t off = pl.rec_off[t], len = pl.rec_off[t + 1] - off;
+        if ((off & 15) || len < (int64_t)sizeof(RecHead) || len > pl.max_rec) { bad = 1; continue; }
+        const uint8_t* B = pl.rec.data() + off;
+        RecHead H;
+        std::memcpy(&H, B, sizeof(RecHead));
+        auto in = [&](int64_t o, int64_t n) { return o >= 0 && (o & 15) == 0 && o + n <= len; };
+        if (H.bytes != len || H.n_seg < 0 || H.n_ent < 0 || H.n_cells < 0 || H.n_items < 0 || H.n_red < 0 ||
+            H.n_nodes < 0 || H.n_nodes > pl.max_nodes || H.n_slots < 0 || H.n_fslots < 0 ||
+            (int64_t)sizeof(RecHead) + (int64_t)H.n_seg * 32 > len || !in(H.off_ent, (int64_t)H.n_ent * 16) ||
+            !in(H.off_fk, (int64_t)H.n_ent * 4) || !in(H.off_red, (int64_t)H.n_red * 4) || H.n_runs < 0 ||
+            H.n_runs > H.n_red || !in(H.off_runs, (int64_t)H.n_runs * 16) ||
+            !in(H.off_items, (int64_t)H.n_items * 4) || !in(H.off_cells, (int64_t)H.n_cells * 8) ||
+            !in(H.off_nodes, (int64_t)H.n_nodes * 4) || H.n_ent > MAX_TILE_ENTS ||
+            (int64_t)H.n_slots * ((nc * nc + 1) & ~1) + (int64_t)H.n_fslots * nc > pl.max_stage) {
+            bad = 1;
+            continue;
         }
-        if (bad || e != T.n_ent || stage != T.stage_vals || map != T.map_bytes || red != T.n_red) { bad = 1; continue; }
-        {
-            std::vector<char> seen(T.n_red, 0);
-            for (int32_t q = 0; q < T.n_red && !bad; ++q) {
-                const uint32_t key = pl.red_list[T.red_begin + q];
-                const int te = (int)(key >> 22), r = (int)(key & ((1u << 22) - 1));
-                if (te >= T.n_ent) { bad = 1; break; }
-                const EntMeta m = pl.emeta[T.ent_begin + te];
-                if (r >= (m.w >> 8) || seen[m.z + r]) { bad = 1; break; }
-                seen[m.z + r] = 1;
-            }
-        }
-        if (T.seg_end > T.seg_begin) {
-            const SegDesc& G0 = pl.segs[T.seg_begin];
-            const SegDesc& G1 = pl.segs[T.seg_end - 1];
-            if (G0.cell_begin != T.cell_begin || G1.cell_begin + G1.n_cells != T.cell_begin + T.n_cells ||
-                pl.cell_items[T.cell_begin] != T.item_begin || G1.item_end != T.item_begin + T.n_items)
+        const RecSeg* S = (const RecSeg*)(B + sizeof(RecHead));
+        const RecEnt* E = (const RecEnt*)(B + H.off_ent);
+        const uint32_t* FK = (const uint32_t*)(B + H.off_fk);
+        const uint32_t* RED = (const uint32_t*)(B + H.off_red);
+        const RecRun* RU = (const RecRun*)(B + H.off_runs);
+        const uint32_t* IT = (const uint32_t*)(B + H.off_items);
+        const RecCell* C = (const RecCell*)(B + H.off_cells);
+        const int32_t* ND = (const int32_t*)(B + H.off_nodes);
+        // entities: column base and length as in colptr; f slots inside the f area
+        for (int32_t e = 0; e < H.n_ent && !bad; ++e) {
+            const int64_t n = E[e].id;
+            if (n < 0 || n >= hp.n_ent || E[e].colbase != cp[nc * n] - 1 || E[e].L != cp[nc * n + 1] - cp[nc * n] ||
+                E[e].colbase + (int64_t)nc * E[e].L > hp.nnz || (int64_t)(FK[e] & 0xFFFF) + (FK[e] >> 16) > H.n_fslots)
                 bad = 1;
         }
-        for (int g = T.seg_begin; g < T.seg_end && !bad; ++g) {
-            const SegDesc& G = pl.segs[g];
-            if (G.sub < 0 || G.sub >= (int)hp.subs.size() || G.n_cells < 1) { bad = 1; break; }
+        // owned blocks: ranks inside the column; runs cover the blocks in order and their slot
+        // ranges are consecutive and cover all slots (the kernel's lookup is restated here)
+        std::vector<int32_t> slot_block(H.n_slots, -1), RB(H.n_red + 1, 0);
+        if (H.n_red > 0 && (H.n_runs < 1 || RU[0].first != 0 || RU[0].base != 0)) bad = 1;
+        for (int32_t u = 0; u < H.n_runs && !bad; ++u) {
+            const int32_t end = u + 1 < H.n_runs ? RU[u + 1].first : H.n_red;
+            if (RU[u].first < 0 || end <= RU[u].first || end > H.n_red || RU[u].count < 0 || RU[u].count > MAX_ENT_CELLS ||
+                (u + 1 < H.n_runs && RU[u + 1].base != RU[u].base + (end - RU[u].first) * RU[u].count)) { bad = 1; break; }
+            for (int32_t q = RU[u].first; q < end; ++q) {
+                RB[q] = RU[u].base + (q - RU[u].first) * RU[u].count;
+                RB[q + 1] = RB[q] + RU[u].count;
+            }
+        }
+        for (int32_t q = 0; q < H.n_red && !bad; ++q) {
+            const int32_t e = (int32_t)(RED[q] >> RED_RANK_BITS), r = (int32_t)(RED[q] & ((1u << RED_RANK_BITS) - 1));
+            if (e >= H.n_ent || (int64_t)nc * r >= E[e].L || RB[q + 1] < RB[q] || RB[q + 1] > H.n_slots) { bad = 1; break; }
+            for (int32_t sl = RB[q]; sl < RB[q + 1]; ++sl) slot_block[sl] = q;
+        }
+        if (bad || RB[H.n_red] != H.n_slots) { bad = 1; continue; }
+        for (int32_t e = 0; e < H.n_nodes && !bad; ++e)
+            if (ND[e] < 0 || ND[e] >= hp.n_nodes) bad = 1;
+        // segments, cells, items, slots
+        std::vector<int32_t> slot_writes(H.n_slots, 0), fslot_writes(H.n_fslots, 0);
+        std::vector<int64_t> slot_cell(H.n_slots, -1);  // (sub, cell) of each slot's contribution
+        int32_t cell_next = 0, item_next = 0;
+        for (int32_t g = 0; g < H.n_seg && !bad; ++g) {
+            const RecSeg& G = S[g];
+            if (G.sub < 0 || G.sub >= (int)hp.subs.size() || G.cell_begin != cell_next || G.cell_end < G.cell_begin ||
+                G.cell_end > H.n_cells || G.item_begin != item_next || G.item_end < G.item_begin || G.item_end > H.n_items) {
+                bad = 1;
+                break;
+            }
             const HostSub& hs = hp.subs[G.sub];
-            for (int c = 0; c < G.n_cells && !bad; ++c) {
-                const int32_t cell = pl.tile_cells[G.cell_begin + c];
-                if (cell < 0 || cell >= hs.n_cells) { bad = 1; break; }
-                const int32_t i0 = pl.cell_items[G.cell_begin + c];
-                const int32_t i1 = c + 1 < G.n_cells ? pl.cell_items[G.cell_begin + c + 1] : G.item_end;
-                if (i1 < i0) { bad = 1; break; }
-                for (int32_t it = i0; it < i1; ++it) {
-                    const uint32_t w = pl.items[it];
-                    const int j = (int)(w & ((1u << ITEM_J_BITS) - 1));
-                    const int te = (int)((w >> ITEM_J_BITS) & ((1u << ITEM_ENT_BITS) - 1));
-                    const int k = (int)(w >> (ITEM_J_BITS + ITEM_ENT_BITS));
-                    if (j >= hs.nb || te >= T.n_ent || pl.eids[T.ent_begin + te] != hs.ents[(int64_t)cell * hs.nb + j]) { bad = 1; break; }
-                    const EntMeta m = pl.emeta[T.ent_begin + te];
-                    const int kcnt = m.w & 0xFF, nnb = m.w >> 8;
-                    if (k >= kcnt) { bad = 1; break; }
+            if (!in(G.conn_off, (int64_t)(G.cell_end - G.cell_begin) * hs.ng * 2) ||
+                !in(G.slot_off, (int64_t)(G.item_end - G.item_begin) * hs.nb * 2)) { bad = 1; break; }
+            const uint16_t* CN = (const uint16_t*)(B + G.conn_off);
+            const uint16_t* SL = (const uint16_t*)(B + G.slot_off);
+            int32_t it_expect = G.item_begin;
+            for (int32_t c = G.cell_begin; c < G.cell_end && !bad; ++c) {
+                const int64_t cell = C[c].cell;
+                if (cell < 0 || cell >= hs.n_cells || C[c].item_begin != it_expect || C[c].item_end < C[c].item_begin ||
+                    C[c].item_end > G.item_end) { bad = 1; break; }
+                it_expect = C[c].item_end;
+                for (int a = 0; a < hs.ng; ++a) {
+                    const int ln = CN[(int64_t)(c - G.cell_begin) * hs.ng + a];
+                    if (ln >= H.n_nodes || ND[ln] != hs.conn[cell * hs.ng + a]) { bad = 1; break; }
+                }
+                for (int32_t it = C[c].item_begin; it < C[c].item_end && !bad; ++it) {
+                    const int j = (int)(IT[it] & 0xFF);
+                    const int32_t fs = (int32_t)(IT[it] >> 16);
+                    if (j >= hs.nb || fs >= H.n_fslots) { bad = 1; break; }
+                    fslot_writes[fs]++;
+                    const int64_t n = hs.ents[cell * hs.nb + j];
                     for (int i = 0; i < hs.nb; ++i) {
-                        const size_t q = ((size_t)cell * hs.nb + j) * hs.nb + i;
-                        const int r = hs.wide_rank ? (hs.rank16[q] == 0xFFFF ? -1 : hs.rank16[q]) : (hs.rank8[q] == 255 ? -1 : hs.rank8[q]);
-                        if (r >= nnb || m.y + (int64_t)r * kcnt + k >= T.map_bytes) { bad = 1; break; }
+                        const uint16_t sl = SL[(int64_t)(it - G.item_begin) * hs.nb + i];
+                        const int r = rank_of(hs, cell, j, i);
+                        if (sl == SLOT_MISS) {
+                            if (r >= 0) { bad = 1; break; }
+                            continue;
+                        }
+                        if (sl >= H.n_slots || r < 0) { bad = 1; break; }
+                        const int32_t q = slot_block[sl];
+                        const int32_t e = (int32_t)(RED[q] >> RED_RANK_BITS);
+                        if (E[e].id != n || (int32_t)(RED[q] & ((1u << RED_RANK_BITS) - 1)) != r) { bad = 1; break; }
+                        slot_writes[sl]++;
+                        slot_cell[sl] = ((int64_t)G.sub << 32) | cell;
                     }
-                    if ((int64_t)m.x + ((int64_t)k * nbm + hs.nb) * bs > T.stage_vals ||
-                        (int64_t)m.x + (int64_t)kcnt * nbm * bs + (int64_t)(k + 1) * nc > T.stage_vals) { bad = 1; break; }
                 }
             }
+            if (it_expect != G.item_end) bad = 1;
+            cell_next = G.cell_end;
+            item_next = G.item_end;
         }
+        if (bad || cell_next != H.n_cells || item_next != H.n_items) { bad = 1; continue; }
+        for (int32_t sl = 0; sl < H.n_slots; ++sl)
+            if (slot_writes[sl] != 1) { bad = 1; break; }
+        // each block sums its contributions in cell order: (sub, cell) increasing along its slots
+        for (int32_t q = 0; q < H.n_red && !bad; ++q)
+            for (int32_t sl = RB[q] + 1; sl < RB[q + 1]; ++sl)
+                if (slot_cell[sl] <= slot_cell[sl - 1]) { bad = 1; break; }
+        for (int32_t fs = 0; fs < H.n_fslots; ++fs)
+            if (fslot_writes[fs] != 1) { bad = 1; break; }
     }
     if (bad) return fail(err, FE_ERR_ARG, "internal: tile plan failed its bounds check");
     return FE_OK;

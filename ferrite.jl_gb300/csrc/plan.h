@@ -40,24 +40,16 @@ struct HostProblem {
 
 struct PlanOptions {
     int32_t stage_cap = 12288;  // staging values per tile (4 bytes each in mixed precision)
-    int32_t map_cap = 16384;    // contribution-map bytes per tile
-    int32_t ent_cap = MAX_TILE_ENTS;
+    int32_t ent_cap = 1024;     // owned entities per tile
     int32_t red_cap = 2048;     // owned blocks (reduce lanes) per tile
 };
 
 struct Plan {
-    std::vector<TileDesc> tiles;
-    std::vector<RangeDesc> ranges;
-    std::vector<SegDesc> segs;
-    std::vector<EntMeta> emeta;
-    std::vector<int32_t> eids;
-    std::vector<int32_t> tile_cells;
-    std::vector<int32_t> cell_items;
-    std::vector<uint32_t> items;
-    std::vector<uint32_t> red_list;
-    int32_t nb_max = 0;
-    int32_t max_stage = 0, max_map = 0, max_ent = 0, max_cells = 0, max_red = 0, max_items = 0;
-    int64_t visits = 0;
+    std::vector<uint8_t> rec;       // tile records, concatenated (each 16-byte aligned)
+    std::vector<int64_t> rec_off;   // [n_tiles + 1] byte offsets
+    int64_t n_tiles = 0;
+    int32_t max_rec = 0, max_nodes = 0, max_stage = 0;
+    int64_t visits = 0, items = 0;
 };
 
 struct Error {
@@ -80,5 +72,11 @@ struct CreateInput {
 int build_problem(const CreateInput& in, HostProblem& hp, Error& err);
 int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error& err);
 int check_plan(const HostProblem& hp, const Plan& plan, Error& err);
+// rank of entity(i) among the row entities of entity(j)'s columns for cell k of sub s, or -1
+inline int rank_of(const HostSub& hs, int64_t k, int j, int i) {
+    const size_t q = ((size_t)k * hs.nb + j) * hs.nb + i;
+    if (hs.wide_rank) return hs.rank16[q] == 0xFFFF ? -1 : hs.rank16[q];
+    return hs.rank8[q] == 255 ? -1 : hs.rank8[q];
+}
 
 }  // namespace fe

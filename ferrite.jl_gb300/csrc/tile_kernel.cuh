@@ -1,20 +1,21 @@
 // tile_kernel.cuh -- the owner-tile assembly kernel.
 //
-// One CTA assembles one tile: the nzval columns (and f entries) of a compact set of dof
-// entities, written exactly once.
-//   0. reference shape tables staged into shared memory with a TMA bulk copy
-//      (cp.async.bulk + mbarrier); the tile's entity table; an empty contribution map.
-//   1. for every subdomain segment and chunk of the tile's cells:
-//      A. one thread per (cell, quadrature point): Jacobian from the node coordinates
-//         (float hi+lo split, so cell-size differences keep FP32 relative accuracy), detJ,
-//         J^-1 and sqrt(detJ w)-scaled physical gradients -> a shared-memory table, points
-//         taken in pairs so one FFMA2 serves two points. Cells whose Jacobian condition
-//         number exceeds a threshold are redone in FP64.
-//      B. one lane group per cell, lane i = row base function, its table row kept in
-//         registers: for every owned base function j of the cell, the nc x nc block
-//         Ke[(i,:),(j,:)] (and fe_j on lane j) goes to its own staging slot
-//         (entity(j), k, i), k = position of the cell among the entity's cells.
-//   2. reduce: one lane per owned (entity, row entity) block sums its slots in k order
+// A persistent CTA assembles tiles t = blockIdx.x, + gridDim.x, ...: each tile is the nzval
+// columns (and f entries) of a compact set of dof entities, written exactly once. A tile's
+// plan data is one contiguous record (common.h), so the CTA streams it:
+//   pipeline. While tile t is computed, the record of tile t + 2G arrives by one TMA bulk
+//      copy (cp.async.bulk + mbarrier) and the node coordinates of tile t + G are gathered
+//      into shared memory (cp.async); the reference shape tables are copied once per CTA.
+//   1. for every subdomain segment of the tile, one lane group per cell:
+//      A. lane q = quadrature point: Jacobian from the node coordinates (float hi+lo split,
+//         so cell-size differences keep FP32 relative accuracy), detJ, J^-1 and
+//         sqrt(detJ w)-scaled physical gradients -> the group's shared-memory table, points
+//         paired so one FFMA2 serves two points. Cells whose Jacobian condition number
+//         exceeds a threshold are redone in FP64.
+//      B. lane i = row base function, its table row kept in registers: for every owned
+//         base function j of the cell, the nc x nc block Ke[(i,:),(j,:)] (and fe_j on lane
+//         j) goes to the staging slot the plan assigned to it.
+//   2. reduce: one lane per owned (entity, row entity) block sums its consecutive slots
 //      (cell order, compensated FP32 pair = FP64-class), rounds to FP64 and stores it.
 // No atomics, no coloring, bitwise reproducible; the summation order of each entry is the
 // reference's own cell order.
@@ -192,45 +193,23 @@ __device__ __forceinline__ void neo_hooke_point(R mu, R lam, const R* H, R* out)
 }
 
 // ---------------------------------------------------------------------------------------
-// per-CTA shared memory views
+// per-CTA shared memory
 // ---------------------------------------------------------------------------------------
-template <typename Real>
-struct Smem {
-    Real* stage;     // [stage_cap] block and f contributions, one slot each
-    uint8_t* map;    // [map_cap] row function i of each (entity, row entity, k), 0xFF = none
-    int4* emeta;     // [ent_cap] EntMeta of the owned entities
-    int* eid;        // [ent_cap] their global ids
-    unsigned long long* red_mask;  // [red_cap] which k hold a contribution, per owned block
-    uint32_t* red;       // [red_cap] the tile's reduce order (prefetched)
-    int4* col;           // [ent_cap] (colbase lo, colbase hi, column length, -) per owned entity
-    uint32_t* items;     // [items_cap] the tile's items (prefetched)
-    int* cells;          // [cells_cap] the tile's cells (subdomain-local ids)
-    int* citems;         // [cells_cap] first item of each cell, relative to the tile
-    int* conn;           // [cells_cap][ng_max] node ids of each cell
-    Real* shape;     // staged reference tables of all subdomains
-    char* chunk;     // per-chunk cell tables
-};
+constexpr int REC_RING = 3;     // records in flight: tile t (computing), t + G, t + 2G
+constexpr int NODE_BYTES = 32;  // gathered coordinates per node (two 16-byte halves)
 
-// Shared-memory layout of a tile CTA, computed in one place for the kernel and the host.
+// Shared-memory layout of a CTA, computed in one place for the kernel and the host.
 struct SmemLayout {
-    int shape, stage, map, emeta, eid, red_mask, red, col, items, cells, citems, conn, chunk;
+    int shape, rec, coords, stage, chunk;
 };
 __host__ __device__ inline int pad16i(int b) { return (b + 15) & ~15; }
 __host__ __device__ inline SmemLayout smem_layout(const KernelArgs& a, int shape_bytes, int real_bytes) {
     SmemLayout L;
     int o = 0;
     L.shape = o; o += pad16i(shape_bytes);
+    L.rec = o; o += REC_RING * pad16i(a.rec_cap);
+    L.coords = o; o += 2 * a.node_cap * NODE_BYTES;
     L.stage = o; o += pad16i(a.stage_cap * real_bytes);
-    L.map = o; o += pad16i(a.map_cap);
-    L.emeta = o; o += a.ent_cap * 16;
-    L.eid = o; o += pad16i(a.ent_cap * 4);
-    L.red_mask = o; o += pad16i(a.red_cap * 8);
-    L.red = o; o += pad16i(a.red_cap * 4);
-    L.col = o; o += a.ent_cap * 16;
-    L.items = o; o += pad16i(a.items_cap * 4);
-    L.cells = o; o += pad16i(a.cells_cap * 4);
-    L.citems = o; o += pad16i(a.cells_cap * 4);
-    L.conn = o; o += pad16i(a.cells_cap * a.ng_max * 4);
     L.chunk = o;
     return L;
 }
@@ -279,127 +258,127 @@ __host__ __device__ inline int shape_block_bytes(int nq, int nb, int ng, int dim
            pad16(nq * ng * dim * (int)sizeof(Real));
 }
 
+
 // ---------------------------------------------------------------------------------------
-// phase A: geometry of one cell at one pair of quadrature points (q0 = 2p, q1 = 2p + 1)
+// geometry of one cell by its lane group: lane q = quadrature point (NQ <= GS, NG <= GS).
+// Node coordinates are loaded once per node (lane k loads node k) and shared with shuffles.
+// Results go to the q-paired table layout; a padded point (odd NQ) is written as zeros.
 // ---------------------------------------------------------------------------------------
 template <int K, int NQ, int PHYS, typename Real>
-__device__ __forceinline__ void geometry_pair(const KernelArgs& a, const SubDev& sd, const Real* w_s, const Real* N_s,
-                                              const Real* dN_s, const Real* dM_s, int cell, const int* cn, int p, Real* tb) {
+__device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev& sd, const Real* w_s, const Real* N_s,
+                                               const Real* dN_s, const Real* dM_s, int cell, const uint16_t* cn,
+                                               const char* xs, const int32_t* nodes, int lane, unsigned gmask, int gbase,
+                                               Real* tb) {
     using E = ElemT<K>;
     using CT = CellTable<K, NQ, PHYS, Real>;
-    using P = typename Pair<Real>::type;
     constexpr int NB = E::NB, NG = E::NG, DIM = E::DIM;
+    static_assert(NQ <= E::GS && NG <= E::GS, "one lane per point and per node");
     Real* grad = tb;
     Real* sq = tb + CT::GRAD;
     Real* cellp = sq + CT::SQ;
     Real* neo = cellp + 4;
-    const int nq = (2 * p + 1 < NQ) ? 2 : 1;
-    // node offsets from node 0 (float hi/lo split keeps them accurate to FP32 relative)
+    // node offsets from node 0, shared through the group (coordinates: NODE_BYTES per node)
     Real off[NG][DIM];
-    const int n0 = cn[0];
     if constexpr (sizeof(Real) == 4) {
-        float h0[DIM], l0[DIM];
+        const int ln = cn[lane < NG ? lane : 0];
+        const float4 h4 = *(const float4*)(xs + ln * NODE_BYTES);
+        const float4 l4 = *(const float4*)(xs + ln * NODE_BYTES + 16);
+        const float h[3] = {h4.x, h4.y, h4.z}, l[3] = {l4.x, l4.y, l4.z};
+        float o[DIM];
         #pragma unroll
-        for (int x = 0; x < DIM; ++x) { h0[x] = __ldg(a.xh[x] + n0); l0[x] = __ldg(a.xl[x] + n0); }
-        #pragma unroll
-        for (int k = 1; k < NG; ++k) {
-            const int nk = cn[k];
-            #pragma unroll
-            for (int x = 0; x < DIM; ++x) off[k][x] = (__ldg(a.xh[x] + nk) - h0[x]) + (__ldg(a.xl[x] + nk) - l0[x]);
+        for (int x = 0; x < DIM; ++x) {
+            const float h0 = __shfl_sync(gmask, h[x], gbase), l0 = __shfl_sync(gmask, l[x], gbase);
+            o[x] = (h[x] - h0) + (l[x] - l0);
         }
+        #pragma unroll
+        for (int k = 0; k < NG; ++k)
+            #pragma unroll
+            for (int x = 0; x < DIM; ++x) off[k][x] = __shfl_sync(gmask, o[x], gbase + k);
     } else {
-        double x0[DIM];
+        const double* x0 = (const double*)(xs + cn[0] * NODE_BYTES);
         #pragma unroll
-        for (int x = 0; x < DIM; ++x) x0[x] = a.xd[(int64_t)n0 * a.dim + x];
-        #pragma unroll
-        for (int k = 1; k < NG; ++k) {
-            const int nk = cn[k];
+        for (int k = 0; k < NG; ++k) {
+            const double* xk = (const double*)(xs + cn[k] * NODE_BYTES);
             #pragma unroll
-            for (int x = 0; x < DIM; ++x) off[k][x] = a.xd[(int64_t)nk * a.dim + x] - x0[x];
+            for (int x = 0; x < DIM; ++x) off[k][x] = xk[x] - x0[x];
         }
     }
-    Real Ji[2][DIM * DIM], sc[2];
+    if (lane >= NQ) return;
+    const int q = lane;
+    Real J[DIM * DIM];
     #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        sc[h] = Real(0);
+    for (int t = 0; t < DIM * DIM; ++t) J[t] = Real(0);
+    #pragma unroll
+    for (int k = 1; k < NG; ++k)
         #pragma unroll
-        for (int t = 0; t < DIM * DIM; ++t) Ji[h][t] = Real(0);
-        if (h >= nq) continue;
-        const int q = 2 * p + h;
-        Real J[DIM * DIM];
-        #pragma unroll
-        for (int t = 0; t < DIM * DIM; ++t) J[t] = Real(0);
-        #pragma unroll
-        for (int k = 1; k < NG; ++k)
+        for (int x = 0; x < DIM; ++x)
             #pragma unroll
-            for (int x = 0; x < DIM; ++x)
-                #pragma unroll
-                for (int b = 0; b < DIM; ++b) J[x * DIM + b] += off[k][x] * dM_s[(q * NG + k) * DIM + b];
-        Real dt = Mat<Real, DIM>::det(J);
-        bool bad = !(dt > Real(0));
-        if (!bad) Mat<Real, DIM>::inv(J, dt, Ji[h]);
-        if constexpr (sizeof(Real) == 4) {
-            // FP64 Jacobian for flagged cells: Frobenius condition estimate
-            float nJ = 0, nJi = 0;
+            for (int b = 0; b < DIM; ++b) J[x * DIM + b] += off[k][x] * dM_s[(q * NG + k) * DIM + b];
+    Real dt = Mat<Real, DIM>::det(J);
+    Real Ji[DIM * DIM];
+    bool bad = !(dt > Real(0));
+    if (!bad) Mat<Real, DIM>::inv(J, dt, Ji);
+    if constexpr (sizeof(Real) == 4) {
+        float nJ = 0, nJi = 0;
+        if (!bad) {
+            #pragma unroll
+            for (int t = 0; t < DIM * DIM; ++t) { nJ += J[t] * J[t]; nJi += Ji[t] * Ji[t]; }
+        }
+        if (bad || nJ * nJi > a.phys.cond_threshold * a.phys.cond_threshold * DIM * DIM) {
+            double Jd[DIM * DIM], Jid[DIM * DIM];
+            #pragma unroll
+            for (int t = 0; t < DIM * DIM; ++t) Jd[t] = 0.0;
+            const int n0 = nodes[cn[0]];
+            double x0[DIM];
+            #pragma unroll
+            for (int x = 0; x < DIM; ++x) x0[x] = a.xd[(int64_t)n0 * a.dim + x];
+            for (int k = 1; k < NG; ++k) {
+                const int nk = nodes[cn[k]];
+                for (int x = 0; x < DIM; ++x) {
+                    const double o = a.xd[(int64_t)nk * a.dim + x] - x0[x];
+                    for (int b = 0; b < DIM; ++b) Jd[x * DIM + b] += o * sd.dM_d[(q * NG + k) * DIM + b];
+                }
+            }
+            const double dtd = Mat<double, DIM>::det(Jd);
+            bad = !(dtd > 0.0);
             if (!bad) {
+                Mat<double, DIM>::inv(Jd, dtd, Jid);
                 #pragma unroll
-                for (int t = 0; t < DIM * DIM; ++t) { nJ += J[t] * J[t]; nJi += Ji[h][t] * Ji[h][t]; }
+                for (int t = 0; t < DIM * DIM; ++t) Ji[t] = (float)Jid[t];
             }
-            if (bad || nJ * nJi > a.phys.cond_threshold * a.phys.cond_threshold * DIM * DIM) {
-                double Jd[DIM * DIM], Jid[DIM * DIM];
-                #pragma unroll
-                for (int t = 0; t < DIM * DIM; ++t) Jd[t] = 0.0;
-                double x0[DIM];
-                #pragma unroll
-                for (int x = 0; x < DIM; ++x) x0[x] = a.xd[(int64_t)n0 * a.dim + x];
-                for (int k = 1; k < NG; ++k) {
-                    const int nk = cn[k];
-                    for (int x = 0; x < DIM; ++x) {
-                        const double o = a.xd[(int64_t)nk * a.dim + x] - x0[x];
-                        for (int b = 0; b < DIM; ++b) Jd[x * DIM + b] += o * sd.dM_d[(q * NG + k) * DIM + b];
-                    }
-                }
-                const double dtd = Mat<double, DIM>::det(Jd);
-                bad = !(dtd > 0.0);
-                if (!bad) {
-                    Mat<double, DIM>::inv(Jd, dtd, Jid);
-                    #pragma unroll
-                    for (int t = 0; t < DIM * DIM; ++t) Ji[h][t] = (float)Jid[t];
-                }
-                dt = (float)dtd;
-                if (q == 0) atomicAdd(&a.status->flagged, 1u);
-            }
+            dt = (float)dtd;
+            if (q == 0) atomicAdd(&a.status->flagged, 1u);
         }
-        if (bad) {
-            record_detj(a.status, sd.cellid[cell], (float)dt);
-            dt = Real(0);
-            #pragma unroll
-            for (int t = 0; t < DIM * DIM; ++t) Ji[h][t] = Real(0);
-        }
-        sc[h] = sqrt(dt * w_s[q]);
     }
-    *(P*)(sq + 2 * p) = P{sc[0], sc[1]};
-    Real H[2][9];
-    #pragma unroll
-    for (int h = 0; h < 2; ++h)
+    if (bad) {
+        record_detj(a.status, sd.cellid[cell], (float)dt);
+        dt = Real(0);
         #pragma unroll
-        for (int t = 0; t < 9; ++t) H[h][t] = Real(0);
+        for (int t = 0; t < DIM * DIM; ++t) Ji[t] = Real(0);
+    }
+    const Real s = sqrt(dt * w_s[q]);
+    const int p = q >> 1, hh = q & 1;
+    const bool pad = (NQ & 1) && q == NQ - 1;
+    sq[2 * p + hh] = s;
+    if (pad) sq[2 * p + 1] = Real(0);
+    Real H[9];
+    #pragma unroll
+    for (int t = 0; t < 9; ++t) H[t] = Real(0);
     #pragma unroll
     for (int i = 0; i < NB; ++i) {
-        Real g[2][3];
-        Real nn[2];
+        Real g[3] = {0, 0, 0};
         #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int q = min(2 * p + h, NQ - 1);
+        for (int b = 0; b < DIM; ++b)
             #pragma unroll
-            for (int b = 0; b < 3; ++b) g[h][b] = Real(0);
-            #pragma unroll
-            for (int b = 0; b < DIM; ++b)
-                #pragma unroll
-                for (int c = 0; c < DIM; ++c) g[h][b] += dN_s[(q * NB + i) * DIM + c] * Ji[h][c * DIM + b];
-            nn[h] = N_s[q * NB + i];
-        }
+            for (int c = 0; c < DIM; ++c) g[b] += dN_s[(q * NB + i) * DIM + c] * Ji[c * DIM + b];
+        Real* o = grad + (p * NB + i) * 8 + hh;
+        o[0] = g[0] * s;
+        o[2] = g[1] * s;
+        o[4] = g[2] * s;
+        o[6] = N_s[q * NB + i] * s;
+        if (pad) { o[1] = Real(0); o[3] = Real(0); o[5] = Real(0); o[7] = Real(0); }
         if constexpr (PHYS == PHYS_NEO) {
+            // H = grad u = sum_i u_i (x) gradN_i (function_gradient, common_values.jl:217-227)
             const int64_t e3 = (int64_t)sd.ents[(int64_t)cell * NB + i] * 3;
             #pragma unroll
             for (int c = 0; c < 3; ++c) {
@@ -407,18 +386,11 @@ __device__ __forceinline__ void geometry_pair(const KernelArgs& a, const SubDev&
                 if constexpr (sizeof(Real) == 4) uc = a.phys.u_f[e3 + c];
                 else uc = a.phys.u_d[e3 + c];
                 #pragma unroll
-                for (int h = 0; h < 2; ++h)
-                    #pragma unroll
-                    for (int J2 = 0; J2 < 3; ++J2) H[h][c * 3 + J2] += uc * g[h][J2];
+                for (int J2 = 0; J2 < 3; ++J2) H[c * 3 + J2] += uc * g[J2];
             }
         }
-        P* o = (P*)(grad + (p * NB + i) * 8);
-        o[0] = P{g[0][0] * sc[0], g[1][0] * sc[1]};
-        o[1] = P{g[0][1] * sc[0], g[1][1] * sc[1]};
-        o[2] = P{g[0][2] * sc[0], g[1][2] * sc[1]};
-        o[3] = P{nn[0] * sc[0], nn[1] * sc[1]};
     }
-    if (p == 0) {
+    if (q == 0) {
         Real scale = Real(1);
         if (a.phys.scale_f) {
             if constexpr (sizeof(Real) == 4) scale = a.phys.scale_f[sd.cellid[cell]];
@@ -432,19 +404,15 @@ __device__ __forceinline__ void geometry_pair(const KernelArgs& a, const SubDev&
             cellp[1] = (Real)a.phys.p1;
         }
     }
-    if constexpr (PHYS == PHYS_NEO) {
-        #pragma unroll
-        for (int h = 0; h < 2; ++h)
-            if (h < nq) neo_hooke_point<Real>((Real)a.phys.p0, (Real)a.phys.p1, H[h], neo + (2 * p + h) * NEO_EXTRA);
-    }
+    if constexpr (PHYS == PHYS_NEO) neo_hooke_point<Real>((Real)a.phys.p0, (Real)a.phys.p1, H, neo + q * NEO_EXTRA);
 }
 
 // ---------------------------------------------------------------------------------------
 // phase B: the blocks of one cell into its owned columns; lane i = row base function
 // ---------------------------------------------------------------------------------------
 template <int K, int NQ, int PHYS, typename Real>
-__device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& sd, const Smem<Real>& sm, const Real* tb,
-                                            int cell, int i, int it0, int it1) {
+__device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& sd, const char* R, const uint16_t* slot_rows,
+                                            Real* stage, int f_off, const Real* tb, int cell, int i, int it0, int it1) {
     using E = ElemT<K>;
     using CT = CellTable<K, NQ, PHYS, Real>;
     using P = typename Pair<Real>::type;
@@ -456,6 +424,7 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
     const Real* sq = tb + CT::GRAD;
     const Real* cellp = sq + CT::SQ;
     const Real* neo = cellp + 4;
+    const uint32_t* items = (const uint32_t*)(R + ((const RecHead*)R)->off_items);
     P gi[CACHE ? NQP : 1][4];
     if constexpr (CACHE) {
         #pragma unroll
@@ -463,39 +432,11 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
             #pragma unroll
             for (int c = 0; c < 4; ++c) gi[p][c] = *(const P*)(grad + (p * NB + i) * 8 + 2 * c);
     }
-    // this lane's rank row: the rank of entity(i) in the columns of every entity(j) of the cell
-    constexpr int RW8 = (NB + 7) / 8, RW16 = (NB + 3) / 4;
-    unsigned long long rrow[RW8 > RW16 ? RW8 : RW16];
-    if (sd.rank8) {
-        const unsigned long long* rp = (const unsigned long long*)(sd.rank8 + ((int64_t)cell * NB + i) * (8 * RW8));
-        #pragma unroll
-        for (int t = 0; t < RW8; ++t) rrow[t] = __ldg(rp + t);
-    } else {
-        const unsigned long long* rp = (const unsigned long long*)(sd.rank16 + ((int64_t)cell * NB + i) * (4 * RW16));
-        #pragma unroll
-        for (int t = 0; t < RW16; ++t) rrow[t] = __ldg(rp + t);
-    }
     for (int it = it0; it < it1; ++it) {
-        const uint32_t word = sm.items[it];
-        const int j = (int)(word & ((1u << ITEM_J_BITS) - 1));
-        const int tent = (int)((word >> ITEM_J_BITS) & ((1u << ITEM_ENT_BITS) - 1));
-        const int kk = (int)(word >> (ITEM_J_BITS + ITEM_ENT_BITS));
-        int rank;
-        if (sd.rank8) {
-            unsigned long long w = rrow[0];
-            #pragma unroll
-            for (int t = 1; t < RW8; ++t)
-                if (t == (j >> 3)) w = rrow[t];
-            const int v = (int)((w >> ((j & 7) * 8)) & 0xFF);
-            rank = v == 0xFF ? -1 : v;
-        } else {
-            unsigned long long w = rrow[0];
-            #pragma unroll
-            for (int t = 1; t < RW16; ++t)
-                if (t == (j >> 2)) w = rrow[t];
-            const int v = (int)((w >> ((j & 3) * 16)) & 0xFFFF);
-            rank = v == 0xFFFF ? -1 : v;
-        }
+        const uint32_t word = items[it];
+        const int j = (int)(word & 0xFF);
+        const int fslot = (int)(word >> 16);
+        const int slot = slot_rows[(it - it0) * NB + i];
         Real Kb[NC_MAX * NC_MAX];
         Real fe[NC_MAX];
         #pragma unroll
@@ -581,11 +522,9 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
                                   nj * (Real)a.phys.body[x]);
             }
         }
-        // one staging slot per (entity, k, i): no two lanes of the CTA ever write the same one
-        const int4 m = sm.emeta[tent];
-        const int kcnt = m.w & 0xFF;
+        // the plan gives every (item, row) its own staging slot: no two lanes write the same one
         if (a.do_k) {
-            if (rank < 0) {
+            if (slot == SLOT_MISS) {
                 #pragma unroll
                 for (int x = 0; x < NC_MAX; ++x)
                     #pragma unroll
@@ -593,7 +532,7 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
                         if (x < nc && y < nc && Kb[x * NC_MAX + y] != Real(0))
                             record_miss(a.status, sd.cellid[cell], i * nc + x, j * nc + y);
             } else {
-                Real* dst = sm.stage + m.x + (kk * a.nb_max + i) * a.bs;
+                Real* dst = stage + slot * a.bs;
                 if (nc == 1) {
                     dst[0] = Kb[0];
                 } else {
@@ -609,12 +548,10 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
                     #pragma unroll
                     for (int t = 0; t < (NC_MAX * NC_MAX + 1) / 2; ++t) ((P*)dst)[t] = P{col[2 * t], col[2 * t + 1]};
                 }
-                sm.map[m.y + rank * kcnt + kk] = (uint8_t)i;
-                atomicOr(&sm.red_mask[m.z + rank], 1ull << kk);
             }
         }
         if (a.do_f && i == j) {
-            Real* dst = sm.stage + m.x + kcnt * a.nb_max * a.bs + kk * nc;
+            Real* dst = stage + f_off + fslot * nc;
             #pragma unroll
             for (int x = 0; x < NC_MAX; ++x)
                 if (x < nc) dst[x] = fe[x];
@@ -623,45 +560,49 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
 }
 
 // ---------------------------------------------------------------------------------------
-// the cells of one subdomain in a tile, in chunks that fit the table memory
+// the cells of one subdomain in a tile
 // ---------------------------------------------------------------------------------------
 template <int K, int NQ, int PHYS, typename Real>
-__device__ __forceinline__ void process_segment(const KernelArgs& a, const SubDev& sd, const Real* shp, const SegDesc& g,
-                                                const TileDesc& T, const Smem<Real>& sm) {
+__device__ __forceinline__ void process_segment(const KernelArgs& a, const SubDev& sd, const Real* shp, const RecSeg& g,
+                                                const char* R, const char* xs, Real* stage, char* chunk) {
     using E = ElemT<K>;
     using CT = CellTable<K, NQ, PHYS, Real>;
-    constexpr int NB = E::NB, DIM = E::DIM, GS = E::GS;
+    constexpr int NB = E::NB, NG = E::NG, DIM = E::DIM, GS = E::GS;
     const Real* w_s = shp;
     const Real* N_s = (const Real*)((const char*)w_s + pad16(NQ * sizeof(Real)));
     const Real* dN_s = (const Real*)((const char*)N_s + pad16(NQ * NB * sizeof(Real)));
     const Real* dM_s = (const Real*)((const char*)dN_s + pad16(NQ * NB * DIM * sizeof(Real)));
+    const RecHead* H = (const RecHead*)R;
+    const RecCell* cells = (const RecCell*)(R + H->off_cells);
+    const int32_t* nodes = (const int32_t*)(R + H->off_nodes);
+    const uint16_t* conn = (const uint16_t*)(R + g.conn_off);
+    const uint16_t* slots = (const uint16_t*)(R + g.slot_off);
+    const int f_off = H->n_slots * a.bs;
     const int tid = threadIdx.x;
-    const int tb0 = g.cell_begin - T.cell_begin, item_end = g.item_end - T.item_begin;
     // one lane group per cell (round robin), each with a private table buffer: the group
-    // computes its cell's geometry (lanes = quadrature point pairs), syncs within the warp,
-    // then its lanes (= row base functions) compute and stage the blocks
-    constexpr int NQP = CT::NQP;
+    // computes its cell's geometry (lane = quadrature point), syncs within the warp, then
+    // its lanes (= row base functions) compute and stage the blocks
     const int ngrp = a.groups[g.sub];  // <= THREADS / GS, bounded by the table memory
     const int lane = tid % GS, grp = tid / GS;
     const unsigned gmask = GS >= 32 ? 0xFFFFFFFFu : (((1u << GS) - 1u) << ((tid & 31) / GS * GS));
-    Real* tb = (Real*)(sm.chunk + grp * CT::BYTES);
-    for (int c = grp < ngrp ? grp : g.n_cells; c < g.n_cells; c += ngrp) {
-        const int ts = tb0 + c;
-        const int cell = sm.cells[ts];
-        for (int pp = lane; pp < NQP; pp += GS) geometry_pair<K, NQ, PHYS, Real>(a, sd, w_s, N_s, dN_s, dM_s, cell, sm.conn + ts * a.ng_max, pp, tb);
+    Real* tb = (Real*)(chunk + grp * CT::BYTES);
+    const int n_cells = g.cell_end - g.cell_begin;
+    for (int c = grp < ngrp ? grp : n_cells; c < n_cells; c += ngrp) {
+        const RecCell ce = cells[g.cell_begin + c];
+        geometry_lanes<K, NQ, PHYS, Real>(a, sd, w_s, N_s, dN_s, dM_s, ce.cell, conn + c * NG, xs, nodes, lane, gmask,
+                                          (tid & 31) - lane, tb);
         __syncwarp(gmask);
-        if (lane < NB) {
-            const int it0 = sm.citems[ts];
-            const int it1 = (c + 1 < g.n_cells) ? sm.citems[ts + 1] : item_end;
-            cell_blocks<K, NQ, PHYS, Real>(a, sd, sm, tb, cell, lane, it0, it1);
-        }
+        if (lane < NB)
+            cell_blocks<K, NQ, PHYS, Real>(a, sd, R, slots + (ce.item_begin - g.item_begin) * NB, stage, f_off, tb, ce.cell,
+                                           lane, ce.item_begin, ce.item_end);
         __syncwarp(gmask);  // the next cell overwrites the table
     }
 }
 
 // ---------------------------------------------------------------------------------------
-// reduce: one lane per owned (entity n, row entity r) block. The block's contributions are
-// summed in cell order (k), compensated, rounded to FP64 and stored: nc columns of nc rows.
+// reduce: one lane per owned (entity n, row entity r) block. The block's contributions sit
+// in consecutive slots in cell order; they are summed compensated, rounded to FP64 and
+// stored: nc columns of nc rows.
 // ---------------------------------------------------------------------------------------
 // Packed compensated sum over two entries (FP32 pairs); exact TwoSum per component.
 __device__ __forceinline__ float2 fsub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
@@ -673,28 +614,32 @@ __device__ __forceinline__ void acc_add2(float2& hi, float2& lo, float2 x) {
     lo = __fadd2_rn(lo, e);
 }
 
-// One lane per owned (entity, row entity) block, in the plan's order (most contributions
-// first, so the lanes of a warp run loops of equal length; the lane does not change any
-// value). The block's slots are summed in k order (cell order) and the block is stored.
+// Blocks are taken in the plan's order (most contributions first, so the lanes of a warp
+// run loops of equal length; the lane does not change any value).
 template <int NC, typename Real>
-__device__ __forceinline__ void reduce_tile(const KernelArgs& a, const TileDesc& T, const Smem<Real>& sm) {
+__device__ __forceinline__ void reduce_tile(const KernelArgs& a, const char* R, const Real* stage) {
     constexpr int NCC = NC * NC, BS = (NCC + 1) & ~1, NP = BS / 2;
-    using P = typename Pair<Real>::type;
-    for (int pos = threadIdx.x; pos < T.n_red; pos += THREADS) {
-        const uint32_t key = sm.red[pos];
-        const int e = (int)(key >> 22), r = (int)(key & ((1u << 22) - 1));
-        const int4 m = sm.emeta[e];
-        const int kcnt = m.w & 0xFF;
-        unsigned long long mask = sm.red_mask[m.z + r];
-        const int4 cl = sm.col[e];
-        const int64_t c0 = (int64_t)(uint32_t)cl.x | ((int64_t)cl.y << 32);
-        const int64_t L = cl.z;
-        const uint8_t* mp = sm.map + m.y + r * kcnt;
+    const RecHead* H = (const RecHead*)R;
+    const RecEnt* ents = (const RecEnt*)(R + H->off_ent);
+    const uint32_t* red = (const uint32_t*)(R + H->off_red);
+    const RecRun* runs = (const RecRun*)(R + H->off_runs);
+    const int n_red = H->n_red, n_runs = H->n_runs;
+    int u = 0;  // run of the current block (positions only grow)
+    for (int pos = threadIdx.x; pos < n_red; pos += THREADS) {
+        const uint32_t key = red[pos];
+        const int e = (int)(key >> RED_RANK_BITS), r = (int)(key & ((1u << RED_RANK_BITS) - 1));
+        while (u + 1 < n_runs && runs[u + 1].first <= pos) ++u;
+        const int4 ru = *(const int4*)(runs + u);
+        const int s0 = ru.z + (pos - ru.x) * ru.y, s1 = s0 + ru.y;
+        const RecEnt en = ents[e];
+        const int64_t c0 = en.colbase + (int64_t)NC * r;
+        const int64_t L = en.L;
         double out[NCC];
         if constexpr (sizeof(Real) == 4) {
             float2 hi[NP], lo[NP];
             #pragma unroll
             for (int t = 0; t < NP; ++t) { hi[t] = make_float2(0.f, 0.f); lo[t] = make_float2(0.f, 0.f); }
+            int s = s0;
             if (!a.fillzero) {
                 float hv[BS], lv[BS];
                 #pragma unroll
@@ -704,23 +649,20 @@ __device__ __forceinline__ void reduce_tile(const KernelArgs& a, const TileDesc&
                     #pragma unroll
                     for (int x = 0; x < NC; ++x) {
                         float2 q;
-                        acc_set(q, a.nzval[c0 + b * L + NC * r + x]);
+                        acc_set(q, a.nzval[c0 + b * L + x]);
                         hv[b * NC + x] = q.x;
                         lv[b * NC + x] = q.y;
                     }
                 #pragma unroll
                 for (int t = 0; t < NP; ++t) { hi[t] = make_float2(hv[2 * t], hv[2 * t + 1]); lo[t] = make_float2(lv[2 * t], lv[2 * t + 1]); }
-            } else if (mask) {
-                const int k = __ffsll((long long)mask) - 1;
-                mask &= mask - 1;
-                const float2* v = (const float2*)(sm.stage + m.x + (k * a.nb_max + mp[k]) * BS);
+            } else if (s < s1) {
+                const float2* v = (const float2*)(stage + s * BS);
                 #pragma unroll
                 for (int t = 0; t < NP; ++t) hi[t] = v[t];
+                ++s;
             }
-            while (mask) {
-                const int k = __ffsll((long long)mask) - 1;
-                mask &= mask - 1;
-                const float2* v = (const float2*)(sm.stage + m.x + (k * a.nb_max + mp[k]) * BS);
+            for (; s < s1; ++s) {
+                const float2* v = (const float2*)(stage + s * BS);
                 #pragma unroll
                 for (int t = 0; t < NP; ++t) acc_add2(hi[t], lo[t], v[t]);
             }
@@ -737,12 +679,10 @@ __device__ __forceinline__ void reduce_tile(const KernelArgs& a, const TileDesc&
                 #pragma unroll
                 for (int b = 0; b < NC; ++b)
                     #pragma unroll
-                    for (int x = 0; x < NC; ++x) acc[b * NC + x] = a.nzval[c0 + b * L + NC * r + x];
+                    for (int x = 0; x < NC; ++x) acc[b * NC + x] = a.nzval[c0 + b * L + x];
             }
-            while (mask) {
-                const int k = __ffsll((long long)mask) - 1;
-                mask &= mask - 1;
-                const Real* v = sm.stage + m.x + (k * a.nb_max + mp[k]) * BS;
+            for (int s = s0; s < s1; ++s) {
+                const Real* v = stage + s * BS;
                 #pragma unroll
                 for (int t = 0; t < NCC; ++t) acc[t] += v[t];
             }
@@ -752,31 +692,39 @@ __device__ __forceinline__ void reduce_tile(const KernelArgs& a, const TileDesc&
         #pragma unroll
         for (int b = 0; b < NC; ++b)
             #pragma unroll
-            for (int x = 0; x < NC; ++x) __stcs(a.nzval + c0 + b * L + NC * r + x, out[b * NC + x]);
+            for (int x = 0; x < NC; ++x) __stcs(a.nzval + c0 + b * L + x, out[b * NC + x]);
     }
 }
 
+// f: one lane per (owned entity, component), its cells' contributions in cell order
 template <typename Real>
-__device__ __forceinline__ void reduce_f(const KernelArgs& a, const TileDesc& T, const Smem<Real>& sm) {
+__device__ __forceinline__ void reduce_f(const KernelArgs& a, const char* R, const Real* stage) {
     using Acc = typename AccT<Real>::type;
+    const RecHead* H = (const RecHead*)R;
+    const RecEnt* ents = (const RecEnt*)(R + H->off_ent);
+    const uint32_t* fk = (const uint32_t*)(R + H->off_fk);
     const int nc = a.nc;
-    for (int idx = threadIdx.x; idx < T.n_ent * nc; idx += THREADS) {
+    const Real* fst = stage + H->n_slots * a.bs;
+    for (int idx = threadIdx.x; idx < H->n_ent * nc; idx += THREADS) {
         const int e = idx / nc, x = idx - e * nc;
-        const int4 m = sm.emeta[e];
-        const int kcnt = m.w & 0xFF;
-        const int64_t gi = (int64_t)sm.eid[e] * nc + x;
+        const uint32_t w = fk[e];
+        const int fb = (int)(w & 0xFFFF), kcnt = (int)(w >> 16);
+        const int64_t gi = (int64_t)ents[e].id * nc + x;
         Acc acc;
         acc_zero(acc);
         if (!a.fillzero) acc_set(acc, a.f[gi]);
-        const Real* v = sm.stage + m.x + kcnt * a.nb_max * a.bs + x;
+        const Real* v = fst + fb * nc + x;
         for (int k = 0; k < kcnt; ++k) acc_add(acc, v[k * nc]);
         __stcs(a.f + gi, acc_value(acc));
     }
 }
 
 // ---------------------------------------------------------------------------------------
-// bounded wait on an mbarrier phase (TMA bulk copy completion)
+// asynchronous copies
 // ---------------------------------------------------------------------------------------
+constexpr long long WAIT_LIMIT = 1ll << 24;  // mbarrier polls before a copy counts as lost
+
+// bounded wait on an mbarrier phase (TMA bulk copy completion)
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase, long long limit) {
     for (long long it = 0; it < limit; ++it) {
         uint32_t done;
@@ -792,15 +740,38 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase, long lon
     return false;
 }
 
+// one TMA bulk copy global -> shared, completing on an mbarrier (bytes: multiple of 16,
+// both addresses 16-byte aligned)
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, int bytes, uint32_t bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst), "l"(src),
+                 "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+// gather the coordinates of a tile's nodes (two 16-byte halves per node) into shared memory
+template <typename Real>
+__device__ __forceinline__ void gather_nodes(const KernelArgs& a, const char* R, char* xs) {
+    const RecHead* H = (const RecHead*)R;
+    const int32_t* nodes = (const int32_t*)(R + H->off_nodes);
+    const char* src = sizeof(Real) == 4 ? (const char*)a.xf8 : (const char*)a.xd4;
+    const uint32_t dst = (uint32_t)__cvta_generic_to_shared(xs);
+    const int n = 2 * H->n_nodes;
+    for (int k = threadIdx.x; k < n; k += THREADS) {
+        const char* p = src + (int64_t)nodes[k >> 1] * NODE_BYTES + (k & 1) * 16;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + k * 16), "l"(p) : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
 // ---------------------------------------------------------------------------------------
-// the kernel
+// the kernel: persistent CTAs, tiles blockIdx.x + it * gridDim.x
 // ---------------------------------------------------------------------------------------
 template <int K0, int Q0, int K1, int Q1, int K2, int Q2, int PHYS, typename Real>
 __global__ void __launch_bounds__(THREADS, 2) tile_kernel(const KernelArgs a, const Real* __restrict__ shape_g, int shape_bytes,
                                                            int shape_off1, int shape_off2) {
-    extern __shared__ __align__(16) char smem_raw[];
-    __shared__ __align__(8) unsigned long long bar;
-    Smem<Real> sm;
+    extern __shared__ __align__(128) char smem_raw[];
+    __shared__ __align__(8) unsigned long long bars[1 + REC_RING];  // shape tables, record ring
     const SmemLayout lay = smem_layout(a, shape_bytes, (int)sizeof(Real));
     {
         // the host sized the allocation from the same layout; refuse to run past it
@@ -811,93 +782,89 @@ __global__ void __launch_bounds__(THREADS, 2) tile_kernel(const KernelArgs a, co
             return;
         }
     }
-    sm.shape = (Real*)(smem_raw + lay.shape);
-    sm.stage = (Real*)(smem_raw + lay.stage);
-    sm.map = (uint8_t*)(smem_raw + lay.map);
-    sm.emeta = (int4*)(smem_raw + lay.emeta);
-    sm.eid = (int*)(smem_raw + lay.eid);
-    sm.red_mask = (unsigned long long*)(smem_raw + lay.red_mask);
-    sm.red = (uint32_t*)(smem_raw + lay.red);
-    sm.col = (int4*)(smem_raw + lay.col);
-    sm.items = (uint32_t*)(smem_raw + lay.items);
-    sm.cells = (int*)(smem_raw + lay.cells);
-    sm.citems = (int*)(smem_raw + lay.citems);
-    sm.conn = (int*)(smem_raw + lay.conn);
-    sm.chunk = smem_raw + lay.chunk;
-
+    Real* shape = (Real*)(smem_raw + lay.shape);
+    char* rec_ring = smem_raw + lay.rec;
+    char* xs_ring = smem_raw + lay.coords;
+    Real* stage = (Real*)(smem_raw + lay.stage);
+    char* chunk = smem_raw + lay.chunk;
+    const int rec_stride = pad16i(a.rec_cap), xs_stride = a.node_cap * NODE_BYTES;
     const int tid = threadIdx.x;
-    const uint32_t bar_s = (uint32_t)__cvta_generic_to_shared(&bar);
-    // stage the reference tables with one TMA bulk copy
+    const int G = gridDim.x;
+    const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(&bars[0]);
+    auto rec_bar = [&](int b) { return bar0 + 8u * (uint32_t)(1 + b); };
+    auto issue_record = [&](int t, int b) {
+        const int64_t o = a.rec_off[t];
+        const int bytes = (int)(a.rec_off[t + 1] - o);
+        bulk_load((uint32_t)__cvta_generic_to_shared(rec_ring + b * rec_stride), a.rec + o, bytes, rec_bar(b));
+    };
+    int t = blockIdx.x;
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_s) : "memory");
+        for (int b = 0; b < 1 + REC_RING; ++b) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8u * b) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_s), "r"(shape_bytes) : "memory");
-        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(sm.shape);
-        asm volatile("cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-                     "l"(shape_g), "r"(shape_bytes), "r"(bar_s)
-                     : "memory");
+        bulk_load((uint32_t)__cvta_generic_to_shared(shape), shape_g, shape_bytes, bar0);
+        if (t < a.n_tiles) issue_record(t, 0);
+        if (t + G < a.n_tiles) issue_record(t + G, 1);
     }
-    __syncthreads();  // the initialised barrier is visible to every thread
-    const TileDesc T = a.tiles[blockIdx.x];
-    // one burst of independent loads: owned entities with their column bases, the reduce
-    // order, the tile's cells, items and connectivity
-    for (int e = tid; e < T.n_ent; e += THREADS) {
-        sm.emeta[e] = reinterpret_cast<const int4*>(a.emeta)[T.ent_begin + e];
-        const int n = a.eids[T.ent_begin + e];
-        sm.eid[e] = n;
-        const int64_t c0 = a.colptr[(int64_t)a.nc * n] - 1;
-        const int L = (int)(a.colptr[(int64_t)a.nc * n + 1] - a.colptr[(int64_t)a.nc * n]);
-        sm.col[e] = make_int4((int)(c0 & 0xFFFFFFFF), (int)(c0 >> 32), L, 0);
+    __syncthreads();  // the initialised barriers are visible to every thread
+    bool failed = false;
+    if (t < a.n_tiles) {
+        if (mbar_wait(rec_bar(0), 0, WAIT_LIMIT)) gather_nodes<Real>(a, rec_ring, xs_ring);
+        else failed = true;
     }
-    for (int k = tid; k < T.n_red; k += THREADS) sm.red[k] = a.red_list[T.red_begin + k];
-    for (int k = tid; k < T.n_items; k += THREADS) sm.items[k] = a.items[T.item_begin + k];
-    for (int k = tid; k < T.n_cells; k += THREADS) {
-        sm.cells[k] = a.tile_cells[T.cell_begin + k];
-        sm.citems[k] = a.cell_items[T.cell_begin + k] - T.item_begin;
-    }
-    for (int gi = T.seg_begin; gi < T.seg_end; ++gi) {
-        const SegDesc g = a.segs[gi];
-        const SubDev& sd = a.sub[g.sub];
-        const int ng = sd.ng, t0 = g.cell_begin - T.cell_begin;
-        for (int idx = tid; idx < g.n_cells * ng; idx += THREADS) {
-            const int c = idx / ng, k = idx - c * ng;
-            const int cell = a.tile_cells[g.cell_begin + c];
-            sm.conn[(t0 + c) * a.ng_max + k] = sd.conn[(int64_t)cell * ng + k];
+    if (!failed && !mbar_wait(bar0, 0, WAIT_LIMIT)) failed = true;
+    int it = 0;
+    for (; t < a.n_tiles; ++it, t += G) {
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        if (__syncthreads_or(failed)) break;  // this tile's record and coordinates are in place
+        const char* R = rec_ring + (it % REC_RING) * rec_stride;
+        const char* xs = xs_ring + (it & 1) * xs_stride;
+        // keep the pipeline full: record of t + 2G, coordinates of t + G
+        if (tid == 0 && t + 2 * G < a.n_tiles) issue_record(t + 2 * G, (it + 2) % REC_RING);
+        if (t + G < a.n_tiles) {
+            const int nb = (it + 1) % REC_RING;
+            if (mbar_wait(rec_bar(nb), (uint32_t)(((it + 1) / REC_RING) & 1), WAIT_LIMIT))
+                gather_nodes<Real>(a, rec_ring + nb * rec_stride, xs_ring + ((it + 1) & 1) * xs_stride);
+            else
+                failed = true;
         }
+        const RecHead* H = (const RecHead*)R;
+        const int n_seg = H->n_seg;
+        for (int gi = 0; gi < n_seg; ++gi) {
+            if (gi) __syncthreads();  // table buffers are laid out per element kind
+            const RecSeg g = ((const RecSeg*)(R + sizeof(RecHead)))[gi];
+            if (g.sub == 0) {
+                process_segment<K0, Q0, PHYS, Real>(a, a.sub[0], shape, g, R, xs, stage, chunk);
+            } else if constexpr (K1 >= 0) {
+                if (g.sub == 1) {
+                    process_segment<K1, Q1, PHYS, Real>(a, a.sub[1], (const Real*)((const char*)shape + shape_off1), g, R, xs,
+                                                        stage, chunk);
+                } else if constexpr (K2 >= 0) {
+                    process_segment<K2, Q2, PHYS, Real>(a, a.sub[2], (const Real*)((const char*)shape + shape_off2), g, R, xs,
+                                                        stage, chunk);
+                }
+            }
+        }
+        __syncthreads();  // all staging slots written
+        if (a.do_k) {
+            if (a.nc == 3) reduce_tile<3, Real>(a, R, stage);
+            else if (a.nc == 2) reduce_tile<2, Real>(a, R, stage);
+            else reduce_tile<1, Real>(a, R, stage);
+        }
+        if (a.do_f) reduce_f<Real>(a, R, stage);
     }
-    {
-        int4* mp = (int4*)sm.map;
-        const int n16 = (T.map_bytes + 15) >> 4;
-        for (int k = tid; k < n16; k += THREADS) mp[k] = make_int4(-1, -1, -1, -1);
-        for (int k = tid; k < T.n_red; k += THREADS) sm.red_mask[k] = 0ull;
-    }
-    // every thread waits for the table copy (bounded; a timeout skips the tile)
-    const bool ok = mbar_wait(bar_s, 0, 1ll << 26);
-    if (!ok) {
-        if (tid == 0) atomicAdd(&a.status->timeout, 1u);
-        return;
-    }
-    __syncthreads();
-    for (int gi = T.seg_begin; gi < T.seg_end; ++gi) {
-        const SegDesc g = a.segs[gi];
-        if (gi > T.seg_begin) __syncthreads();  // table buffers are laid out per element kind
-        if (g.sub == 0) {
-            process_segment<K0, Q0, PHYS, Real>(a, a.sub[0], sm.shape, g, T, sm);
-        } else if constexpr (K1 >= 0) {
-            if (g.sub == 1) {
-                process_segment<K1, Q1, PHYS, Real>(a, a.sub[1], (const Real*)((const char*)sm.shape + shape_off1), g, T, sm);
-            } else if constexpr (K2 >= 0) {
-                process_segment<K2, Q2, PHYS, Real>(a, a.sub[2], (const Real*)((const char*)sm.shape + shape_off2), g, T, sm);
+    if (t < a.n_tiles) {
+        // a copy was lost: report it, and wait (bounded) for this CTA's copies still in
+        // flight before its shared memory is released
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        if (tid == 0) {
+            atomicAdd(&a.status->timeout, 1u);
+            mbar_wait(bar0, 0, WAIT_LIMIT);
+            for (int d = 0; d < 2; ++d) {
+                const int tt = t + d * G;
+                if (tt < a.n_tiles) mbar_wait(rec_bar((it + d) % REC_RING), (uint32_t)(((it + d) / REC_RING) & 1), WAIT_LIMIT);
             }
         }
     }
-    __syncthreads();  // all staging slots and masks written
-    if (a.do_k) {
-        if (a.nc == 3) reduce_tile<3, Real>(a, T, sm);
-        else if (a.nc == 2) reduce_tile<2, Real>(a, T, sm);
-        else reduce_tile<1, Real>(a, T, sm);
-    }
-    if (a.do_f) reduce_f<Real>(a, T, sm);
 }
 
 }  // namespace fe
