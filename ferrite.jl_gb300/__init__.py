@@ -36,7 +36,7 @@ ERROR_NAMES = {0: "OK", 1: "ARG", 2: "BOUNDS", 3: "DETJ", 4: "PATTERN_MISSING", 
 TRIANGLE, QUADRILATERAL, TETRAHEDRON, HEXAHEDRON, WEDGE = 1, 2, 3, 4, 5
 HEAT, LINEAR_ELASTIC, NEO_HOOKE = 1, 2, 3
 PREC_MIXED, PREC_FP64 = 0, 1
-FILLZERO, NO_K, NO_F, ASYNC, PROFILE = 1, 2, 4, 8, 16
+FILLZERO, NO_K, NO_F, ASYNC, PROFILE, COMPENSATED = 1, 2, 4, 8, 16, 32
 
 EXPORTED = ["fe_abi_version", "fe_create", "fe_assemble", "fe_sync", "fe_last_error", "fe_get_info",
             "fe_get_index_map", "fe_plan_dry_run", "fe_distribute_dofs", "fe_sparsity_pattern", "fe_kernel_time", "fe_assemble_noalloc", "fe_destroy"]
@@ -264,8 +264,9 @@ class Handle:
 
     def assemble(self, nzval, f, physics: int, p0: float, p1: float, body=(0.0, 0.0, 0.0), cell_scale=None, u=None,
                  precision: int = PREC_MIXED, fillzero: bool = True, stream=None, sync: bool = True,
-                 cond_threshold: float = 0.0, profile: bool = False):
-        """One fe_assemble call. ``stream`` is a torch.cuda.Stream, a raw handle or None."""
+                 cond_threshold: float = 0.0, profile: bool = False, compensated: bool = False):
+        """One fe_assemble call. ``stream`` is a torch.cuda.Stream, a raw handle or None.
+        ``compensated`` (mixed precision): sum each entry as a compensated FP32 pair."""
         p = AssembleParams()
         p.physics, p.precision = physics, precision
         flags = FILLZERO if fillzero else 0
@@ -277,6 +278,8 @@ class Handle:
             flags |= ASYNC
         if profile:
             flags |= PROFILE
+        if compensated:
+            flags |= COMPENSATED
         p.flags = flags
         p.p0, p.p1 = float(p0), float(p1)
         for k in range(3):

@@ -169,9 +169,9 @@ int launch_assembly(fe_handle* h, const KernelEntry* ke, KernelArgs& A, bool fp6
         A.groups[s] = std::max(1, std::min(ke->groups[s], room));
         tb = std::max(tb, ke->table_bytes[s] * A.groups[s]);
     }
-    if (fixed + tb > budget) return set_error(h, FE_ERR_UNSUPPORTED, "tile does not fit in shared memory");
     A.chunk_bytes = tb;
-    const int smem = fixed + tb;
+    const int smem = fixed + chunk_region_bytes(A);
+    if (smem > budget) return set_error(h, FE_ERR_UNSUPPORTED, "tile does not fit in shared memory");
     if ((e = cudaFuncSetAttribute(ke->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
         return cuda_fail(h, e, "cudaFuncSetAttribute");
     int per_sm = 0;
@@ -245,28 +245,28 @@ int fe_create(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain
     A.nc = hp.nc;
     A.dim = hp.dim;
     A.n_sub = (int32_t)hp.subs.size();
-    // node coordinates: FP64 [n][dim], and 32 bytes per node for the gathers: float hi (x, y,
-    // z, 0) then float lo, or FP64 (x, y, z, 0)
+    // node coordinates: FP64 [n][dim], and 24 bytes per node for the gathers: float hi
+    // (x, y, z) then float lo, or FP64 (x, y, z)
     {
         double* xd;
         CK(h->upload(&xd, hp.nodes.data(), hp.nodes.size()));
         A.xd = xd;
-        std::vector<float> x8((size_t)hp.n_nodes * 8, 0.f);
-        std::vector<double> x4((size_t)hp.n_nodes * 4, 0.0);
+        std::vector<float> x6((size_t)hp.n_nodes * 6, 0.f);
+        std::vector<double> x3((size_t)hp.n_nodes * 3, 0.0);
         for (int64_t n = 0; n < hp.n_nodes; ++n)
             for (int x = 0; x < hp.dim; ++x) {
                 const double v = hp.nodes[n * hp.dim + x];
                 const float hi = (float)v;
-                x8[n * 8 + x] = hi;
-                x8[n * 8 + 4 + x] = (float)(v - (double)hi);
-                x4[n * 4 + x] = v;
+                x6[n * 6 + x] = hi;
+                x6[n * 6 + 3 + x] = (float)(v - (double)hi);
+                x3[n * 3 + x] = v;
             }
-        float* xf8;
-        double* xd4;
-        CK(h->upload(&xf8, x8.data(), x8.size()));
-        CK(h->upload(&xd4, x4.data(), x4.size()));
-        A.xf8 = xf8;
-        A.xd4 = xd4;
+        float* xf6;
+        double* xd3;
+        CK(h->upload(&xf6, x6.data(), x6.size()));
+        CK(h->upload(&xd3, x3.data(), x3.size()));
+        A.xf6 = xf6;
+        A.xd3 = xd3;
     }
     // subdomains
     std::vector<float> shf;
@@ -281,19 +281,24 @@ int fe_create(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain
         CK(h->upload(&cid, hs.cellid.data(), hs.cellid.size()));
         CK(h->upload(&ents, hs.ents.data(), hs.ents.size()));
         sd.cellid = cid; sd.ents = ents;
-        // reference tables: w, N, dN (physical layout [q][i][c]), dM; padded blocks
-        auto push_block = [&](auto& vec, const std::vector<double>& src) {
+        // reference tables: one record per quadrature point (dM, dN, N, w; layout shape_q)
+        auto push_records = [&](auto& vec) {
             using T = typename std::remove_reference<decltype(vec)>::type::value_type;
+            const ShapeQ L = shape_q(hs.nb, hs.ng, hs.dim, (int)sizeof(T));
             const size_t start = vec.size();
-            for (double v : src) vec.push_back((T)v);
-            while (((vec.size() - start) * sizeof(T)) % 16) vec.push_back((T)0);
+            vec.resize(start + (size_t)hs.nq * L.qs, (T)0);
+            for (int q = 0; q < hs.nq; ++q) {
+                T* r = vec.data() + start + (size_t)q * L.qs;
+                for (int t = 0; t < hs.ng * hs.dim; ++t) r[L.dm + t] = (T)hs.dM[(size_t)q * hs.ng * hs.dim + t];
+                for (int t = 0; t < hs.nb * hs.dim; ++t) r[L.dn + t] = (T)hs.dN[(size_t)q * hs.nb * hs.dim + t];
+                for (int t = 0; t < hs.nb; ++t) r[L.n + t] = (T)hs.N[(size_t)q * hs.nb + t];
+                r[L.w] = (T)hs.w[q];
+            }
         };
         offs_f[s] = (int)(shf.size() * sizeof(float));
         offs_d[s] = (int)(shd.size() * sizeof(double));
-        for (auto* src : {&hs.w, &hs.N, &hs.dN, &hs.dM}) {
-            push_block(shf, *src);
-            push_block(shd, *src);
-        }
+        push_records(shf);
+        push_records(shd);
         float *wf, *Nf, *dNf, *dMf;
         double *wd, *Nd, *dNd, *dMd;
         std::vector<float> tmp;
@@ -330,6 +335,7 @@ int fe_create(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain
     A.rec_cap = std::max(pl.max_rec, 64);
     A.node_cap = std::max(pl.max_nodes, 1);
     A.stage_cap = std::max(pl.max_stage, 2);
+    A.out_cap = std::max(pl.max_out, 2);
     if (pl.n_tiles >= (int64_t)INT32_MAX) {
         set_error(h, FE_ERR_UNSUPPORTED, "too many tiles");
         g_create_error = h->last;
@@ -459,6 +465,7 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
     A.do_k = do_k;
     A.do_f = do_f;
     A.fillzero = fill;
+    A.compensated = (p->flags & FE_COMPENSATED) != 0;
     // inputs
     Physics& ph = A.phys;
     ph = Physics{};
@@ -690,6 +697,7 @@ extern "C" int fe_assemble_noalloc(fe_handle* h, const fe_assemble_params* p, do
     A.do_k = do_k;
     A.do_f = do_f;
     A.fillzero = (p->flags & FE_FILLZERO) != 0;
+    A.compensated = (p->flags & FE_COMPENSATED) != 0;
     Physics& ph = A.phys;
     ph = Physics{};
     ph.kind = p->physics;

@@ -31,6 +31,9 @@ enum Kind : int32_t {
     NKIND = 7
 };
 
+constexpr int CTA_THREADS = 256;  // threads of a tile CTA
+// lanes per cell ("lane group") of each kind; CTA_THREADS / GROUP_LANES[kind] groups per CTA
+constexpr int GROUP_LANES[NKIND] = {4, 4, 4, 8, 8, 32, 16};
 constexpr int MAX_NB = 27;   // base functions per cell
 constexpr int MAX_NG = 8;    // geometric nodes per cell
 constexpr int MAX_NQ = 27;   // quadrature points per cell
@@ -41,17 +44,27 @@ constexpr int MAX_SUB = 3;   // subdomains one kernel handles
 // of global memory that a CTA copies to shared memory with a single TMA bulk copy. All
 // section offsets are bytes from the record start, multiples of 16; the record size is a
 // multiple of 16. Sections:
-//   RecHead                                   80 bytes
+//   RecHead                                   96 bytes
 //   RecSeg[n_seg]                             the tile's cells, one segment per subdomain
-//   RecEnt[n_ent]       (off_ent)             owned entities: column base, length, id
+//   RecEnt[n_ent]       (off_ent)             owned entities: column base and length, offset of
+//                                             the entity's columns in its pass's output buffer
+//   int32 eid[n_ent]    (off_eid)             entity ids (f rows id*nc .. id*nc+nc-1)
 //   uint32 fk[n_ent]    (off_fk)              f staging: first f slot | cell count << 16
-//   uint32 red[n_red]   (off_red)             owned (entity, row entity) blocks: ent << 22 | rank,
-//                                             most contributions first
+//   uint32 red[n_red]   (off_red)             owned (entity, row entity) blocks: ent << 22 | rank;
+//                                             pass after pass, within a pass most contributions first
 //   RecRun runs[n_runs] (off_runs)            the blocks as runs of equal contribution count:
-//                                             block b of run u has its slots at
-//                                             base + (b - first) * count .. + count - 1, in cell order
+//                                             contribution k of block first + j of a run is in
+//                                             slot base + k * nblk + j (cell order in k)
+//   RecPass pass[n_pass] (off_pass)           reduce passes: blocks, runs and output ranges whose
+//                                             values fit the shared output buffer at once
+//   RecRng rng[n_rng]   (off_rng)             contiguous nzval ranges of a pass's output buffer
 //   uint32 items[n_items] (off_items)         per (cell, owned base function j): j | f slot << 16
-//   RecCell[n_cells]    (off_cells)           sub-local cell index, its items
+//   int32 cells[n_cells] (off_cells)          sub-local cell index of each tile cell
+//   RecTask[n_tasks]    (off_tasks)           (cell, item range) pieces of work for a lane group:
+//                                             geometry of the cell, then the blocks of the items
+//   uint16 gt[..]       (RecSeg::gt_off)      per segment: tasks gt[g] .. gt[g+1]-1 belong to
+//                                             planned lane group g (n_grp groups); a CTA with
+//                                             fewer groups runs planned groups g, g + groups, ...
 //   uint16 conn[..]     (RecSeg::conn_off)    per segment: [cells][NG] tile-local node index
 //   uint16 slots[..]    (RecSeg::slot_off)    per segment: [items][NB] staging slot of row i,
 //                                             SLOT_MISS where the pattern has no entry
@@ -65,30 +78,41 @@ constexpr int RED_RANK_BITS = 22;
 constexpr int MAX_TILE_ENTS = 1 << (32 - RED_RANK_BITS);
 constexpr int MAX_ENT_CELLS = 255;   // cells of one dof entity
 constexpr int MAX_TILE_SLOTS = 0xFFFF;
+constexpr int OUT_CAP_DOUBLES = 4096; // output buffer of one reduce pass (32 KiB)
 
 struct RecHead {
     int32_t bytes;
     int32_t n_seg, n_ent, n_cells;
     int32_t n_items, n_red, n_nodes, n_slots;
-    int32_t n_fslots, off_ent, off_fk, off_red;
-    int32_t n_runs, off_runs, off_items, off_cells;
-    int32_t off_nodes, pad[3];
+    int32_t n_fslots, n_runs, n_pass, n_rng;
+    int32_t off_ent, off_eid, off_fk, off_red;
+    int32_t off_runs, off_pass, off_rng, off_items;
+    int32_t off_cells, off_nodes, n_tasks, off_tasks;
 };
-static_assert(sizeof(RecHead) == 80, "record head is 80 bytes");
+static_assert(sizeof(RecHead) == 96, "record head is 96 bytes");
 
 struct RecSeg {
     int32_t sub;
     int32_t cell_begin, cell_end;  // tile cells of the segment
     int32_t item_begin, item_end;  // tile items of the segment
     int32_t conn_off, slot_off;    // byte offsets of the segment's conn and slot rows
-    int32_t pad;
+    int32_t gt_off;                // byte offset of the segment's group task table
+    int32_t n_grp;                 // planned lane groups
+    int32_t pad[3];
 };
-static_assert(sizeof(RecSeg) == 32, "segment entry is 32 bytes");
+static_assert(sizeof(RecSeg) == 48, "segment entry is 48 bytes");
+
+struct RecTask {
+    uint16_t cell;                  // tile cell index
+    uint16_t item_begin, item_end;  // tile items
+    uint16_t pad;
+};
+static_assert(sizeof(RecTask) == 8, "task entry is 8 bytes");
 
 struct RecEnt {
     int64_t colbase;  // 0-based nzval index of the entity's first column
     int32_t L;        // column length (entries)
-    int32_t id;       // entity id (0-based): f rows id*nc .. id*nc+nc-1
+    int32_t out_off;  // offset of the entity's nc columns in its pass's output buffer (doubles)
 };
 static_assert(sizeof(RecEnt) == 16, "entity entry is 16 bytes");
 
@@ -96,15 +120,25 @@ struct RecRun {
     int32_t first;  // first block (position in red[]) of the run
     int32_t count;  // contributions (slots) of each block of the run
     int32_t base;   // first slot of the run
-    int32_t pad;
+    int32_t nblk;   // blocks in the run
 };
 static_assert(sizeof(RecRun) == 16, "run entry is 16 bytes");
 
-struct RecCell {
-    int32_t cell;                  // subdomain-local cell index
-    uint16_t item_begin, item_end; // tile items of the cell
+struct RecPass {
+    int32_t red_begin, red_end;  // blocks of the pass (positions in red[])
+    int32_t run_begin, run_end;  // their runs
+    int32_t rng_begin, rng_end;  // output ranges
+    int32_t out_len;             // output buffer doubles used
+    int32_t pad;
 };
-static_assert(sizeof(RecCell) == 8, "cell entry is 8 bytes");
+static_assert(sizeof(RecPass) == 32, "pass entry is 32 bytes");
+
+struct RecRng {
+    int64_t nz0;      // first nzval index (0-based)
+    int32_t buf_off;  // its position in the output buffer; buf_off - nz0 is even
+    int32_t len;      // doubles
+};
+static_assert(sizeof(RecRng) == 16, "range entry is 16 bytes");
 
 // per-subdomain device data
 struct SubDev {
@@ -151,16 +185,18 @@ struct KernelArgs {
     SubDev sub[MAX_SUB];
     const char* rec;         // tile records (16-byte aligned)
     const int64_t* rec_off;  // [n_tiles + 1] byte offset of each record
-    const float* xf8;        // [n_nodes][8]: x, y, z, 0 as float hi, then the float lo parts
-    const double* xd4;       // [n_nodes][4]: x, y, z, 0 in FP64
+    const float* xf6;        // [n_nodes][6]: x, y, z as float hi, then the float lo parts
+    const double* xd3;       // [n_nodes][3]: x, y, z in FP64 (z = 0 in 2D)
     const double* xd;        // [n_nodes][dim] FP64 (Jacobians recomputed in FP64)
     int32_t dim;
     double* nzval;
     double* f;
     int32_t do_k, do_f, fillzero;
+    int32_t compensated;     // mixed precision: compensated FP32 pair sums
     Physics phys;
     DevStatus* status;
     int32_t rec_cap;         // record bytes per ring buffer (max over tiles)
+    int32_t out_cap;         // output-buffer doubles of one reduce pass (max over tiles)
     int32_t node_cap;        // nodes per tile, max
     int32_t stage_cap;       // staging values per tile, max
     int32_t chunk_bytes;     // bytes of the per-group cell table buffers of the launched kernel

@@ -230,6 +230,10 @@ namespace {
 
 inline int32_t pad16(int64_t b) { return (int32_t)((b + 15) & ~15ll); }
 
+// relative cost of a lane group's work: the geometry of a cell against the blocks of one item
+// (measured on Q1 hexahedra: about 2.6 items per cell geometry)
+constexpr int64_t TASK_GEO_COST = 26, TASK_ITEM_COST = 10;
+
 struct TileItem {
     int32_t cell;  // tile cell index (before the per-segment reorder)
     int32_t j, te, k;
@@ -239,7 +243,7 @@ struct TileItem {
 // j) triples in (sub, cell, j) order. Returns 0 or an error code (internal inconsistency).
 int build_record(const HostProblem& hp, const std::vector<int32_t>& kcount, const std::vector<int32_t>& tile_local,
                  const int32_t* ents, int32_t n_ent, const uint64_t* trip, int64_t n_trip, std::vector<uint8_t>& out,
-                 int32_t& n_nodes_out, int32_t& stage_out, int32_t& n_cells_out, int32_t& n_items_out) {
+                 int32_t& n_nodes_out, int32_t& stage_out, int32_t& n_cells_out, int32_t& n_items_out, int32_t& out_len_out) {
     const int nc = hp.nc;
     const int bs = (nc * nc + 1) & ~1;
     const int64_t* cp = hp.colptr.data();
@@ -313,20 +317,73 @@ int build_record(const HostProblem& hp, const std::vector<int32_t>& kcount, cons
     }
     for (int32_t b = 0; b < n_red; ++b)
         if (cnt[b] > MAX_ENT_CELLS) return 2;
-    // reduce order: most contributions first (stable in (entity, rank)); slots follow it
+    // reduce passes: consecutive owned entities whose columns fit the output buffer; within a
+    // pass, contiguous nzval ranges, each placed in the buffer with the parity of its start so
+    // the 16-byte aligned middle can be stored with one bulk copy
+    std::vector<RecEnt> rent(n_ent);
+    std::vector<RecPass> passes;
+    std::vector<RecRng> rngs;
+    {
+        int32_t e = 0;
+        while (e < n_ent) {
+            RecPass P{};
+            P.rng_begin = (int32_t)rngs.size();
+            int32_t used = 0, e1 = e;
+            while (e1 < n_ent) {
+                const int64_t n = ents[e1];
+                const int64_t cb = cp[nc * n] - 1, len = cp[nc * n + nc] - cp[nc * n];
+                const bool joins = (int32_t)rngs.size() > P.rng_begin && rngs.back().nz0 + rngs.back().len == cb;
+                int32_t start = joins ? rngs.back().buf_off + rngs.back().len : used;
+                if (!joins && ((start - cb) & 1)) ++start;
+                if (start + len > OUT_CAP_DOUBLES) {
+                    if (e1 == e) return 4;  // one entity's columns exceed the buffer
+                    break;
+                }
+                if (joins) {
+                    rngs.back().len += (int32_t)len;
+                } else {
+                    rngs.push_back(RecRng{cb, start, (int32_t)len});
+                }
+                rent[e1] = RecEnt{cb, (int32_t)(cp[nc * n + 1] - cp[nc * n]), start};
+                used = (int32_t)(start + len);
+                ++e1;
+            }
+            P.rng_end = (int32_t)rngs.size();
+            P.out_len = used;
+            P.red_begin = z[e];   // filled with positions below; z ranges of the pass's entities
+            P.red_end = z[e1];
+            passes.push_back(P);
+            e = e1;
+        }
+    }
+    // reduce order within each pass: most contributions first (stable in (entity, rank)); the
+    // slots of a run are k-major so the lanes of a warp read consecutive slots
     std::vector<int32_t> ord(n_red);
     for (int32_t b = 0; b < n_red; ++b) ord[b] = b;
-    std::stable_sort(ord.begin(), ord.end(), [&](int32_t x, int32_t y) { return cnt[x] > cnt[y]; });
-    std::vector<int32_t> base(n_red);
+    for (const RecPass& P : passes)
+        std::stable_sort(ord.begin() + P.red_begin, ord.begin() + P.red_end, [&](int32_t x, int32_t y) { return cnt[x] > cnt[y]; });
+    std::vector<int32_t> base(n_red), stride(n_red);
     std::vector<RecRun> runs;
     int32_t n_slots = 0;
-    for (int32_t q = 0; q < n_red; ++q) {
-        base[ord[q]] = n_slots;
-        if (runs.empty() || runs.back().count != cnt[ord[q]]) runs.push_back(RecRun{q, cnt[ord[q]], n_slots, 0});
-        n_slots += cnt[ord[q]];
-        if (n_slots > MAX_TILE_SLOTS - 1) return 3;
+    for (RecPass& P : passes) {
+        P.run_begin = (int32_t)runs.size();
+        int32_t q = P.red_begin;
+        while (q < P.red_end) {
+            int32_t q1 = q;
+            while (q1 < P.red_end && cnt[ord[q1]] == cnt[ord[q]]) ++q1;
+            RecRun U{q, cnt[ord[q]], n_slots, q1 - q};
+            for (int32_t x = q; x < q1; ++x) {
+                base[ord[x]] = n_slots + (x - q);
+                stride[ord[x]] = U.nblk;
+            }
+            n_slots += U.count * U.nblk;
+            if (n_slots > MAX_TILE_SLOTS - 1) return 3;
+            runs.push_back(U);
+            q = q1;
+        }
+        P.run_end = (int32_t)runs.size();
     }
-    const int32_t n_runs = (int32_t)runs.size();
+    const int32_t n_runs = (int32_t)runs.size(), n_pass = (int32_t)passes.size(), n_rng = (int32_t)rngs.size();
     std::vector<uint32_t> red(n_red);
     for (int32_t te = 0; te < n_ent; ++te)
         for (int32_t r = 0; r < z[te + 1] - z[te]; ++r) red[z[te] + r] = ((uint32_t)te << RED_RANK_BITS) | (uint32_t)r;
@@ -337,17 +394,50 @@ int build_record(const HostProblem& hp, const std::vector<int32_t>& kcount, cons
     for (int32_t te = 0; te < n_ent; ++te) fbase[te + 1] = fbase[te] + kc[te];
     const int32_t n_fslots = fbase[n_ent];
     if (n_fslots > 0xFFFF) return 3;
-    // within a segment, cells with more items first: the lane groups of one warp then run
-    // loops of similar length (the values do not depend on this order)
-    std::vector<int32_t> cell_order(cells.size());
-    for (size_t c = 0; c < cells.size(); ++c) cell_order[c] = (int32_t)c;
-    auto n_items_of = [&](int32_t c) {
-        const int32_t e = c + 1 < (int32_t)cells.size() ? cell_item0[c + 1] : (int32_t)items.size();
-        return e - cell_item0[c];
-    };
-    for (const Seg& g : segs)
-        std::stable_sort(cell_order.begin() + g.cell_begin, cell_order.begin() + g.cell_end,
-                         [&](int32_t x, int32_t y) { return n_items_of(x) > n_items_of(y); });
+    // work of the lane groups: per segment, (cell, item range) tasks scheduled longest first
+    // onto the least loaded of the planned groups; a cell whose geometry plus blocks would
+    // exceed the even share is split into pieces that each redo the geometry
+    struct Task { int32_t cell, i0, i1, cost; };
+    std::vector<std::vector<std::vector<Task>>> seg_tasks(segs.size());
+    for (size_t g = 0; g < segs.size(); ++g) {
+        const HostSub& hs = hp.subs[segs[g].sub];
+        const int G = CTA_THREADS / GROUP_LANES[hs.kind];
+        const int32_t c0 = segs[g].cell_begin, c1 = segs[g].cell_end;
+        auto n_items_of = [&](int32_t c) {
+            return (c + 1 < (int32_t)cells.size() ? cell_item0[c + 1] : (int32_t)items.size()) - cell_item0[c];
+        };
+        std::vector<int32_t> pieces(c1 - c0, 1);
+        for (int pass = 0; pass < 3; ++pass) {
+            int64_t total = 0;
+            for (int32_t c = c0; c < c1; ++c)
+                total += (int64_t)pieces[c - c0] * TASK_GEO_COST + (int64_t)n_items_of(c) * TASK_ITEM_COST;
+            const int64_t share = std::max<int64_t>((total + G - 1) / G, TASK_GEO_COST + TASK_ITEM_COST);
+            for (int32_t c = c0; c < c1; ++c) {
+                const int32_t n = n_items_of(c);
+                int32_t m = 1;
+                while (m < n && TASK_GEO_COST + (int64_t)((n + m - 1) / m) * TASK_ITEM_COST > share) ++m;
+                pieces[c - c0] = m;
+            }
+        }
+        std::vector<Task> tasks;
+        for (int32_t c = c0; c < c1; ++c) {
+            const int32_t n = n_items_of(c), m = pieces[c - c0];
+            int32_t i = cell_item0[c];
+            for (int32_t q = 0; q < m; ++q) {
+                const int32_t len = n / m + (q < n % m ? 1 : 0);
+                tasks.push_back(Task{c, i, i + len, (int32_t)(TASK_GEO_COST + len * TASK_ITEM_COST)});
+                i += len;
+            }
+        }
+        std::stable_sort(tasks.begin(), tasks.end(), [](const Task& x, const Task& y) { return x.cost > y.cost; });
+        std::vector<int64_t> load(G, 0);
+        seg_tasks[g].assign(G, {});
+        for (const Task& T : tasks) {
+            const int w = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+            load[w] += T.cost;
+            seg_tasks[g][w].push_back(T);
+        }
+    }
     // nodes of the tile, ascending
     std::vector<int32_t> nodes;
     for (size_t c = 0; c < cells.size(); ++c) {
@@ -363,14 +453,17 @@ int build_record(const HostProblem& hp, const std::vector<int32_t>& kcount, cons
     RecHead H{};
     H.n_seg = n_seg; H.n_ent = n_ent; H.n_cells = n_cells; H.n_items = n_items;
     H.n_red = n_red; H.n_nodes = (int32_t)nodes.size(); H.n_slots = n_slots; H.n_fslots = n_fslots;
-    H.n_runs = n_runs;
-    int64_t o = (int64_t)sizeof(RecHead) + (int64_t)n_seg * 32;
+    H.n_runs = n_runs; H.n_pass = n_pass; H.n_rng = n_rng;
+    int64_t o = (int64_t)sizeof(RecHead) + (int64_t)n_seg * (int64_t)sizeof(RecSeg);
     H.off_ent = pad16(o); o = H.off_ent + (int64_t)n_ent * 16;
+    H.off_eid = pad16(o); o = H.off_eid + (int64_t)n_ent * 4;
     H.off_fk = pad16(o); o = H.off_fk + (int64_t)n_ent * 4;
     H.off_red = pad16(o); o = H.off_red + (int64_t)n_red * 4;
     H.off_runs = pad16(o); o = H.off_runs + (int64_t)n_runs * 16;
+    H.off_pass = pad16(o); o = H.off_pass + (int64_t)n_pass * 32;
+    H.off_rng = pad16(o); o = H.off_rng + (int64_t)n_rng * 16;
     H.off_items = pad16(o); o = H.off_items + (int64_t)n_items * 4;
-    H.off_cells = pad16(o); o = H.off_cells + (int64_t)n_cells * 8;
+    H.off_cells = pad16(o); o = H.off_cells + (int64_t)n_cells * 4;
     std::vector<RecSeg> rsegs(n_seg);
     for (int32_t g = 0; g < n_seg; ++g) {
         const HostSub& hs = hp.subs[segs[g].sub];
@@ -380,46 +473,68 @@ int build_record(const HostProblem& hp, const std::vector<int32_t>& kcount, cons
         R.item_begin = segs[g].item_begin; R.item_end = segs[g].item_end;
         R.conn_off = pad16(o); o = R.conn_off + (int64_t)(R.cell_end - R.cell_begin) * hs.ng * 2;
         R.slot_off = pad16(o); o = R.slot_off + (int64_t)(R.item_end - R.item_begin) * hs.nb * 2;
-        R.pad = 0;
+        R.n_grp = (int32_t)seg_tasks[g].size();
+        R.gt_off = pad16(o); o = R.gt_off + (int64_t)(R.n_grp + 1) * 2;
+        R.pad[0] = R.pad[1] = R.pad[2] = 0;
     }
+    int32_t n_tasks = 0;
+    for (const auto& st : seg_tasks)
+        for (const auto& gl : st) n_tasks += (int32_t)gl.size();
+    if (n_tasks > 0xFFFF) return 3;
+    H.n_tasks = n_tasks;
+    H.off_tasks = pad16(o); o = H.off_tasks + (int64_t)n_tasks * 8;
     H.off_nodes = pad16(o); o = H.off_nodes + (int64_t)nodes.size() * 4;
     H.bytes = pad16(o);
     if (H.bytes > (1 << 20)) return 3;
     out.assign(H.bytes, 0);
     uint8_t* B = out.data();
     std::memcpy(B, &H, sizeof(RecHead));
-    std::memcpy(B + sizeof(RecHead), rsegs.data(), (size_t)n_seg * 32);
+    std::memcpy(B + sizeof(RecHead), rsegs.data(), (size_t)n_seg * sizeof(RecSeg));
     for (int32_t te = 0; te < n_ent; ++te) {
-        const int64_t n = ents[te];
-        RecEnt E{cp[nc * n] - 1, (int32_t)(cp[nc * n + 1] - cp[nc * n]), (int32_t)n};
-        std::memcpy(B + H.off_ent + (int64_t)te * 16, &E, 16);
+        std::memcpy(B + H.off_ent + (int64_t)te * 16, &rent[te], 16);
+        const int32_t id = ents[te];
+        std::memcpy(B + H.off_eid + (int64_t)te * 4, &id, 4);
         const uint32_t fk = (uint32_t)fbase[te] | ((uint32_t)kc[te] << 16);
         std::memcpy(B + H.off_fk + (int64_t)te * 4, &fk, 4);
     }
     std::memcpy(B + H.off_red, red_sorted.data(), (size_t)n_red * 4);
     std::memcpy(B + H.off_runs, runs.data(), (size_t)n_runs * 16);
-    // cells and items in the reordered cell order
-    int32_t it_out = 0;
+    std::memcpy(B + H.off_pass, passes.data(), (size_t)n_pass * 32);
+    std::memcpy(B + H.off_rng, rngs.data(), (size_t)n_rng * 16);
+    // cells, items and slot rows in cell order
     for (int32_t g = 0; g < n_seg; ++g) {
         const HostSub& hs = hp.subs[segs[g].sub];
         const RecSeg& R = rsegs[g];
-        for (int32_t pc = R.cell_begin; pc < R.cell_end; ++pc) {
-            const int32_t c = cell_order[pc];
+        for (int32_t c = R.cell_begin; c < R.cell_end; ++c) {
             const int32_t i0 = cell_item0[c], i1 = c + 1 < n_cells ? cell_item0[c + 1] : n_items;
-            RecCell C{cells[c], (uint16_t)it_out, (uint16_t)(it_out + i1 - i0)};
-            std::memcpy(B + H.off_cells + (int64_t)pc * 8, &C, 8);
-            uint16_t* cn = (uint16_t*)(B + R.conn_off) + (int64_t)(pc - R.cell_begin) * hs.ng;
+            std::memcpy(B + H.off_cells + (int64_t)c * 4, &cells[c], 4);
+            uint16_t* cn = (uint16_t*)(B + R.conn_off) + (int64_t)(c - R.cell_begin) * hs.ng;
             for (int a = 0; a < hs.ng; ++a) cn[a] = local_node(hs.conn[(int64_t)cells[c] * hs.ng + a]);
-            for (int32_t it = i0; it < i1; ++it, ++it_out) {
+            for (int32_t it = i0; it < i1; ++it) {
                 const TileItem& I = items[it];
                 const uint32_t w = (uint32_t)I.j | ((uint32_t)(fbase[I.te] + I.k) << 16);
-                std::memcpy(B + H.off_items + (int64_t)it_out * 4, &w, 4);
-                uint16_t* sl = (uint16_t*)(B + R.slot_off) + (int64_t)(it_out - R.item_begin) * hs.nb;
+                std::memcpy(B + H.off_items + (int64_t)it * 4, &w, 4);
+                uint16_t* sl = (uint16_t*)(B + R.slot_off) + (int64_t)(it - R.item_begin) * hs.nb;
                 for (int i = 0; i < hs.nb; ++i) {
                     const int32_t b = row_block[item_row0[it] + i];
-                    sl[i] = b < 0 ? SLOT_MISS : (uint16_t)(base[b] + row_ord[item_row0[it] + i]);
+                    sl[i] = b < 0 ? SLOT_MISS : (uint16_t)(base[b] + row_ord[item_row0[it] + i] * stride[b]);
                 }
             }
+        }
+    }
+    {
+        int32_t tn = 0;
+        for (int32_t g = 0; g < n_seg; ++g) {
+            uint16_t* gt = (uint16_t*)(B + rsegs[g].gt_off);
+            for (int32_t w = 0; w < rsegs[g].n_grp; ++w) {
+                gt[w] = (uint16_t)tn;
+                for (const Task& T : seg_tasks[g][w]) {
+                    RecTask rt{(uint16_t)T.cell, (uint16_t)T.i0, (uint16_t)T.i1, 0};
+                    std::memcpy(B + H.off_tasks + (int64_t)tn * 8, &rt, 8);
+                    ++tn;
+                }
+            }
+            gt[rsegs[g].n_grp] = (uint16_t)tn;
         }
     }
     std::memcpy(B + H.off_nodes, nodes.data(), nodes.size() * 4);
@@ -427,6 +542,8 @@ int build_record(const HostProblem& hp, const std::vector<int32_t>& kcount, cons
     stage_out = n_slots * bs + n_fslots * nc;
     n_cells_out = n_cells;
     n_items_out = n_items;
+    out_len_out = 0;
+    for (const RecPass& P : passes) out_len_out = std::max(out_len_out, P.out_len);
     return 0;
 }
 
@@ -556,26 +673,28 @@ int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error&
         }
     }
     std::vector<std::vector<uint8_t>> recs(n_tiles);
-    std::vector<int32_t> rn(n_tiles), rs(n_tiles), rc(n_tiles), ri(n_tiles);
+    std::vector<int32_t> rn(n_tiles), rs(n_tiles), rc(n_tiles), ri(n_tiles), ro(n_tiles);
     int status = 0;
 #pragma omp parallel for schedule(dynamic, 16) reduction(max : status)
     for (int64_t t = 0; t < n_tiles; ++t) {
         const int st = build_record(hp, kcount, tile_local, eids.data() + tent[t], (int32_t)(tent[t + 1] - tent[t]),
-                                    trip.data() + tstart[t], tstart[t + 1] - tstart[t], recs[t], rn[t], rs[t], rc[t], ri[t]);
+                                    trip.data() + tstart[t], tstart[t + 1] - tstart[t], recs[t], rn[t], rs[t], rc[t], ri[t], ro[t]);
         status = std::max(status, st);
     }
     if (status == 1) return fail(err, FE_ERR_ARG, "internal: incident cell count mismatch");
     if (status == 2) return fail(err, FE_ERR_UNSUPPORTED, "an owned block has more than 255 contributions");
+    if (status == 4) return fail(err, FE_ERR_UNSUPPORTED, "the columns of one dof entity exceed the output buffer");
     if (status) return fail(err, FE_ERR_UNSUPPORTED, "a tile record exceeds its limits");
     plan.n_tiles = n_tiles;
     plan.rec_off.assign(n_tiles + 1, 0);
-    plan.max_rec = plan.max_nodes = plan.max_stage = 0;
+    plan.max_rec = plan.max_nodes = plan.max_stage = plan.max_out = 0;
     plan.visits = plan.items = 0;
     for (int64_t t = 0; t < n_tiles; ++t) {
         plan.rec_off[t + 1] = plan.rec_off[t] + (int64_t)recs[t].size();
         plan.max_rec = std::max(plan.max_rec, (int32_t)recs[t].size());
         plan.max_nodes = std::max(plan.max_nodes, rn[t]);
         plan.max_stage = std::max(plan.max_stage, rs[t]);
+        plan.max_out = std::max(plan.max_out, ro[t]);
         plan.visits += rc[t];
         plan.items += ri[t];
     }
@@ -607,56 +726,113 @@ int check_plan(const HostProblem& hp, const Plan& pl, Error& err) {
         std::memcpy(&H, B, sizeof(RecHead));
         auto in = [&](int64_t o, int64_t n) { return o >= 0 && (o & 15) == 0 && o + n <= len; };
         if (H.bytes != len || H.n_seg < 0 || H.n_ent < 0 || H.n_cells < 0 || H.n_items < 0 || H.n_red < 0 ||
-            H.n_nodes < 0 || H.n_nodes > pl.max_nodes || H.n_slots < 0 || H.n_fslots < 0 ||
-            (int64_t)sizeof(RecHead) + (int64_t)H.n_seg * 32 > len || !in(H.off_ent, (int64_t)H.n_ent * 16) ||
-            !in(H.off_fk, (int64_t)H.n_ent * 4) || !in(H.off_red, (int64_t)H.n_red * 4) || H.n_runs < 0 ||
-            H.n_runs > H.n_red || !in(H.off_runs, (int64_t)H.n_runs * 16) ||
-            !in(H.off_items, (int64_t)H.n_items * 4) || !in(H.off_cells, (int64_t)H.n_cells * 8) ||
-            !in(H.off_nodes, (int64_t)H.n_nodes * 4) || H.n_ent > MAX_TILE_ENTS ||
+            H.n_nodes < 0 || H.n_nodes > pl.max_nodes || H.n_slots < 0 || H.n_fslots < 0 || H.n_runs < 0 ||
+            H.n_pass < 0 || H.n_rng < 0 || H.n_tasks < 0 || !in(H.off_tasks, (int64_t)H.n_tasks * 8) ||
+            (int64_t)sizeof(RecHead) + (int64_t)H.n_seg * (int64_t)sizeof(RecSeg) > len ||
+            !in(H.off_ent, (int64_t)H.n_ent * 16) || !in(H.off_eid, (int64_t)H.n_ent * 4) ||
+            !in(H.off_fk, (int64_t)H.n_ent * 4) || !in(H.off_red, (int64_t)H.n_red * 4) ||
+            !in(H.off_runs, (int64_t)H.n_runs * 16) || !in(H.off_pass, (int64_t)H.n_pass * 32) ||
+            !in(H.off_rng, (int64_t)H.n_rng * 16) || !in(H.off_items, (int64_t)H.n_items * 4) ||
+            !in(H.off_cells, (int64_t)H.n_cells * 4) || !in(H.off_nodes, (int64_t)H.n_nodes * 4) ||
+            H.n_ent > MAX_TILE_ENTS ||
             (int64_t)H.n_slots * ((nc * nc + 1) & ~1) + (int64_t)H.n_fslots * nc > pl.max_stage) {
             bad = 1;
             continue;
         }
         const RecSeg* S = (const RecSeg*)(B + sizeof(RecHead));
         const RecEnt* E = (const RecEnt*)(B + H.off_ent);
+        const int32_t* EID = (const int32_t*)(B + H.off_eid);
         const uint32_t* FK = (const uint32_t*)(B + H.off_fk);
         const uint32_t* RED = (const uint32_t*)(B + H.off_red);
         const RecRun* RU = (const RecRun*)(B + H.off_runs);
+        const RecPass* PS = (const RecPass*)(B + H.off_pass);
+        const RecRng* RG = (const RecRng*)(B + H.off_rng);
         const uint32_t* IT = (const uint32_t*)(B + H.off_items);
-        const RecCell* C = (const RecCell*)(B + H.off_cells);
+        const int32_t* C = (const int32_t*)(B + H.off_cells);
         const int32_t* ND = (const int32_t*)(B + H.off_nodes);
         // entities: column base and length as in colptr; f slots inside the f area
         for (int32_t e = 0; e < H.n_ent && !bad; ++e) {
-            const int64_t n = E[e].id;
+            const int64_t n = EID[e];
             if (n < 0 || n >= hp.n_ent || E[e].colbase != cp[nc * n] - 1 || E[e].L != cp[nc * n + 1] - cp[nc * n] ||
                 E[e].colbase + (int64_t)nc * E[e].L > hp.nnz || (int64_t)(FK[e] & 0xFFFF) + (FK[e] >> 16) > H.n_fslots)
                 bad = 1;
         }
-        // owned blocks: ranks inside the column; runs cover the blocks in order and their slot
-        // ranges are consecutive and cover all slots (the kernel's lookup is restated here)
-        std::vector<int32_t> slot_block(H.n_slots, -1), RB(H.n_red + 1, 0);
-        if (H.n_red > 0 && (H.n_runs < 1 || RU[0].first != 0 || RU[0].base != 0)) bad = 1;
-        for (int32_t u = 0; u < H.n_runs && !bad; ++u) {
-            const int32_t end = u + 1 < H.n_runs ? RU[u + 1].first : H.n_red;
-            if (RU[u].first < 0 || end <= RU[u].first || end > H.n_red || RU[u].count < 0 || RU[u].count > MAX_ENT_CELLS ||
-                (u + 1 < H.n_runs && RU[u + 1].base != RU[u].base + (end - RU[u].first) * RU[u].count)) { bad = 1; break; }
-            for (int32_t q = RU[u].first; q < end; ++q) {
-                RB[q] = RU[u].base + (q - RU[u].first) * RU[u].count;
-                RB[q + 1] = RB[q] + RU[u].count;
+        // passes partition the blocks, runs and ranges in order; within a pass the runs cover
+        // its blocks and hand out k-major slot ranges, consecutive over the whole tile
+        std::vector<int32_t> slot_block(H.n_slots, -1), blk_pass(H.n_red, -1);
+        {
+            int32_t red_next = 0, run_next = 0, rng_next = 0, slot_next = 0;
+            for (int32_t p = 0; p < H.n_pass && !bad; ++p) {
+                const RecPass& P = PS[p];
+                if (P.red_begin != red_next || P.red_end < P.red_begin || P.red_end > H.n_red || P.run_begin != run_next ||
+                    P.run_end < P.run_begin || P.run_end > H.n_runs || P.rng_begin != rng_next || P.rng_end < P.rng_begin ||
+                    P.rng_end > H.n_rng || P.out_len < 0 || P.out_len > pl.max_out || P.out_len > OUT_CAP_DOUBLES) {
+                    bad = 1;
+                    break;
+                }
+                int32_t q = P.red_begin;
+                for (int32_t u = P.run_begin; u < P.run_end; ++u) {
+                    const RecRun& U = RU[u];
+                    if (U.first != q || U.nblk < 1 || q + U.nblk > P.red_end || U.count < 0 || U.count > MAX_ENT_CELLS ||
+                        U.base != slot_next || (int64_t)U.base + (int64_t)U.count * U.nblk > H.n_slots) { bad = 1; break; }
+                    // the kernel's lookup: block first + j, contribution k -> base + k * nblk + j
+                    for (int32_t j = 0; j < U.nblk; ++j) {
+                        blk_pass[q + j] = p;
+                        for (int32_t k = 0; k < U.count; ++k) slot_block[U.base + k * U.nblk + j] = q + j;
+                    }
+                    q += U.nblk;
+                    slot_next += U.count * U.nblk;
+                }
+                if (bad || q != P.red_end) { bad = 1; break; }
+                for (int32_t g = P.rng_begin; g < P.rng_end; ++g)
+                    if (RG[g].len < 1 || RG[g].buf_off < 0 || RG[g].buf_off + RG[g].len > P.out_len || ((RG[g].buf_off - RG[g].nz0) & 1) ||
+                        RG[g].nz0 < 0 || RG[g].nz0 + RG[g].len > hp.nnz) { bad = 1; break; }
+                red_next = P.red_end;
+                run_next = P.run_end;
+                rng_next = P.rng_end;
+            }
+            if (bad || red_next != H.n_red || run_next != H.n_runs || rng_next != H.n_rng || slot_next != H.n_slots) {
+                bad = 1;
+                continue;
             }
         }
-        for (int32_t q = 0; q < H.n_red && !bad; ++q) {
-            const int32_t e = (int32_t)(RED[q] >> RED_RANK_BITS), r = (int32_t)(RED[q] & ((1u << RED_RANK_BITS) - 1));
-            if (e >= H.n_ent || (int64_t)nc * r >= E[e].L || RB[q + 1] < RB[q] || RB[q + 1] > H.n_slots) { bad = 1; break; }
-            for (int32_t sl = RB[q]; sl < RB[q + 1]; ++sl) slot_block[sl] = q;
+        // blocks: ranks inside the column; every output entry lands in a buffer position of its
+        // pass that one range maps to that entry's nzval index, and every range position is written once
+        {
+            std::vector<std::vector<int32_t>> writes(H.n_pass);
+            for (int32_t p = 0; p < H.n_pass; ++p) writes[p].assign(PS[p].out_len, 0);
+            for (int32_t q = 0; q < H.n_red && !bad; ++q) {
+                const int32_t e = (int32_t)(RED[q] >> RED_RANK_BITS), r = (int32_t)(RED[q] & ((1u << RED_RANK_BITS) - 1));
+                const int32_t p = blk_pass[q];
+                if (e >= H.n_ent || (int64_t)nc * r >= E[e].L || p < 0) { bad = 1; break; }
+                const RecPass& P = PS[p];
+                for (int b = 0; b < nc && !bad; ++b)
+                    for (int x = 0; x < nc; ++x) {
+                        const int64_t i = (int64_t)E[e].out_off + (int64_t)b * E[e].L + (int64_t)nc * r + x;
+                        if (E[e].out_off < 0 || i >= P.out_len) { bad = 1; break; }
+                        const int64_t want = E[e].colbase + (int64_t)b * E[e].L + (int64_t)nc * r + x;
+                        int hits = 0;
+                        for (int32_t g = P.rng_begin; g < P.rng_end; ++g)
+                            if (i >= RG[g].buf_off && i < RG[g].buf_off + RG[g].len) {
+                                ++hits;
+                                if (RG[g].nz0 + (i - RG[g].buf_off) != want) bad = 1;
+                            }
+                        if (hits != 1) bad = 1;
+                        writes[p][i]++;
+                    }
+            }
+            for (int32_t p = 0; p < H.n_pass && !bad; ++p)
+                for (int32_t g = PS[p].rng_begin; g < PS[p].rng_end && !bad; ++g)
+                    for (int32_t i = RG[g].buf_off; i < RG[g].buf_off + RG[g].len; ++i)
+                        if (writes[p][i] != 1) { bad = 1; break; }
         }
-        if (bad || RB[H.n_red] != H.n_slots) { bad = 1; continue; }
+        if (bad) continue;
         for (int32_t e = 0; e < H.n_nodes && !bad; ++e)
             if (ND[e] < 0 || ND[e] >= hp.n_nodes) bad = 1;
         // segments, cells, items, slots
         std::vector<int32_t> slot_writes(H.n_slots, 0), fslot_writes(H.n_fslots, 0);
         std::vector<int64_t> slot_cell(H.n_slots, -1);  // (sub, cell) of each slot's contribution
-        int32_t cell_next = 0, item_next = 0;
+        int32_t cell_next = 0, item_next = 0, task_next = 0;
         for (int32_t g = 0; g < H.n_seg && !bad; ++g) {
             const RecSeg& G = S[g];
             if (G.sub < 0 || G.sub >= (int)hp.subs.size() || G.cell_begin != cell_next || G.cell_end < G.cell_begin ||
@@ -669,49 +845,68 @@ int check_plan(const HostProblem& hp, const Plan& pl, Error& err) {
                 !in(G.slot_off, (int64_t)(G.item_end - G.item_begin) * hs.nb * 2)) { bad = 1; break; }
             const uint16_t* CN = (const uint16_t*)(B + G.conn_off);
             const uint16_t* SL = (const uint16_t*)(B + G.slot_off);
-            int32_t it_expect = G.item_begin;
+            // cells: node list entries of the cell's nodes
             for (int32_t c = G.cell_begin; c < G.cell_end && !bad; ++c) {
-                const int64_t cell = C[c].cell;
-                if (cell < 0 || cell >= hs.n_cells || C[c].item_begin != it_expect || C[c].item_end < C[c].item_begin ||
-                    C[c].item_end > G.item_end) { bad = 1; break; }
-                it_expect = C[c].item_end;
+                const int64_t cell = C[c];
+                if (cell < 0 || cell >= hs.n_cells) { bad = 1; break; }
                 for (int a = 0; a < hs.ng; ++a) {
                     const int ln = CN[(int64_t)(c - G.cell_begin) * hs.ng + a];
                     if (ln >= H.n_nodes || ND[ln] != hs.conn[cell * hs.ng + a]) { bad = 1; break; }
                 }
-                for (int32_t it = C[c].item_begin; it < C[c].item_end && !bad; ++it) {
-                    const int j = (int)(IT[it] & 0xFF);
-                    const int32_t fs = (int32_t)(IT[it] >> 16);
-                    if (j >= hs.nb || fs >= H.n_fslots) { bad = 1; break; }
-                    fslot_writes[fs]++;
-                    const int64_t n = hs.ents[cell * hs.nb + j];
-                    for (int i = 0; i < hs.nb; ++i) {
-                        const uint16_t sl = SL[(int64_t)(it - G.item_begin) * hs.nb + i];
-                        const int r = rank_of(hs, cell, j, i);
-                        if (sl == SLOT_MISS) {
-                            if (r >= 0) { bad = 1; break; }
-                            continue;
+            }
+            // group task table: consecutive task ranges; tasks inside the segment, together
+            // covering each item of the segment exactly once; each item's j, f slot and slots
+            // are those of the task's cell
+            if (bad || G.n_grp < 1 || !in(G.gt_off, (int64_t)(G.n_grp + 1) * 2)) { bad = 1; break; }
+            const uint16_t* GT = (const uint16_t*)(B + G.gt_off);
+            const RecTask* TK = (const RecTask*)(B + H.off_tasks);
+            if (GT[0] != task_next || GT[G.n_grp] > H.n_tasks) { bad = 1; break; }
+            std::vector<int32_t> cover(G.item_end - G.item_begin, 0);
+            for (int32_t w = 0; w < G.n_grp && !bad; ++w) {
+                if (GT[w + 1] < GT[w]) { bad = 1; break; }
+                for (int32_t q = GT[w]; q < GT[w + 1] && !bad; ++q) {
+                    const RecTask& T = TK[q];
+                    if (T.cell < G.cell_begin || T.cell >= G.cell_end || T.item_begin < G.item_begin || T.item_end > G.item_end ||
+                        T.item_end < T.item_begin) { bad = 1; break; }
+                    const int64_t cell = C[T.cell];
+                    for (int32_t it = T.item_begin; it < T.item_end && !bad; ++it) {
+                        cover[it - G.item_begin]++;
+                        const int j = (int)(IT[it] & 0xFF);
+                        const int32_t fs = (int32_t)(IT[it] >> 16);
+                        if (j >= hs.nb || fs >= H.n_fslots) { bad = 1; break; }
+                        fslot_writes[fs]++;
+                        const int64_t n = hs.ents[cell * hs.nb + j];
+                        for (int i = 0; i < hs.nb; ++i) {
+                            const uint16_t sl = SL[(int64_t)(it - G.item_begin) * hs.nb + i];
+                            const int r = rank_of(hs, cell, j, i);
+                            if (sl == SLOT_MISS) {
+                                if (r >= 0) { bad = 1; break; }
+                                continue;
+                            }
+                            if (sl >= H.n_slots || r < 0) { bad = 1; break; }
+                            const int32_t qb = slot_block[sl];
+                            const int32_t e = (int32_t)(RED[qb] >> RED_RANK_BITS);
+                            if (EID[e] != n || (int32_t)(RED[qb] & ((1u << RED_RANK_BITS) - 1)) != r) { bad = 1; break; }
+                            slot_writes[sl]++;
+                            slot_cell[sl] = ((int64_t)G.sub << 32) | cell;
                         }
-                        if (sl >= H.n_slots || r < 0) { bad = 1; break; }
-                        const int32_t q = slot_block[sl];
-                        const int32_t e = (int32_t)(RED[q] >> RED_RANK_BITS);
-                        if (E[e].id != n || (int32_t)(RED[q] & ((1u << RED_RANK_BITS) - 1)) != r) { bad = 1; break; }
-                        slot_writes[sl]++;
-                        slot_cell[sl] = ((int64_t)G.sub << 32) | cell;
                     }
                 }
             }
-            if (it_expect != G.item_end) bad = 1;
+            for (int32_t it = 0; it < G.item_end - G.item_begin && !bad; ++it)
+                if (cover[it] != 1) bad = 1;
+            task_next = GT[G.n_grp];
             cell_next = G.cell_end;
             item_next = G.item_end;
         }
-        if (bad || cell_next != H.n_cells || item_next != H.n_items) { bad = 1; continue; }
+        if (bad || cell_next != H.n_cells || item_next != H.n_items || task_next != H.n_tasks) { bad = 1; continue; }
         for (int32_t sl = 0; sl < H.n_slots; ++sl)
             if (slot_writes[sl] != 1) { bad = 1; break; }
         // each block sums its contributions in cell order: (sub, cell) increasing along its slots
-        for (int32_t q = 0; q < H.n_red && !bad; ++q)
-            for (int32_t sl = RB[q] + 1; sl < RB[q + 1]; ++sl)
-                if (slot_cell[sl] <= slot_cell[sl - 1]) { bad = 1; break; }
+        for (int32_t u = 0; u < H.n_runs && !bad; ++u)
+            for (int32_t j = 0; j < RU[u].nblk && !bad; ++j)
+                for (int32_t k = 1; k < RU[u].count; ++k)
+                    if (slot_cell[RU[u].base + k * RU[u].nblk + j] <= slot_cell[RU[u].base + (k - 1) * RU[u].nblk + j]) { bad = 1; break; }
         for (int32_t fs = 0; fs < H.n_fslots; ++fs)
             if (fslot_writes[fs] != 1) { bad = 1; break; }
     }

@@ -48,7 +48,7 @@ struct Plan {
     std::vector<uint8_t> rec;       // tile records, concatenated (each 16-byte aligned)
     std::vector<int64_t> rec_off;   // [n_tiles + 1] byte offsets
     int64_t n_tiles = 0;
-    int32_t max_rec = 0, max_nodes = 0, max_stage = 0;
+    int32_t max_rec = 0, max_nodes = 0, max_stage = 0, max_out = 0;
     int64_t visits = 0, items = 0;
 };
 

@@ -46,9 +46,15 @@ template <> struct ElemT<KIND_WEDGE6> { static constexpr int DIM = 3, NG = 6, NB
 template <> struct ElemT<KIND_HEX27>  { static constexpr int DIM = 3, NG = 8, NB = 27, GS = 32; };
 template <> struct ElemT<KIND_QUAD9>  { static constexpr int DIM = 2, NG = 4, NB = 9, GS = 16; };
 
+static_assert(ElemT<KIND_TRI3>::GS == GROUP_LANES[KIND_TRI3] && ElemT<KIND_QUAD4>::GS == GROUP_LANES[KIND_QUAD4] &&
+                  ElemT<KIND_TET4>::GS == GROUP_LANES[KIND_TET4] && ElemT<KIND_HEX8>::GS == GROUP_LANES[KIND_HEX8] &&
+                  ElemT<KIND_WEDGE6>::GS == GROUP_LANES[KIND_WEDGE6] && ElemT<KIND_HEX27>::GS == GROUP_LANES[KIND_HEX27] &&
+                  ElemT<KIND_QUAD9>::GS == GROUP_LANES[KIND_QUAD9],
+              "lane groups agree with the planner");
+
 constexpr int PHYS_HEAT = 1, PHYS_ELASTIC = 2, PHYS_NEO = 3;
 constexpr int NEO_EXTRA = 32;  // per (cell, qp): T = S + c1 C^-1 (9), B = F^-T (9), c1, 2c2, P (9), pad
-constexpr int THREADS = 256;
+constexpr int THREADS = CTA_THREADS;
 
 struct __align__(16) D4 {
     double x, y, z, w;
@@ -196,13 +202,17 @@ __device__ __forceinline__ void neo_hooke_point(R mu, R lam, const R* H, R* out)
 // per-CTA shared memory
 // ---------------------------------------------------------------------------------------
 constexpr int REC_RING = 3;     // records in flight: tile t (computing), t + G, t + 2G
-constexpr int NODE_BYTES = 32;  // gathered coordinates per node (two 16-byte halves)
+constexpr int NODE_BYTES = 24;  // gathered coordinates per node (three 8-byte pieces)
 
 // Shared-memory layout of a CTA, computed in one place for the kernel and the host.
 struct SmemLayout {
-    int shape, rec, coords, stage, chunk;
+    int shape, rec, coords, stage, chunk;  // chunk: cell tables, then the reduce's output buffer
 };
 __host__ __device__ inline int pad16i(int b) { return (b + 15) & ~15; }
+__host__ __device__ inline int chunk_region_bytes(const KernelArgs& a) {
+    const int out = pad16i(a.out_cap * 8);
+    return a.chunk_bytes > out ? a.chunk_bytes : out;
+}
 __host__ __device__ inline SmemLayout smem_layout(const KernelArgs& a, int shape_bytes, int real_bytes) {
     SmemLayout L;
     int o = 0;
@@ -227,21 +237,65 @@ template <typename P> __device__ __forceinline__ P pzero();
 template <> __device__ __forceinline__ float2 pzero<float2>() { return make_float2(0.f, 0.f); }
 template <> __device__ __forceinline__ double2 pzero<double2>() { return make_double2(0.0, 0.0); }
 
-// Cell table layout (one cell of a chunk), quadrature points taken in pairs (q0 = 2p, q1 = 2p+1;
-// an odd count is padded with a zero-weight point):
-//   grad[NQP][NB][8] : (gx0, gx1, gy0, gy1, gz0, gz1, n0, n1), g = sqrt(detJ w) gradN, n = sqrt(detJ w) N
+// Reference tables in shared memory, one record per quadrature point q (element offsets):
+//   dM[NG][DIM] at dm, dN[NB][DIM] at dn, N[NB] at n, w at w; every section starts on 16
+//   bytes and the record stride qs is an odd multiple of 16 bytes, so the 8 lanes of a quarter
+//   warp (lane = q) read their records with conflict-free 16-byte loads.
+struct ShapeQ {
+    int dm, dn, n, w, qs;
+};
+__host__ __device__ constexpr int round_up(int x, int m) { return (x + m - 1) / m * m; }
+__host__ __device__ constexpr ShapeQ shape_q(int nb, int ng, int dim, int real_bytes) {
+    const int v = 16 / real_bytes;
+    ShapeQ s{};
+    s.dm = 0;
+    s.dn = round_up(ng * dim, v);
+    s.n = s.dn + round_up(nb * dim, v);
+    s.w = s.n + round_up(nb, v);
+    int q = s.w + v;
+    if ((q / v) % 2 == 0) q += v;
+    s.qs = q;
+    return s;
+}
+
+// Cell table layout (one per lane group), quadrature points taken in pairs (q0 = 2p,
+// q1 = 2p+1; an odd count is padded with a zero-weight point):
+//   grad[NQP][SP]    : at p*SP + i*6: (gx0, gx1, gy0, gy1, gz0, gz1), g = sqrt(detJ w) gradN
 //   sq[NQP][2]       : sqrt(detJ w) per point
 //   cellp[4]         : per-cell material values
 //   neo[NQ][NEO_EXTRA] (Neo-Hooke only)
+// SP (>= 6 NB) is chosen so that the lanes of a warp (lane = point, GS lanes per group, group
+// tables GS words apart modulo 32) write their values to distinct shared-memory banks.
+__host__ __device__ constexpr int table_sp(int nb, int nqp, int gs) {
+    const int groups = gs >= 32 ? 1 : 32 / gs;
+    const int pmax = nqp < gs / 2 ? nqp : gs / 2;
+    for (int sp = nb * 6; sp < nb * 6 + 64; sp += 2) {
+        unsigned mask = 0;
+        bool ok = true;
+        for (int g = 0; g < groups && ok; ++g)
+            for (int p = 0; p < pmax && ok; ++p)
+                for (int h = 0; h < 2 && ok; ++h) {
+                    const int bank = (g * gs + p * sp + h) % 32;
+                    if ((mask >> bank) & 1u) ok = false;
+                    mask |= 1u << bank;
+                }
+        if (ok) return sp;
+    }
+    return nb * 6;
+}
 template <int K, int NQ, int PHYS, typename Real>
 struct CellTable {
-    static constexpr int NB = ElemT<K>::NB;
+    static constexpr int NB = ElemT<K>::NB, GS = ElemT<K>::GS;
     static constexpr int NQP = (NQ + 1) / 2;
-    static constexpr int GRAD = NQP * NB * 8;
+    static constexpr int SP = table_sp(NB, NQP, GS);
+    static constexpr int GRAD = NQP * SP;
     static constexpr int SQ = NQP * 2;
     static constexpr int NEO = PHYS == PHYS_NEO ? NQ * NEO_EXTRA : 0;
-    static constexpr int REALS = GRAD + SQ + 4 + NEO;
-    static constexpr int BYTES = (REALS * (int)sizeof(Real) + 15) & ~15;
+    static constexpr int USED = GRAD + SQ + 4 + NEO;
+    // group stride = GS (mod 32) elements
+    static constexpr int REALS = USED + ((GS % 32 - USED % 32) + 32) % 32;
+    static constexpr int BYTES = REALS * (int)sizeof(Real);
+    static_assert(BYTES % 16 == 0, "group tables stay 16-byte aligned");
 };
 
 template <int K, int NQ, int PHYS, typename Real>
@@ -249,29 +303,41 @@ __host__ __device__ constexpr int cell_table_bytes() {
     return CellTable<K, NQ, PHYS, Real>::BYTES;
 }
 
-// shape table block per subdomain: w[NQ], N[NQ][NB], dN[NQ][NB][DIM], dM[NQ][NG][DIM],
-// each padded to a multiple of 16 bytes
 __host__ __device__ inline int pad16(int bytes) { return (bytes + 15) & ~15; }
-template <typename Real>
-__host__ __device__ inline int shape_block_bytes(int nq, int nb, int ng, int dim) {
-    return pad16(nq * (int)sizeof(Real)) + pad16(nq * nb * (int)sizeof(Real)) + pad16(nq * nb * dim * (int)sizeof(Real)) +
-           pad16(nq * ng * dim * (int)sizeof(Real));
-}
 
+// 16-byte vector loads of N (a multiple of 16 bytes) reals from a 16-byte aligned address
+template <typename Real, int N>
+__device__ __forceinline__ void lds16(const Real* p, Real* out) {
+    if constexpr (sizeof(Real) == 4) {
+        #pragma unroll
+        for (int t = 0; t < N / 4; ++t) {
+            const float4 v = ((const float4*)p)[t];
+            out[4 * t] = v.x; out[4 * t + 1] = v.y; out[4 * t + 2] = v.z; out[4 * t + 3] = v.w;
+        }
+    } else {
+        #pragma unroll
+        for (int t = 0; t < N / 2; ++t) {
+            const double2 v = ((const double2*)p)[t];
+            out[2 * t] = v.x; out[2 * t + 1] = v.y;
+        }
+    }
+}
 
 // ---------------------------------------------------------------------------------------
 // geometry of one cell by its lane group: lane q = quadrature point (NQ <= GS, NG <= GS).
-// Node coordinates are loaded once per node (lane k loads node k) and shared with shuffles.
-// Results go to the q-paired table layout; a padded point (odd NQ) is written as zeros.
+// Node coordinates are loaded once per node (lane k loads node k) and shared with shuffles;
+// the lane's reference-table record comes in 16-byte loads. Results go to the q-paired table
+// layout; a padded point (odd NQ) is written as zeros.
 // ---------------------------------------------------------------------------------------
 template <int K, int NQ, int PHYS, typename Real>
-__device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev& sd, const Real* w_s, const Real* N_s,
-                                               const Real* dN_s, const Real* dM_s, int cell, const uint16_t* cn,
-                                               const char* xs, const int32_t* nodes, int lane, unsigned gmask, int gbase,
-                                               Real* tb) {
+__device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev& sd, const Real* shp, int cell,
+                                               const uint16_t* cn, const char* xs, const int32_t* nodes, int lane,
+                                               unsigned gmask, int gbase, Real* tb) {
     using E = ElemT<K>;
     using CT = CellTable<K, NQ, PHYS, Real>;
     constexpr int NB = E::NB, NG = E::NG, DIM = E::DIM;
+    constexpr ShapeQ SQL = shape_q(NB, NG, DIM, (int)sizeof(Real));
+    constexpr int V = 16 / (int)sizeof(Real);
     static_assert(NQ <= E::GS && NG <= E::GS, "one lane per point and per node");
     Real* grad = tb;
     Real* sq = tb + CT::GRAD;
@@ -281,9 +347,10 @@ __device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev
     Real off[NG][DIM];
     if constexpr (sizeof(Real) == 4) {
         const int ln = cn[lane < NG ? lane : 0];
-        const float4 h4 = *(const float4*)(xs + ln * NODE_BYTES);
-        const float4 l4 = *(const float4*)(xs + ln * NODE_BYTES + 16);
-        const float h[3] = {h4.x, h4.y, h4.z}, l[3] = {l4.x, l4.y, l4.z};
+        const float2 p0 = *(const float2*)(xs + ln * NODE_BYTES);
+        const float2 p1 = *(const float2*)(xs + ln * NODE_BYTES + 8);
+        const float2 p2 = *(const float2*)(xs + ln * NODE_BYTES + 16);
+        const float h[3] = {p0.x, p0.y, p1.x}, l[3] = {p1.y, p2.x, p2.y};
         float o[DIM];
         #pragma unroll
         for (int x = 0; x < DIM; ++x) {
@@ -305,15 +372,20 @@ __device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev
     }
     if (lane >= NQ) return;
     const int q = lane;
+    const Real* Q = shp + q * SQL.qs;
     Real J[DIM * DIM];
-    #pragma unroll
-    for (int t = 0; t < DIM * DIM; ++t) J[t] = Real(0);
-    #pragma unroll
-    for (int k = 1; k < NG; ++k)
+    {
+        Real dm[round_up(NG * DIM, V)];
+        lds16<Real, round_up(NG * DIM, V)>(Q + SQL.dm, dm);
         #pragma unroll
-        for (int x = 0; x < DIM; ++x)
+        for (int t = 0; t < DIM * DIM; ++t) J[t] = Real(0);
+        #pragma unroll
+        for (int k = 1; k < NG; ++k)
             #pragma unroll
-            for (int b = 0; b < DIM; ++b) J[x * DIM + b] += off[k][x] * dM_s[(q * NG + k) * DIM + b];
+            for (int x = 0; x < DIM; ++x)
+                #pragma unroll
+                for (int b = 0; b < DIM; ++b) J[x * DIM + b] += off[k][x] * dm[k * DIM + b];
+    }
     Real dt = Mat<Real, DIM>::det(J);
     Real Ji[DIM * DIM];
     bool bad = !(dt > Real(0));
@@ -356,7 +428,14 @@ __device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev
         #pragma unroll
         for (int t = 0; t < DIM * DIM; ++t) Ji[t] = Real(0);
     }
-    const Real s = sqrt(dt * w_s[q]);
+    // small elements keep the whole dN record in registers; large ones read it per node
+    constexpr bool DN_REG = NB * DIM <= 32;
+    Real dN[DN_REG ? round_up(NB * DIM, V) : 1];
+    if constexpr (DN_REG) lds16<Real, round_up(NB * DIM, V)>(Q + SQL.dn, dN);
+    const Real s = sqrt(dt * Q[SQL.w]);
+    // scale J^-1 by sqrt(detJ w) once: every gradient below is then a plain product
+    #pragma unroll
+    for (int t = 0; t < DIM * DIM; ++t) Ji[t] *= s;
     const int p = q >> 1, hh = q & 1;
     const bool pad = (NQ & 1) && q == NQ - 1;
     sq[2 * p + hh] = s;
@@ -370,15 +449,18 @@ __device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev
         #pragma unroll
         for (int b = 0; b < DIM; ++b)
             #pragma unroll
-            for (int c = 0; c < DIM; ++c) g[b] += dN_s[(q * NB + i) * DIM + c] * Ji[c * DIM + b];
-        Real* o = grad + (p * NB + i) * 8 + hh;
-        o[0] = g[0] * s;
-        o[2] = g[1] * s;
-        o[4] = g[2] * s;
-        o[6] = N_s[q * NB + i] * s;
-        if (pad) { o[1] = Real(0); o[3] = Real(0); o[5] = Real(0); o[7] = Real(0); }
+            for (int c = 0; c < DIM; ++c) {
+                if constexpr (DN_REG) g[b] += dN[i * DIM + c] * Ji[c * DIM + b];
+                else g[b] += Q[SQL.dn + i * DIM + c] * Ji[c * DIM + b];
+            }
+        Real* o = grad + p * CT::SP + i * 6 + hh;
+        o[0] = g[0];
+        o[2] = g[1];
+        o[4] = g[2];
+        if (pad) { o[1] = Real(0); o[3] = Real(0); o[5] = Real(0); }
         if constexpr (PHYS == PHYS_NEO) {
-            // H = grad u = sum_i u_i (x) gradN_i (function_gradient, common_values.jl:217-227)
+            // H = grad u = sum_i u_i (x) gradN_i (function_gradient, common_values.jl:217-227),
+            // accumulated with the scaled gradients and unscaled below
             const int64_t e3 = (int64_t)sd.ents[(int64_t)cell * NB + i] * 3;
             #pragma unroll
             for (int c = 0; c < 3; ++c) {
@@ -404,7 +486,12 @@ __device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev
             cellp[1] = (Real)a.phys.p1;
         }
     }
-    if constexpr (PHYS == PHYS_NEO) neo_hooke_point<Real>((Real)a.phys.p0, (Real)a.phys.p1, H, neo + q * NEO_EXTRA);
+    if constexpr (PHYS == PHYS_NEO) {
+        const Real is = s > Real(0) ? Real(1) / s : Real(0);
+        #pragma unroll
+        for (int t = 0; t < 9; ++t) H[t] *= is;
+        neo_hooke_point<Real>((Real)a.phys.p0, (Real)a.phys.p1, H, neo + q * NEO_EXTRA);
+    }
 }
 
 // ---------------------------------------------------------------------------------------
@@ -412,11 +499,13 @@ __device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev
 // ---------------------------------------------------------------------------------------
 template <int K, int NQ, int PHYS, typename Real>
 __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& sd, const char* R, const uint16_t* slot_rows,
-                                            Real* stage, int f_off, const Real* tb, int cell, int i, int it0, int it1) {
+                                            Real* stage, int f_off, const Real* tb, const Real* shp, int cell, int i, int it0,
+                                            int it1) {
     using E = ElemT<K>;
     using CT = CellTable<K, NQ, PHYS, Real>;
     using P = typename Pair<Real>::type;
-    constexpr int NB = E::NB, DIM = E::DIM, NQP = CT::NQP;
+    constexpr int NB = E::NB, NG = E::NG, DIM = E::DIM, NQP = CT::NQP;
+    constexpr ShapeQ SQL = shape_q(NB, NG, DIM, (int)sizeof(Real));
     constexpr int NC_MAX = DIM;
     constexpr bool CACHE = NQP <= 4;  // keep the row function's table in registers
     const int nc = a.nc;
@@ -425,12 +514,23 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
     const Real* cellp = sq + CT::SQ;
     const Real* neo = cellp + 4;
     const uint32_t* items = (const uint32_t*)(R + ((const RecHead*)R)->off_items);
-    P gi[CACHE ? NQP : 1][4];
+    P gi[CACHE ? NQP : 1][3];
     if constexpr (CACHE) {
         #pragma unroll
         for (int p = 0; p < NQP; ++p)
             #pragma unroll
-            for (int c = 0; c < 4; ++c) gi[p][c] = *(const P*)(grad + (p * NB + i) * 8 + 2 * c);
+            for (int c = 0; c < 3; ++c) gi[p][c] = *(const P*)(grad + p * CT::SP + i * 6 + 2 * c);
+    }
+    // volume load of this lane's function: sum_q N_i(q) detJ w (the body-force / source term)
+    Real Fi = Real(0);
+    if constexpr (PHYS != PHYS_NEO) {
+        if (a.do_f) {
+            #pragma unroll
+            for (int q = 0; q < NQ; ++q) {
+                const Real s = sq[q];
+                Fi += s * s * shp[q * SQL.qs + SQL.n + i];
+            }
+        }
     }
     for (int it = it0; it < it1; ++it) {
         const uint32_t word = items[it];
@@ -445,19 +545,18 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
         for (int t = 0; t < NC_MAX; ++t) fe[t] = Real(0);
         if constexpr (PHYS == PHYS_HEAT || PHYS == PHYS_ELASTIC) {
             P G[DIM][DIM];
-            P ff = pzero<P>();
             #pragma unroll
             for (int x = 0; x < DIM; ++x)
                 #pragma unroll
                 for (int y = 0; y < DIM; ++y) G[x][y] = pzero<P>();
             #pragma unroll
             for (int p = 0; p < NQP; ++p) {
-                P ri[4], rj[4];
+                P ri[3], rj[3];
                 #pragma unroll
-                for (int c = 0; c < 4; ++c) {
+                for (int c = 0; c < 3; ++c) {
                     if constexpr (CACHE) ri[c] = gi[p][c];
-                    else ri[c] = *(const P*)(grad + (p * NB + i) * 8 + 2 * c);
-                    rj[c] = *(const P*)(grad + (p * NB + j) * 8 + 2 * c);
+                    else ri[c] = *(const P*)(grad + p * CT::SP + i * 6 + 2 * c);
+                    rj[c] = *(const P*)(grad + p * CT::SP + j * 6 + 2 * c);
                 }
                 if constexpr (PHYS == PHYS_HEAT) {
                     #pragma unroll
@@ -468,11 +567,10 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
                         #pragma unroll
                         for (int y = 0; y < DIM; ++y) G[x][y] = pfma(ri[x], rj[y], G[x][y]);
                 }
-                ff = pfma(*(const P*)(sq + 2 * p), rj[3], ff);
             }
             if constexpr (PHYS == PHYS_HEAT) {
                 Kb[0] = cellp[0] * (G[0][0].x + G[0][0].y);
-                fe[0] = cellp[1] * (ff.x + ff.y);
+                fe[0] = cellp[1] * Fi;
             } else {
                 Real g[DIM][DIM];
                 #pragma unroll
@@ -487,18 +585,18 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
                 for (int x = 0; x < DIM; ++x)
                     #pragma unroll
                     for (int y = 0; y < DIM; ++y) Kb[x * DIM + y] = lam * g[x][y] + mu * g[y][x] + (x == y ? mu * tr : Real(0));
-                const Real fs = ff.x + ff.y;
                 #pragma unroll
-                for (int x = 0; x < DIM; ++x) fe[x] = fs * (Real)a.phys.body[x];
+                for (int x = 0; x < DIM; ++x) fe[x] = Fi * (Real)a.phys.body[x];
             }
         } else {  // PHYS_NEO: per point, scalar
             #pragma unroll 1
             for (int q = 0; q < NQ; ++q) {
                 const int p = q >> 1, h = q & 1;
-                const Real* gio = grad + (p * NB + i) * 8 + h;
-                const Real* gjo = grad + (p * NB + j) * 8 + h;
+                const Real* gio = grad + p * CT::SP + i * 6 + h;
+                const Real* gjo = grad + p * CT::SP + j * 6 + h;
                 const Real ai[3] = {gio[0], gio[2], gio[4]}, aj[3] = {gjo[0], gjo[2], gjo[4]};
-                const Real nj = gjo[6];
+                const Real s = sq[q];
+                const Real nj = shp[q * SQL.qs + SQL.n + j] * s;
                 const Real* nq_ = neo + q * NEO_EXTRA;
                 Real Bi[3], Bj[3], tij = 0;
                 #pragma unroll
@@ -515,7 +613,6 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
                     for (int y = 0; y < 3; ++y)
                         Kb[x * 3 + y] += (x == y ? tij : Real(0)) + c1 * Bi[y] * Bj[x] + c2x2 * Bi[x] * Bj[y];
                 // residual: (gradN_j : P - N_j b) dV
-                const Real s = sq[2 * p + h];
                 #pragma unroll
                 for (int x = 0; x < 3; ++x)
                     fe[x] += s * (nq_[20 + x * 3] * aj[0] + nq_[20 + x * 3 + 1] * aj[1] + nq_[20 + x * 3 + 2] * aj[2] -
@@ -568,12 +665,8 @@ __device__ __forceinline__ void process_segment(const KernelArgs& a, const SubDe
     using E = ElemT<K>;
     using CT = CellTable<K, NQ, PHYS, Real>;
     constexpr int NB = E::NB, NG = E::NG, DIM = E::DIM, GS = E::GS;
-    const Real* w_s = shp;
-    const Real* N_s = (const Real*)((const char*)w_s + pad16(NQ * sizeof(Real)));
-    const Real* dN_s = (const Real*)((const char*)N_s + pad16(NQ * NB * sizeof(Real)));
-    const Real* dM_s = (const Real*)((const char*)dN_s + pad16(NQ * NB * DIM * sizeof(Real)));
     const RecHead* H = (const RecHead*)R;
-    const RecCell* cells = (const RecCell*)(R + H->off_cells);
+    const int32_t* cells = (const int32_t*)(R + H->off_cells);
     const int32_t* nodes = (const int32_t*)(R + H->off_nodes);
     const uint16_t* conn = (const uint16_t*)(R + g.conn_off);
     const uint16_t* slots = (const uint16_t*)(R + g.slot_off);
@@ -586,16 +679,22 @@ __device__ __forceinline__ void process_segment(const KernelArgs& a, const SubDe
     const int lane = tid % GS, grp = tid / GS;
     const unsigned gmask = GS >= 32 ? 0xFFFFFFFFu : (((1u << GS) - 1u) << ((tid & 31) / GS * GS));
     Real* tb = (Real*)(chunk + grp * CT::BYTES);
-    const int n_cells = g.cell_end - g.cell_begin;
-    for (int c = grp < ngrp ? grp : n_cells; c < n_cells; c += ngrp) {
-        const RecCell ce = cells[g.cell_begin + c];
-        geometry_lanes<K, NQ, PHYS, Real>(a, sd, w_s, N_s, dN_s, dM_s, ce.cell, conn + c * NG, xs, nodes, lane, gmask,
-                                          (tid & 31) - lane, tb);
-        __syncwarp(gmask);
-        if (lane < NB)
-            cell_blocks<K, NQ, PHYS, Real>(a, sd, R, slots + (ce.item_begin - g.item_begin) * NB, stage, f_off, tb, ce.cell,
-                                           lane, ce.item_begin, ce.item_end);
-        __syncwarp(gmask);  // the next cell overwrites the table
+    const uint16_t* gt = (const uint16_t*)(R + g.gt_off);
+    const RecTask* tasks = (const RecTask*)(R + H->off_tasks);
+    // the plan's groups run on this CTA's groups round robin (the same when the counts agree)
+    for (int pg = grp; grp < ngrp && pg < g.n_grp; pg += ngrp) {
+        const int t1 = gt[pg + 1];
+        for (int ti = gt[pg]; ti < t1; ++ti) {
+            const RecTask tk = tasks[ti];
+            const int cell = cells[tk.cell];
+            geometry_lanes<K, NQ, PHYS, Real>(a, sd, shp, cell, conn + (tk.cell - g.cell_begin) * NG, xs, nodes, lane, gmask,
+                                              (tid & 31) - lane, tb);
+            __syncwarp(gmask);
+            if (lane < NB)
+                cell_blocks<K, NQ, PHYS, Real>(a, sd, R, slots + (tk.item_begin - g.item_begin) * NB, stage, f_off, tb, shp, cell,
+                                               lane, tk.item_begin, tk.item_end);
+            __syncwarp(gmask);  // the next task overwrites the table
+        }
     }
 }
 
@@ -614,109 +713,205 @@ __device__ __forceinline__ void acc_add2(float2& hi, float2& lo, float2 x) {
     lo = __fadd2_rn(lo, e);
 }
 
-// Blocks are taken in the plan's order (most contributions first, so the lanes of a warp
-// run loops of equal length; the lane does not change any value).
+// TMA bulk stores shared -> global (both addresses 16-byte aligned, size a multiple of 16)
+__device__ __forceinline__ void bulk_store(double* dst, uint32_t src, int bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+// One f entry (owned entity e, component x): its cells' contributions in cell order.
 template <int NC, typename Real>
-__device__ __forceinline__ void reduce_tile(const KernelArgs& a, const char* R, const Real* stage) {
+__device__ __forceinline__ void f_entry(const KernelArgs& a, const char* R, const Real* stage, int idx) {
+    const RecHead* H = (const RecHead*)R;
+    const int32_t* eid = (const int32_t*)(R + H->off_eid);
+    const uint32_t* fk = (const uint32_t*)(R + H->off_fk);
+    const int e = idx / NC, x = idx - e * NC;
+    const uint32_t w = fk[e];
+    const int fb = (int)(w & 0xFFFF), kcnt = (int)(w >> 16);
+    const int64_t gi = (int64_t)eid[e] * NC + x;
+    const Real* v = stage + H->n_slots * ((NC * NC + 1) & ~1) + fb * NC + x;
+    double out;
+    if constexpr (sizeof(Real) == 4) {
+        if (a.compensated) {
+            float2 acc = make_float2(0.f, 0.f);
+            if (!a.fillzero) acc_set(acc, a.f[gi]);
+            for (int k = 0; k < kcnt; ++k) acc_add(acc, v[k * NC]);
+            out = acc_value(acc);
+        } else {
+            float acc = 0.f;
+            for (int k = 0; k < kcnt; ++k) acc += v[k * NC];
+            out = float_to_double(acc);
+            if (!a.fillzero) out += a.f[gi];
+        }
+    } else {
+        double acc = a.fillzero ? 0.0 : a.f[gi];
+        for (int k = 0; k < kcnt; ++k) acc += v[k * NC];
+        out = acc;
+    }
+    __stcs(a.f + gi, out);
+}
+
+// Per pass: blocks in the plan's order (most contributions first, so the lanes of a warp run
+// loops of equal length and read consecutive slots; the lane does not change any value) are
+// summed into the shared output buffer in nzval order; then each contiguous nzval range is
+// written by one bulk store (its 16-byte aligned middle) and plain stores (its ends). With an
+// nzval pointer that is only 8-byte aligned, all threads copy the buffer out instead. The f
+// entries ride on the lanes of the last pass that have no block left.
+template <int NC, typename Real>
+__device__ __forceinline__ void reduce_tile(const KernelArgs& a, const char* R, const Real* stage, double* outb) {
     constexpr int NCC = NC * NC, BS = (NCC + 1) & ~1, NP = BS / 2;
     const RecHead* H = (const RecHead*)R;
+    const int nf = a.do_f ? H->n_ent * NC : 0;
+    if (!a.do_k) {
+        for (int idx = threadIdx.x; idx < nf; idx += THREADS) f_entry<NC, Real>(a, R, stage, idx);
+        return;
+    }
     const RecEnt* ents = (const RecEnt*)(R + H->off_ent);
     const uint32_t* red = (const uint32_t*)(R + H->off_red);
     const RecRun* runs = (const RecRun*)(R + H->off_runs);
-    const int n_red = H->n_red, n_runs = H->n_runs;
-    int u = 0;  // run of the current block (positions only grow)
-    for (int pos = threadIdx.x; pos < n_red; pos += THREADS) {
-        const uint32_t key = red[pos];
-        const int e = (int)(key >> RED_RANK_BITS), r = (int)(key & ((1u << RED_RANK_BITS) - 1));
-        while (u + 1 < n_runs && runs[u + 1].first <= pos) ++u;
-        const int4 ru = *(const int4*)(runs + u);
-        const int s0 = ru.z + (pos - ru.x) * ru.y, s1 = s0 + ru.y;
-        const RecEnt en = ents[e];
-        const int64_t c0 = en.colbase + (int64_t)NC * r;
-        const int64_t L = en.L;
-        double out[NCC];
-        if constexpr (sizeof(Real) == 4) {
-            float2 hi[NP], lo[NP];
-            #pragma unroll
-            for (int t = 0; t < NP; ++t) { hi[t] = make_float2(0.f, 0.f); lo[t] = make_float2(0.f, 0.f); }
-            int s = s0;
-            if (!a.fillzero) {
-                float hv[BS], lv[BS];
-                #pragma unroll
-                for (int t = 0; t < BS; ++t) { hv[t] = 0.f; lv[t] = 0.f; }
-                #pragma unroll
-                for (int b = 0; b < NC; ++b)
+    const RecPass* passes = (const RecPass*)(R + H->off_pass);
+    const RecRng* rngs = (const RecRng*)(R + H->off_rng);
+    const bool bulk = ((uintptr_t)a.nzval & 15) == 0;
+    const uint32_t outb_s = (uint32_t)__cvta_generic_to_shared(outb);
+    const int n_pass = H->n_pass;
+    for (int p = 0; p < n_pass; ++p) {
+        const RecPass P = passes[p];
+        if (p > 0) {  // the previous pass's copies still read the buffer
+            if (threadIdx.x == 0) bulk_wait_read();
+            __syncthreads();
+        }
+        const int end = P.red_end + (p + 1 == n_pass ? nf : 0);
+        int u = P.run_begin;  // run of the current block (positions only grow)
+        for (int pos = P.red_begin + (int)threadIdx.x; pos < end; pos += THREADS) {
+            if (pos >= P.red_end) {
+                f_entry<NC, Real>(a, R, stage, pos - P.red_end);
+                continue;
+            }
+            const uint32_t key = red[pos];
+            const int e = (int)(key >> RED_RANK_BITS), r = (int)(key & ((1u << RED_RANK_BITS) - 1));
+            while (u + 1 < P.run_end && runs[u + 1].first <= pos) ++u;
+            const int4 ru = *(const int4*)(runs + u);  // first, count, base, nblk
+            const int s0 = ru.z + (pos - ru.x), ds = ru.w, cnt = ru.y;
+            const RecEnt en = ents[e];
+            const int64_t L = en.L;
+            double out[NCC];
+            if constexpr (sizeof(Real) == 4) {
+                if (a.compensated) {
+                    float2 hi[NP], lo[NP];
                     #pragma unroll
-                    for (int x = 0; x < NC; ++x) {
-                        float2 q;
-                        acc_set(q, a.nzval[c0 + b * L + x]);
-                        hv[b * NC + x] = q.x;
-                        lv[b * NC + x] = q.y;
+                    for (int t = 0; t < NP; ++t) { hi[t] = make_float2(0.f, 0.f); lo[t] = make_float2(0.f, 0.f); }
+                    int k = 0;
+                    if (!a.fillzero) {
+                        const int64_t c0 = en.colbase + (int64_t)NC * r;
+                        float hv[BS], lv[BS];
+                        #pragma unroll
+                        for (int t = 0; t < BS; ++t) { hv[t] = 0.f; lv[t] = 0.f; }
+                        #pragma unroll
+                        for (int b = 0; b < NC; ++b)
+                            #pragma unroll
+                            for (int x = 0; x < NC; ++x) {
+                                float2 q;
+                                acc_set(q, a.nzval[c0 + b * L + x]);
+                                hv[b * NC + x] = q.x;
+                                lv[b * NC + x] = q.y;
+                            }
+                        #pragma unroll
+                        for (int t = 0; t < NP; ++t) { hi[t] = make_float2(hv[2 * t], hv[2 * t + 1]); lo[t] = make_float2(lv[2 * t], lv[2 * t + 1]); }
+                    } else if (cnt > 0) {
+                        const float2* v = (const float2*)(stage + s0 * BS);
+                        #pragma unroll
+                        for (int t = 0; t < NP; ++t) hi[t] = v[t];
+                        k = 1;
                     }
+                    for (; k < cnt; ++k) {
+                        const float2* v = (const float2*)(stage + (s0 + k * ds) * BS);
+                        #pragma unroll
+                        for (int t = 0; t < NP; ++t) acc_add2(hi[t], lo[t], v[t]);
+                    }
+                    #pragma unroll
+                    for (int t = 0; t < NP; ++t) {
+                        out[2 * t] = pair_to_double_fast(hi[t].x, lo[t].x);
+                        if (2 * t + 1 < NCC) out[2 * t + 1] = pair_to_double_fast(hi[t].y, lo[t].y);
+                    }
+                } else {
+                    // packed FP32 sums in cell order, each rounded exactly to FP64
+                    float2 acc[NP];
+                    #pragma unroll
+                    for (int t = 0; t < NP; ++t) acc[t] = make_float2(0.f, 0.f);
+                    for (int k = 0; k < cnt; ++k) {
+                        const float2* v = (const float2*)(stage + (s0 + k * ds) * BS);
+                        #pragma unroll
+                        for (int t = 0; t < NP; ++t) acc[t] = __fadd2_rn(acc[t], v[t]);
+                    }
+                    #pragma unroll
+                    for (int t = 0; t < NP; ++t) {
+                        out[2 * t] = float_to_double(acc[t].x);
+                        if (2 * t + 1 < NCC) out[2 * t + 1] = float_to_double(acc[t].y);
+                    }
+                    if (!a.fillzero) {
+                        const int64_t c0 = en.colbase + (int64_t)NC * r;
+                        #pragma unroll
+                        for (int b = 0; b < NC; ++b)
+                            #pragma unroll
+                            for (int x = 0; x < NC; ++x) out[b * NC + x] += a.nzval[c0 + b * L + x];
+                    }
+                }
+            } else {
+                double acc[NCC];
                 #pragma unroll
-                for (int t = 0; t < NP; ++t) { hi[t] = make_float2(hv[2 * t], hv[2 * t + 1]); lo[t] = make_float2(lv[2 * t], lv[2 * t + 1]); }
-            } else if (s < s1) {
-                const float2* v = (const float2*)(stage + s * BS);
+                for (int t = 0; t < NCC; ++t) acc[t] = 0.0;
+                if (!a.fillzero) {
+                    const int64_t c0 = en.colbase + (int64_t)NC * r;
+                    #pragma unroll
+                    for (int b = 0; b < NC; ++b)
+                        #pragma unroll
+                        for (int x = 0; x < NC; ++x) acc[b * NC + x] = a.nzval[c0 + b * L + x];
+                }
+                for (int k = 0; k < cnt; ++k) {
+                    const Real* v = stage + (s0 + k * ds) * BS;
+                    #pragma unroll
+                    for (int t = 0; t < NCC; ++t) acc[t] += v[t];
+                }
                 #pragma unroll
-                for (int t = 0; t < NP; ++t) hi[t] = v[t];
-                ++s;
+                for (int t = 0; t < NCC; ++t) out[t] = acc[t];
             }
-            for (; s < s1; ++s) {
-                const float2* v = (const float2*)(stage + s * BS);
-                #pragma unroll
-                for (int t = 0; t < NP; ++t) acc_add2(hi[t], lo[t], v[t]);
-            }
+            double* o = outb + en.out_off + NC * r;
             #pragma unroll
-            for (int t = 0; t < NP; ++t) {
-                out[2 * t] = pair_to_double_fast(hi[t].x, lo[t].x);
-                if (2 * t + 1 < NCC) out[2 * t + 1] = pair_to_double_fast(hi[t].y, lo[t].y);
+            for (int b = 0; b < NC; ++b)
+                #pragma unroll
+                for (int x = 0; x < NC; ++x) o[b * L + x] = out[b * NC + x];
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // buffer writes -> bulk copies
+        __syncthreads();
+        if (bulk) {
+            // the ends of each range with plain stores, the aligned middle with one bulk store
+            const int nrg = P.rng_end - P.rng_begin;
+            for (int q = threadIdx.x; q < 2 * nrg; q += THREADS) {
+                const RecRng g = rngs[P.rng_begin + (q >> 1)];
+                const int64_t z = (q & 1) ? g.nz0 + g.len - 1 : g.nz0;
+                const bool lone = (q & 1) ? ((g.nz0 + g.len) & 1) != 0 : (g.nz0 & 1) != 0;
+                if (lone) __stcs(a.nzval + z, outb[g.buf_off + (z - g.nz0)]);
+            }
+            if (threadIdx.x == 0) {
+                for (int gi = P.rng_begin; gi < P.rng_end; ++gi) {
+                    const RecRng g = rngs[gi];
+                    const int64_t a0 = g.nz0 + (g.nz0 & 1), a1 = (g.nz0 + g.len) & ~(int64_t)1;
+                    if (a1 > a0) bulk_store(a.nzval + a0, outb_s + (uint32_t)(g.buf_off + (a0 - g.nz0)) * 8u, (int)(a1 - a0) * 8);
+                }
+                bulk_commit();
             }
         } else {
-            double acc[NCC];
-            #pragma unroll
-            for (int t = 0; t < NCC; ++t) acc[t] = 0.0;
-            if (!a.fillzero) {
-                #pragma unroll
-                for (int b = 0; b < NC; ++b)
-                    #pragma unroll
-                    for (int x = 0; x < NC; ++x) acc[b * NC + x] = a.nzval[c0 + b * L + x];
+            for (int gi = P.rng_begin; gi < P.rng_end; ++gi) {
+                const RecRng g = rngs[gi];
+                for (int k = threadIdx.x; k < g.len; k += THREADS) __stcs(a.nzval + g.nz0 + k, outb[g.buf_off + k]);
             }
-            for (int s = s0; s < s1; ++s) {
-                const Real* v = stage + s * BS;
-                #pragma unroll
-                for (int t = 0; t < NCC; ++t) acc[t] += v[t];
-            }
-            #pragma unroll
-            for (int t = 0; t < NCC; ++t) out[t] = acc[t];
+            if (p + 1 < n_pass) __syncthreads();
         }
-        #pragma unroll
-        for (int b = 0; b < NC; ++b)
-            #pragma unroll
-            for (int x = 0; x < NC; ++x) __stcs(a.nzval + c0 + b * L + x, out[b * NC + x]);
     }
-}
-
-// f: one lane per (owned entity, component), its cells' contributions in cell order
-template <typename Real>
-__device__ __forceinline__ void reduce_f(const KernelArgs& a, const char* R, const Real* stage) {
-    using Acc = typename AccT<Real>::type;
-    const RecHead* H = (const RecHead*)R;
-    const RecEnt* ents = (const RecEnt*)(R + H->off_ent);
-    const uint32_t* fk = (const uint32_t*)(R + H->off_fk);
-    const int nc = a.nc;
-    const Real* fst = stage + H->n_slots * a.bs;
-    for (int idx = threadIdx.x; idx < H->n_ent * nc; idx += THREADS) {
-        const int e = idx / nc, x = idx - e * nc;
-        const uint32_t w = fk[e];
-        const int fb = (int)(w & 0xFFFF), kcnt = (int)(w >> 16);
-        const int64_t gi = (int64_t)ents[e].id * nc + x;
-        Acc acc;
-        acc_zero(acc);
-        if (!a.fillzero) acc_set(acc, a.f[gi]);
-        const Real* v = fst + fb * nc + x;
-        for (int k = 0; k < kcnt; ++k) acc_add(acc, v[k * nc]);
-        __stcs(a.f + gi, acc_value(acc));
-    }
+    // the next tile writes its cell tables over the buffer
+    if (threadIdx.x == 0) bulk_wait_read();
 }
 
 // ---------------------------------------------------------------------------------------
@@ -749,17 +944,18 @@ __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, int byt
                  : "memory");
 }
 
-// gather the coordinates of a tile's nodes (two 16-byte halves per node) into shared memory
+// gather the coordinates of a tile's nodes (three 8-byte pieces per node) into shared memory
 template <typename Real>
 __device__ __forceinline__ void gather_nodes(const KernelArgs& a, const char* R, char* xs) {
     const RecHead* H = (const RecHead*)R;
     const int32_t* nodes = (const int32_t*)(R + H->off_nodes);
-    const char* src = sizeof(Real) == 4 ? (const char*)a.xf8 : (const char*)a.xd4;
+    const char* src = sizeof(Real) == 4 ? (const char*)a.xf6 : (const char*)a.xd3;
     const uint32_t dst = (uint32_t)__cvta_generic_to_shared(xs);
-    const int n = 2 * H->n_nodes;
+    const int n = 3 * H->n_nodes;
     for (int k = threadIdx.x; k < n; k += THREADS) {
-        const char* p = src + (int64_t)nodes[k >> 1] * NODE_BYTES + (k & 1) * 16;
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + k * 16), "l"(p) : "memory");
+        const int nd = k / 3, piece = k - nd * 3;
+        const char* p = src + (int64_t)nodes[nd] * NODE_BYTES + piece * 8;
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst + k * 8), "l"(p) : "memory");
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
 }
@@ -777,7 +973,7 @@ __global__ void __launch_bounds__(THREADS, 2) tile_kernel(const KernelArgs a, co
         // the host sized the allocation from the same layout; refuse to run past it
         uint32_t dyn;
         asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
-        if ((uint32_t)(lay.chunk + a.chunk_bytes) > dyn) {
+        if ((uint32_t)(lay.chunk + chunk_region_bytes(a)) > dyn) {
             if (threadIdx.x == 0) atomicAdd(&a.status->timeout, 1u);
             return;
         }
@@ -792,18 +988,18 @@ __global__ void __launch_bounds__(THREADS, 2) tile_kernel(const KernelArgs a, co
     const int G = gridDim.x;
     const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(&bars[0]);
     auto rec_bar = [&](int b) { return bar0 + 8u * (uint32_t)(1 + b); };
-    auto issue_record = [&](int t, int b) {
-        const int64_t o = a.rec_off[t];
-        const int bytes = (int)(a.rec_off[t + 1] - o);
-        bulk_load((uint32_t)__cvta_generic_to_shared(rec_ring + b * rec_stride), a.rec + o, bytes, rec_bar(b));
+    auto issue_record = [&](int64_t o, int64_t o1, int b) {
+        bulk_load((uint32_t)__cvta_generic_to_shared(rec_ring + b * rec_stride), a.rec + o, (int)(o1 - o), rec_bar(b));
     };
+    int64_t pf0 = 0, pf1 = 0;  // thread 0: offsets of the record it issues next (loaded a tile ahead)
     int t = blockIdx.x;
     if (tid == 0) {
         for (int b = 0; b < 1 + REC_RING; ++b) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8u * b) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         bulk_load((uint32_t)__cvta_generic_to_shared(shape), shape_g, shape_bytes, bar0);
-        if (t < a.n_tiles) issue_record(t, 0);
-        if (t + G < a.n_tiles) issue_record(t + G, 1);
+        if (t < a.n_tiles) issue_record(a.rec_off[t], a.rec_off[t + 1], 0);
+        if (t + G < a.n_tiles) issue_record(a.rec_off[t + G], a.rec_off[t + G + 1], 1);
+        if (t + 2 * G < a.n_tiles) { pf0 = a.rec_off[t + 2 * G]; pf1 = a.rec_off[t + 2 * G + 1]; }
     }
     __syncthreads();  // the initialised barriers are visible to every thread
     bool failed = false;
@@ -819,7 +1015,10 @@ __global__ void __launch_bounds__(THREADS, 2) tile_kernel(const KernelArgs a, co
         const char* R = rec_ring + (it % REC_RING) * rec_stride;
         const char* xs = xs_ring + (it & 1) * xs_stride;
         // keep the pipeline full: record of t + 2G, coordinates of t + G
-        if (tid == 0 && t + 2 * G < a.n_tiles) issue_record(t + 2 * G, (it + 2) % REC_RING);
+        if (tid == 0 && t + 2 * G < a.n_tiles) {
+            issue_record(pf0, pf1, (it + 2) % REC_RING);
+            if (t + 3 * G < a.n_tiles) { pf0 = a.rec_off[t + 3 * G]; pf1 = a.rec_off[t + 3 * G + 1]; }
+        }
         if (t + G < a.n_tiles) {
             const int nb = (it + 1) % REC_RING;
             if (mbar_wait(rec_bar(nb), (uint32_t)(((it + 1) / REC_RING) & 1), WAIT_LIMIT))
@@ -832,6 +1031,7 @@ __global__ void __launch_bounds__(THREADS, 2) tile_kernel(const KernelArgs a, co
         for (int gi = 0; gi < n_seg; ++gi) {
             if (gi) __syncthreads();  // table buffers are laid out per element kind
             const RecSeg g = ((const RecSeg*)(R + sizeof(RecHead)))[gi];
+            static_assert(sizeof(RecSeg) % 16 == 0, "segment entries are 16-byte multiples");
             if (g.sub == 0) {
                 process_segment<K0, Q0, PHYS, Real>(a, a.sub[0], shape, g, R, xs, stage, chunk);
             } else if constexpr (K1 >= 0) {
@@ -845,13 +1045,11 @@ __global__ void __launch_bounds__(THREADS, 2) tile_kernel(const KernelArgs a, co
             }
         }
         __syncthreads();  // all staging slots written
-        if (a.do_k) {
-            if (a.nc == 3) reduce_tile<3, Real>(a, R, stage);
-            else if (a.nc == 2) reduce_tile<2, Real>(a, R, stage);
-            else reduce_tile<1, Real>(a, R, stage);
-        }
-        if (a.do_f) reduce_f<Real>(a, R, stage);
+        if (a.nc == 3) reduce_tile<3, Real>(a, R, stage, (double*)chunk);
+        else if (a.nc == 2) reduce_tile<2, Real>(a, R, stage, (double*)chunk);
+        else reduce_tile<1, Real>(a, R, stage, (double*)chunk);
     }
+    if (tid == 0) bulk_wait_all();  // this CTA's output stores have completed
     if (t < a.n_tiles) {
         // a copy was lost: report it, and wait (bounded) for this CTA's copies still in
         // flight before its shared memory is released

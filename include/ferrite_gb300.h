@@ -61,7 +61,8 @@ extern "C" {
 #define FE_NEO_HOOKE 3      /* tangent and residual of hyperelasticity.jl:157-276 (cell part) */
 
 /* precision */
-#define FE_PREC_MIXED 0 /* FP32 element math, FP64 Jacobians for flagged cells, FP64-class accumulation */
+#define FE_PREC_MIXED 0 /* FP32 element math (FP64 Jacobians for flagged cells), FP32 sums per entry, each entry
+                           rounded exactly to FP64; with FE_COMPENSATED the sums are compensated FP32 pairs */
 #define FE_PREC_FP64 1  /* the plain FP64 drop-in: all math and accumulation in FP64 */
 
 /* fe_assemble flags */
@@ -70,6 +71,8 @@ extern "C" {
 #define FE_NO_F 4u     /* skip f (f may be NULL) */
 #define FE_ASYNC 8u    /* do not wait for the kernels; read the status later with fe_sync() */
 #define FE_PROFILE 16u /* bracket the assembly kernel with CUDA events; read with fe_kernel_time() */
+#define FE_COMPENSATED 32u /* FE_PREC_MIXED: sum each entry's contributions as a compensated FP32 pair
+                              (TwoSum, FP64-class summation error) and round the pair exactly to FP64 */
 
 typedef struct fe_handle fe_handle;
 
