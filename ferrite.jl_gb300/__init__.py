@@ -39,7 +39,8 @@ PREC_MIXED, PREC_FP64 = 0, 1
 FILLZERO, NO_K, NO_F, ASYNC, PROFILE, COMPENSATED = 1, 2, 4, 8, 16, 32
 
 EXPORTED = ["fe_abi_version", "fe_create", "fe_assemble", "fe_sync", "fe_last_error", "fe_get_info",
-            "fe_get_index_map", "fe_plan_dry_run", "fe_distribute_dofs", "fe_sparsity_pattern", "fe_kernel_time", "fe_assemble_noalloc", "fe_destroy"]
+            "fe_get_index_map", "fe_plan_dry_run", "fe_distribute_dofs", "fe_sparsity_pattern", "fe_kernel_time", "fe_assemble_noalloc",
+            "fe_assemble_adjoint", "fe_destroy"]
 
 i64p = ctypes.POINTER(ctypes.c_int64)
 f64p = ctypes.POINTER(ctypes.c_double)
@@ -68,6 +69,12 @@ class AssembleParams(ctypes.Structure):
                 ("p0", ctypes.c_double), ("p1", ctypes.c_double), ("body", ctypes.c_double * 3),
                 ("cell_scale", ctypes.c_void_p), ("u", ctypes.c_void_p), ("cond_threshold", ctypes.c_double),
                 ("stream", ctypes.c_void_p)]
+
+
+class AdjointParams(ctypes.Structure):
+    _fields_ = [("physics", ctypes.c_int32), ("precision", ctypes.c_int32), ("flags", ctypes.c_uint32),
+                ("p0", ctypes.c_double), ("p1", ctypes.c_double), ("body", ctypes.c_double * 3),
+                ("cell_scale", ctypes.c_void_p), ("dscale", ctypes.c_void_p), ("stream", ctypes.c_void_p)]
 
 
 class ErrorInfo(ctypes.Structure):
@@ -117,6 +124,8 @@ def lib():
                                           ctypes.POINTER(DofDesc), i64p, i64p, i64p]
         L.fe_kernel_time.argtypes = [ctypes.c_void_p, f64p, i64p]
         L.fe_assemble_noalloc.argtypes = [ctypes.c_void_p, ctypes.POINTER(AssembleParams), ctypes.c_void_p, ctypes.c_void_p]
+        L.fe_assemble_adjoint.argtypes = [ctypes.c_void_p, ctypes.POINTER(AdjointParams), ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_void_p]
         L.fe_destroy.argtypes = [ctypes.c_void_p]
         L.fe_destroy.restype = None
         _lib = L
@@ -294,6 +303,26 @@ class Handle:
         if rc != FE_OK:
             self._raise(rc)
         return nzval, f
+
+    def adjoint(self, u, lam, d_rho, d_X, physics: int, p0: float, p1: float, body=(0.0, 0.0, 0.0), cell_scale=None,
+                dscale=None, precision: int = PREC_MIXED, stream=None, sync: bool = True):
+        """fe_assemble_adjoint: d_rho[n_cells] = dscale * lam^T (dK/ds) u and d_X[n_nodes*dim] =
+        lam^T d(K u - f)/dX, written in place (numpy or torch CUDA buffers; d_X may be None)."""
+        p = AdjointParams()
+        p.physics, p.precision = physics, precision
+        p.flags = 0 if sync else ASYNC
+        p.p0, p.p1 = float(p0), float(p1)
+        for k in range(3):
+            p.body[k] = float(body[k]) if k < len(body) else 0.0
+        p.cell_scale = _ptr(cell_scale)
+        p.dscale = _ptr(dscale)
+        if stream is not None and hasattr(stream, "cuda_stream"):
+            stream = stream.cuda_stream
+        p.stream = stream
+        rc = lib().fe_assemble_adjoint(self._h, ctypes.byref(p), _ptr(u), _ptr(lam), _ptr(d_rho), _ptr(d_X))
+        if rc != FE_OK:
+            self._raise(rc)
+        return d_rho, d_X
 
     def sync(self):
         rc = lib().fe_sync(self._h)

@@ -12,6 +12,7 @@
 #include "ferrite_gb300.h"
 #include "plan.h"
 #include "registry.h"
+#include "adjoint.cuh"
 #include "tile_kernel.cuh"
 
 using namespace fe;
@@ -26,6 +27,13 @@ const std::vector<KernelEntry>& registry() {
         register_elastic(reg);
         register_neo(reg);
     });
+    return reg;
+}
+
+const std::vector<AdjEntry>& adj_registry() {
+    static std::vector<AdjEntry> reg;
+    static std::once_flag once;
+    std::call_once(once, [] { register_adjoint(reg); });
     return reg;
 }
 
@@ -65,6 +73,17 @@ struct fe_handle {
     double* scale_stage = nullptr;
     float* u_f = nullptr;
     float* scale_f = nullptr;
+    // adjoint: node -> (cell, geometric node) rows in cell order, per-row contributions,
+    // staging for host-pointer calls
+    int64_t adj_rows = 0;
+    int64_t* adj_ptr = nullptr;
+    int32_t* adj_row_ids = nullptr;
+    void* adj_contrib = nullptr;
+    double* lam_stage = nullptr;
+    float* lam_f = nullptr;
+    double* dscale_stage = nullptr;
+    double* drho_stage = nullptr;
+    double* dX_stage = nullptr;
     cudaStream_t last_stream = 0;
     int pending = 0;  // an FE_ASYNC assembly whose status has not been read
     fe_error_info last{};
@@ -277,10 +296,11 @@ int fe_create(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain
         SubDev& sd = A.sub[s];
         sd.kind = hs.kind; sd.nb = hs.nb; sd.ng = hs.ng; sd.nq = hs.nq; sd.dim = hs.dim; sd.nc = hs.nc;
         sd.n_cells = hs.n_cells;
-        int32_t *cid, *ents;
+        int32_t *cid, *ents, *cconn;
         CK(h->upload(&cid, hs.cellid.data(), hs.cellid.size()));
         CK(h->upload(&ents, hs.ents.data(), hs.ents.size()));
-        sd.cellid = cid; sd.ents = ents;
+        CK(h->upload(&cconn, hs.conn.data(), hs.conn.size()));
+        sd.cellid = cid; sd.ents = ents; sd.conn = cconn;
         // reference tables: one record per quadrature point (dM, dN, N, w; layout shape_q)
         auto push_records = [&](auto& vec) {
             using T = typename std::remove_reference<decltype(vec)>::type::value_type;
@@ -529,6 +549,150 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
     h->last_stream = st;
     h->pending = 1;
     const bool host_out = (do_k && !nz_dev) || (do_f && !f_dev);
+    if ((p->flags & FE_ASYNC) && !host_out) return FE_OK;
+    return fe_sync(h);
+}
+
+int fe_assemble_adjoint(fe_handle* h, const fe_adjoint_params* p, const double* u, const double* lambda, double* d_rho,
+                        double* d_X) {
+    if (!h || !p || !u || !lambda || !d_rho) return FE_ERR_ARG;
+    const HostProblem& hp = h->hp;
+    const int nc = hp.nc, dim = hp.dim;
+    int phys = 0;
+    if (p->physics == FE_HEAT) {
+        if (nc != 1) return set_error(h, FE_ERR_ARG, "FE_HEAT needs a scalar field");
+        phys = PHYS_HEAT;
+    } else if (p->physics == FE_LINEAR_ELASTIC) {
+        if (nc != dim) return set_error(h, FE_ERR_ARG, "FE_LINEAR_ELASTIC needs a dim-component field");
+        phys = PHYS_ELASTIC;
+    } else {
+        return set_error(h, FE_ERR_UNSUPPORTED, "the adjoint supports FE_HEAT and FE_LINEAR_ELASTIC");
+    }
+    if (p->precision != FE_PREC_MIXED && p->precision != FE_PREC_FP64) return set_error(h, FE_ERR_ARG, "unknown precision");
+    const bool fp64 = p->precision == FE_PREC_FP64;
+    std::vector<const AdjEntry*> ke(hp.subs.size(), nullptr);
+    for (size_t s = 0; s < hp.subs.size(); ++s) {
+        for (const AdjEntry& e : adj_registry())
+            if (e.kind == hp.subs[s].kind && e.nq == hp.subs[s].nq && e.phys == phys && e.fp64 == (int)fp64) ke[s] = &e;
+        if (!ke[s]) return set_error(h, FE_ERR_UNSUPPORTED, "no adjoint kernel for this element / quadrature / physics");
+    }
+    if (h->pending) fe_sync(h);
+    cudaStream_t st = (cudaStream_t)p->stream;
+    cudaError_t e;
+    // node -> rows (once per handle): rows of subdomain s start at row0[s], cell c, node k
+    std::vector<int64_t> row0(hp.subs.size() + 1, 0);
+    for (size_t s = 0; s < hp.subs.size(); ++s) row0[s + 1] = row0[s] + hp.subs[s].n_cells * hp.subs[s].ng;
+    if (!h->adj_ptr) {
+        if (row0.back() >= (int64_t)INT32_MAX) return set_error(h, FE_ERR_UNSUPPORTED, "too many cells for the adjoint");
+        std::vector<int64_t> ptr(hp.n_nodes + 1, 0);
+        for (const HostSub& hs : hp.subs)
+            for (int32_t v : hs.conn) ptr[v + 1]++;
+        for (int64_t n = 0; n < hp.n_nodes; ++n) ptr[n + 1] += ptr[n];
+        std::vector<int32_t> ids(ptr[hp.n_nodes]);
+        std::vector<int64_t> cur(ptr.begin(), ptr.end() - 1);
+        for (size_t s = 0; s < hp.subs.size(); ++s) {
+            const HostSub& hs = hp.subs[s];
+            for (int64_t c = 0; c < hs.n_cells; ++c)
+                for (int k = 0; k < hs.ng; ++k) ids[cur[hs.conn[c * hs.ng + k]]++] = (int32_t)(row0[s] + c * hs.ng + k);
+        }
+        if ((e = h->upload(&h->adj_ptr, ptr.data(), ptr.size())) != cudaSuccess) return cuda_fail(h, e, "adjoint index");
+        if ((e = h->upload(&h->adj_row_ids, ids.data(), ids.size())) != cudaSuccess) return cuda_fail(h, e, "adjoint index");
+        char* cb = nullptr;
+        if ((e = h->alloc(&cb, (size_t)row0.back() * dim * sizeof(double))) != cudaSuccess) return cuda_fail(h, e, "adjoint rows");
+        h->adj_contrib = cb;
+        h->adj_rows = row0.back();
+    }
+    AdjArgs A{};
+    A.xf6 = h->base.xf6;
+    A.xd3 = h->base.xd3;
+    // inputs: device pointers are used in place, host pointers staged
+    auto stage = [&](const double* src, int64_t n, double** buf) -> const double* {
+        if (is_device_ptr(src)) return src;
+        if (!*buf && (e = h->alloc(buf, n)) != cudaSuccess) return nullptr;
+        if ((e = cudaMemcpyAsync(*buf, src, n * 8, cudaMemcpyHostToDevice, st)) != cudaSuccess) return nullptr;
+        return *buf;
+    };
+    auto to_f = [&](const double* src, int64_t n, float** buf) -> const float* {
+        if (!*buf && (e = h->alloc(buf, n)) != cudaSuccess) return nullptr;
+        to_float_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, st>>>(src, *buf, n);
+        return *buf;
+    };
+    if (!(A.u_d = stage(u, hp.ndofs, &h->u_stage)) || !(A.l_d = stage(lambda, hp.ndofs, &h->lam_stage)))
+        return cuda_fail(h, e, "adjoint inputs");
+    if (!fp64 && (!(A.u_f = to_f(A.u_d, hp.ndofs, &h->u_f)) || !(A.l_f = to_f(A.l_d, hp.ndofs, &h->lam_f))))
+        return cuda_fail(h, e, "adjoint inputs");
+    if (p->cell_scale) {
+        if (!(A.scale_d = stage(p->cell_scale, hp.n_cells, &h->scale_stage))) return cuda_fail(h, e, "cell_scale");
+        if (!fp64 && !(A.scale_f = to_f(A.scale_d, hp.n_cells, &h->scale_f))) return cuda_fail(h, e, "cell_scale");
+    }
+    if (p->dscale && !(A.dscale = stage(p->dscale, hp.n_cells, &h->dscale_stage))) return cuda_fail(h, e, "dscale");
+    if (phys == PHYS_HEAT) {
+        A.m0 = p->p0;
+        A.load[0] = p->p1;
+    } else {
+        const double E = p->p0, nu = p->p1;
+        A.m0 = E * nu / ((1 + nu) * (1 - 2 * nu));
+        A.m1 = E / (2 * (1 + nu));
+        for (int x = 0; x < 3; ++x) A.load[x] = p->body[x];
+    }
+    // outputs
+    const bool rho_dev = is_device_ptr(d_rho), x_dev = d_X && is_device_ptr(d_X);
+    double* drho = d_rho;
+    if (!rho_dev) {
+        if (!h->drho_stage && (e = h->alloc(&h->drho_stage, hp.n_cells)) != cudaSuccess) return cuda_fail(h, e, "alloc d_rho");
+        drho = h->drho_stage;
+    }
+    double* dX = d_X;
+    if (d_X && !x_dev) {
+        if (!h->dX_stage && (e = h->alloc(&h->dX_stage, hp.n_nodes * dim)) != cudaSuccess) return cuda_fail(h, e, "alloc d_X");
+        dX = h->dX_stage;
+    }
+    if ((e = cudaMemsetAsync(drho, 0, hp.n_cells * sizeof(double), st)) != cudaSuccess) return cuda_fail(h, e, "d_rho");
+    A.d_cell = drho;
+    A.contrib = h->adj_contrib;
+    DevStatus init{~0ull, ~0ull, 0u, 0u};
+    *h->status_h = init;
+    if ((e = cudaMemcpyAsync(h->status_d, h->status_h, sizeof(DevStatus), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return cuda_fail(h, e, "status reset");
+    A.status = h->status_d;
+    int n_sm = 0;
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, h->device);
+    for (size_t s = 0; s < hp.subs.size(); ++s) {
+        A.row0 = row0[s];
+        const SubDev sd = h->base.sub[s];
+        const int32_t* conn = sd.conn;
+        const void* shp = fp64 ? (const void*)((const char*)h->shape_d + (s ? (s == 1 ? h->shape_off1[1] : h->shape_off2[1]) : 0))
+                               : (const void*)((const char*)h->shape_f + (s ? (s == 1 ? h->shape_off1[0] : h->shape_off2[0]) : 0));
+        if ((e = cudaFuncSetAttribute(ke[s]->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, ke[s]->smem)) != cudaSuccess)
+            return cuda_fail(h, e, "cudaFuncSetAttribute");
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ke[s]->fn, THREADS, ke[s]->smem);
+        const int gs = CTA_THREADS / GROUP_LANES[hp.subs[s].kind];
+        const int64_t need = (sd.n_cells + gs - 1) / gs;
+        const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)std::max(per_sm, 1) * n_sm * 4));
+        void* args[] = {(void*)&A, (void*)&sd, (void*)&conn, (void*)&shp};
+        if ((e = cudaLaunchKernel(ke[s]->fn, dim3(grid), dim3(THREADS), args, (size_t)ke[s]->smem, st)) != cudaSuccess)
+            return cuda_fail(h, e, "adjoint kernel launch");
+    }
+    if (d_X) {
+        const int64_t n_out = hp.n_nodes * dim;
+        const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n_out + 255) / 256, (int64_t)n_sm * 16));
+        const void* contrib = h->adj_contrib;
+        int dim32 = dim;
+        int64_t nn = hp.n_nodes;
+        void* args[] = {(void*)&h->adj_ptr, (void*)&h->adj_row_ids, (void*)&contrib, (void*)&dim32, (void*)&nn, (void*)&dX};
+        if ((e = cudaLaunchKernel(adjoint_node_sum_fn(fp64), dim3(grid), dim3(256), args, 0, st)) != cudaSuccess)
+            return cuda_fail(h, e, "adjoint node sum launch");
+    }
+    if ((e = cudaMemcpyAsync(h->status_h, h->status_d, sizeof(DevStatus), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return cuda_fail(h, e, "status read");
+    if (!rho_dev && (e = cudaMemcpyAsync(d_rho, drho, hp.n_cells * 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return cuda_fail(h, e, "copy d_rho back");
+    if (d_X && !x_dev && (e = cudaMemcpyAsync(d_X, dX, hp.n_nodes * dim * 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return cuda_fail(h, e, "copy d_X back");
+    h->last_stream = st;
+    h->pending = 1;
+    const bool host_out = !rho_dev || (d_X && !x_dev);
     if ((p->flags & FE_ASYNC) && !host_out) return FE_OK;
     return fe_sync(h);
 }

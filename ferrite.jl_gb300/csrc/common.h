@@ -146,6 +146,7 @@ struct SubDev {
     int64_t n_cells;
     const int32_t* cellid;   // [n] 0-based Ferrite cell id
     const int32_t* ents;     // [n][nb] entity ids
+    const int32_t* conn;     // [n][ng] 0-based node ids (adjoint kernel)
     // reference tables (float and double copies), row-major as in the C ABI
     const float* w_f;        // [nq]
     const float* N_f;        // [nq][nb]

@@ -16,8 +16,17 @@ struct KernelEntry {
     int groups[MAX_SUB];       // lane groups per CTA of each slot
 };
 
+// adjoint kernels: one instantiation per (kind, quadrature points, physics, precision)
+struct AdjEntry {
+    int kind, nq, phys, fp64;
+    const void* fn;      // __global__ adjoint_kernel<...>
+    int smem;            // dynamic shared memory per CTA
+};
+
 void register_heat(std::vector<KernelEntry>& out);
 void register_elastic(std::vector<KernelEntry>& out);
 void register_neo(std::vector<KernelEntry>& out);
+void register_adjoint(std::vector<AdjEntry>& out);
+const void* adjoint_node_sum_fn(bool fp64);
 
 }  // namespace fe

@@ -225,6 +225,34 @@ int fe_kernel_time(fe_handle* h, double* total_ms, int64_t* launches);
  */
 int fe_assemble_noalloc(fe_handle* h, const fe_assemble_params* params, double* nzval, double* f);
 
+/* Adjoint of the assembly: vector-Jacobian products of Phi = lambda^T (K(X, s) u - f(X)).
+ * No counterpart in the reference (Ferrite has no adjoint); the Julia binding exposes it as the
+ * pullback of assemble_csc! (a ChainRulesCore.rrule), replacing differentiation of the cell
+ * loop of docs/src/literate-gallery/topology_optimization.jl:347-383 (SIMP: s_e = rho_e^p).
+ *   physics      FE_HEAT (p0 = k, p1 = source) or FE_LINEAR_ELASTIC (p0 = E, p1 = nu, body)
+ *   cell_scale   per Ferrite cell material factor s_e (E_e = s_e p0; NULL = 1)
+ *   dscale       per Ferrite cell ds_e/drho_e (NULL = 1: d_rho is then dPhi/ds_e)
+ *   d_rho[n_cells]        = dscale_e * lambda_e^T (dK_e/ds_e) u_e  (0 for cells outside the subdomains)
+ *   d_X[n_nodes * dim]    = dPhi/dX, node-major like grid.nodes (NULL: skipped)
+ * Quadrature-point geometry is recomputed, not stored. FE_PREC_MIXED computes each cell in FP32
+ * and sums the cells of a node in FP64; FE_PREC_FP64 is FP64 throughout. Deterministic. u,
+ * lambda (ndofs), cell_scale, dscale and the outputs may be host or device memory. Errors:
+ * FE_ERR_DETJ as fe_assemble; FE_ERR_UNSUPPORTED for element kinds without an adjoint kernel
+ * (second-order elements, Neo-Hooke). */
+typedef struct {
+    int32_t physics;
+    int32_t precision;
+    uint32_t flags;           /* FE_ASYNC */
+    double p0, p1;
+    double body[3];
+    const double* cell_scale;
+    const double* dscale;
+    void* stream;
+} fe_adjoint_params;
+
+int fe_assemble_adjoint(fe_handle* h, const fe_adjoint_params* params, const double* u, const double* lambda,
+                        double* d_rho, double* d_X);
+
 void fe_destroy(fe_handle* h);
 
 int fe_abi_version(void);

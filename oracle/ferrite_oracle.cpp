@@ -1078,4 +1078,125 @@ int or_assemble(const or_problem* p, const or_physics* ph, int32_t nthreads, int
     return status;
 }
 
+
+// ---------------------------------------------------------------------------------------
+// Adjoint (vector-Jacobian products) of the heat and linear-elastic assembly, FP64. The
+// formulas are derived from Phi = lambda^T (K u - f) with J = sum_k x_k (x) dM_k/dxi:
+// d(dV) = dV tr(J^-1 dJ), d(grad v) = -grad(v) dJ J^-1, so dPhi/dJ = dV Sigma J^-T and
+// dPhi/dx_k = dV Sigma (J^-T dM_k/dxi) (declaration in ferrite_oracle.h).
+// ---------------------------------------------------------------------------------------
+int or_adjoint(const or_problem* p, const or_physics* ph, const double* u, const double* lam, const double* dscale,
+               double* d_cell, double* d_X, or_error* err) {
+    Setup S;
+    int rc = S.init(p);
+    err->code = OR_OK;
+    err->cell = 0;
+    if (rc) { err->code = rc; return rc; }
+    if (ph->physics != OR_HEAT && ph->physics != OR_LINEAR_ELASTIC) return OR_ERR_UNSUPPORTED;
+    const int dim = p->dim;
+    if (d_X) std::memset(d_X, 0, sizeof(double) * p->n_nodes * dim);
+    std::vector<double> x;
+    for (int s = 0; s < p->n_sdh; ++s) {
+        CellValues& cv = S.cvs[s];
+        const int nc = p->sdh_ncomp[s];
+        const int nb = cv.nb, ng = cv.ng;
+        if (ph->physics == OR_LINEAR_ELASTIC && nc != dim) return OR_ERR_ARG;
+        if (ph->physics == OR_HEAT && nc != 1) return OR_ERR_ARG;
+        for (int64_t kk = p->sdh_cellset_offset[s]; kk < p->sdh_cellset_offset[s + 1]; ++kk) {
+            const int64_t c = p->sdh_cellset[kk] - 1;
+            const int64_t off = p->cell_nodes_offset[c];
+            x.resize(ng * dim);
+            for (int k = 0; k < ng; ++k) {
+                const int64_t nid = p->cell_nodes[off + k] - 1;
+                for (int a = 0; a < dim; ++a) x[k * dim + a] = p->nodes[nid * p->dim + a];
+            }
+            double bad = 0;
+            if (cv.reinit(x.data(), &bad)) {
+                err->code = OR_ERR_DETJ;
+                err->cell = c + 1;
+                err->detJ = bad;
+                return OR_ERR_DETJ;
+            }
+            const int64_t* dofs = p->cell_dofs + p->cell_dofs_offset[c] - 1;
+            const double scale = ph->cell_scale ? ph->cell_scale[c] : 1.0;
+            double m0 = 0, m1 = 0;  // unscaled material: heat k; elastic lambda, mu (E = p0)
+            if (ph->physics == OR_HEAT) {
+                m0 = ph->p0;
+            } else {
+                const double E = ph->p0, nu = ph->p1;
+                m0 = E * nu / ((1 + nu) * (1 - 2 * nu));
+                m1 = E / (2 * (1 + nu));
+            }
+            double gcell = 0.0;
+            for (int q = 0; q < cv.nq; ++q) {
+                const double dV = cv.detJdV[q];
+                // gradients of u and lambda: G[c][d] = d v_c / d x_d; lambda at the point
+                double Gu[9] = {0}, Gl[9] = {0}, lq[3] = {0};
+                for (int i = 0; i < nb; ++i) {
+                    const double* g = &cv.dNdx[(q * nb + i) * dim];
+                    const double Ni = cv.N[q * nb + i];
+                    for (int a = 0; a < nc; ++a) {
+                        const double ui = u[dofs[i * nc + a] - 1], li = lam[dofs[i * nc + a] - 1];
+                        lq[a] += Ni * li;
+                        for (int d = 0; d < dim; ++d) {
+                            Gu[a * dim + d] += ui * g[d];
+                            Gl[a * dim + d] += li * g[d];
+                        }
+                    }
+                }
+                // fluxes / stresses with the unscaled material, then the scaled ones
+                double Su[9] = {0}, Sl[9] = {0};
+                if (ph->physics == OR_HEAT) {
+                    for (int d = 0; d < dim; ++d) { Su[d] = m0 * Gu[d]; Sl[d] = m0 * Gl[d]; }
+                } else {
+                    double tu = 0, tl = 0;
+                    for (int d = 0; d < dim; ++d) { tu += Gu[d * dim + d]; tl += Gl[d * dim + d]; }
+                    for (int a = 0; a < dim; ++a)
+                        for (int b = 0; b < dim; ++b) {
+                            Su[a * dim + b] = m1 * (Gu[a * dim + b] + Gu[b * dim + a]) + (a == b ? m0 * tu : 0.0);
+                            Sl[a * dim + b] = m1 * (Gl[a * dim + b] + Gl[b * dim + a]) + (a == b ? m0 * tl : 0.0);
+                        }
+                }
+                double psi0 = 0;
+                for (int t = 0; t < nc * dim; ++t) psi0 += Su[t] * Gl[t];
+                gcell += dV * psi0;
+                const double psi = scale * psi0;
+                double fl = 0;
+                if (ph->physics == OR_HEAT) fl = ph->p1 * lq[0];
+                else for (int a = 0; a < nc; ++a) fl += lq[a] * ph->body[a];
+                // Sigma = (psi - fl) I - Gu^T sigma(lambda) - Gl^T sigma(u), sigma scaled
+                double Sg[9];
+                for (int b = 0; b < dim; ++b)
+                    for (int d = 0; d < dim; ++d) {
+                        double v = (b == d) ? (psi - fl) : 0.0;
+                        for (int a = 0; a < nc; ++a)
+                            v -= scale * (Gu[a * dim + b] * Sl[a * dim + d] + Gl[a * dim + b] * Su[a * dim + d]);
+                        Sg[b * dim + d] = v;
+                    }
+                if (d_X) {
+                    // grad M_k = J^-T dM_k/dxi: recompute J^-1 for this point
+                    double J[9] = {0}, Ji[9];
+                    for (int k = 0; k < ng; ++k)
+                        for (int a = 0; a < dim; ++a)
+                            for (int b = 0; b < dim; ++b) J[a * dim + b] += x[k * dim + a] * cv.dMdxi[(q * ng + k) * dim + b];
+                    inv_n(dim, J, det_n(dim, J), Ji);
+                    for (int k = 0; k < ng; ++k) {
+                        double gM[3] = {0, 0, 0};
+                        for (int b = 0; b < dim; ++b)
+                            for (int a = 0; a < dim; ++a) gM[b] += cv.dMdxi[(q * ng + k) * dim + a] * Ji[a * dim + b];
+                        const int64_t nid = p->cell_nodes[off + k] - 1;
+                        for (int b = 0; b < dim; ++b) {
+                            double v = 0;
+                            for (int d = 0; d < dim; ++d) v += Sg[b * dim + d] * gM[d];
+                            d_X[nid * dim + b] += dV * v;
+                        }
+                    }
+                }
+            }
+            if (d_cell) d_cell[c] = (dscale ? dscale[c] : 1.0) * gcell;
+        }
+    }
+    return OR_OK;
+}
+
 }  // extern "C"

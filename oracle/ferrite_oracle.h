@@ -98,6 +98,18 @@ int or_element_matrix(const or_problem* p, const or_physics* phys, int64_t cell,
 int or_index_map(const or_problem* p, int64_t cell, int64_t* positions);
 int or_greedy_coloring(const or_problem* p, int32_t* cell_color, int32_t* n_colors);
 
+/* Adjoint of the assembly (heat, linear elasticity): for Phi = lambda^T (K(X, s) u - f(X)),
+ *   d_cell[c] = dscale[c] * dPhi/ds_c   (s_c = cell_scale[c], the factor on the material;
+ *                                        dscale NULL = 1: the derivative w.r.t. s_c itself)
+ *   d_X[n*dim + a] = dPhi/dX_{n,a}      (node coordinates)
+ * Per quadrature point, with psi = sigma(u) : grad(lambda) (heat: k grad u . grad lambda) and
+ * the load density fl = lambda(x_q) . b (heat: source * lambda(x_q)):
+ *   dPhi/ds = sum_q dV psi / s,   dPhi/dX_k = sum_q dV Sigma grad M_k,
+ *   Sigma = (psi - fl) I - grad(u)^T sigma(lambda) - grad(lambda)^T sigma(u),
+ * grad M_k the physical gradient of the geometric shape function of node k. */
+int or_adjoint(const or_problem* p, const or_physics* phys, const double* u, const double* lambda,
+               const double* dscale, double* d_cell, double* d_X, or_error* err);
+
 #ifdef __cplusplus
 }
 #endif

@@ -88,6 +88,8 @@ def lib():
                                             ctypes.c_int64, f64p, f64p, ctypes.POINTER(_Error)]
             L.or_index_map.argtypes = [ctypes.POINTER(_Problem), ctypes.c_int64, i64p]
             L.or_greedy_coloring.argtypes = [ctypes.POINTER(_Problem), i32p, i32p]
+            L.or_adjoint.argtypes = [ctypes.POINTER(_Problem), ctypes.POINTER(_Physics), f64p, f64p, f64p, f64p, f64p,
+                                     ctypes.POINTER(_Error)]
             _lib = L
     return _lib
 
@@ -345,6 +347,24 @@ class Problem:
         if rc:
             raise OracleError(rc, err)
         return Ke, fe
+
+    def adjoint(self, physics, p0, p1, u, lam, body=None, cell_scale=None, dscale=None):
+        """Vector-Jacobian products of Phi = lam^T (K u - f): (d_cell[n_cells], d_X[n_nodes, dim]),
+        d_cell = dscale * dPhi/d(cell_scale) (dscale None: 1)."""
+        P = self._struct()
+        ph = self._physics(physics, p0, p1, body, cell_scale, None)
+        uu = np.ascontiguousarray(u, np.float64)
+        ll = np.ascontiguousarray(lam, np.float64)
+        ds = None if dscale is None else np.ascontiguousarray(dscale, np.float64)
+        d_cell = np.zeros(self.n_cells)
+        d_X = np.zeros((self.nodes.shape[0], self.dim))
+        err = _Error()
+        rc = lib().or_adjoint(ctypes.byref(P), ctypes.byref(ph), _p(uu, f64p), _p(ll, f64p),
+                              _p(ds, f64p) if ds is not None else ctypes.cast(None, f64p), _p(d_cell, f64p),
+                              _p(d_X, f64p), ctypes.byref(err))
+        if rc:
+            raise OracleError(rc, err)
+        return d_cell, d_X
 
     def index_map(self, c0: int):
         """1-based nzval positions of Ke entries of cell c0 ([ld, ld], Ke[I, J])."""
