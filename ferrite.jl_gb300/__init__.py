@@ -40,7 +40,7 @@ FILLZERO, NO_K, NO_F, ASYNC, PROFILE, COMPENSATED = 1, 2, 4, 8, 16, 32
 
 EXPORTED = ["fe_abi_version", "fe_create", "fe_assemble", "fe_sync", "fe_last_error", "fe_get_info",
             "fe_get_index_map", "fe_plan_dry_run", "fe_distribute_dofs", "fe_sparsity_pattern", "fe_kernel_time", "fe_assemble_noalloc",
-            "fe_assemble_adjoint", "fe_destroy"]
+            "fe_assemble_adjoint", "fe_graph_capture", "fe_graph_replay", "fe_graph_destroy", "fe_destroy"]
 
 i64p = ctypes.POINTER(ctypes.c_int64)
 f64p = ctypes.POINTER(ctypes.c_double)
@@ -126,6 +126,11 @@ def lib():
         L.fe_assemble_noalloc.argtypes = [ctypes.c_void_p, ctypes.POINTER(AssembleParams), ctypes.c_void_p, ctypes.c_void_p]
         L.fe_assemble_adjoint.argtypes = [ctypes.c_void_p, ctypes.POINTER(AdjointParams), ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p, ctypes.c_void_p]
+        L.fe_graph_capture.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(AssembleParams),
+                                       ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
+                                       ctypes.POINTER(ctypes.c_int32)]
+        L.fe_graph_replay.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_uint32]
+        L.fe_graph_destroy.argtypes = [ctypes.c_void_p, ctypes.c_int32]
         L.fe_destroy.argtypes = [ctypes.c_void_p]
         L.fe_destroy.restype = None
         _lib = L
@@ -323,6 +328,49 @@ class Handle:
         if rc != FE_OK:
             self._raise(rc)
         return d_rho, d_X
+
+    @staticmethod
+    def _params(physics, p0, p1, body=(0.0, 0.0, 0.0), cell_scale=None, u=None, precision=PREC_MIXED, fillzero=True,
+                cond_threshold=0.0, compensated=False, stream=None):
+        p = AssembleParams()
+        p.physics, p.precision = physics, precision
+        p.flags = (FILLZERO if fillzero else 0) | (COMPENSATED if compensated else 0)
+        p.p0, p.p1 = float(p0), float(p1)
+        for k in range(3):
+            p.body[k] = float(body[k]) if k < len(body) else 0.0
+        p.cell_scale = _ptr(cell_scale)
+        p.u = _ptr(u)
+        p.cond_threshold = float(cond_threshold)
+        p.stream = stream
+        return p
+
+    def graph_capture(self, steps, nzvals, fs, stream):
+        """fe_graph_capture: steps = list of dicts of assemble() keywords (physics, p0, p1, body,
+        cell_scale, u, precision, ...); nzvals / fs = device buffers per step. Returns the graph id."""
+        n = len(steps)
+        if stream is not None and hasattr(stream, "cuda_stream"):
+            stream = stream.cuda_stream
+        arr = (AssembleParams * n)(*[self._params(stream=stream, **st) for st in steps])
+        nz = (ctypes.c_void_p * n)(*[_ptr(x) for x in nzvals])
+        ff = (ctypes.c_void_p * n)(*[_ptr(x) for x in fs])
+        gid = ctypes.c_int32()
+        rc = lib().fe_graph_capture(self._h, stream, n, arr, nz, ff, ctypes.byref(gid))
+        if rc != FE_OK:
+            self._raise(rc)
+        return gid.value
+
+    def graph_replay(self, graph: int, stream=None, sync: bool = True, profile: bool = False):
+        if stream is not None and hasattr(stream, "cuda_stream"):
+            stream = stream.cuda_stream
+        flags = (0 if sync else ASYNC) | (PROFILE if profile else 0)
+        rc = lib().fe_graph_replay(self._h, int(graph), stream, flags)
+        if rc != FE_OK:
+            self._raise(rc)
+
+    def graph_destroy(self, graph: int):
+        rc = lib().fe_graph_destroy(self._h, int(graph))
+        if rc != FE_OK:
+            self._raise(rc)
 
     def sync(self):
         rc = lib().fe_sync(self._h)

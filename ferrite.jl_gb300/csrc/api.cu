@@ -86,6 +86,10 @@ struct fe_handle {
     double* dX_stage = nullptr;
     cudaStream_t last_stream = 0;
     int pending = 0;  // an FE_ASYNC assembly whose status has not been read
+    // CUDA graphs of captured assembly sequences (fe_graph_capture)
+    int capturing = 0;
+    cudaStream_t cap_stream = 0;
+    std::vector<std::pair<cudaGraph_t, cudaGraphExec_t>> graphs;
     fe_error_info last{};
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_events;  // recorded, unread
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_pool;    // free for reuse
@@ -111,6 +115,10 @@ struct fe_handle {
         return e;
     }
     ~fe_handle() {
+        for (auto& g : graphs) {
+            if (g.second) cudaGraphExecDestroy(g.second);
+            if (g.first) cudaGraphDestroy(g.first);
+        }
         for (auto& e : prof_events) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
         for (auto& e : prof_pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
         for (void* p : allocs) cudaFree(p);
@@ -168,6 +176,13 @@ int finish_status(fe_handle* h) {
     return FE_OK;
 }
 
+// Device status to "no error": keys all ones, counters zero (memsets, so it can be captured)
+cudaError_t status_reset(fe_handle* h, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(h->status_d, 0xFF, 2 * sizeof(unsigned long long), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(&h->status_d->flagged, 0, 2 * sizeof(unsigned int), st);
+    return e;
+}
+
 // Shared-memory sizing, status reset and the launch of one assembly: persistent CTAs, as
 // many as fit on the device at once (never more than there are tiles).
 int launch_assembly(fe_handle* h, const KernelEntry* ke, KernelArgs& A, bool fp64, cudaStream_t st,
@@ -197,10 +212,7 @@ int launch_assembly(fe_handle* h, const KernelEntry* ke, KernelArgs& A, bool fp6
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ke->fn, THREADS, smem)) != cudaSuccess)
         return cuda_fail(h, e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     const int64_t grid = std::min<int64_t>(A.n_tiles, (int64_t)std::max(per_sm, 1) * std::max(n_sm, 1));
-    DevStatus init{~0ull, ~0ull, 0u, 0u};
-    *h->status_h = init;
-    if ((e = cudaMemcpyAsync(h->status_d, h->status_h, sizeof(DevStatus), cudaMemcpyHostToDevice, st)) != cudaSuccess)
-        return cuda_fail(h, e, "status reset");
+    if (!h->capturing && (e = status_reset(h, st)) != cudaSuccess) return cuda_fail(h, e, "status reset");
     A.status = h->status_d;
     const void* shp = fp64 ? (const void*)h->shape_d : (const void*)h->shape_f;
     int sb = h->shape_bytes[pi], o1 = h->shape_off1[pi], o2 = h->shape_off2[pi];
@@ -444,7 +456,14 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
     const bool do_k = !(p->flags & FE_NO_K), do_f = !(p->flags & FE_NO_F);
     if (do_k && !nzval) return set_error(h, FE_ERR_ARG, "nzval is NULL");
     if (do_f && !f) return set_error(h, FE_ERR_ARG, "f is NULL");
-    if (h->pending) {
+    if (h->capturing) {
+        // inside fe_graph_capture: device buffers only, the capture stream, no host work
+        if ((cudaStream_t)p->stream != h->cap_stream) return set_error(h, FE_ERR_STATE, "capture: steps run on the capture stream");
+        if (p->flags & FE_PROFILE) return set_error(h, FE_ERR_STATE, "capture: FE_PROFILE is not capturable");
+        if ((do_k && !is_device_ptr(nzval)) || (do_f && !is_device_ptr(f)) || (p->u && !is_device_ptr(p->u)) ||
+            (p->cell_scale && !is_device_ptr(p->cell_scale)))
+            return set_error(h, FE_ERR_STATE, "capture: nzval, f, u and cell_scale must be device memory");
+    } else if (h->pending) {
         int rc = fe_sync(h);
         (void)rc;
     }
@@ -540,6 +559,7 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
         if (prof) (rc == FE_OK ? h->prof_events : h->prof_pool).push_back(ev);
         if (rc != FE_OK) return rc;
     }
+    if (h->capturing) return FE_OK;  // the capture reads the status once, after its last step
     if ((e = cudaMemcpyAsync(h->status_h, h->status_d, sizeof(DevStatus), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
         return cuda_fail(h, e, "status read");
     if (do_k && !nz_dev && (e = cudaMemcpyAsync(nzval, h->nz_stage, hp.nnz * 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
@@ -650,10 +670,7 @@ int fe_assemble_adjoint(fe_handle* h, const fe_adjoint_params* p, const double* 
     if ((e = cudaMemsetAsync(drho, 0, hp.n_cells * sizeof(double), st)) != cudaSuccess) return cuda_fail(h, e, "d_rho");
     A.d_cell = drho;
     A.contrib = h->adj_contrib;
-    DevStatus init{~0ull, ~0ull, 0u, 0u};
-    *h->status_h = init;
-    if ((e = cudaMemcpyAsync(h->status_d, h->status_h, sizeof(DevStatus), cudaMemcpyHostToDevice, st)) != cudaSuccess)
-        return cuda_fail(h, e, "status reset");
+    if ((e = status_reset(h, st)) != cudaSuccess) return cuda_fail(h, e, "status reset");
     A.status = h->status_d;
     int n_sm = 0;
     cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, h->device);
@@ -695,6 +712,95 @@ int fe_assemble_adjoint(fe_handle* h, const fe_adjoint_params* p, const double* 
     const bool host_out = !rho_dev || (d_X && !x_dev);
     if ((p->flags & FE_ASYNC) && !host_out) return FE_OK;
     return fe_sync(h);
+}
+
+int fe_graph_capture(fe_handle* h, void* stream, int32_t n_steps, const fe_assemble_params* steps, double* const* nzval,
+                     double* const* f, int32_t* graph) {
+    if (!h || !steps || !nzval || !f || !graph || n_steps < 1) return FE_ERR_ARG;
+    if (h->capturing) return set_error(h, FE_ERR_STATE, "a capture is already open");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!st) return set_error(h, FE_ERR_ARG, "fe_graph_capture needs a created (non-default) stream");
+    for (int32_t k = 0; k < n_steps; ++k) {
+        const fe_assemble_params& q = steps[k];
+        const bool do_k = !(q.flags & FE_NO_K), do_f = !(q.flags & FE_NO_F);
+        if ((do_k && !is_device_ptr(nzval[k])) || (do_f && !is_device_ptr(f[k])) || (q.u && !is_device_ptr(q.u)) ||
+            (q.cell_scale && !is_device_ptr(q.cell_scale)))
+            return set_error(h, FE_ERR_ARG, "fe_graph_capture: nzval, f, u and cell_scale must be device memory");
+    }
+    // Run every step once, uncaptured: that allocates the FP32 input copies, sets the kernels'
+    // shared-memory attributes and reports element errors before anything is recorded.
+    for (int32_t k = 0; k < n_steps; ++k) {
+        fe_assemble_params q = steps[k];
+        q.stream = st;
+        q.flags &= ~(uint32_t)(FE_ASYNC | FE_PROFILE);
+        const int rc = fe_assemble(h, &q, nzval[k], f[k]);
+        if (rc != FE_OK) return rc;
+    }
+    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamBeginCapture");
+    h->capturing = 1;
+    h->cap_stream = st;
+    int rc = FE_OK;
+    if ((e = status_reset(h, st)) != cudaSuccess) rc = cuda_fail(h, e, "status reset");
+    for (int32_t k = 0; k < n_steps && rc == FE_OK; ++k) {
+        fe_assemble_params q = steps[k];
+        q.stream = st;
+        q.flags = (q.flags & ~(uint32_t)FE_PROFILE) | FE_ASYNC;
+        rc = fe_assemble(h, &q, nzval[k], f[k]);
+    }
+    if (rc == FE_OK && (e = cudaMemcpyAsync(h->status_h, h->status_d, sizeof(DevStatus), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        rc = cuda_fail(h, e, "status read");
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(st, &g);
+    h->capturing = 0;
+    if (rc == FE_OK && e != cudaSuccess) rc = cuda_fail(h, e, "cudaStreamEndCapture");
+    cudaGraphExec_t x = nullptr;
+    if (rc == FE_OK && (e = cudaGraphInstantiate(&x, g, 0)) != cudaSuccess) rc = cuda_fail(h, e, "cudaGraphInstantiate");
+    if (rc != FE_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    h->graphs.push_back({g, x});
+    *graph = (int32_t)h->graphs.size() - 1;
+    return FE_OK;
+}
+
+int fe_graph_replay(fe_handle* h, int32_t graph, void* stream, uint32_t flags) {
+    if (!h || graph < 0 || graph >= (int32_t)h->graphs.size() || !h->graphs[graph].second) return FE_ERR_ARG;
+    if (h->capturing) return set_error(h, FE_ERR_STATE, "replay during a capture");
+    if (h->pending) fe_sync(h);
+    cudaStream_t st = (cudaStream_t)stream;
+    std::pair<cudaEvent_t, cudaEvent_t> ev{nullptr, nullptr};
+    cudaError_t e;
+    const bool prof = (flags & FE_PROFILE) != 0;
+    if (prof) {
+        if (!h->prof_pool.empty()) {
+            ev = h->prof_pool.back();
+            h->prof_pool.pop_back();
+        } else if ((e = cudaEventCreate(&ev.first)) != cudaSuccess || (e = cudaEventCreate(&ev.second)) != cudaSuccess) {
+            return cuda_fail(h, e, "cudaEventCreate");
+        }
+        cudaEventRecord(ev.first, st);
+    }
+    if ((e = cudaGraphLaunch(h->graphs[graph].second, st)) != cudaSuccess) return cuda_fail(h, e, "cudaGraphLaunch");
+    if (prof) {
+        cudaEventRecord(ev.second, st);
+        h->prof_events.push_back(ev);
+    }
+    h->last_stream = st;
+    h->pending = 1;
+    if (flags & FE_ASYNC) return FE_OK;
+    return fe_sync(h);
+}
+
+int fe_graph_destroy(fe_handle* h, int32_t graph) {
+    if (!h || graph < 0 || graph >= (int32_t)h->graphs.size()) return FE_ERR_ARG;
+    if (h->pending) fe_sync(h);
+    auto& g = h->graphs[graph];
+    if (g.second) cudaGraphExecDestroy(g.second);
+    if (g.first) cudaGraphDestroy(g.first);
+    g = {nullptr, nullptr};
+    return FE_OK;
 }
 
 int fe_kernel_time(fe_handle* h, double* total_ms, int64_t* launches) {

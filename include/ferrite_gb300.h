@@ -253,6 +253,22 @@ typedef struct {
 int fe_assemble_adjoint(fe_handle* h, const fe_adjoint_params* params, const double* u, const double* lambda,
                         double* d_rho, double* d_X);
 
+/* CUDA graphs of repeated assemblies (Newton-style re-assembly: the same pattern, new u).
+ * fe_graph_capture records n_steps fe_assemble calls (steps[k] with nzval[k], f[k]; all
+ * buffers device memory; different steps may use different u or outputs) into one CUDA graph on
+ * `stream` (a created stream). It first runs each step once, uncaptured, so element errors are
+ * reported here and the graph needs no allocation. fe_graph_replay launches the graph: it
+ * re-reads the buffers' current contents, so updating u in place between replays re-assembles
+ * with the new u. The device status (detJ, pattern misses) is reset at the start of a replay and
+ * covers all its steps; fe_sync / a synchronous replay reports it. FE_ASYNC and FE_PROFILE
+ * (bracketing the whole replay) are honoured by fe_graph_replay.
+ * No counterpart in the reference: it replaces the repeated start_assemble + cell-loop passes of
+ * a Newton iteration (docs/src/literate-tutorials/hyperelasticity.jl:386-420). */
+int fe_graph_capture(fe_handle* h, void* stream, int32_t n_steps, const fe_assemble_params* steps, double* const* nzval,
+                     double* const* f, int32_t* graph);
+int fe_graph_replay(fe_handle* h, int32_t graph, void* stream, uint32_t flags);
+int fe_graph_destroy(fe_handle* h, int32_t graph);
+
 void fe_destroy(fe_handle* h);
 
 int fe_abi_version(void);
