@@ -299,6 +299,17 @@ def run_ours(args):
                "note": "fe_assemble with pinned host nzval/f; per-step inputs are scalars (grid, dofs and "
                        "pattern stay resident from fe_create)"}
 
+    # ---- the other configurations: heat 100^2, SIMP adjoint, mixed-cell Neo-Hooke graph ----
+    configs = None
+    if rank == 0 and not args.skip_configs:
+        configs = {}
+        for name, fn in (("heat", config_heat), ("adjoint", config_adjoint), ("mixed_graph", config_mixed_graph)):
+            try:
+                configs[name] = fn(fg, stream)
+            except Exception as exc:  # reported, not fatal: the headline line still prints
+                configs[name] = {"error": f"{type(exc).__name__}: {exc}"}
+            torch.cuda.empty_cache()
+
     # ---- CPU baseline: the oracle's colored threaded assembly on a slab ----
     cpu = None
     if rank == 0 and not args.skip_cpu:
@@ -323,18 +334,145 @@ def run_ours(args):
             "vs_baseline": None, "dtype": "f32+f64acc", "data": "synthetic",
             "config": {"workload": WORKLOAD, "nel": list(NEL), "cells": n_cells, "ndofs": ndofs, "nnz": nnz, "seed": SEED,
                        "perturbation": "interior nodes +-0.2h uniform", "E": E_MOD, "nu": NU, "body": BODY,
-                       "l2": "inputs (~0.35 GB) and outputs (4.1 GB) larger than L2; no flush",
+                       "l2": f"outputs ({8 * (nnz + ndofs) / 1e9:.2f} GB) and inputs larger than the 129 MB L2; no flush",
                        "parallelism": "replicas" if world > 1 else "single-gpu",
                        "tiles": info["n_tiles"], "cell_visits_per_cell": info["n_cell_visits"] / n_cells},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "algorithmic_bytes": balg, "kernel_ms": kernel_ms,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy)" if peaks else "fallback"},
             "clocks": clk.summary(), "gpu_launches": args.steps, "e2e": e2e, "fp64_gpu": fp64,
-            "cpu_baseline": cpu, "checks": checks,
+            "cpu_baseline": cpu, "checks": checks, "configs": configs,
             "setup_s": {"host_setup": P["setup_s"], "fe_create": P["create_s"]}}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def _timed(stream, fn, reps, warmup=2):
+    """CUDA-event time of fn() per call on `stream` (fn enqueues asynchronously)."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(reps):
+        fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def config_heat(fg, stream):
+    """2D Poisson as in the heat tutorial: Quadrilateral 100x100 on [-1,1]^2, k = 1, source 1."""
+    import torch
+    host = __import__("ferrite_gb300.host", fromlist=["host"])
+    g = host.generate_grid(host.QUADRILATERAL, (100, 100), (-1, -1), (1, 1))
+    dh = host.DofHandler.from_grid(g, ip_order=1, n_components=1).close()
+    colptr, rowval = dh.allocate_matrix()
+    h = dh.handle([host.CellValues(host.QUADRILATERAL, 1, 2)], colptr, rowval)
+    nz = torch.empty(h.nnz, dtype=torch.float64, device="cuda")
+    f = torch.empty(dh.ndofs, dtype=torch.float64, device="cuda")
+    out = {"workload": "heat_quad100x100", "cells": dh.n_cells, "ndofs": dh.ndofs, "nnz": h.nnz}
+    for name, prec in (("mixed", fg.PREC_MIXED), ("fp64", fg.PREC_FP64)):
+        ms = _timed(stream, lambda: h.assemble(nz, f, physics=fg.HEAT, p0=1.0, p1=1.0, precision=prec, stream=stream,
+                                               sync=False), 200)
+        h.sync()
+        out[name] = {"us_per_assembly": ms * 1e3, "Melem_s": dh.n_cells / (ms * 1e-3) / 1e6}
+    out["note"] = "launch-bound (10,000 cells); one kernel launch per assembly"
+    h.close()
+    return out
+
+
+def config_adjoint(fg, stream):
+    """SIMP cantilever (96,48,48) on [0,2]x[0,1]^2: rho ~ U(0.01,1), E = rho^3, nu = 0.3, u and
+    lambda ~ N(0, 1e-3^2); adjoint (d/d rho, d/dX) against the forward K+f assembly."""
+    import torch
+    host = __import__("ferrite_gb300.host", fromlist=["host"])
+    nel = (96, 48, 48)
+    g = host.generate_grid(host.HEXAHEDRON, nel, (0, 0, 0), (2, 1, 1))
+    dh = host.DofHandler.from_grid(g, ip_order=1, n_components=3).close()
+    colptr, rowval = dh.allocate_matrix()
+    h = dh.handle([host.CellValues(host.HEXAHEDRON, 1, 2)], colptr, rowval)
+    rng = np.random.default_rng(SEED + 4)
+    rho = rng.uniform(0.01, 1.0, dh.n_cells)
+    d = lambda a: torch.as_tensor(a, device="cuda")
+    scale, dscale = d(rho ** 3), d(3 * rho ** 2)
+    u, lam = d(rng.normal(0, 1e-3, dh.ndofs)), d(rng.normal(0, 1e-3, dh.ndofs))
+    nz = torch.empty(h.nnz, dtype=torch.float64, device="cuda")
+    f = torch.empty(dh.ndofs, dtype=torch.float64, device="cuda")
+    d_rho = torch.empty(dh.n_cells, dtype=torch.float64, device="cuda")
+    d_X = torch.empty(g.nodes.shape[0] * 3, dtype=torch.float64, device="cuda")
+    kw = dict(physics=fg.LINEAR_ELASTIC, p0=1.0, p1=NU, body=BODY, cell_scale=scale, stream=stream)
+    fwd = _timed(stream, lambda: h.assemble(nz, f, sync=False, **kw), 20)
+    h.sync()
+    out = {"workload": "simp_cantilever_hex96x48x48", "cells": dh.n_cells, "ndofs": dh.ndofs, "forward_ms": fwd}
+    res = {}
+    for name, prec in (("mixed", fg.PREC_MIXED), ("fp64", fg.PREC_FP64)):
+        ms = _timed(stream, lambda: h.adjoint(u, lam, d_rho, d_X, fg.LINEAR_ELASTIC, 1.0, NU, body=BODY, cell_scale=scale,
+                                              dscale=dscale, precision=prec, stream=stream, sync=False), 20)
+        h.sync()
+        res[name] = (d_rho.clone(), d_X.clone())
+        out[f"adjoint_{name}_ms"] = ms
+    out["adjoint_over_forward"] = out["adjoint_mixed_ms"] / fwd
+    rel = lambda a, b: float((a - b).abs().max() / b.abs().max())
+    out["mixed_vs_fp64_rel_max"] = {"d_rho": rel(res["mixed"][0], res["fp64"][0]), "d_X": rel(res["mixed"][1], res["fp64"][1])}
+    out["note"] = ("forward = mixed K+f assembly with E_e = rho^3; adjoint recomputes the geometry; "
+                   "finite-difference checks of the formulas are in the tests")
+    h.close()
+    return out
+
+
+def config_mixed_graph(fg, stream, steps=20):
+    """~2M cells over three x-slabs sharing vertex nodes (Hex Q1 50%, Tet P1 25% as 6 per cube,
+    Wedge P1 25% as 2 per cube), compressible Neo-Hooke (mu 1, lambda 10), u = 0.05 U(-1,1)
+    seeded per step; the tile plan autotuned, then `steps` re-assemblies with updated u captured
+    as one CUDA graph and replayed."""
+    import torch
+    host = __import__("ferrite_gb300.host", fromlist=["host"])
+    nh, nt, nw, ny, nzc = 100, 8, 25, 100, 100
+    nx = nh + nt + nw
+    g = host.generate_grid(host.HEXAHEDRON, (nx, ny, nzc), (0, 0, 0), (nx / 100.0, 1, 1))
+    g = host.perturb_interior(g, (nx, ny, nzc), 0.15, SEED + 5, (0, 0, 0), (nx / 100.0, 1, 1))
+    cubes = g.cells  # [n, 8], 1-based, x fastest
+    ix = np.arange(cubes.shape[0]) % nx
+    T = np.array([[1, 2, 4, 8], [1, 5, 2, 8], [2, 3, 4, 8], [2, 7, 3, 8], [2, 5, 6, 8], [2, 6, 7, 8]]) - 1
+    W = np.array([[1, 2, 4, 5, 6, 8], [2, 3, 4, 6, 7, 8]]) - 1
+    hexes = cubes[ix < nh]
+    tets = cubes[(ix >= nh) & (ix < nh + nt)][:, T].reshape(-1, 4)
+    wedges = cubes[ix >= nh + nt][:, W].reshape(-1, 6)
+    n_cells = len(hexes) + len(tets) + len(wedges)
+    dh = host.DofHandler(g.nodes, n_cells)
+    o = 0
+    for ct, cn in ((host.HEXAHEDRON, hexes), (host.TETRAHEDRON, tets), (host.WEDGE, wedges)):
+        dh.add(ct, np.ascontiguousarray(cn, np.int64), np.arange(o + 1, o + len(cn) + 1, dtype=np.int64), 1, 3)
+        o += len(cn)
+    dh.close()
+    colptr, rowval = dh.allocate_matrix()
+    cvs = [host.CellValues(host.HEXAHEDRON, 1, 2), host.CellValues(host.TETRAHEDRON, 1, 1), host.CellValues(host.WEDGE, 1, 2)]
+    h = dh.handle(cvs, colptr, rowval)
+    rng = np.random.default_rng(SEED + 6)
+    us = [torch.as_tensor(0.05 * rng.uniform(-1, 1, dh.ndofs), device="cuda") for _ in range(steps)]
+    nz = torch.empty(h.nnz, dtype=torch.float64, device="cuda")
+    f = torch.empty(dh.ndofs, dtype=torch.float64, device="cuda")
+    kw = dict(physics=fg.NEO_HOOKE, p0=1.0, p1=10.0, body=(0.0, 0.0, 0.0))
+    tune = h.autotune(nz, f, stage_caps=[8192, 12288, 16384], reps=2, stream=stream, u=us[0], **kw)
+    single = _timed(stream, lambda: h.assemble(nz, f, u=us[0], stream=stream, sync=False, **kw), 5)
+    h.sync()
+    gid = h.graph_capture([dict(u=u, **kw) for u in us], [nz] * steps, [f] * steps, stream)
+    replay = _timed(stream, lambda: h.graph_replay(gid, stream, sync=False), 3, warmup=1)
+    h.sync()
+    info = h.info()
+    out = {"workload": "mixed_hex_tet_wedge_neo_hooke_2M", "cells": n_cells, "hex": len(hexes), "tet": len(tets),
+           "wedge": len(wedges), "ndofs": dh.ndofs, "nnz": h.nnz, "steps_per_graph": steps,
+           "graph_replay_ms": replay, "ms_per_assembly_in_graph": replay / steps,
+           "Melem_s_in_graph": n_cells * steps / (replay * 1e-3) / 1e6, "ms_single_assembly": single,
+           "autotune": {"best_stage_cap": tune["best_stage_cap"],
+                        "candidates": [{"stage_cap": c, "ms": ms, "tiles": t} for c, ms, t, _ in tune["candidates"]]},
+           "tiles": info["n_tiles"], "cell_visits_per_cell": info["n_cell_visits"] / n_cells,
+           "quadrature": "hex 2x2x2 Gauss, tet 1 point, wedge 5-point order-2 rule"}
+    h.close()
+    return out
 
 
 def main():
@@ -346,6 +484,7 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-configs", action="store_true", help="skip the heat / adjoint / mixed-graph configurations")
     ap.add_argument("--nel", type=int, default=128, help="cells per axis (128 = the benchmark workload)")
     args = ap.parse_args()
     if args.warmup < 3:

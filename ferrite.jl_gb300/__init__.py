@@ -40,7 +40,8 @@ FILLZERO, NO_K, NO_F, ASYNC, PROFILE, COMPENSATED = 1, 2, 4, 8, 16, 32
 
 EXPORTED = ["fe_abi_version", "fe_create", "fe_assemble", "fe_sync", "fe_last_error", "fe_get_info",
             "fe_get_index_map", "fe_plan_dry_run", "fe_distribute_dofs", "fe_sparsity_pattern", "fe_kernel_time", "fe_assemble_noalloc",
-            "fe_assemble_adjoint", "fe_graph_capture", "fe_graph_replay", "fe_graph_destroy", "fe_destroy"]
+            "fe_assemble_adjoint", "fe_graph_capture", "fe_graph_replay", "fe_graph_destroy",
+            "fe_autotune", "fe_destroy"]
 
 i64p = ctypes.POINTER(ctypes.c_int64)
 f64p = ctypes.POINTER(ctypes.c_double)
@@ -75,6 +76,16 @@ class AdjointParams(ctypes.Structure):
     _fields_ = [("physics", ctypes.c_int32), ("precision", ctypes.c_int32), ("flags", ctypes.c_uint32),
                 ("p0", ctypes.c_double), ("p1", ctypes.c_double), ("body", ctypes.c_double * 3),
                 ("cell_scale", ctypes.c_void_p), ("dscale", ctypes.c_void_p), ("stream", ctypes.c_void_p)]
+
+
+TUNE_MAX = 16
+
+
+class TuneResult(ctypes.Structure):
+    _fields_ = [("n_candidates", ctypes.c_int32), ("stage_cap", ctypes.c_int32 * TUNE_MAX),
+                ("ms", ctypes.c_double * TUNE_MAX), ("n_tiles", ctypes.c_int64 * TUNE_MAX),
+                ("n_cell_visits", ctypes.c_int64 * TUNE_MAX), ("best_stage_cap", ctypes.c_int32),
+                ("best_ms", ctypes.c_double)]
 
 
 class ErrorInfo(ctypes.Structure):
@@ -131,6 +142,8 @@ def lib():
                                        ctypes.POINTER(ctypes.c_int32)]
         L.fe_graph_replay.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_uint32]
         L.fe_graph_destroy.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+        L.fe_autotune.argtypes = [ctypes.c_void_p, ctypes.POINTER(AssembleParams), ctypes.c_void_p, ctypes.c_void_p,
+                                  ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), ctypes.c_int32, ctypes.POINTER(TuneResult)]
         L.fe_destroy.argtypes = [ctypes.c_void_p]
         L.fe_destroy.restype = None
         _lib = L
@@ -343,6 +356,24 @@ class Handle:
         p.cond_threshold = float(cond_threshold)
         p.stream = stream
         return p
+
+    def autotune(self, nzval, f, stage_caps=None, reps: int = 3, stream=None, **assemble_kw):
+        """fe_autotune: re-plan with each candidate staging capacity, time it, keep the fastest.
+        Returns {"best_stage_cap", "best_ms", "candidates": [(cap, ms, tiles, visits), ...]}."""
+        if stream is not None and hasattr(stream, "cuda_stream"):
+            stream = stream.cuda_stream
+        p = self._params(stream=stream, **assemble_kw)
+        caps = None
+        n = 0
+        if stage_caps:
+            n = len(stage_caps)
+            caps = (ctypes.c_int32 * n)(*[int(c) for c in stage_caps])
+        res = TuneResult()
+        rc = lib().fe_autotune(self._h, ctypes.byref(p), _ptr(nzval), _ptr(f), n, caps, int(reps), ctypes.byref(res))
+        if rc != FE_OK:
+            self._raise(rc)
+        cands = [(res.stage_cap[k], res.ms[k], res.n_tiles[k], res.n_cell_visits[k]) for k in range(res.n_candidates)]
+        return {"best_stage_cap": res.best_stage_cap, "best_ms": res.best_ms, "candidates": cands}
 
     def graph_capture(self, steps, nzvals, fs, stream):
         """fe_graph_capture: steps = list of dicts of assemble() keywords (physics, p0, p1, body,

@@ -96,6 +96,7 @@ struct fe_handle {
     int64_t flagged = 0;
     double create_seconds = 0;
     int device = 0;
+    int32_t stage_cap = 0;  // staging values per tile the current plan was built with
 
     template <typename T>
     cudaError_t alloc(T** p, size_t count) {
@@ -106,6 +107,14 @@ struct fe_handle {
             device_bytes += (int64_t)(count * sizeof(T));
         }
         return e;
+    }
+    void release(void* p) {  // free one allocation made by alloc()
+        for (size_t k = 0; k < allocs.size(); ++k)
+            if (allocs[k] == p) {
+                cudaFree(p);
+                allocs.erase(allocs.begin() + (long)k);
+                return;
+            }
     }
     template <typename T>
     cudaError_t upload(T** p, const T* src, size_t count) {
@@ -174,6 +183,32 @@ int finish_status(fe_handle* h) {
     }
     h->last = fe_error_info{};
     return FE_OK;
+}
+
+// Upload h->plan's records (replacing the previous plan's device copy) and set the caps the
+// kernel's shared-memory layout is sized from. The host copy of the records is released.
+cudaError_t install_plan(fe_handle* h) {
+    Plan& pl = h->plan;
+    KernelArgs& A = h->base;
+    char* rec = nullptr;
+    int64_t* roff = nullptr;
+    cudaError_t e = h->upload(&rec, (const char*)pl.rec.data(), pl.rec.size());
+    if (e == cudaSuccess) e = h->upload(&roff, pl.rec_off.data(), pl.rec_off.size());
+    if (e != cudaSuccess) {
+        if (rec) h->release(rec);
+        return e;
+    }
+    if (A.rec) h->release((void*)A.rec);
+    if (A.rec_off) h->release((void*)A.rec_off);
+    A.rec = rec;
+    A.rec_off = roff;
+    std::vector<uint8_t>().swap(pl.rec);  // the device copy is the one in use
+    A.n_tiles = (int32_t)pl.n_tiles;
+    A.rec_cap = std::max(pl.max_rec, 64);
+    A.node_cap = std::max(pl.max_nodes, 1);
+    A.stage_cap = std::max(pl.max_stage, 2);
+    A.out_cap = std::max(pl.max_out, 2);
+    return cudaSuccess;
 }
 
 // Device status to "no error": keys all ones, counters zero (memsets, so it can be captured)
@@ -247,6 +282,7 @@ int fe_create(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain
         if (const char* s = std::getenv("FE_GB300_STAGE_CAP")) opt.stage_cap = std::atoi(s);
         rc = build_plan(h->hp, opt, h->plan, err);
         if (rc == FE_OK) rc = check_plan(h->hp, h->plan, err);
+        h->stage_cap = opt.stage_cap;
     }
     if (rc != FE_OK) {
         g_create_error = fe_error_info{};
@@ -353,27 +389,14 @@ int fe_create(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain
     h->shape_off1[0] = offs_f[1]; h->shape_off2[0] = offs_f[2];
     h->shape_off1[1] = offs_d[1]; h->shape_off2[1] = offs_d[2];
     // tile records
-    {
-        char* rec;
-        int64_t* roff;
-        CK(h->upload(&rec, (const char*)pl.rec.data(), pl.rec.size()));
-        CK(h->upload(&roff, pl.rec_off.data(), pl.rec_off.size()));
-        A.rec = rec;
-        A.rec_off = roff;
-        std::vector<uint8_t>().swap(h->plan.rec);  // the device copy is the one in use
-    }
-    A.n_tiles = (int32_t)pl.n_tiles;
     A.bs = (hp.nc * hp.nc + 1) & ~1;
-    A.rec_cap = std::max(pl.max_rec, 64);
-    A.node_cap = std::max(pl.max_nodes, 1);
-    A.stage_cap = std::max(pl.max_stage, 2);
-    A.out_cap = std::max(pl.max_out, 2);
     if (pl.n_tiles >= (int64_t)INT32_MAX) {
         set_error(h, FE_ERR_UNSUPPORTED, "too many tiles");
         g_create_error = h->last;
         delete h;
         return FE_ERR_UNSUPPORTED;
     }
+    CK(install_plan(h));
     CK(h->alloc(&h->status_d, 1));
     CK(cudaMallocHost((void**)&h->status_h, sizeof(DevStatus)));
 #undef CK
@@ -800,6 +823,85 @@ int fe_graph_destroy(fe_handle* h, int32_t graph) {
     if (g.second) cudaGraphExecDestroy(g.second);
     if (g.first) cudaGraphDestroy(g.first);
     g = {nullptr, nullptr};
+    return FE_OK;
+}
+
+int fe_autotune(fe_handle* h, const fe_assemble_params* p, double* nzval, double* f, int32_t n_candidates,
+                const int32_t* stage_caps, int32_t reps, fe_tune_result* out) {
+    static const int32_t defaults[] = {6144, 8192, 10240, 12288, 16384, 24576};
+    if (!h || !p || !out) return FE_ERR_ARG;
+    if (h->capturing) return set_error(h, FE_ERR_STATE, "autotune during a capture");
+    if (!stage_caps || n_candidates < 1) {
+        stage_caps = defaults;
+        n_candidates = (int32_t)(sizeof(defaults) / sizeof(defaults[0]));
+    }
+    if (n_candidates > FE_TUNE_MAX) n_candidates = FE_TUNE_MAX;
+    if (reps < 1) reps = 3;
+    *out = fe_tune_result{};
+    if (h->pending) fe_sync(h);
+    cudaStream_t st = (cudaStream_t)p->stream;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    fe_assemble_params q = *p;
+    q.flags = (q.flags & ~(uint32_t)(FE_PROFILE)) | FE_ASYNC;
+    double best_ms = 1e300;
+    int32_t best_cap = h->stage_cap;
+    int rc = FE_OK;
+    for (int32_t k = 0; k < n_candidates && rc == FE_OK; ++k) {
+        out->stage_cap[k] = stage_caps[k];
+        out->ms[k] = -1.0;
+        PlanOptions opt;
+        opt.stage_cap = stage_caps[k];
+        Error err;
+        Plan pl;
+        if (build_plan(h->hp, opt, pl, err) != FE_OK || check_plan(h->hp, pl, err) != FE_OK) continue;
+        h->plan = std::move(pl);
+        cudaError_t ce = install_plan(h);
+        if (ce != cudaSuccess) { rc = cuda_fail(h, ce, "autotune: upload plan"); break; }
+        h->stage_cap = opt.stage_cap;
+        out->n_tiles[k] = h->plan.n_tiles;
+        out->n_cell_visits[k] = h->plan.visits;
+        // one warm-up, then reps timed assemblies; a candidate whose tiles do not fit shared
+        // memory is skipped
+        if (fe_assemble(h, &q, nzval, f) != FE_OK || fe_sync(h) != FE_OK) {
+            h->last = fe_error_info{};
+            continue;
+        }
+        cudaEventRecord(e0, st);
+        for (int32_t r = 0; r < reps && rc == FE_OK; ++r) rc = fe_assemble(h, &q, nzval, f);
+        cudaEventRecord(e1, st);
+        if (rc != FE_OK) break;
+        rc = fe_sync(h);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        out->ms[k] = ms / reps;
+        out->n_candidates = k + 1;
+        if (ms / reps < best_ms) {
+            best_ms = ms / reps;
+            best_cap = stage_caps[k];
+        }
+    }
+    out->n_candidates = n_candidates;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != FE_OK) return rc;
+    if (best_ms == 1e300) return set_error(h, FE_ERR_UNSUPPORTED, "autotune: no candidate ran");
+    // keep the fastest plan
+    if (best_cap != h->stage_cap) {
+        PlanOptions opt;
+        opt.stage_cap = best_cap;
+        Error err;
+        Plan pl;
+        if (build_plan(h->hp, opt, pl, err) != FE_OK || check_plan(h->hp, pl, err) != FE_OK)
+            return set_error(h, FE_ERR_ARG, "autotune: rebuilding the chosen plan failed");
+        h->plan = std::move(pl);
+        cudaError_t ce = install_plan(h);
+        if (ce != cudaSuccess) return cuda_fail(h, ce, "autotune: upload plan");
+        h->stage_cap = best_cap;
+    }
+    out->best_stage_cap = best_cap;
+    out->best_ms = best_ms;
     return FE_OK;
 }
 

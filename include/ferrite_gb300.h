@@ -269,6 +269,26 @@ int fe_graph_capture(fe_handle* h, void* stream, int32_t n_steps, const fe_assem
 int fe_graph_replay(fe_handle* h, int32_t graph, void* stream, uint32_t flags);
 int fe_graph_destroy(fe_handle* h, int32_t graph);
 
+/* Autotuner of the tile plan: for each candidate staging capacity (values per tile, which sets
+ * the tile size and hence the cells recomputed at tile borders and the CTAs that fit per SM),
+ * re-plan the handle, time `reps` assemblies of `params` (after one warm-up) with CUDA events,
+ * and keep the fastest plan for later calls. stage_caps NULL: a built-in candidate list.
+ * Candidates whose tiles do not fit shared memory are skipped (ms = -1). nzval and f receive
+ * the assembled values. No counterpart in the reference. */
+#define FE_TUNE_MAX 16
+typedef struct {
+    int32_t n_candidates;
+    int32_t stage_cap[FE_TUNE_MAX];
+    double ms[FE_TUNE_MAX];            /* per assembly, -1 = not run */
+    int64_t n_tiles[FE_TUNE_MAX];
+    int64_t n_cell_visits[FE_TUNE_MAX];
+    int32_t best_stage_cap;
+    double best_ms;
+} fe_tune_result;
+
+int fe_autotune(fe_handle* h, const fe_assemble_params* params, double* nzval, double* f, int32_t n_candidates,
+                const int32_t* stage_caps, int32_t reps, fe_tune_result* out);
+
 void fe_destroy(fe_handle* h);
 
 int fe_abi_version(void);

@@ -70,3 +70,26 @@ def test_graph_capture_rejects_host_buffers(built, oracle):
         h.graph_capture([dict(physics=fg.LINEAR_ELASTIC, p0=1.0, p1=0.3)], [np.zeros(prob.nnz)], [np.zeros(prob.ndofs)],
                         stream)
     assert e.value.code == 1
+
+
+def test_autotune_keeps_fastest_plan_and_results(built, oracle, torch_cuda):
+    """fe_autotune re-plans with each staging capacity; every candidate assembles the same
+    matrix (the plan does not change values), and the handle keeps the fastest plan."""
+    torch = torch_cuda
+    fg, O = built, oracle
+    prob = O.box_problem(O.HEXAHEDRON, (10, 9, 8), ncomp=3, perturb=0.2, seed=5)
+    h = make_handle(fg, O, prob)
+    nz = torch.zeros(prob.nnz, dtype=torch.float64, device="cuda")
+    f = torch.zeros(prob.ndofs, dtype=torch.float64, device="cuda")
+    kw = dict(physics=fg.LINEAR_ELASTIC, p0=200e3, p1=0.3, body=(0.0, 0.0, -1.0))
+    h.assemble(nz, f, **kw)
+    nz0, f0 = nz.clone(), f.clone()
+    res = h.autotune(nz, f, stage_caps=[4096, 8192, 12288], reps=2, **kw)
+    assert res["best_stage_cap"] in (4096, 8192, 12288)
+    assert all(ms > 0 for _, ms, _, _ in res["candidates"])
+    assert res["candidates"][0][2] > res["candidates"][2][2]  # smaller tiles, more of them
+    nz.zero_()
+    f.zero_()
+    h.assemble(nz, f, **kw)
+    # summation order is cell order whatever the tiles: bitwise the same
+    assert torch.equal(nz, nz0) and torch.equal(f, f0)
