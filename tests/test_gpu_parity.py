@@ -2,7 +2,7 @@
 
 Tolerances (relative Frobenius norm of nzval and f against the FP64 oracle):
   * FE_PREC_FP64 (the plain FP64 drop-in):      <= 1e-12
-  * FE_PREC_MIXED (FP32 element math, FP64-class accumulation): <= 1e-6
+  * FE_PREC_MIXED (FP32 element math, FP32 sums per entry rounded exactly to FP64): <= 1e-6
 Sparsity structure and index maps are bit-exact. Runs are bitwise reproducible.
 """
 import numpy as np
