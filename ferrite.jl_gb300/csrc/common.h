@@ -78,7 +78,6 @@ constexpr int RED_RANK_BITS = 22;
 constexpr int MAX_TILE_ENTS = 1 << (32 - RED_RANK_BITS);
 constexpr int MAX_ENT_CELLS = 255;   // cells of one dof entity
 constexpr int MAX_TILE_SLOTS = 0xFFFF;
-constexpr int OUT_CAP_DOUBLES = 4096; // output buffer of one reduce pass (32 KiB)
 
 struct RecHead {
     int32_t bytes;

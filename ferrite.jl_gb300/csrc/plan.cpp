@@ -243,7 +243,8 @@ struct TileItem {
 // j) triples in (sub, cell, j) order. Returns 0 or an error code (internal inconsistency).
 int build_record(const HostProblem& hp, const std::vector<int32_t>& kcount, const std::vector<int32_t>& tile_local,
                  const int32_t* ents, int32_t n_ent, const uint64_t* trip, int64_t n_trip, std::vector<uint8_t>& out,
-                 int32_t& n_nodes_out, int32_t& stage_out, int32_t& n_cells_out, int32_t& n_items_out, int32_t& out_len_out) {
+                 int32_t& n_nodes_out, int32_t& stage_out, int32_t& n_cells_out, int32_t& n_items_out, int32_t& out_len_out,
+                 int32_t out_cap) {
     const int nc = hp.nc;
     const int bs = (nc * nc + 1) & ~1;
     const int64_t* cp = hp.colptr.data();
@@ -335,7 +336,7 @@ int build_record(const HostProblem& hp, const std::vector<int32_t>& kcount, cons
                 const bool joins = (int32_t)rngs.size() > P.rng_begin && rngs.back().nz0 + rngs.back().len == cb;
                 int32_t start = joins ? rngs.back().buf_off + rngs.back().len : used;
                 if (!joins && ((start - cb) & 1)) ++start;
-                if (start + len > OUT_CAP_DOUBLES) {
+                if (start + len > out_cap) {
                     if (e1 == e) return 4;  // one entity's columns exceed the buffer
                     break;
                 }
@@ -572,87 +573,122 @@ int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error&
             }
         }
     }
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
     for (int64_t n = 0; n < n_ent; ++n) {
         if (kcount[n] > MAX_ENT_CELLS) return fail(err, FE_ERR_UNSUPPORTED, "a dof entity belongs to more than 255 cells");
         if (!kcount[n]) continue;
-        for (int x = 0; x < dim; ++x) {
-            pos[n * 3 + x] /= kcount[n];
-            lo[x] = std::min(lo[x], pos[n * 3 + x]);
-            hi[x] = std::max(hi[x], pos[n * 3 + x]);
-        }
+        for (int x = 0; x < dim; ++x) pos[n * 3 + x] /= kcount[n];
     }
     auto nnb_of = [&](int64_t n) { return (int64_t)((cp[nc * n + 1] - cp[nc * n]) / nc); };
     const int bs = (nc * nc + 1) & ~1;
-    // staging values of an entity: an upper bound (every row of every cell gets a slot)
+    const int32_t out_cap = opt.resolved_out_cap();
+    // per-entity loads of a tile: staging values (an upper bound: every row of every cell gets a
+    // slot), reduce lanes, and output doubles (the reduce's one-pass buffer)
     auto stage_of = [&](int64_t n) { return (int64_t)kcount[n] * (nb_max * bs + nc); };
-    // target entities per tile from the staging capacity
-    double avg_stage = 0, avg_nnb = 0;
+    auto out_of = [&](int64_t n) { return (int64_t)(cp[nc * n + nc] - cp[nc * n]); };
+    for (int64_t n = 0; n < n_ent; ++n)
+        if (stage_of(n) > opt.stage_cap || nnb_of(n) > opt.red_cap || out_of(n) > out_cap)
+            return fail(err, FE_ERR_UNSUPPORTED, "a dof entity's contributions exceed the tile capacity");
+    // sized for the heaviest entities (the interior ones), so interior tiles fit without splits
+    double max_stage = 1, max_nnb = 1, max_out = 1;
     for (int64_t n = 0; n < n_ent; ++n) {
-        avg_stage += (double)stage_of(n);
-        avg_nnb += (double)nnb_of(n);
+        max_stage = std::max(max_stage, (double)stage_of(n));
+        max_nnb = std::max(max_nnb, (double)nnb_of(n));
+        max_out = std::max(max_out, (double)out_of(n));
     }
-    avg_stage = std::max(1.0, avg_stage / (double)n_ent);
-    avg_nnb = std::max(1.0, avg_nnb / (double)n_ent);
-    const double target_ent = std::max(1.0, std::min({0.85 * opt.stage_cap / avg_stage, 0.85 * opt.ent_cap,
-                                                       0.85 * opt.red_cap / avg_nnb}));
-    const double n_tiles_target = std::max(1.0, (double)n_ent / target_ent);
-    double ext[3] = {1, 1, 1}, vol = 1;
-    for (int x = 0; x < dim; ++x) {
-        ext[x] = std::max(hi[x] - lo[x], 1e-300);
-        vol *= ext[x];
-    }
-    const double side = std::pow(vol / n_tiles_target, 1.0 / dim);
-    int64_t nt[3] = {1, 1, 1};
-    for (int x = 0; x < dim; ++x) nt[x] = std::max<int64_t>(1, (int64_t)std::llround(ext[x] / side));
-    const int64_t nbk = nt[0] * nt[1] * nt[2];
-    std::vector<int64_t> bstart(nbk + 1, 0);
-    std::vector<int64_t> bucket(n_ent);
-    for (int64_t n = 0; n < n_ent; ++n) {
-        int64_t id[3] = {0, 0, 0};
-        if (kcount[n])
-            for (int x = 0; x < dim; ++x) {
-                int64_t t = (int64_t)((pos[n * 3 + x] - lo[x]) / ext[x] * nt[x]);
-                id[x] = std::min(std::max<int64_t>(t, 0), nt[x] - 1);
-            }
-        bucket[n] = id[0] + nt[0] * (id[1] + nt[1] * id[2]);
-        bstart[bucket[n] + 1]++;
-    }
-    for (int64_t b = 0; b < nbk; ++b) bstart[b + 1] += bstart[b];
+    // Tiles by recursive coordinate bisection: the entities are split along the longest extent
+    // into as many equal parts as an average tile size allows, so tiles are compact, of nearly
+    // equal size and all fit the capacities (a part that does not is split again). Within a
+    // tile entities are ordered by id, so its nzval is a few contiguous ranges.
+    const double target = std::max(1.0, std::min({std::floor(opt.stage_cap / max_stage), std::floor(opt.red_cap / max_nnb),
+                                                  std::floor(out_cap / max_out), (double)opt.ent_cap,
+                                                  (double)MAX_TILE_ENTS}));
     std::vector<int32_t> order(n_ent);
-    {
-        std::vector<int64_t> cur(bstart.begin(), bstart.end() - 1);
-        for (int64_t n = 0; n < n_ent; ++n) order[cur[bucket[n]]++] = (int32_t)n;
-    }
-    // tiles: split buckets by capacity
+    for (int64_t n = 0; n < n_ent; ++n) order[n] = (int32_t)n;
     std::vector<int32_t> tile_of(n_ent), tile_local(n_ent);
     std::vector<int32_t> eids;              // owned entities, tile after tile
     std::vector<int64_t> tent = {0};        // tile t owns eids[tent[t] .. tent[t+1])
     eids.reserve(n_ent);
-    for (int64_t b = 0; b < nbk; ++b) {
-        int64_t k = bstart[b];
-        while (k < bstart[b + 1]) {
-            int64_t stage = 0, red = 0;
-            int32_t ne = 0;
-            const int32_t tid = (int32_t)(tent.size() - 1);
-            while (k < bstart[b + 1]) {
-                const int64_t n = order[k];
-                const int64_t st = stage_of(n);
-                if (st > opt.stage_cap || nnb_of(n) > opt.red_cap)
-                    return fail(err, FE_ERR_UNSUPPORTED, "a dof entity's contributions exceed the tile staging capacity");
-                if (ne && (stage + st > opt.stage_cap || ne + 1 > opt.ent_cap || ne + 1 > MAX_TILE_ENTS ||
-                           red + nnb_of(n) > opt.red_cap))
-                    break;
-                eids.push_back((int32_t)n);
-                tile_of[n] = tid;
-                tile_local[n] = ne;
-                stage += st;
-                red += nnb_of(n);
-                ++ne;
-                ++k;
-            }
-            tent.push_back((int64_t)eids.size());
+    auto fits = [&](int64_t lo, int64_t hi) {
+        if (hi - lo > opt.ent_cap || hi - lo > MAX_TILE_ENTS) return false;
+        int64_t st = 0, rd = 0, ot = 0;
+        for (int64_t q = lo; q < hi; ++q) {
+            st += stage_of(order[q]);
+            rd += nnb_of(order[q]);
+            ot += out_of(order[q]);
         }
+        return st <= opt.stage_cap && rd <= opt.red_cap && ot <= out_cap;
+    };
+    auto emit = [&](int64_t lo, int64_t hi) {
+        std::sort(order.begin() + lo, order.begin() + hi);
+        const int32_t tid = (int32_t)(tent.size() - 1);
+        for (int64_t q = lo; q < hi; ++q) {
+            tile_of[order[q]] = tid;
+            tile_local[order[q]] = (int32_t)(q - lo);
+            eids.push_back(order[q]);
+        }
+        tent.push_back((int64_t)eids.size());
+    };
+    // explicit stack (depth ~ log2 of the tile count): (lo, hi, parts)
+    struct Part { int64_t lo, hi, k; };
+    std::vector<Part> stack;
+    // leaves average 88 % of the target: the layer-snapped cuts vary part sizes by up to 15 %
+    stack.push_back({0, n_ent, std::max<int64_t>(1, (int64_t)std::ceil((double)n_ent / (0.88 * target)))});
+    while (!stack.empty()) {
+        Part P = stack.back();
+        stack.pop_back();
+        const int64_t n = P.hi - P.lo;
+        if (n == 0) continue;
+        int64_t k = std::min(P.k, n);
+        if (k == 1) {
+            if (fits(P.lo, P.hi) || n == 1) {
+                emit(P.lo, P.hi);
+                continue;
+            }
+            k = 2;
+        }
+        double lo_[3] = {1e300, 1e300, 1e300}, hi_[3] = {-1e300, -1e300, -1e300};
+        for (int64_t q = P.lo; q < P.hi; ++q)
+            for (int x = 0; x < dim; ++x) {
+                lo_[x] = std::min(lo_[x], pos[(int64_t)order[q] * 3 + x]);
+                hi_[x] = std::max(hi_[x], pos[(int64_t)order[q] * 3 + x]);
+            }
+        int ax = 0;
+        for (int x = 1; x < dim; ++x)
+            if (hi_[x] - lo_[x] > hi_[ax] - lo_[ax]) ax = x;
+        const int64_t kl = k / 2;
+        int64_t nl = (int64_t)std::llround((double)n * (double)kl / (double)k);
+        // order along the axis (ties by the other coordinates, then id) and move the cut to the
+        // nearest change of the axis coordinate within 15 %, so cuts follow element layers
+        const int ax1 = (ax + 1) % dim, ax2 = (ax + 2) % dim;
+        auto less = [&](int32_t x, int32_t y) {
+            const double* px = &pos[(int64_t)x * 3];
+            const double* py = &pos[(int64_t)y * 3];
+            if (px[ax] != py[ax]) return px[ax] < py[ax];
+            if (px[ax1] != py[ax1]) return px[ax1] < py[ax1];
+            if (dim > 2 && px[ax2] != py[ax2]) return px[ax2] < py[ax2];
+            return x < y;
+        };
+        std::sort(order.begin() + P.lo, order.begin() + P.hi, less);
+        {
+            const int64_t slack = std::max<int64_t>(1, (int64_t)(0.15 * (double)nl));
+            int64_t best = nl;
+            for (int64_t d = 0; d <= slack; ++d) {
+                bool hit = false;
+                for (const int64_t c : {nl - d, nl + d}) {
+                    if (c <= 0 || c >= n) continue;
+                    if (pos[(int64_t)order[P.lo + c - 1] * 3 + ax] != pos[(int64_t)order[P.lo + c] * 3 + ax]) {
+                        best = c;
+                        hit = true;
+                        break;
+                    }
+                }
+                if (hit) break;
+            }
+            nl = best;
+        }
+        // right part first on the stack so the left part is emitted first (spatial order)
+        stack.push_back({P.lo + nl, P.hi, k - kl});
+        stack.push_back({P.lo, P.lo + nl, kl});
     }
     const int64_t n_tiles = (int64_t)tent.size() - 1;
     // (sub, cell, j) triples per tile, in (sub, cell, j) order
@@ -678,7 +714,7 @@ int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error&
 #pragma omp parallel for schedule(dynamic, 16) reduction(max : status)
     for (int64_t t = 0; t < n_tiles; ++t) {
         const int st = build_record(hp, kcount, tile_local, eids.data() + tent[t], (int32_t)(tent[t + 1] - tent[t]),
-                                    trip.data() + tstart[t], tstart[t + 1] - tstart[t], recs[t], rn[t], rs[t], rc[t], ri[t], ro[t]);
+                                    trip.data() + tstart[t], tstart[t + 1] - tstart[t], recs[t], rn[t], rs[t], rc[t], ri[t], ro[t], out_cap);
         status = std::max(status, st);
     }
     if (status == 1) return fail(err, FE_ERR_ARG, "internal: incident cell count mismatch");
@@ -766,7 +802,7 @@ int check_plan(const HostProblem& hp, const Plan& pl, Error& err) {
                 const RecPass& P = PS[p];
                 if (P.red_begin != red_next || P.red_end < P.red_begin || P.red_end > H.n_red || P.run_begin != run_next ||
                     P.run_end < P.run_begin || P.run_end > H.n_runs || P.rng_begin != rng_next || P.rng_end < P.rng_begin ||
-                    P.rng_end > H.n_rng || P.out_len < 0 || P.out_len > pl.max_out || P.out_len > OUT_CAP_DOUBLES) {
+                    P.rng_end > H.n_rng || P.out_len < 0 || P.out_len > pl.max_out) {
                     bad = 1;
                     break;
                 }

@@ -42,6 +42,12 @@ struct PlanOptions {
     int32_t stage_cap = 12288;  // staging values per tile (4 bytes each in mixed precision)
     int32_t ent_cap = 1024;     // owned entities per tile
     int32_t red_cap = 2048;     // owned blocks (reduce lanes) per tile
+    int32_t out_cap = 0;        // output-buffer doubles of one reduce pass; 0: 37.5 % of stage_cap
+    int32_t resolved_out_cap() const {
+        if (out_cap > 0) return out_cap;
+        const int32_t v = (int32_t)(0.375 * stage_cap) / 256 * 256;
+        return v < 1024 ? 1024 : (v > 16384 ? 16384 : v);
+    }
 };
 
 struct Plan {

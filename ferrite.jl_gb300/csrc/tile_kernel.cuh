@@ -29,6 +29,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "common.h"
 #include "dfloat.h"
 
@@ -532,94 +534,8 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
             }
         }
     }
-    for (int it = it0; it < it1; ++it) {
-        const uint32_t word = items[it];
-        const int j = (int)(word & 0xFF);
-        const int fslot = (int)(word >> 16);
-        const int slot = slot_rows[(it - it0) * NB + i];
-        Real Kb[NC_MAX * NC_MAX];
-        Real fe[NC_MAX];
-        #pragma unroll
-        for (int t = 0; t < NC_MAX * NC_MAX; ++t) Kb[t] = Real(0);
-        #pragma unroll
-        for (int t = 0; t < NC_MAX; ++t) fe[t] = Real(0);
-        if constexpr (PHYS == PHYS_HEAT || PHYS == PHYS_ELASTIC) {
-            P G[DIM][DIM];
-            #pragma unroll
-            for (int x = 0; x < DIM; ++x)
-                #pragma unroll
-                for (int y = 0; y < DIM; ++y) G[x][y] = pzero<P>();
-            #pragma unroll
-            for (int p = 0; p < NQP; ++p) {
-                P ri[3], rj[3];
-                #pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    if constexpr (CACHE) ri[c] = gi[p][c];
-                    else ri[c] = *(const P*)(grad + p * CT::SP + i * 6 + 2 * c);
-                    rj[c] = *(const P*)(grad + p * CT::SP + j * 6 + 2 * c);
-                }
-                if constexpr (PHYS == PHYS_HEAT) {
-                    #pragma unroll
-                    for (int x = 0; x < DIM; ++x) G[0][0] = pfma(ri[x], rj[x], G[0][0]);
-                } else {
-                    #pragma unroll
-                    for (int x = 0; x < DIM; ++x)
-                        #pragma unroll
-                        for (int y = 0; y < DIM; ++y) G[x][y] = pfma(ri[x], rj[y], G[x][y]);
-                }
-            }
-            if constexpr (PHYS == PHYS_HEAT) {
-                Kb[0] = cellp[0] * (G[0][0].x + G[0][0].y);
-                fe[0] = cellp[1] * Fi;
-            } else {
-                Real g[DIM][DIM];
-                #pragma unroll
-                for (int x = 0; x < DIM; ++x)
-                    #pragma unroll
-                    for (int y = 0; y < DIM; ++y) g[x][y] = G[x][y].x + G[x][y].y;
-                const Real lam = cellp[0], mu = cellp[1];
-                Real tr = 0;
-                #pragma unroll
-                for (int x = 0; x < DIM; ++x) tr += g[x][x];
-                #pragma unroll
-                for (int x = 0; x < DIM; ++x)
-                    #pragma unroll
-                    for (int y = 0; y < DIM; ++y) Kb[x * DIM + y] = lam * g[x][y] + mu * g[y][x] + (x == y ? mu * tr : Real(0));
-                #pragma unroll
-                for (int x = 0; x < DIM; ++x) fe[x] = Fi * (Real)a.phys.body[x];
-            }
-        } else {  // PHYS_NEO: per point, scalar
-            #pragma unroll 1
-            for (int q = 0; q < NQ; ++q) {
-                const int p = q >> 1, h = q & 1;
-                const Real* gio = grad + p * CT::SP + i * 6 + h;
-                const Real* gjo = grad + p * CT::SP + j * 6 + h;
-                const Real ai[3] = {gio[0], gio[2], gio[4]}, aj[3] = {gjo[0], gjo[2], gjo[4]};
-                const Real s = sq[q];
-                const Real nj = shp[q * SQL.qs + SQL.n + j] * s;
-                const Real* nq_ = neo + q * NEO_EXTRA;
-                Real Bi[3], Bj[3], tij = 0;
-                #pragma unroll
-                for (int x = 0; x < 3; ++x) {
-                    Bi[x] = nq_[9 + x * 3] * ai[0] + nq_[9 + x * 3 + 1] * ai[1] + nq_[9 + x * 3 + 2] * ai[2];
-                    Bj[x] = nq_[9 + x * 3] * aj[0] + nq_[9 + x * 3 + 1] * aj[1] + nq_[9 + x * 3 + 2] * aj[2];
-                    tij += ai[x] * (nq_[x * 3] * aj[0] + nq_[x * 3 + 1] * aj[1] + nq_[x * 3 + 2] * aj[2]);
-                }
-                const Real c1 = nq_[18], c2x2 = nq_[19];
-                // K_ab += delta_ab giT.T.gj + c1 (B gi)_b (B gj)_a + 2c2 (B gi)_a (B gj)_b
-                #pragma unroll
-                for (int x = 0; x < 3; ++x)
-                    #pragma unroll
-                    for (int y = 0; y < 3; ++y)
-                        Kb[x * 3 + y] += (x == y ? tij : Real(0)) + c1 * Bi[y] * Bj[x] + c2x2 * Bi[x] * Bj[y];
-                // residual: (gradN_j : P - N_j b) dV
-                #pragma unroll
-                for (int x = 0; x < 3; ++x)
-                    fe[x] += s * (nq_[20 + x * 3] * aj[0] + nq_[20 + x * 3 + 1] * aj[1] + nq_[20 + x * 3 + 2] * aj[2] -
-                                  nj * (Real)a.phys.body[x]);
-            }
-        }
-        // the plan gives every (item, row) its own staging slot: no two lanes write the same one
+    // the plan gives every (item, row) its own staging slot: no two lanes write the same one
+    auto store_block = [&](int j, int fslot, int slot, const Real* Kb, const Real* fe) {
         if (a.do_k) {
             if (slot == SLOT_MISS) {
                 #pragma unroll
@@ -652,6 +568,124 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
             #pragma unroll
             for (int x = 0; x < NC_MAX; ++x)
                 if (x < nc) dst[x] = fe[x];
+        }
+    };
+    if constexpr (PHYS == PHYS_HEAT || PHYS == PHYS_ELASTIC) {
+        // M items at a time: their FFMA2 chains are independent, so one lane keeps more
+        // instructions in flight
+        auto items_m = [&](auto Mc, int it) {
+            constexpr int M = decltype(Mc)::value;
+            int jm[M], fsm[M], slm[M];
+            #pragma unroll
+            for (int m = 0; m < M; ++m) {
+                const uint32_t word = items[it + m];
+                jm[m] = (int)(word & 0xFF);
+                fsm[m] = (int)(word >> 16);
+                slm[m] = slot_rows[(it + m - it0) * NB + i];
+            }
+            P G[M][DIM][DIM];
+            #pragma unroll
+            for (int m = 0; m < M; ++m)
+                #pragma unroll
+                for (int x = 0; x < DIM; ++x)
+                    #pragma unroll
+                    for (int y = 0; y < DIM; ++y) G[m][x][y] = pzero<P>();
+            #pragma unroll
+            for (int p = 0; p < NQP; ++p) {
+                P ri[3], rj[M][3];
+                #pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    if constexpr (CACHE) ri[c] = gi[p][c];
+                    else ri[c] = *(const P*)(grad + p * CT::SP + i * 6 + 2 * c);
+                    #pragma unroll
+                    for (int m = 0; m < M; ++m) rj[m][c] = *(const P*)(grad + p * CT::SP + jm[m] * 6 + 2 * c);
+                }
+                #pragma unroll
+                for (int m = 0; m < M; ++m) {
+                    if constexpr (PHYS == PHYS_HEAT) {
+                        #pragma unroll
+                        for (int x = 0; x < DIM; ++x) G[m][0][0] = pfma(ri[x], rj[m][x], G[m][0][0]);
+                    } else {
+                        #pragma unroll
+                        for (int x = 0; x < DIM; ++x)
+                            #pragma unroll
+                            for (int y = 0; y < DIM; ++y) G[m][x][y] = pfma(ri[x], rj[m][y], G[m][x][y]);
+                    }
+                }
+            }
+            #pragma unroll
+            for (int m = 0; m < M; ++m) {
+                Real Kb[NC_MAX * NC_MAX];
+                Real fe[NC_MAX];
+                if constexpr (PHYS == PHYS_HEAT) {
+                    Kb[0] = cellp[0] * (G[m][0][0].x + G[m][0][0].y);
+                    fe[0] = cellp[1] * Fi;
+                } else {
+                    Real g[DIM][DIM];
+                    #pragma unroll
+                    for (int x = 0; x < DIM; ++x)
+                        #pragma unroll
+                        for (int y = 0; y < DIM; ++y) g[x][y] = G[m][x][y].x + G[m][x][y].y;
+                    const Real lam = cellp[0], mu = cellp[1];
+                    Real tr = 0;
+                    #pragma unroll
+                    for (int x = 0; x < DIM; ++x) tr += g[x][x];
+                    #pragma unroll
+                    for (int x = 0; x < DIM; ++x)
+                        #pragma unroll
+                        for (int y = 0; y < DIM; ++y) Kb[x * DIM + y] = lam * g[x][y] + mu * g[y][x] + (x == y ? mu * tr : Real(0));
+                    #pragma unroll
+                    for (int x = 0; x < DIM; ++x) fe[x] = Fi * (Real)a.phys.body[x];
+                }
+                store_block(jm[m], fsm[m], slm[m], Kb, fe);
+            }
+        };
+        int it = it0;
+        if constexpr (sizeof(Real) == 4)  // FP64 keeps one item at a time (registers)
+            for (; it + 1 < it1; it += 2) items_m(std::integral_constant<int, 2>{}, it);
+        for (; it < it1; ++it) items_m(std::integral_constant<int, 1>{}, it);
+    } else {  // PHYS_NEO: per item and point, scalar
+        for (int it = it0; it < it1; ++it) {
+            const uint32_t word = items[it];
+            const int j = (int)(word & 0xFF);
+            const int fslot = (int)(word >> 16);
+            const int slot = slot_rows[(it - it0) * NB + i];
+            Real Kb[NC_MAX * NC_MAX];
+            Real fe[NC_MAX];
+            #pragma unroll
+            for (int t = 0; t < NC_MAX * NC_MAX; ++t) Kb[t] = Real(0);
+            #pragma unroll
+            for (int t = 0; t < NC_MAX; ++t) fe[t] = Real(0);
+            #pragma unroll 1
+            for (int q = 0; q < NQ; ++q) {
+                const int p = q >> 1, h = q & 1;
+                const Real* gio = grad + p * CT::SP + i * 6 + h;
+                const Real* gjo = grad + p * CT::SP + j * 6 + h;
+                const Real ai[3] = {gio[0], gio[2], gio[4]}, aj[3] = {gjo[0], gjo[2], gjo[4]};
+                const Real s = sq[q];
+                const Real nj = shp[q * SQL.qs + SQL.n + j] * s;
+                const Real* nq_ = neo + q * NEO_EXTRA;
+                Real Bi[3], Bj[3], tij = 0;
+                #pragma unroll
+                for (int x = 0; x < 3; ++x) {
+                    Bi[x] = nq_[9 + x * 3] * ai[0] + nq_[9 + x * 3 + 1] * ai[1] + nq_[9 + x * 3 + 2] * ai[2];
+                    Bj[x] = nq_[9 + x * 3] * aj[0] + nq_[9 + x * 3 + 1] * aj[1] + nq_[9 + x * 3 + 2] * aj[2];
+                    tij += ai[x] * (nq_[x * 3] * aj[0] + nq_[x * 3 + 1] * aj[1] + nq_[x * 3 + 2] * aj[2]);
+                }
+                const Real c1 = nq_[18], c2x2 = nq_[19];
+                // K_ab += delta_ab giT.T.gj + c1 (B gi)_b (B gj)_a + 2c2 (B gi)_a (B gj)_b
+                #pragma unroll
+                for (int x = 0; x < 3; ++x)
+                    #pragma unroll
+                    for (int y = 0; y < 3; ++y)
+                        Kb[x * 3 + y] += (x == y ? tij : Real(0)) + c1 * Bi[y] * Bj[x] + c2x2 * Bi[x] * Bj[y];
+                // residual: (gradN_j : P - N_j b) dV
+                #pragma unroll
+                for (int x = 0; x < 3; ++x)
+                    fe[x] += s * (nq_[20 + x * 3] * aj[0] + nq_[20 + x * 3 + 1] * aj[1] + nq_[20 + x * 3 + 2] * aj[2] -
+                                  nj * (Real)a.phys.body[x]);
+            }
+            store_block(j, fslot, slot, Kb, fe);
         }
     }
 }
@@ -840,6 +874,7 @@ __device__ __forceinline__ void reduce_tile(const KernelArgs& a, const char* R, 
                     float2 acc[NP];
                     #pragma unroll
                     for (int t = 0; t < NP; ++t) acc[t] = make_float2(0.f, 0.f);
+                    #pragma unroll 4
                     for (int k = 0; k < cnt; ++k) {
                         const float2* v = (const float2*)(stage + (s0 + k * ds) * BS);
                         #pragma unroll
