@@ -813,7 +813,7 @@ __device__ __forceinline__ void reduce_tile(const KernelArgs& a, const char* R, 
     for (int p = 0; p < n_pass; ++p) {
         const RecPass P = passes[p];
         if (p > 0) {  // the previous pass's copies still read the buffer
-            if (threadIdx.x == 0) bulk_wait_read();
+            bulk_wait_read();
             __syncthreads();
         }
         const int end = P.red_end + (p + 1 == n_pass ? nf : 0);
@@ -921,20 +921,16 @@ __device__ __forceinline__ void reduce_tile(const KernelArgs& a, const char* R, 
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // buffer writes -> bulk copies
         __syncthreads();
         if (bulk) {
-            // the ends of each range with plain stores, the aligned middle with one bulk store
+            // one thread per range (the last threads of the CTA, which hold the fewest blocks):
+            // the ends with plain stores, the aligned middle with one bulk store of its own group
             const int nrg = P.rng_end - P.rng_begin;
-            for (int q = threadIdx.x; q < 2 * nrg; q += THREADS) {
-                const RecRng g = rngs[P.rng_begin + (q >> 1)];
-                const int64_t z = (q & 1) ? g.nz0 + g.len - 1 : g.nz0;
-                const bool lone = (q & 1) ? ((g.nz0 + g.len) & 1) != 0 : (g.nz0 & 1) != 0;
-                if (lone) __stcs(a.nzval + z, outb[g.buf_off + (z - g.nz0)]);
-            }
-            if (threadIdx.x == 0) {
-                for (int gi = P.rng_begin; gi < P.rng_end; ++gi) {
-                    const RecRng g = rngs[gi];
-                    const int64_t a0 = g.nz0 + (g.nz0 & 1), a1 = (g.nz0 + g.len) & ~(int64_t)1;
-                    if (a1 > a0) bulk_store(a.nzval + a0, outb_s + (uint32_t)(g.buf_off + (a0 - g.nz0)) * 8u, (int)(a1 - a0) * 8);
-                }
+            for (int q = THREADS - 1 - (int)threadIdx.x; q < nrg; q += THREADS) {
+                const RecRng g = rngs[P.rng_begin + q];
+                const int64_t e = g.nz0 + g.len;
+                if (g.nz0 & 1) __stcs(a.nzval + g.nz0, outb[g.buf_off]);
+                if (e & 1) __stcs(a.nzval + e - 1, outb[g.buf_off + g.len - 1]);  // never the head element
+                const int64_t a0 = g.nz0 + (g.nz0 & 1), a1 = e & ~(int64_t)1;
+                if (a1 > a0) bulk_store(a.nzval + a0, outb_s + (uint32_t)(g.buf_off + (a0 - g.nz0)) * 8u, (int)(a1 - a0) * 8);
                 bulk_commit();
             }
         } else {
@@ -945,8 +941,9 @@ __device__ __forceinline__ void reduce_tile(const KernelArgs& a, const char* R, 
             if (p + 1 < n_pass) __syncthreads();
         }
     }
-    // the next tile writes its cell tables over the buffer
-    if (threadIdx.x == 0) bulk_wait_read();
+    // the next tile writes its cell tables over the buffer: each issuing thread waits until its
+    // bulk stores have read it (the CTA barrier of the next tile orders the rest)
+    bulk_wait_read();
 }
 
 // ---------------------------------------------------------------------------------------
@@ -1084,7 +1081,7 @@ __global__ void __launch_bounds__(THREADS, 2) tile_kernel(const KernelArgs a, co
         else if (a.nc == 2) reduce_tile<2, Real>(a, R, stage, (double*)chunk);
         else reduce_tile<1, Real>(a, R, stage, (double*)chunk);
     }
-    if (tid == 0) bulk_wait_all();  // this CTA's output stores have completed
+    bulk_wait_all();  // this CTA's output stores have completed
     if (t < a.n_tiles) {
         // a copy was lost: report it, and wait (bounded) for this CTA's copies still in
         // flight before its shared memory is released
