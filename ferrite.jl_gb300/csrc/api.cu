@@ -541,6 +541,11 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
         ph.mu = E / (2 * (1 + nu));
     }
     ph.cond_threshold = p->cond_threshold > 0 ? (float)p->cond_threshold : 64.0f;
+    ph.p0_f = (float)ph.p0;
+    ph.p1_f = (float)ph.p1;
+    ph.lam_f = (float)ph.lam;
+    ph.mu_f = (float)ph.mu;
+    for (int x = 0; x < 3; ++x) ph.body_f[x] = (float)ph.body[x];
     auto stage_input = [&](const double* src, int64_t n, double** stage, float** stage_f, const double** out_d,
                            const float** out_f) -> int {
         const double* dsrc = src;
@@ -1082,6 +1087,11 @@ extern "C" int fe_assemble_noalloc(fe_handle* h, const fe_assemble_params* p, do
         ph.mu = E / (2 * (1 + nu));
     }
     ph.cond_threshold = p->cond_threshold > 0 ? (float)p->cond_threshold : 64.0f;
+    ph.p0_f = (float)ph.p0;
+    ph.p1_f = (float)ph.p1;
+    ph.lam_f = (float)ph.lam;
+    ph.mu_f = (float)ph.mu;
+    for (int x = 0; x < 3; ++x) ph.body_f[x] = (float)ph.body[x];
     // FP32 inputs in the static scratch: u first, then the per-cell factors. Both are fully
     // overwritten here, so nothing needs clearing between calls.
     int64_t off = 0;

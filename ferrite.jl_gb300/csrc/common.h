@@ -170,6 +170,8 @@ struct Physics {
     double p0, p1;           // as in fe_assemble_params
     double body[3];
     double lam, mu;          // elastic: Lame parameters from E, nu
+    // the same constants in FP32 (set by the host: the kernels convert nothing per cell)
+    float p0_f, p1_f, lam_f, mu_f, body_f[3];
     const float* scale_f;    // per Ferrite cell material factor (NULL = 1)
     const double* scale_d;
     const float* u_f;        // neo-hooke solution (float copy)

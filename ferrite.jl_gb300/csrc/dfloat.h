@@ -42,7 +42,17 @@ __host__ __device__ __forceinline__ double u2d(uint64_t u) {
 // Round hi + lo to the nearest double (ties to even). After a Fast2Sum the pair (s, e) has
 // |e| <= ulp(s)/2; the double of s is exact and e only touches the 29 mantissa bits below
 // s's FP32 precision, so the result is an integer add/subtract on the bit pattern.
-__host__ __device__ __forceinline__ double pair_to_double(float hi, float lo) {
+#ifdef __CUDA_ARCH__
+__device__ __noinline__ double pair_to_double(float hi, float lo);
+#endif
+// (kept out of line on the device: the rare paths of pair_to_double_fast call it, and a call
+// cannot be turned into predicated FP64 instructions on the common path)
+#ifdef __CUDA_ARCH__
+__device__ __noinline__
+#else
+__host__ __forceinline__
+#endif
+double pair_to_double(float hi, float lo) {
     const float s = hi + lo;
     const float e = lo - (s - hi);
     if (s == 0.0f) return 0.0;
@@ -111,15 +121,38 @@ __host__ __device__ __forceinline__ double pair_to_double_fast(float hi, float l
     return u2d(D);
 }
 
-// Exact FP32 -> FP64 with integer operations (no FP64 pipe) for normal numbers.
+__host__ __device__ __forceinline__ int clz32(uint32_t x) {  // x != 0
+#ifdef __CUDA_ARCH__
+    return __clz((int)x);
+#else
+    return __builtin_clz(x);
+#endif
+}
+
+// Exact FP32 -> FP64 with integer operations only (GB300's FP64 pipe, which also runs the
+// F2F conversion, issues at a small fraction of the integer rate). Every class is handled
+// without it: normal numbers by rebasing the exponent, zero and subnormals by normalising
+// the mantissa, infinities and NaNs (payload kept) by widening the field.
 __host__ __device__ __forceinline__ double float_to_double(float v) {
     const uint32_t b = f2u(v);
+    const uint32_t sign = b & 0x80000000u;
     const uint32_t mag = b & 0x7FFFFFFFu;
     const uint32_t ex = mag >> 23;
-    if (mag == 0u) return (b >> 31) ? -0.0 : 0.0;
-    if (ex == 0u || ex == 0xFFu) return (double)v;
-    const uint32_t dhi = (b & 0x80000000u) | ((mag >> 3) + (896u << 20));
-    return u2d(((uint64_t)dhi << 32) | (uint64_t)(mag << 29));
+    uint32_t hi = sign | ((mag >> 3) + (896u << 20));
+    uint32_t lo = mag << 29;
+    if (ex == 0u) {
+        hi = sign;
+        lo = 0u;
+        if (mag) {  // subnormal: mag * 2^-149 with the leading bit at position p
+            const int p = 31 - clz32(mag);
+            const uint64_t D = ((uint64_t)(p + 874) << 52) | (((uint64_t)mag << (52 - p)) & 0xFFFFFFFFFFFFFull);
+            hi = sign | (uint32_t)(D >> 32);
+            lo = (uint32_t)D;
+        }
+    } else if (ex == 0xFFu) {
+        hi = sign | 0x7FF00000u | ((mag & 0x7FFFFFu) >> 3);
+    }
+    return u2d(((uint64_t)hi << 32) | lo);
 }
 
 }  // namespace fe

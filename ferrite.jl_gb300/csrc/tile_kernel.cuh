@@ -226,6 +226,11 @@ __host__ __device__ inline SmemLayout smem_layout(const KernelArgs& a, int shape
     return L;
 }
 
+// a physics constant in the kernel's precision: the host's FP32 copy, or the FP64 value
+template <typename Real> __device__ __forceinline__ Real pconst(double d, float f);
+template <> __device__ __forceinline__ float pconst<float>(double, float f) { return f; }
+template <> __device__ __forceinline__ double pconst<double>(double d, float) { return d; }
+
 template <typename Real> struct Pair;
 template <> struct Pair<float> { using type = float2; };
 template <> struct Pair<double> { using type = double2; };
@@ -481,18 +486,19 @@ __device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev
             else scale = a.phys.scale_d[sd.cellid[cell]];
         }
         if constexpr (PHYS == PHYS_ELASTIC) {
-            cellp[0] = (Real)a.phys.lam * scale;
-            cellp[1] = (Real)a.phys.mu * scale;
+            cellp[0] = pconst<Real>(a.phys.lam, a.phys.lam_f) * scale;
+            cellp[1] = pconst<Real>(a.phys.mu, a.phys.mu_f) * scale;
         } else {
-            cellp[0] = (Real)a.phys.p0 * scale;
-            cellp[1] = (Real)a.phys.p1;
+            cellp[0] = pconst<Real>(a.phys.p0, a.phys.p0_f) * scale;
+            cellp[1] = pconst<Real>(a.phys.p1, a.phys.p1_f);
         }
     }
     if constexpr (PHYS == PHYS_NEO) {
         const Real is = s > Real(0) ? Real(1) / s : Real(0);
         #pragma unroll
         for (int t = 0; t < 9; ++t) H[t] *= is;
-        neo_hooke_point<Real>((Real)a.phys.p0, (Real)a.phys.p1, H, neo + q * NEO_EXTRA);
+        neo_hooke_point<Real>(pconst<Real>(a.phys.p0, a.phys.p0_f), pconst<Real>(a.phys.p1, a.phys.p1_f), H,
+                              neo + q * NEO_EXTRA);
     }
 }
 
@@ -635,7 +641,7 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
                         #pragma unroll
                         for (int y = 0; y < DIM; ++y) Kb[x * DIM + y] = lam * g[x][y] + mu * g[y][x] + (x == y ? mu * tr : Real(0));
                     #pragma unroll
-                    for (int x = 0; x < DIM; ++x) fe[x] = Fi * (Real)a.phys.body[x];
+                    for (int x = 0; x < DIM; ++x) fe[x] = Fi * pconst<Real>(a.phys.body[x], a.phys.body_f[x]);
                 }
                 store_block(jm[m], fsm[m], slm[m], Kb, fe);
             }
@@ -683,7 +689,7 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
                 #pragma unroll
                 for (int x = 0; x < 3; ++x)
                     fe[x] += s * (nq_[20 + x * 3] * aj[0] + nq_[20 + x * 3 + 1] * aj[1] + nq_[20 + x * 3 + 2] * aj[2] -
-                                  nj * (Real)a.phys.body[x]);
+                                  nj * pconst<Real>(a.phys.body[x], a.phys.body_f[x]));
             }
             store_block(j, fslot, slot, Kb, fe);
         }

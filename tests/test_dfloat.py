@@ -43,6 +43,18 @@ int main() {
         const double w = (double)v, z = fe::float_to_double(v);
         if (std::memcmp(&w, &z, 8) != 0) { ++bad; if (bad < 5) std::printf("f2d %a\n", v); }
     }
+    // every exponent field (zero, subnormal, normal, inf, quiet NaN) with random mantissas
+    for (uint32_t e = 0; e < 256; ++e)
+        for (int k = 0; k < 4000; ++k) {
+            uint32_t m = (uint32_t)(g() & 0x7FFFFF);
+            if (k == 0) m = 0;
+            if (e == 255 && m) m |= 0x400000;  // quiet NaNs (the integer path keeps payloads exactly)
+            const uint32_t bits = ((uint32_t)(g() & 1) << 31) | (e << 23) | m;
+            float v;
+            std::memcpy(&v, &bits, 4);
+            const double w = (double)v, z = fe::float_to_double(v);
+            if (std::memcmp(&w, &z, 8) != 0) { ++bad; if (bad < 10) std::printf("f2d bits %08x\n", bits); }
+        }
     std::printf("%ld %ld\n", bad, n);
     return bad != 0;
 }
