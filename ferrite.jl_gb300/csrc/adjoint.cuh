@@ -31,6 +31,7 @@ struct AdjArgs {
     const double* dscale;    // per Ferrite cell ds/drho (NULL = 1)
     double m0, m1;           // unscaled material: heat k; elastic Lame lambda, mu
     double load[3];          // elastic body force; heat: load[0] = source
+    float m0_f, m1_f, load_f[3];  // the same in FP32 (no per-point conversions)
     double* d_cell;          // [n_cells], by Ferrite cell id
     void* contrib;           // Real [rows][DIM]: per (cell, geometric node)
     int64_t row0;            // first contribution row of this subdomain
@@ -145,12 +146,15 @@ __global__ void __launch_bounds__(THREADS) adjoint_kernel(const AdjArgs a, const
             Real Su[NC * DIM], Sl[NC * DIM];
             if constexpr (PHYS == PHYS_HEAT) {
                 #pragma unroll
-                for (int d = 0; d < DIM; ++d) { Su[d] = (Real)a.m0 * Gu[d]; Sl[d] = (Real)a.m0 * Gl[d]; }
+                for (int d = 0; d < DIM; ++d) {
+                    Su[d] = pconst<Real>(a.m0, a.m0_f) * Gu[d];
+                    Sl[d] = pconst<Real>(a.m0, a.m0_f) * Gl[d];
+                }
             } else {
                 Real tu = 0, tl = 0;
                 #pragma unroll
                 for (int d = 0; d < DIM; ++d) { tu += Gu[d * DIM + d]; tl += Gl[d * DIM + d]; }
-                const Real lam = (Real)a.m0, mu = (Real)a.m1;
+                const Real lam = pconst<Real>(a.m0, a.m0_f), mu = pconst<Real>(a.m1, a.m1_f);
                 #pragma unroll
                 for (int x = 0; x < DIM; ++x)
                     #pragma unroll
@@ -169,7 +173,7 @@ __global__ void __launch_bounds__(THREADS) adjoint_kernel(const AdjArgs a, const
             }
             Real fl = 0;
             #pragma unroll
-            for (int m = 0; m < NC; ++m) fl += lq[m] * (Real)a.load[m];
+            for (int m = 0; m < NC; ++m) fl += lq[m] * pconst<Real>(a.load[m], a.load_f[m]);
             Real Sg[DIM * DIM];
             #pragma unroll
             for (int b = 0; b < DIM; ++b)

@@ -361,6 +361,7 @@ int fe_create(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain
                 for (int t = 0; t < hs.nb * hs.dim; ++t) r[L.dn + t] = (T)hs.dN[(size_t)q * hs.nb * hs.dim + t];
                 for (int t = 0; t < hs.nb; ++t) r[L.n + t] = (T)hs.N[(size_t)q * hs.nb + t];
                 r[L.w] = (T)hs.w[q];
+                r[L.w + 1] = (T)std::sqrt(hs.w[q]);
             }
         };
         offs_f[s] = (int)(shf.size() * sizeof(float));
@@ -683,6 +684,9 @@ int fe_assemble_adjoint(fe_handle* h, const fe_adjoint_params* p, const double* 
         A.m1 = E / (2 * (1 + nu));
         for (int x = 0; x < 3; ++x) A.load[x] = p->body[x];
     }
+    A.m0_f = (float)A.m0;
+    A.m1_f = (float)A.m1;
+    for (int x = 0; x < 3; ++x) A.load_f[x] = (float)A.load[x];
     // outputs
     const bool rho_dev = is_device_ptr(d_rho), x_dev = d_X && is_device_ptr(d_X);
     double* drho = d_rho;

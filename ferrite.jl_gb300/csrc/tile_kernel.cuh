@@ -101,6 +101,17 @@ template <typename R> struct Mat<R, 3> {
     static __device__ __forceinline__ R det(const R* J) {
         return J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) + J[2] * (J[3] * J[7] - J[4] * J[6]);
     }
+    static __device__ __forceinline__ void adj(const R* J, R* A) {  // J^-1 = A / det
+        A[0] = J[4] * J[8] - J[5] * J[7];
+        A[1] = -(J[1] * J[8] - J[2] * J[7]);
+        A[2] = J[1] * J[5] - J[2] * J[4];
+        A[3] = -(J[3] * J[8] - J[5] * J[6]);
+        A[4] = J[0] * J[8] - J[2] * J[6];
+        A[5] = -(J[0] * J[5] - J[2] * J[3]);
+        A[6] = J[3] * J[7] - J[4] * J[6];
+        A[7] = -(J[0] * J[7] - J[1] * J[6]);
+        A[8] = J[0] * J[4] - J[1] * J[3];
+    }
     static __device__ __forceinline__ void inv(const R* J, R dt, R* Ji) {
         const R id = R(1) / dt;
         Ji[0] = (J[4] * J[8] - J[5] * J[7]) * id;
@@ -116,6 +127,10 @@ template <typename R> struct Mat<R, 3> {
 };
 template <typename R> struct Mat<R, 2> {
     static __device__ __forceinline__ R det(const R* J) { return J[0] * J[3] - J[1] * J[2]; }
+    static __device__ __forceinline__ void adj(const R* J, R* A) {  // J^-1 = A / det
+        A[0] = J[3]; A[1] = -J[1];
+        A[2] = -J[2]; A[3] = J[0];
+    }
     static __device__ __forceinline__ void inv(const R* J, R dt, R* Ji) {
         const R id = R(1) / dt;
         Ji[0] = J[3] * id; Ji[1] = -J[1] * id;
@@ -245,7 +260,7 @@ template <> __device__ __forceinline__ float2 pzero<float2>() { return make_floa
 template <> __device__ __forceinline__ double2 pzero<double2>() { return make_double2(0.0, 0.0); }
 
 // Reference tables in shared memory, one record per quadrature point q (element offsets):
-//   dM[NG][DIM] at dm, dN[NB][DIM] at dn, N[NB] at n, w at w; every section starts on 16
+//   dM[NG][DIM] at dm, dN[NB][DIM] at dn, N[NB] at n, w and sqrt(w) at w; every section starts on 16
 //   bytes and the record stride qs is an odd multiple of 16 bytes, so the 8 lanes of a quarter
 //   warp (lane = q) read their records with conflict-free 16-byte loads.
 struct ShapeQ {
@@ -394,16 +409,20 @@ __device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev
                 for (int b = 0; b < DIM; ++b) J[x * DIM + b] += off[k][x] * dm[k * DIM + b];
     }
     Real dt = Mat<Real, DIM>::det(J);
-    Real Ji[DIM * DIM];
     bool bad = !(dt > Real(0));
-    if (!bad) Mat<Real, DIM>::inv(J, dt, Ji);
+    // Ji = J^-1 scaled by s = sqrt(detJ w); every gradient below is then a plain product
+    Real Ji[DIM * DIM];
+    Real s;
     if constexpr (sizeof(Real) == 4) {
-        float nJ = 0, nJi = 0;
-        if (!bad) {
-            #pragma unroll
-            for (int t = 0; t < DIM * DIM; ++t) { nJ += J[t] * J[t]; nJi += Ji[t] * Ji[t]; }
-        }
-        if (bad || nJ * nJi > a.phys.cond_threshold * a.phys.cond_threshold * DIM * DIM) {
+        // J^-1 s = adj(J) sqrt(w) / sqrt(detJ): one reciprocal square root, no division
+        Real A[DIM * DIM];
+        Mat<Real, DIM>::adj(J, A);
+        float nJ = 0, nA = 0;
+        #pragma unroll
+        for (int t = 0; t < DIM * DIM; ++t) { nJ += J[t] * J[t]; nA += A[t] * A[t]; }
+        // Frobenius condition estimate |J| |J^-1| = sqrt(nJ nA) / detJ against the threshold
+        const float thr = a.phys.cond_threshold * (float)DIM;
+        if (bad || nJ * nA > thr * thr * dt * dt) {
             double Jd[DIM * DIM], Jid[DIM * DIM];
             #pragma unroll
             for (int t = 0; t < DIM * DIM; ++t) Jd[t] = 0.0;
@@ -420,18 +439,32 @@ __device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev
             }
             const double dtd = Mat<double, DIM>::det(Jd);
             bad = !(dtd > 0.0);
+            s = 0.f;
             if (!bad) {
                 Mat<double, DIM>::inv(Jd, dtd, Jid);
+                const double sd_ = sqrt(dtd * sd.w_d[q]);
                 #pragma unroll
-                for (int t = 0; t < DIM * DIM; ++t) Ji[t] = (float)Jid[t];
+                for (int t = 0; t < DIM * DIM; ++t) Ji[t] = (float)(Jid[t] * sd_);
+                s = (float)sd_;
             }
             dt = (float)dtd;
             if (q == 0) atomicAdd(&a.status->flagged, 1u);
+        } else {
+            const float r = rsqrtf(dt);
+            const float sc = Q[SQL.w + 1] * r;  // sqrt(w) / sqrt(detJ)
+            #pragma unroll
+            for (int t = 0; t < DIM * DIM; ++t) Ji[t] = A[t] * sc;
+            s = dt * sc;
         }
+    } else {
+        if (!bad) Mat<Real, DIM>::inv(J, dt, Ji);
+        s = bad ? Real(0) : sqrt(dt * Q[SQL.w]);
+        #pragma unroll
+        for (int t = 0; t < DIM * DIM; ++t) Ji[t] *= s;
     }
     if (bad) {
         record_detj(a.status, sd.cellid[cell], (float)dt);
-        dt = Real(0);
+        s = Real(0);
         #pragma unroll
         for (int t = 0; t < DIM * DIM; ++t) Ji[t] = Real(0);
     }
@@ -439,10 +472,6 @@ __device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev
     constexpr bool DN_REG = NB * DIM <= 32;
     Real dN[DN_REG ? round_up(NB * DIM, V) : 1];
     if constexpr (DN_REG) lds16<Real, round_up(NB * DIM, V)>(Q + SQL.dn, dN);
-    const Real s = sqrt(dt * Q[SQL.w]);
-    // scale J^-1 by sqrt(detJ w) once: every gradient below is then a plain product
-    #pragma unroll
-    for (int t = 0; t < DIM * DIM; ++t) Ji[t] *= s;
     const int p = q >> 1, hh = q & 1;
     const bool pad = (NQ & 1) && q == NQ - 1;
     sq[2 * p + hh] = s;
@@ -516,7 +545,9 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
     constexpr ShapeQ SQL = shape_q(NB, NG, DIM, (int)sizeof(Real));
     constexpr int NC_MAX = DIM;
     constexpr bool CACHE = NQP <= 4;  // keep the row function's table in registers
-    const int nc = a.nc;
+    // components per entity and staging stride, fixed by the physics (the host checks a.nc)
+    constexpr int nc = PHYS == PHYS_HEAT ? 1 : DIM;
+    constexpr int BSC = (nc * nc + 1) & ~1;
     const Real* grad = tb;
     const Real* sq = tb + CT::GRAD;
     const Real* cellp = sq + CT::SQ;
@@ -551,7 +582,7 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
                         if (x < nc && y < nc && Kb[x * NC_MAX + y] != Real(0))
                             record_miss(a.status, sd.cellid[cell], i * nc + x, j * nc + y);
             } else {
-                Real* dst = stage + slot * a.bs;
+                Real* dst = stage + slot * BSC;
                 if (nc == 1) {
                     dst[0] = Kb[0];
                 } else {
