@@ -97,6 +97,10 @@ struct fe_handle {
     double create_seconds = 0;
     int device = 0;
     int32_t stage_cap = 0;  // staging values per tile the current plan was built with
+    int max_smem = 0, n_sm = 0;      // device attributes (read once)
+    const void* occ_fn = nullptr;    // occupancy of the last launch configuration
+    int occ_smem = -1, occ_per_sm = 1;
+    int accumulate_status = 0;       // a pending FE_ASYNC assembly's status is still being collected
 
     template <typename T>
     cudaError_t alloc(T** p, size_t count) {
@@ -161,6 +165,7 @@ int finish_status(fe_handle* h) {
     const DevStatus& st = *h->status_h;
     h->flagged = st.flagged;
     h->pending = 0;
+    h->accumulate_status = 0;
     if (st.timeout) return set_error(h, FE_ERR_CUDA, "a tile gave up: table copy timed out or shared memory too small");
     if (st.detj_key != ~0ull) {
         const int64_t cell = (int64_t)(st.detj_key >> 32) + 1;
@@ -211,6 +216,24 @@ cudaError_t install_plan(fe_handle* h) {
     return cudaSuccess;
 }
 
+// The dynamic shared-memory limit is a per-kernel, process-wide attribute: raise it when a
+// launch needs more than any earlier one (never lower it under another handle's launches).
+cudaError_t ensure_smem_attribute(const void* fn, int smem) {
+    static std::mutex mu;
+    static std::vector<std::pair<const void*, int>> set;
+    std::lock_guard<std::mutex> lock(mu);
+    for (auto& x : set)
+        if (x.first == fn) {
+            if (x.second >= smem) return cudaSuccess;
+            const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e == cudaSuccess) x.second = smem;
+            return e;
+        }
+    const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) set.push_back({fn, smem});
+    return e;
+}
+
 // Device status to "no error": keys all ones, counters zero (memsets, so it can be captured)
 cudaError_t status_reset(fe_handle* h, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(h->status_d, 0xFF, 2 * sizeof(unsigned long long), st);
@@ -225,9 +248,11 @@ int launch_assembly(fe_handle* h, const KernelEntry* ke, KernelArgs& A, bool fp6
     cudaError_t e;
     const int pi = fp64 ? 1 : 0;
     const int fixed = smem_layout(A, h->shape_bytes[pi], fp64 ? 8 : 4).chunk;
-    int max_smem = 0, n_sm = 0;
-    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
-    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, h->device);
+    if (!h->max_smem) {
+        cudaDeviceGetAttribute(&h->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+        cudaDeviceGetAttribute(&h->n_sm, cudaDevAttrMultiProcessorCount, h->device);
+    }
+    const int max_smem = h->max_smem, n_sm = h->n_sm;
     const int budget = max_smem - 1024;  // static shared (mbarriers) headroom
     // cell-table buffers: one per lane group; fewer groups when the tables are large
     int tb = 0;
@@ -241,13 +266,17 @@ int launch_assembly(fe_handle* h, const KernelEntry* ke, KernelArgs& A, bool fp6
     A.chunk_bytes = tb;
     const int smem = fixed + chunk_region_bytes(A);
     if (smem > budget) return set_error(h, FE_ERR_UNSUPPORTED, "tile does not fit in shared memory");
-    if ((e = cudaFuncSetAttribute(ke->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
-        return cuda_fail(h, e, "cudaFuncSetAttribute");
-    int per_sm = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ke->fn, THREADS, smem)) != cudaSuccess)
-        return cuda_fail(h, e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
-    const int64_t grid = std::min<int64_t>(A.n_tiles, (int64_t)std::max(per_sm, 1) * std::max(n_sm, 1));
-    if (!h->capturing && (e = status_reset(h, st)) != cudaSuccess) return cuda_fail(h, e, "status reset");
+    if ((e = ensure_smem_attribute(ke->fn, smem)) != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute");
+    if (ke->fn != h->occ_fn || smem != h->occ_smem) {
+        int per_sm = 0;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ke->fn, THREADS, smem)) != cudaSuccess)
+            return cuda_fail(h, e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+        h->occ_fn = ke->fn;
+        h->occ_smem = smem;
+        h->occ_per_sm = std::max(per_sm, 1);
+    }
+    const int64_t grid = std::min<int64_t>(A.n_tiles, (int64_t)h->occ_per_sm * std::max(n_sm, 1));
+    if (!h->capturing && !h->accumulate_status && (e = status_reset(h, st)) != cudaSuccess) return cuda_fail(h, e, "status reset");
     A.status = h->status_d;
     const void* shp = fp64 ? (const void*)h->shape_d : (const void*)h->shape_f;
     int sb = h->shape_bytes[pi], o1 = h->shape_off1[pi], o2 = h->shape_off2[pi];
@@ -488,8 +517,17 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
             (p->cell_scale && !is_device_ptr(p->cell_scale)))
             return set_error(h, FE_ERR_STATE, "capture: nzval, f, u and cell_scale must be device memory");
     } else if (h->pending) {
-        int rc = fe_sync(h);
-        (void)rc;
+        // An FE_ASYNC assembly on the same stream with device outputs is still running: keep
+        // its status and let this one add to it (fe_sync reports both), without waiting.
+        // Anything else waits for it first.
+        const bool chain = (cudaStream_t)p->stream == h->last_stream && (!do_k || is_device_ptr(nzval)) &&
+                           (!do_f || is_device_ptr(f));
+        if (chain) {
+            h->accumulate_status = 1;
+        } else {
+            int rc = fe_sync(h);
+            (void)rc;
+        }
     }
     // pick the kernel
     const KernelEntry* ke = nullptr;

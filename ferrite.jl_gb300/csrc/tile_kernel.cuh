@@ -677,10 +677,9 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
                 store_block(jm[m], fsm[m], slm[m], Kb, fe);
             }
         };
-        int it = it0;
-        if constexpr (sizeof(Real) == 4)  // FP64 keeps one item at a time (registers)
-            for (; it + 1 < it1; it += 2) items_m(std::integral_constant<int, 2>{}, it);
-        for (; it < it1; ++it) items_m(std::integral_constant<int, 1>{}, it);
+        // one item at a time (two interleaved items measured slower: more instructions, same
+        // registers)
+        for (int it = it0; it < it1; ++it) items_m(std::integral_constant<int, 1>{}, it);
     } else {  // PHYS_NEO: per item and point, scalar
         for (int it = it0; it < it1; ++it) {
             const uint32_t word = items[it];

@@ -171,6 +171,38 @@ def test_detj_error(built, oracle):
         assert ei.value.name == "DETJ" and ei.value.cell == 5 and ei.value.detJ < 0
 
 
+def test_async_chain_matches_sync_and_keeps_errors(built, oracle, torch_cuda):
+    """FE_ASYNC assemblies on one stream with device outputs run back to back without host
+    waits; their statuses accumulate, so an error of any of them is reported at fe_sync."""
+    torch = torch_cuda
+    fg, O = built, oracle
+    prob = O.box_problem(O.HEXAHEDRON, (6, 5, 4), ncomp=3, perturb=0.2, seed=6)
+    h = make_handle(fg, O, prob)
+    kw = dict(physics=fg.LINEAR_ELASTIC, p0=1.0, p1=0.3, body=(0.0, 0.0, -1.0))
+    nz0 = torch.zeros(prob.nnz, dtype=torch.float64, device="cuda")
+    f0 = torch.zeros(prob.ndofs, dtype=torch.float64, device="cuda")
+    h.assemble(nz0, f0, **kw)
+    nz = torch.zeros_like(nz0)
+    f = torch.zeros_like(f0)
+    s = torch.cuda.Stream()
+    for _ in range(4):
+        h.assemble(nz, f, stream=s, sync=False, **kw)
+    h.sync()
+    assert torch.equal(nz, nz0) and torch.equal(f, f0)
+    # an inverted cell in a chain: reported once the chain is synchronised
+    nodes, cells = O.generate_grid(O.QUADRILATERAL, (3, 3))
+    cells[4] = cells[4][[1, 0, 3, 2]]
+    bad = O.Problem.single(O.QUADRILATERAL, nodes, cells).close().allocate_matrix()
+    hb = make_handle(fg, O, bad)
+    nzb = torch.zeros(bad.nnz, dtype=torch.float64, device="cuda")
+    fb = torch.zeros(bad.ndofs, dtype=torch.float64, device="cuda")
+    for _ in range(3):
+        hb.assemble(nzb, fb, physics=fg.HEAT, p0=1.0, p1=1.0, stream=s, sync=False)
+    with pytest.raises(fg.FEError) as ei:
+        hb.sync()
+    assert ei.value.name == "DETJ" and ei.value.cell == 5
+
+
 def test_pattern_missing_error(built, oracle):
     fg, O = built, oracle
     prob = O.box_problem(O.QUADRILATERAL, (3, 3), qr_order=2)
