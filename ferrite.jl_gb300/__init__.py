@@ -97,7 +97,9 @@ class Info(ctypes.Structure):
     _fields_ = [("n_cells", ctypes.c_int64), ("ndofs", ctypes.c_int64), ("nnz", ctypes.c_int64),
                 ("n_tiles", ctypes.c_int64), ("n_cell_visits", ctypes.c_int64), ("n_items", ctypes.c_int64),
                 ("flagged_cells", ctypes.c_int64), ("device_bytes", ctypes.c_int64),
-                ("create_seconds", ctypes.c_double)]
+                ("create_seconds", ctypes.c_double), ("max_record_bytes", ctypes.c_int32),
+                ("max_tile_nodes", ctypes.c_int32), ("max_stage_values", ctypes.c_int32),
+                ("max_out_doubles", ctypes.c_int32), ("stage_cap", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
 _lib = None

@@ -98,6 +98,8 @@ struct fe_handle {
     int device = 0;
     int32_t stage_cap = 0;  // staging values per tile the current plan was built with
     int max_smem = 0, n_sm = 0;      // device attributes (read once)
+    const void* fitted_fn = nullptr;  // kernel the plan was last fitted to (fit_plan)
+    bool plan_pinned = false;         // staging capacity set by the caller or the autotuner
     const void* occ_fn = nullptr;    // occupancy of the last launch configuration
     int occ_smem = -1, occ_per_sm = 1;
     int accumulate_status = 0;       // a pending FE_ASYNC assembly's status is still being collected
@@ -190,6 +192,56 @@ int finish_status(fe_handle* h) {
     return FE_OK;
 }
 
+// Shared-memory caps of the kernel's layout from a plan's largest tile of each kind
+void set_plan_caps(KernelArgs& A, const Plan& pl) {
+    A.rec_cap = std::max(pl.max_rec, 64);
+    A.node_cap = std::max(pl.max_nodes, 1);
+    A.stage_cap = std::max(pl.max_stage, 2);
+    A.out_cap = std::max(pl.max_out, 2);
+}
+
+// The kernel compiled for this problem's subdomains, physics and precision (nullptr: none)
+const KernelEntry* find_kernel(const HostProblem& hp, int phys, bool fp64) {
+    for (const KernelEntry& e : registry()) {
+        if (e.phys != phys || e.fp64 != (int)fp64) continue;
+        bool ok = true;
+        for (int s = 0; s < MAX_SUB; ++s) {
+            if (s < (int)hp.subs.size()) {
+                if (e.kind[s] != hp.subs[s].kind || e.nq[s] != hp.subs[s].nq) ok = false;
+            } else if (e.kind[s] >= 0) {
+                ok = false;
+            }
+        }
+        if (ok) return &e;
+    }
+    return nullptr;
+}
+
+void device_attributes(fe_handle* h) {
+    if (h->max_smem) return;
+    cudaDeviceGetAttribute(&h->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+    cudaDeviceGetAttribute(&h->n_sm, cudaDevAttrMultiProcessorCount, h->device);
+}
+
+// Dynamic shared memory of one CTA of kernel ke with A's caps; sets A.groups (cell-table
+// buffers: one per lane group, fewer when the tables are large) and A.chunk_bytes.
+int tile_smem(fe_handle* h, const KernelEntry* ke, KernelArgs& A, bool fp64) {
+    const int pi = fp64 ? 1 : 0;
+    const int fixed = smem_layout(A, h->shape_bytes[pi], fp64 ? 8 : 4).chunk;
+    device_attributes(h);
+    const int budget = h->max_smem - 1024;  // static shared (mbarriers) headroom
+    int tb = 0;
+    for (int s = 0; s < MAX_SUB; ++s) {
+        A.groups[s] = 0;
+        if (ke->kind[s] < 0) continue;
+        const int room = (budget - fixed) / std::max(ke->table_bytes[s], 1);
+        A.groups[s] = std::max(1, std::min(ke->groups[s], room));
+        tb = std::max(tb, ke->table_bytes[s] * A.groups[s]);
+    }
+    A.chunk_bytes = tb;
+    return fixed + chunk_region_bytes(A);
+}
+
 // Upload h->plan's records (replacing the previous plan's device copy) and set the caps the
 // kernel's shared-memory layout is sized from. The host copy of the records is released.
 cudaError_t install_plan(fe_handle* h) {
@@ -209,10 +261,7 @@ cudaError_t install_plan(fe_handle* h) {
     A.rec_off = roff;
     std::vector<uint8_t>().swap(pl.rec);  // the device copy is the one in use
     A.n_tiles = (int32_t)pl.n_tiles;
-    A.rec_cap = std::max(pl.max_rec, 64);
-    A.node_cap = std::max(pl.max_nodes, 1);
-    A.stage_cap = std::max(pl.max_stage, 2);
-    A.out_cap = std::max(pl.max_out, 2);
+    set_plan_caps(A, pl);
     return cudaSuccess;
 }
 
@@ -241,31 +290,71 @@ cudaError_t status_reset(fe_handle* h, cudaStream_t st) {
     return e;
 }
 
+// Two CTAs per SM hide each other's record and coordinate waits. The plan's tiles are sized
+// from the staging capacity, but its largest record and node list follow from the mesh (on a
+// lattice-aligned mesh more tiles snap to their upper size), so kernel ke may land just past
+// the two-CTA line. Then re-plan with a slightly smaller capacity, once per kernel; a kernel
+// far past the line (more than a tenth) keeps the plan: smaller tiles would cost more visits
+// than the second CTA wins. Returns FE_OK or a CUDA failure of the upload.
+int fit_plan(fe_handle* h, const KernelEntry* ke, cudaStream_t st) {
+    h->fitted_fn = ke->fn;
+    KernelArgs A = h->base;
+    const int smem = tile_smem(h, ke, A, false);
+    if (smem > h->max_smem - 1024 || ensure_smem_attribute(ke->fn, smem) != cudaSuccess) return FE_OK;
+    int n = 0, n0 = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ke->fn, THREADS, smem) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n0, ke->fn, THREADS, 0) != cudaSuccess)
+        return FE_OK;
+    const int want = std::min(n0, 2);
+    if (n >= want) return FE_OK;
+    int per_sm = 0, reserved = 0;
+    cudaFuncAttributes fa{};
+    cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, h->device);
+    cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, h->device);
+    cudaFuncGetAttributes(&fa, ke->fn);
+    const int room = per_sm / want - reserved - (int)fa.sharedSizeBytes;
+    int over = smem - room, cur = smem;
+    if (over <= 0 || over > smem / 10) return FE_OK;
+    int cap = h->stage_cap;
+    for (int k = 0; k < 3; ++k) {
+        cap = std::min(cap - 256, (int)(cap * (1.0 - 2.0 * over / cur)) & ~255);
+        if (cap < 2048) return FE_OK;
+        PlanOptions opt;
+        opt.stage_cap = cap;
+        Plan pl;
+        Error err;
+        if (build_plan(h->hp, opt, pl, err) != FE_OK || check_plan(h->hp, pl, err) != FE_OK) return FE_OK;
+        KernelArgs B = h->base;
+        set_plan_caps(B, pl);
+        cur = tile_smem(h, ke, B, false);
+        over = cur - room;
+        if (over > 0) continue;
+        int m = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, ke->fn, THREADS, cur) != cudaSuccess || m < want) return FE_OK;
+        // the records in use are released: let assemblies still reading them finish
+        if (h->pending) {
+            const int rc = fe_sync(h);
+            (void)rc;
+        }
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return cuda_fail(h, e, "re-plan: stream synchronize");
+        h->plan = std::move(pl);
+        if ((e = install_plan(h)) != cudaSuccess) return cuda_fail(h, e, "re-plan: upload plan");
+        h->stage_cap = cap;
+        return FE_OK;
+    }
+    return FE_OK;
+}
+
 // Shared-memory sizing, status reset and the launch of one assembly: persistent CTAs, as
 // many as fit on the device at once (never more than there are tiles).
 int launch_assembly(fe_handle* h, const KernelEntry* ke, KernelArgs& A, bool fp64, cudaStream_t st,
                     std::pair<cudaEvent_t, cudaEvent_t>* ev) {
     cudaError_t e;
     const int pi = fp64 ? 1 : 0;
-    const int fixed = smem_layout(A, h->shape_bytes[pi], fp64 ? 8 : 4).chunk;
-    if (!h->max_smem) {
-        cudaDeviceGetAttribute(&h->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
-        cudaDeviceGetAttribute(&h->n_sm, cudaDevAttrMultiProcessorCount, h->device);
-    }
-    const int max_smem = h->max_smem, n_sm = h->n_sm;
-    const int budget = max_smem - 1024;  // static shared (mbarriers) headroom
-    // cell-table buffers: one per lane group; fewer groups when the tables are large
-    int tb = 0;
-    for (int s = 0; s < MAX_SUB; ++s) {
-        A.groups[s] = 0;
-        if (ke->kind[s] < 0) continue;
-        const int room = (budget - fixed) / std::max(ke->table_bytes[s], 1);
-        A.groups[s] = std::max(1, std::min(ke->groups[s], room));
-        tb = std::max(tb, ke->table_bytes[s] * A.groups[s]);
-    }
-    A.chunk_bytes = tb;
-    const int smem = fixed + chunk_region_bytes(A);
-    if (smem > budget) return set_error(h, FE_ERR_UNSUPPORTED, "tile does not fit in shared memory");
+    const int smem = tile_smem(h, ke, A, fp64);
+    const int n_sm = h->n_sm;
+    if (smem > h->max_smem - 1024) return set_error(h, FE_ERR_UNSUPPORTED, "tile does not fit in shared memory");
     if ((e = ensure_smem_attribute(ke->fn, smem)) != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute");
     if (ke->fn != h->occ_fn || smem != h->occ_smem) {
         int per_sm = 0;
@@ -426,6 +515,7 @@ int fe_create(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain
         delete h;
         return FE_ERR_UNSUPPORTED;
     }
+    h->plan_pinned = std::getenv("FE_GB300_STAGE_CAP") != nullptr;
     CK(install_plan(h));
     CK(h->alloc(&h->status_d, 1));
     CK(cudaMallocHost((void**)&h->status_h, sizeof(DevStatus)));
@@ -464,6 +554,11 @@ int fe_plan_dry_run(const fe_grid_desc* grid, int32_t n_subdomains, const fe_sub
     out->n_tiles = pl.n_tiles;
     out->n_cell_visits = pl.visits;
     out->n_items = pl.items;
+    out->max_record_bytes = pl.max_rec;
+    out->max_tile_nodes = pl.max_nodes;
+    out->max_stage_values = pl.max_stage;
+    out->max_out_doubles = pl.max_out;
+    out->stage_cap = opt.stage_cap;
     out->create_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return FE_OK;
 }
@@ -509,6 +604,15 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
     const bool do_k = !(p->flags & FE_NO_K), do_f = !(p->flags & FE_NO_F);
     if (do_k && !nzval) return set_error(h, FE_ERR_ARG, "nzval is NULL");
     if (do_f && !f) return set_error(h, FE_ERR_ARG, "f is NULL");
+    const KernelEntry* ke = find_kernel(hp, phys, fp64);
+    if (!ke) return set_error(h, FE_ERR_UNSUPPORTED, "no kernel compiled for this element / quadrature / physics combination");
+    if (!fp64 && !h->capturing && !h->plan_pinned && h->fitted_fn != ke->fn) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing((cudaStream_t)p->stream, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone) {
+            const int rc = fit_plan(h, ke, (cudaStream_t)p->stream);
+            if (rc != FE_OK) return rc;
+        }
+    }
     if (h->capturing) {
         // inside fe_graph_capture: device buffers only, the capture stream, no host work
         if ((cudaStream_t)p->stream != h->cap_stream) return set_error(h, FE_ERR_STATE, "capture: steps run on the capture stream");
@@ -529,21 +633,6 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
             (void)rc;
         }
     }
-    // pick the kernel
-    const KernelEntry* ke = nullptr;
-    for (const KernelEntry& e : registry()) {
-        if (e.phys != phys || e.fp64 != (int)fp64) continue;
-        bool ok = true;
-        for (int s = 0; s < MAX_SUB; ++s) {
-            if (s < (int)hp.subs.size()) {
-                if (e.kind[s] != hp.subs[s].kind || e.nq[s] != hp.subs[s].nq) ok = false;
-            } else if (e.kind[s] >= 0) {
-                ok = false;
-            }
-        }
-        if (ok) { ke = &e; break; }
-    }
-    if (!ke) return set_error(h, FE_ERR_UNSUPPORTED, "no kernel compiled for this element / quadrature / physics combination");
     cudaStream_t st = (cudaStream_t)p->stream;
     cudaError_t e;
     KernelArgs A = h->base;
@@ -878,6 +967,7 @@ int fe_autotune(fe_handle* h, const fe_assemble_params* p, double* nzval, double
     static const int32_t defaults[] = {6144, 8192, 10240, 12288, 16384, 24576};
     if (!h || !p || !out) return FE_ERR_ARG;
     if (h->capturing) return set_error(h, FE_ERR_STATE, "autotune during a capture");
+    h->plan_pinned = true;  // the candidates are timed as planned, and the choice stands
     if (!stage_caps || n_candidates < 1) {
         stage_caps = defaults;
         n_candidates = (int32_t)(sizeof(defaults) / sizeof(defaults[0]));
@@ -983,6 +1073,11 @@ int fe_get_info(const fe_handle* h, fe_info* out) {
     out->n_tiles = h->plan.n_tiles;
     out->n_cell_visits = h->plan.visits;
     out->n_items = h->plan.items;
+    out->max_record_bytes = h->plan.max_rec;
+    out->max_tile_nodes = h->plan.max_nodes;
+    out->max_stage_values = h->plan.max_stage;
+    out->max_out_doubles = h->plan.max_out;
+    out->stage_cap = h->stage_cap;
     out->flagged_cells = h->flagged;
     out->device_bytes = h->device_bytes;
     out->create_seconds = h->create_seconds;
@@ -1092,19 +1187,7 @@ extern "C" int fe_assemble_noalloc(fe_handle* h, const fe_assemble_params* p, do
         return set_error(h, FE_ERR_ARG, buf);
     }
     if (h->pending) fe_sync(h);
-    const KernelEntry* ke = nullptr;
-    for (const KernelEntry& e : registry()) {
-        if (e.phys != phys || e.fp64 != (int)fp64) continue;
-        bool ok = true;
-        for (int s = 0; s < MAX_SUB; ++s) {
-            if (s < (int)hp.subs.size()) {
-                if (e.kind[s] != hp.subs[s].kind || e.nq[s] != hp.subs[s].nq) ok = false;
-            } else if (e.kind[s] >= 0) {
-                ok = false;
-            }
-        }
-        if (ok) { ke = &e; break; }
-    }
+    const KernelEntry* ke = find_kernel(hp, phys, fp64);
     if (!ke) return set_error(h, FE_ERR_UNSUPPORTED, "no kernel compiled for this element / quadrature / physics combination");
     cudaStream_t st = (cudaStream_t)p->stream;
     cudaError_t e;

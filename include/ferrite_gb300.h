@@ -142,6 +142,12 @@ typedef struct {
                                (a cell is evaluated once per owner tile it touches) */
     int64_t device_bytes;   /* device memory held by the handle */
     double create_seconds;  /* host time spent in fe_create */
+    int32_t max_record_bytes;   /* largest tile record (shared-memory ring entry) */
+    int32_t max_tile_nodes;     /* most nodes of one tile (gathered coordinates) */
+    int32_t max_stage_values;   /* most staging values of one tile */
+    int32_t max_out_doubles;    /* largest reduce output buffer of one tile */
+    int32_t stage_cap;          /* staging capacity the plan was built with */
+    int32_t pad;
 } fe_info;
 
 /*
