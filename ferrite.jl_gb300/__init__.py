@@ -36,7 +36,8 @@ ERROR_NAMES = {0: "OK", 1: "ARG", 2: "BOUNDS", 3: "DETJ", 4: "PATTERN_MISSING", 
 TRIANGLE, QUADRILATERAL, TETRAHEDRON, HEXAHEDRON, WEDGE = 1, 2, 3, 4, 5
 HEAT, LINEAR_ELASTIC, NEO_HOOKE = 1, 2, 3
 PREC_MIXED, PREC_FP64 = 0, 1
-FILLZERO, NO_K, NO_F, ASYNC, PROFILE, COMPENSATED = 1, 2, 4, 8, 16, 32
+FILLZERO, NO_K, NO_F, ASYNC, PROFILE, COMPENSATED, TWO_PHASE, FUSED = 1, 2, 4, 8, 16, 32, 64, 128
+_FORMS = {None: 0, "two_phase": TWO_PHASE, "fused": FUSED}
 
 EXPORTED = ["fe_abi_version", "fe_create", "fe_assemble", "fe_sync", "fe_last_error", "fe_get_info",
             "fe_get_index_map", "fe_plan_dry_run", "fe_distribute_dofs", "fe_sparsity_pattern", "fe_kernel_time", "fe_assemble_noalloc",
@@ -293,9 +294,10 @@ class Handle:
 
     def assemble(self, nzval, f, physics: int, p0: float, p1: float, body=(0.0, 0.0, 0.0), cell_scale=None, u=None,
                  precision: int = PREC_MIXED, fillzero: bool = True, stream=None, sync: bool = True,
-                 cond_threshold: float = 0.0, profile: bool = False, compensated: bool = False):
+                 cond_threshold: float = 0.0, profile: bool = False, compensated: bool = False, form=None):
         """One fe_assemble call. ``stream`` is a torch.cuda.Stream, a raw handle or None.
-        ``compensated`` (mixed precision): sum each entry as a compensated FP32 pair."""
+        ``compensated`` (mixed precision): sum each entry as a compensated FP32 pair.
+        ``form``: None (the engine's choice), "two_phase" (element matrices first) or "fused"."""
         p = AssembleParams()
         p.physics, p.precision = physics, precision
         flags = FILLZERO if fillzero else 0
@@ -309,6 +311,7 @@ class Handle:
             flags |= PROFILE
         if compensated:
             flags |= COMPENSATED
+        flags |= _FORMS[form]
         p.flags = flags
         p.p0, p.p1 = float(p0), float(p1)
         for k in range(3):
@@ -346,10 +349,10 @@ class Handle:
 
     @staticmethod
     def _params(physics, p0, p1, body=(0.0, 0.0, 0.0), cell_scale=None, u=None, precision=PREC_MIXED, fillzero=True,
-                cond_threshold=0.0, compensated=False, stream=None):
+                cond_threshold=0.0, compensated=False, stream=None, form=None):
         p = AssembleParams()
         p.physics, p.precision = physics, precision
-        p.flags = (FILLZERO if fillzero else 0) | (COMPENSATED if compensated else 0)
+        p.flags = (FILLZERO if fillzero else 0) | (COMPENSATED if compensated else 0) | _FORMS[form]
         p.p0, p.p1 = float(p0), float(p1)
         for k in range(3):
             p.body[k] = float(body[k]) if k < len(body) else 0.0

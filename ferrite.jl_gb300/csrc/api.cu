@@ -19,15 +19,28 @@ using namespace fe;
 
 namespace {
 
-const std::vector<KernelEntry>& registry() {
-    static std::vector<KernelEntry> reg;
+struct Registries {
+    std::vector<KernelEntry> tiles;
+    std::vector<ElemEntry> elems;
+};
+
+const Registries& registries() {
+    static Registries reg;
     static std::once_flag once;
     std::call_once(once, [] {
-        register_heat(reg);
-        register_elastic(reg);
-        register_neo(reg);
+        register_heat(reg.tiles, reg.elems);
+        register_elastic(reg.tiles, reg.elems);
+        register_neo(reg.tiles, reg.elems);
     });
     return reg;
+}
+
+const std::vector<KernelEntry>& registry() { return registries().tiles; }
+
+const ElemEntry* find_elem(int kind, int nq, int phys, bool fp64) {
+    for (const ElemEntry& e : registries().elems)
+        if (e.kind == kind && e.nq == nq && e.phys == phys && e.fp64 == (int)fp64) return &e;
+    return nullptr;
 }
 
 const std::vector<AdjEntry>& adj_registry() {
@@ -98,11 +111,14 @@ struct fe_handle {
     int device = 0;
     int32_t stage_cap = 0;  // staging values per tile the current plan was built with
     int max_smem = 0, n_sm = 0;      // device attributes (read once)
-    const void* fitted_fn = nullptr;  // kernel the plan was last fitted to (fit_plan)
+    const void* fitted_fn = nullptr;  // kernel and form (two-phase subdomains) the plan was last fitted to
+    unsigned fitted_mask = 0;
     bool plan_pinned = false;         // staging capacity set by the caller or the autotuner
     const void* occ_fn = nullptr;    // occupancy of the last launch configuration
     int occ_smem = -1, occ_per_sm = 1;
     int accumulate_status = 0;       // a pending FE_ASYNC assembly's status is still being collected
+    void* ea_buf = nullptr;          // element-matrix scratch of the two-phase form (grown on demand)
+    size_t ea_bytes = 0;
 
     template <typename T>
     cudaError_t alloc(T** p, size_t count) {
@@ -225,15 +241,26 @@ void device_attributes(fe_handle* h) {
 
 // Dynamic shared memory of one CTA of kernel ke with A's caps; sets A.groups (cell-table
 // buffers: one per lane group, fewer when the tables are large) and A.chunk_bytes.
+// Shape-table bytes the tile kernel copies to shared memory: none when every subdomain is in
+// the two-phase form (no geometry in the tiles)
+int tile_shape_bytes(const fe_handle* h, const KernelArgs& A, bool fp64) {
+    for (int s = 0; s < A.n_sub; ++s)
+        if (!A.ea[s]) return h->shape_bytes[fp64 ? 1 : 0];
+    return 0;
+}
+
 int tile_smem(fe_handle* h, const KernelEntry* ke, KernelArgs& A, bool fp64) {
-    const int pi = fp64 ? 1 : 0;
-    const int fixed = smem_layout(A, h->shape_bytes[pi], fp64 ? 8 : 4).chunk;
+    const int fixed = smem_layout(A, tile_shape_bytes(h, A, fp64), fp64 ? 8 : 4).chunk;
     device_attributes(h);
     const int budget = h->max_smem - 1024;  // static shared (mbarriers) headroom
     int tb = 0;
     for (int s = 0; s < MAX_SUB; ++s) {
         A.groups[s] = 0;
         if (ke->kind[s] < 0) continue;
+        if (s < A.n_sub && A.ea[s]) {  // two-phase: lane groups without cell tables
+            A.groups[s] = ke->groups[s];
+            continue;
+        }
         const int room = (budget - fixed) / std::max(ke->table_bytes[s], 1);
         A.groups[s] = std::max(1, std::min(ke->groups[s], room));
         tb = std::max(tb, ke->table_bytes[s] * A.groups[s]);
@@ -296,9 +323,14 @@ cudaError_t status_reset(fe_handle* h, cudaStream_t st) {
 // the two-CTA line. Then re-plan with a slightly smaller capacity, once per kernel; a kernel
 // far past the line (more than a tenth) keeps the plan: smaller tiles would cost more visits
 // than the second CTA wins. Returns FE_OK or a CUDA failure of the upload.
-int fit_plan(fe_handle* h, const KernelEntry* ke, cudaStream_t st) {
+int fit_plan(fe_handle* h, const KernelEntry* ke, cudaStream_t st, unsigned ea_mask) {
     h->fitted_fn = ke->fn;
+    h->fitted_mask = ea_mask;
+    auto with_form = [&](KernelArgs& X) {
+        for (int s = 0; s < MAX_SUB; ++s) X.ea[s] = (ea_mask >> s) & 1u ? (const void*)&h->base : nullptr;  // markers only
+    };
     KernelArgs A = h->base;
+    with_form(A);
     const int smem = tile_smem(h, ke, A, false);
     if (smem > h->max_smem - 1024 || ensure_smem_attribute(ke->fn, smem) != cudaSuccess) return FE_OK;
     int n = 0, n0 = 0;
@@ -325,6 +357,7 @@ int fit_plan(fe_handle* h, const KernelEntry* ke, cudaStream_t st) {
         Error err;
         if (build_plan(h->hp, opt, pl, err) != FE_OK || check_plan(h->hp, pl, err) != FE_OK) return FE_OK;
         KernelArgs B = h->base;
+        with_form(B);
         set_plan_caps(B, pl);
         cur = tile_smem(h, ke, B, false);
         over = cur - room;
@@ -369,8 +402,35 @@ int launch_assembly(fe_handle* h, const KernelEntry* ke, KernelArgs& A, bool fp6
     A.status = h->status_d;
     const void* shp = fp64 ? (const void*)h->shape_d : (const void*)h->shape_f;
     int sb = h->shape_bytes[pi], o1 = h->shape_off1[pi], o2 = h->shape_off2[pi];
-    void* args[] = {(void*)&A, (void*)&shp, (void*)&sb, (void*)&o1, (void*)&o2};
+    int tsb = tile_shape_bytes(h, A, fp64);
+    void* args[] = {(void*)&A, (void*)&shp, (void*)&tsb, (void*)&o1, (void*)&o2};
     if (ev) cudaEventRecord(ev->first, st);
+    // two-phase form: the element matrices of those subdomains first
+    for (int s = 0; s < A.n_sub; ++s) {
+        if (!A.ea[s]) continue;
+        const SubDev& sd = A.sub[s];
+        const ElemEntry* ee = find_elem(sd.kind, sd.nq, ke->phys, fp64);
+        if (!ee) return set_error(h, FE_ERR_UNSUPPORTED, "no element kernel compiled for this element / physics");
+        const int off = s == 0 ? 0 : (s == 1 ? o1 : o2);
+        const int end = s + 1 < A.n_sub ? (s == 0 ? o1 : o2) : sb;
+        int sub_bytes = end - off;
+        const int esmem = ((sub_bytes + 15) & ~15) + ee->groups * ee->group_bytes;
+        if (esmem > h->max_smem - 1024) return set_error(h, FE_ERR_UNSUPPORTED, "element tables do not fit in shared memory");
+        if ((e = ensure_smem_attribute(ee->fn, esmem)) != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute");
+        int per_sm = 0;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ee->fn, THREADS, esmem)) != cudaSuccess)
+            return cuda_fail(h, e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+        const int64_t need = (sd.n_cells + ee->groups - 1) / ee->groups;
+        const int64_t egrid = std::min<int64_t>(need, (int64_t)std::max(per_sm, 1) * std::max(n_sm, 1));
+        if (egrid <= 0) continue;
+        SubDev sdv = sd;
+        const void* eshp = (const char*)shp + off;
+        void* out = const_cast<void*>(A.ea[s]);
+        int64_t stride = A.ea_stride[s];
+        void* eargs[] = {(void*)&A, (void*)&sdv, (void*)&eshp, (void*)&sub_bytes, (void*)&out, (void*)&stride};
+        e = cudaLaunchKernel(ee->fn, dim3((unsigned)egrid), dim3(THREADS), eargs, (size_t)esmem, st);
+        if (e != cudaSuccess) return cuda_fail(h, e, "element kernel launch");
+    }
     if (grid > 0) {
         e = cudaLaunchKernel(ke->fn, dim3((unsigned)grid), dim3(THREADS), args, (size_t)smem, st);
         if (e != cudaSuccess) return cuda_fail(h, e, "tile kernel launch");
@@ -606,10 +666,16 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
     if (do_f && !f) return set_error(h, FE_ERR_ARG, "f is NULL");
     const KernelEntry* ke = find_kernel(hp, phys, fp64);
     if (!ke) return set_error(h, FE_ERR_UNSUPPORTED, "no kernel compiled for this element / quadrature / physics combination");
-    if (!fp64 && !h->capturing && !h->plan_pinned && h->fitted_fn != ke->fn) {
+    // two-phase form per subdomain: quadratic elements by default (their geometry would be
+    // recomputed in every tile that owns one of their ~27 dof entities)
+    unsigned ea_mask = 0;
+    for (int s = 0; s < (int)hp.subs.size(); ++s)
+        if (hp.subs[s].n_cells > 0 && ((p->flags & FE_TWO_PHASE) || (!(p->flags & FE_FUSED) && hp.subs[s].nb > 16)))
+            ea_mask |= 1u << s;
+    if (!fp64 && !h->capturing && !h->plan_pinned && (h->fitted_fn != ke->fn || h->fitted_mask != ea_mask)) {
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         if (cudaStreamIsCapturing((cudaStream_t)p->stream, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone) {
-            const int rc = fit_plan(h, ke, (cudaStream_t)p->stream);
+            const int rc = fit_plan(h, ke, (cudaStream_t)p->stream, ea_mask);
             if (rc != FE_OK) return rc;
         }
     }
@@ -656,6 +722,34 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
     A.do_f = do_f;
     A.fillzero = fill;
     A.compensated = (p->flags & FE_COMPENSATED) != 0;
+    // element-matrix scratch of the two-phase subdomains
+    {
+        size_t need = 0;
+        int64_t offs[MAX_SUB] = {0, 0, 0};
+        const size_t rb = fp64 ? sizeof(double) : sizeof(float);
+        for (int s = 0; s < (int)hp.subs.size(); ++s) {
+            const HostSub& hs = hp.subs[s];
+            A.ea[s] = nullptr;
+            A.ea_stride[s] = 0;
+            if (!((ea_mask >> s) & 1u)) continue;
+            offs[s] = (int64_t)need;
+            A.ea_stride[s] = ea_cell_values(hs.nb, hs.nc);
+            need += (size_t)hs.n_cells * (size_t)A.ea_stride[s] * rb;
+            A.ea[s] = (const void*)1;  // placed below
+        }
+        if (need > h->ea_bytes) {
+            if (h->capturing) return set_error(h, FE_ERR_STATE, "capture: the two-phase scratch grows; assemble once before capturing");
+            if (h->ea_buf) h->release(h->ea_buf);
+            h->ea_buf = nullptr;
+            h->ea_bytes = 0;
+            char* b = nullptr;
+            if ((e = h->alloc(&b, need)) != cudaSuccess) return cuda_fail(h, e, "alloc element-matrix scratch");
+            h->ea_buf = b;
+            h->ea_bytes = need;
+        }
+        for (int s = 0; s < (int)hp.subs.size(); ++s)
+            if (A.ea[s]) A.ea[s] = (const char*)h->ea_buf + offs[s];
+    }
     // inputs
     Physics& ph = A.phys;
     ph = Physics{};

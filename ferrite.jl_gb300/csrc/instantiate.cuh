@@ -35,8 +35,23 @@ KernelEntry make_entry() {
     return e;
 }
 
+template <int K, int Q, int PH, typename R>
+ElemEntry make_elem_entry() {
+    ElemEntry e;
+    e.kind = K;
+    e.nq = Q;
+    e.phys = PH;
+    e.fp64 = std::is_same<R, double>::value ? 1 : 0;
+    e.fn = (const void*)&element_kernel<K, Q, PH, R>;
+    e.group_bytes = EaGroup<K, Q, PH, R>::BYTES;
+    e.groups = THREADS / ElemT<K>::GS;
+    return e;
+}
+
 #define FE_ONE(K, Q, PH)                                                  \
     out.push_back(make_entry<K, Q, -1, 0, -1, 0, PH, float>());           \
-    out.push_back(make_entry<K, Q, -1, 0, -1, 0, PH, double>());
+    out.push_back(make_entry<K, Q, -1, 0, -1, 0, PH, double>());          \
+    eout.push_back(make_elem_entry<K, Q, PH, float>());                   \
+    eout.push_back(make_elem_entry<K, Q, PH, double>());
 
 }  // namespace fe

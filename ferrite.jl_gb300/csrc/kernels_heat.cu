@@ -2,7 +2,7 @@
 #include "instantiate.cuh"
 
 namespace fe {
-void register_heat(std::vector<KernelEntry>& out) {
+void register_heat(std::vector<KernelEntry>& out, std::vector<ElemEntry>& eout) {
     FE_ONE(KIND_QUAD4, 4, PHYS_HEAT)
     FE_ONE(KIND_QUAD4, 1, PHYS_HEAT)
     FE_ONE(KIND_TRI3, 1, PHYS_HEAT)

@@ -3,7 +3,7 @@
 #include "instantiate.cuh"
 
 namespace fe {
-void register_neo(std::vector<KernelEntry>& out) {
+void register_neo(std::vector<KernelEntry>& out, std::vector<ElemEntry>& eout) {
     FE_ONE(KIND_HEX8, 8, PHYS_NEO)
     FE_ONE(KIND_TET4, 1, PHYS_NEO)
     FE_ONE(KIND_TET4, 4, PHYS_NEO)

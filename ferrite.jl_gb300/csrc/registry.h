@@ -23,9 +23,18 @@ struct AdjEntry {
     int smem;            // dynamic shared memory per CTA
 };
 
-void register_heat(std::vector<KernelEntry>& out);
-void register_elastic(std::vector<KernelEntry>& out);
-void register_neo(std::vector<KernelEntry>& out);
+// per-cell element-matrix kernels (element_kernel): one per (kind, quadrature points, physics,
+// precision)
+struct ElemEntry {
+    int kind, nq, phys, fp64;
+    const void* fn;      // __global__ element_kernel<...>
+    int group_bytes;     // shared memory per lane group (the shape tables come on top)
+    int groups;          // lane groups per CTA
+};
+
+void register_heat(std::vector<KernelEntry>& out, std::vector<ElemEntry>& eout);
+void register_elastic(std::vector<KernelEntry>& out, std::vector<ElemEntry>& eout);
+void register_neo(std::vector<KernelEntry>& out, std::vector<ElemEntry>& eout);
 void register_adjoint(std::vector<AdjEntry>& out);
 const void* adjoint_node_sum_fn(bool fp64);
 

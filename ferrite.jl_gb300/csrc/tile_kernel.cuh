@@ -534,10 +534,53 @@ __device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev
 // ---------------------------------------------------------------------------------------
 // phase B: the blocks of one cell into its owned columns; lane i = row base function
 // ---------------------------------------------------------------------------------------
-template <int K, int NQ, int PHYS, typename Real>
+// One (item, row) block and the row's load entry into the tile's staging slots. The plan gives
+// every (item, row) its own slot, so no two lanes write the same one; a block without a slot
+// is a pattern miss unless it is exactly zero (assembler.jl:413-417, 459-467).
+template <int NC_MAX, int nc, typename Real>
+__device__ __forceinline__ void stage_block(const KernelArgs& a, const SubDev& sd, Real* stage, int f_off, int cell, int i, int j,
+                                            int fslot, int slot, const Real* Kb, const Real* fe) {
+    using P = typename Pair<Real>::type;
+    constexpr int BSC = (nc * nc + 1) & ~1;
+    if (a.do_k) {
+        if (slot == SLOT_MISS) {
+            #pragma unroll
+            for (int x = 0; x < NC_MAX; ++x)
+                #pragma unroll
+                for (int y = 0; y < NC_MAX; ++y)
+                    if (x < nc && y < nc && Kb[x * NC_MAX + y] != Real(0))
+                        record_miss(a.status, sd.cellid[cell], i * nc + x, j * nc + y);
+        } else {
+            Real* dst = stage + slot * BSC;
+            if (nc == 1) {
+                dst[0] = Kb[0];
+            } else {
+                // column-major (b outer) so the reduce step reads in output order; an odd
+                // count is padded with a zero so slots are pairs
+                Real col[NC_MAX * NC_MAX + 1];
+                #pragma unroll
+                for (int y = 0; y < NC_MAX; ++y)
+                    #pragma unroll
+                    for (int x = 0; x < NC_MAX; ++x) col[y * NC_MAX + x] = Kb[x * NC_MAX + y];
+                col[NC_MAX * NC_MAX] = Real(0);
+                // nc is 1 (scalar field) or the dimension (vector field): the host checks it
+                #pragma unroll
+                for (int t = 0; t < (NC_MAX * NC_MAX + 1) / 2; ++t) ((P*)dst)[t] = P{col[2 * t], col[2 * t + 1]};
+            }
+        }
+    }
+    if (a.do_f && i == j) {
+        Real* dst = stage + f_off + fslot * nc;
+        #pragma unroll
+        for (int x = 0; x < NC_MAX; ++x)
+            if (x < nc) dst[x] = fe[x];
+    }
+}
+
+template <int K, int NQ, int PHYS, typename Real, bool EA = false>
 __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& sd, const char* R, const uint16_t* slot_rows,
                                             Real* stage, int f_off, const Real* tb, const Real* shp, int cell, int i, int it0,
-                                            int it1) {
+                                            int it1, Real* ea_out = nullptr) {
     using E = ElemT<K>;
     using CT = CellTable<K, NQ, PHYS, Real>;
     using P = typename Pair<Real>::type;
@@ -547,12 +590,12 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
     constexpr bool CACHE = NQP <= 4;  // keep the row function's table in registers
     // components per entity and staging stride, fixed by the physics (the host checks a.nc)
     constexpr int nc = PHYS == PHYS_HEAT ? 1 : DIM;
-    constexpr int BSC = (nc * nc + 1) & ~1;
     const Real* grad = tb;
     const Real* sq = tb + CT::GRAD;
     const Real* cellp = sq + CT::SQ;
     const Real* neo = cellp + 4;
-    const uint32_t* items = (const uint32_t*)(R + ((const RecHead*)R)->off_items);
+    const uint32_t* items = nullptr;
+    if constexpr (!EA) items = (const uint32_t*)(R + ((const RecHead*)R)->off_items);
     P gi[CACHE ? NQP : 1][3];
     if constexpr (CACHE) {
         #pragma unroll
@@ -571,40 +614,23 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
             }
         }
     }
-    // the plan gives every (item, row) its own staging slot: no two lanes write the same one
+    // phase B: the block goes to the tile's staging slot; element-assembly form (EA): to the
+    // cell's element matrix, [j][t][i] with t = y nc + x, then the load entries [x][i]
     auto store_block = [&](int j, int fslot, int slot, const Real* Kb, const Real* fe) {
-        if (a.do_k) {
-            if (slot == SLOT_MISS) {
+        if constexpr (EA) {
+            constexpr int NCC = nc * nc;
+            if (a.do_k) {
                 #pragma unroll
-                for (int x = 0; x < NC_MAX; ++x)
+                for (int y = 0; y < nc; ++y)
                     #pragma unroll
-                    for (int y = 0; y < NC_MAX; ++y)
-                        if (x < nc && y < nc && Kb[x * NC_MAX + y] != Real(0))
-                            record_miss(a.status, sd.cellid[cell], i * nc + x, j * nc + y);
-            } else {
-                Real* dst = stage + slot * BSC;
-                if (nc == 1) {
-                    dst[0] = Kb[0];
-                } else {
-                    // column-major (b outer) so the reduce step reads in output order; an
-                    // odd count is padded with a zero so slots are pairs
-                    Real col[NC_MAX * NC_MAX + 1];
-                    #pragma unroll
-                    for (int y = 0; y < NC_MAX; ++y)
-                        #pragma unroll
-                        for (int x = 0; x < NC_MAX; ++x) col[y * NC_MAX + x] = Kb[x * NC_MAX + y];
-                    col[NC_MAX * NC_MAX] = Real(0);
-                    // nc is 1 (scalar field) or the dimension (vector field): the host checks it
-                    #pragma unroll
-                    for (int t = 0; t < (NC_MAX * NC_MAX + 1) / 2; ++t) ((P*)dst)[t] = P{col[2 * t], col[2 * t + 1]};
-                }
+                    for (int x = 0; x < nc; ++x) ea_out[(j * NCC + y * nc + x) * NB + i] = Kb[x * NC_MAX + y];
             }
-        }
-        if (a.do_f && i == j) {
-            Real* dst = stage + f_off + fslot * nc;
-            #pragma unroll
-            for (int x = 0; x < NC_MAX; ++x)
-                if (x < nc) dst[x] = fe[x];
+            if (a.do_f && i == j) {
+                #pragma unroll
+                for (int x = 0; x < nc; ++x) ea_out[NB * NB * NCC + x * NB + i] = fe[x];
+            }
+        } else {
+            stage_block<NC_MAX, nc, Real>(a, sd, stage, f_off, cell, i, j, fslot, slot, Kb, fe);
         }
     };
     if constexpr (PHYS == PHYS_HEAT || PHYS == PHYS_ELASTIC) {
@@ -615,10 +641,15 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
             int jm[M], fsm[M], slm[M];
             #pragma unroll
             for (int m = 0; m < M; ++m) {
-                const uint32_t word = items[it + m];
-                jm[m] = (int)(word & 0xFF);
-                fsm[m] = (int)(word >> 16);
-                slm[m] = slot_rows[(it + m - it0) * NB + i];
+                if constexpr (EA) {
+                    jm[m] = it + m;  // every column of the cell
+                    fsm[m] = slm[m] = 0;
+                } else {
+                    const uint32_t word = items[it + m];
+                    jm[m] = (int)(word & 0xFF);
+                    fsm[m] = (int)(word >> 16);
+                    slm[m] = slot_rows[(it + m - it0) * NB + i];
+                }
             }
             P G[M][DIM][DIM];
             #pragma unroll
@@ -682,10 +713,13 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
         for (int it = it0; it < it1; ++it) items_m(std::integral_constant<int, 1>{}, it);
     } else {  // PHYS_NEO: per item and point, scalar
         for (int it = it0; it < it1; ++it) {
-            const uint32_t word = items[it];
-            const int j = (int)(word & 0xFF);
-            const int fslot = (int)(word >> 16);
-            const int slot = slot_rows[(it - it0) * NB + i];
+            int j = it, fslot = 0, slot = 0;
+            if constexpr (!EA) {
+                const uint32_t word = items[it];
+                j = (int)(word & 0xFF);
+                fslot = (int)(word >> 16);
+                slot = slot_rows[(it - it0) * NB + i];
+            }
             Real Kb[NC_MAX * NC_MAX];
             Real fe[NC_MAX];
             #pragma unroll
@@ -727,6 +761,43 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
 }
 
 // ---------------------------------------------------------------------------------------
+// two-phase form, phase B: the items' blocks come from the cell's element matrix in global
+// memory (written by element_kernel); lane i = row base function, coalesced over i
+// ---------------------------------------------------------------------------------------
+template <int K, int PHYS, typename Real>
+__device__ __forceinline__ void gather_blocks(const KernelArgs& a, const SubDev& sd, const char* R, const uint16_t* slot_rows,
+                                              Real* stage, int f_off, const Real* __restrict__ ea, int cell, int i, int it0,
+                                              int it1) {
+    using E = ElemT<K>;
+    constexpr int NB = E::NB, NC_MAX = E::DIM;
+    constexpr int nc = PHYS == PHYS_HEAT ? 1 : E::DIM;
+    constexpr int NCC = nc * nc;
+    const uint32_t* items = (const uint32_t*)(R + ((const RecHead*)R)->off_items);
+    #pragma unroll 2
+    for (int it = it0; it < it1; ++it) {
+        const uint32_t word = items[it];
+        const int j = (int)(word & 0xFF);
+        Real Kb[NC_MAX * NC_MAX], fe[NC_MAX];
+        #pragma unroll
+        for (int t = 0; t < NC_MAX * NC_MAX; ++t) Kb[t] = Real(0);
+        #pragma unroll
+        for (int x = 0; x < NC_MAX; ++x) fe[x] = Real(0);
+        if (a.do_k) {
+            #pragma unroll
+            for (int y = 0; y < nc; ++y)
+                #pragma unroll
+                for (int x = 0; x < nc; ++x) Kb[x * NC_MAX + y] = __ldcs(ea + (j * NCC + y * nc + x) * NB + i);
+        }
+        if (a.do_f && i == j) {
+            #pragma unroll
+            for (int x = 0; x < nc; ++x) fe[x] = __ldcs(ea + NB * NB * NCC + x * NB + i);
+        }
+        stage_block<NC_MAX, nc, Real>(a, sd, stage, f_off, cell, i, j, (int)(word >> 16), slot_rows[(it - it0) * NB + i], Kb,
+                                      fe);
+    }
+}
+
+// ---------------------------------------------------------------------------------------
 // the cells of one subdomain in a tile
 // ---------------------------------------------------------------------------------------
 template <int K, int NQ, int PHYS, typename Real>
@@ -751,6 +822,22 @@ __device__ __forceinline__ void process_segment(const KernelArgs& a, const SubDe
     Real* tb = (Real*)(chunk + grp * CT::BYTES);
     const uint16_t* gt = (const uint16_t*)(R + g.gt_off);
     const RecTask* tasks = (const RecTask*)(R + H->off_tasks);
+    const Real* ea = (const Real*)a.ea[g.sub];
+    if (ea) {
+        // two-phase form: no geometry here, the blocks are loaded
+        const int64_t es = a.ea_stride[g.sub];
+        for (int pg = grp; grp < ngrp && pg < g.n_grp; pg += ngrp) {
+            const int t1 = gt[pg + 1];
+            for (int ti = gt[pg]; ti < t1; ++ti) {
+                const RecTask tk = tasks[ti];
+                const int cell = cells[tk.cell];
+                if (lane < NB)
+                    gather_blocks<K, PHYS, Real>(a, sd, R, slots + (tk.item_begin - g.item_begin) * NB, stage, f_off,
+                                                 ea + (int64_t)cell * es, cell, lane, tk.item_begin, tk.item_end);
+            }
+        }
+        return;
+    }
     // the plan's groups run on this CTA's groups round robin (the same when the counts agree)
     for (int pg = grp; grp < ngrp && pg < g.n_grp; pg += ngrp) {
         const int t1 = gt[pg + 1];
@@ -1064,16 +1151,21 @@ __global__ void __launch_bounds__(THREADS, 2) tile_kernel(const KernelArgs a, co
     if (tid == 0) {
         for (int b = 0; b < 1 + REC_RING; ++b) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8u * b) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        bulk_load((uint32_t)__cvta_generic_to_shared(shape), shape_g, shape_bytes, bar0);
+        // no shape tables when every subdomain's element matrices come precomputed
+        if (shape_bytes > 0) bulk_load((uint32_t)__cvta_generic_to_shared(shape), shape_g, shape_bytes, bar0);
+        else asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar0) : "memory");
         if (t < a.n_tiles) issue_record(a.rec_off[t], a.rec_off[t + 1], 0);
         if (t + G < a.n_tiles) issue_record(a.rec_off[t + G], a.rec_off[t + G + 1], 1);
         if (t + 2 * G < a.n_tiles) { pf0 = a.rec_off[t + 2 * G]; pf1 = a.rec_off[t + 2 * G + 1]; }
     }
     __syncthreads();  // the initialised barriers are visible to every thread
+    // node coordinates are needed unless every subdomain's element matrices come precomputed
+    bool geo = false;
+    for (int s = 0; s < a.n_sub; ++s) geo |= a.ea[s] == nullptr;
     bool failed = false;
     if (t < a.n_tiles) {
-        if (mbar_wait(rec_bar(0), 0, WAIT_LIMIT)) gather_nodes<Real>(a, rec_ring, xs_ring);
-        else failed = true;
+        if (!mbar_wait(rec_bar(0), 0, WAIT_LIMIT)) failed = true;
+        else if (geo) gather_nodes<Real>(a, rec_ring, xs_ring);
     }
     if (!failed && !mbar_wait(bar0, 0, WAIT_LIMIT)) failed = true;
     int it = 0;
@@ -1089,10 +1181,10 @@ __global__ void __launch_bounds__(THREADS, 2) tile_kernel(const KernelArgs a, co
         }
         if (t + G < a.n_tiles) {
             const int nb = (it + 1) % REC_RING;
-            if (mbar_wait(rec_bar(nb), (uint32_t)(((it + 1) / REC_RING) & 1), WAIT_LIMIT))
-                gather_nodes<Real>(a, rec_ring + nb * rec_stride, xs_ring + ((it + 1) & 1) * xs_stride);
-            else
+            if (!mbar_wait(rec_bar(nb), (uint32_t)(((it + 1) / REC_RING) & 1), WAIT_LIMIT))
                 failed = true;
+            else if (geo)
+                gather_nodes<Real>(a, rec_ring + nb * rec_stride, xs_ring + ((it + 1) & 1) * xs_stride);
         }
         const RecHead* H = (const RecHead*)R;
         const int n_seg = H->n_seg;
@@ -1130,6 +1222,79 @@ __global__ void __launch_bounds__(THREADS, 2) tile_kernel(const KernelArgs a, co
                 if (tt < a.n_tiles) mbar_wait(rec_bar((it + d) % REC_RING), (uint32_t)(((it + d) / REC_RING) & 1), WAIT_LIMIT);
             }
         }
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// element matrices: one lane group per cell computes the geometry (lane = quadrature point),
+// then every column j of Ke and the load vector (lane = row function i) into out + cell *
+// stride, laid out [j][t][i] (t = y nc + x, the block's entries column by column) and then
+// fe [x][i]. Phase A of the two-phase assembly; the element-assembly output of the GPU how-to
+// (gpu_assembly.jl:265-303) in this layout.
+// ---------------------------------------------------------------------------------------
+template <int K, int NQ, int PHYS, typename Real>
+struct EaGroup {
+    static constexpr int NG = ElemT<K>::NG;
+    static constexpr int TB = CellTable<K, NQ, PHYS, Real>::BYTES;  // cell table
+    static constexpr int XS = (NG * NODE_BYTES + 15) / 16 * 16;     // node coordinates
+    static constexpr int ND = (NG * 4 + 15) / 16 * 16;              // node ids
+    static constexpr int CN = (NG * 2 + 15) / 16 * 16;              // local node numbers
+    static constexpr int BYTES = TB + XS + ND + CN;
+};
+
+template <int K, int NQ, int PHYS, typename Real>
+__host__ __device__ constexpr int element_smem_bytes(int shape_bytes) {
+    return pad16(shape_bytes) + (THREADS / ElemT<K>::GS) * EaGroup<K, NQ, PHYS, Real>::BYTES;
+}
+
+template <int K, int NQ, int PHYS, typename Real>
+__global__ void __launch_bounds__(THREADS, 2) element_kernel(const KernelArgs a, const SubDev sd, const Real* __restrict__ shape_g,
+                                                              int shape_bytes, Real* __restrict__ out, int64_t stride) {
+    using E = ElemT<K>;
+    using EG = EaGroup<K, NQ, PHYS, Real>;
+    constexpr int NB = E::NB, NG = E::NG, GS = E::GS, NGRP = THREADS / GS;
+    extern __shared__ __align__(128) char smem_raw[];
+    const int tid = threadIdx.x, lane = tid % GS, grp = tid / GS;
+    const unsigned gmask = GS >= 32 ? 0xFFFFFFFFu : (((1u << GS) - 1u) << ((tid & 31) / GS * GS));
+    const int gbase = (tid & 31) - lane;
+    {
+        // the host sized the allocation from the same layout; refuse to run past it
+        uint32_t dyn;
+        asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+        if ((uint32_t)element_smem_bytes<K, NQ, PHYS, Real>(shape_bytes) > dyn) {
+            if (tid == 0) atomicAdd(&a.status->timeout, 1u);
+            return;
+        }
+    }
+    Real* shape = (Real*)smem_raw;
+    for (int k = tid; k < shape_bytes / 16; k += THREADS) ((int4*)shape)[k] = ((const int4*)shape_g)[k];
+    char* base = smem_raw + pad16(shape_bytes);
+    // tables of all groups first, so their strides keep the bank stagger of the tile kernel
+    Real* tb = (Real*)(base + grp * EG::TB);
+    char* xs = base + NGRP * EG::TB + grp * EG::XS;
+    int32_t* nodes = (int32_t*)(base + NGRP * (EG::TB + EG::XS) + grp * EG::ND);
+    uint16_t* cn = (uint16_t*)(base + NGRP * (EG::TB + EG::XS + EG::ND) + grp * EG::CN);
+    if (lane < NG) cn[lane] = (uint16_t)lane;
+    __syncthreads();
+    const char* src = sizeof(Real) == 4 ? (const char*)a.xf6 : (const char*)a.xd3;
+    const int64_t step = (int64_t)gridDim.x * NGRP;
+    for (int64_t c = (int64_t)blockIdx.x * NGRP + grp; c < sd.n_cells; c += step) {
+        if (lane < NG) {
+            const int nd = sd.conn[c * NG + lane];
+            nodes[lane] = nd;
+            const uint2* p = (const uint2*)(src + (int64_t)nd * NODE_BYTES);
+            uint2* d = (uint2*)(xs + lane * NODE_BYTES);
+            d[0] = p[0];
+            d[1] = p[1];
+            d[2] = p[2];
+        }
+        __syncwarp(gmask);
+        geometry_lanes<K, NQ, PHYS, Real>(a, sd, shape, (int)c, cn, xs, nodes, lane, gmask, gbase, tb);
+        __syncwarp(gmask);
+        if (lane < NB)
+            cell_blocks<K, NQ, PHYS, Real, true>(a, sd, nullptr, nullptr, nullptr, 0, tb, shape, (int)c, lane, 0, NB,
+                                                 out + c * stride);
+        __syncwarp(gmask);  // the next cell overwrites the table and the coordinates
     }
 }
 

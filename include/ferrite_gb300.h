@@ -73,6 +73,11 @@ extern "C" {
 #define FE_PROFILE 16u /* bracket the assembly kernel with CUDA events; read with fe_kernel_time() */
 #define FE_COMPENSATED 32u /* FE_PREC_MIXED: sum each entry's contributions as a compensated FP32 pair
                               (TwoSum, FP64-class summation error) and round the pair exactly to FP64 */
+#define FE_TWO_PHASE 64u   /* element matrices first: one pass per cell writes Ke and fe to a device scratch
+                              held by the handle, then the owner tiles load them instead of recomputing the
+                              cell's geometry in every tile that owns one of its dofs. The default for
+                              quadratic elements; results are bitwise those of the fused form */
+#define FE_FUSED 128u      /* element math inside the owner tiles (the default for linear elements) */
 
 typedef struct fe_handle fe_handle;
 

@@ -165,10 +165,12 @@ def test_detj_error(built, oracle):
     cells[4] = cells[4][[1, 0, 3, 2]]
     prob = O.Problem.single(O.QUADRILATERAL, nodes, cells).close().allocate_matrix()
     h = make_handle(fg, O, prob)
-    for prec in (0, 1):
-        with pytest.raises(fg.FEError) as ei:
-            h.assemble(np.zeros(prob.nnz), np.zeros(prob.ndofs), physics=fg.HEAT, p0=1.0, p1=1.0, precision=prec)
-        assert ei.value.name == "DETJ" and ei.value.cell == 5 and ei.value.detJ < 0
+    for form in ("fused", "two_phase"):
+        for prec in (0, 1):
+            with pytest.raises(fg.FEError) as ei:
+                h.assemble(np.zeros(prob.nnz), np.zeros(prob.ndofs), physics=fg.HEAT, p0=1.0, p1=1.0, precision=prec,
+                           form=form)
+            assert ei.value.name == "DETJ" and ei.value.cell == 5 and ei.value.detJ < 0
 
 
 def test_async_chain_matches_sync_and_keeps_errors(built, oracle, torch_cuda):
@@ -215,12 +217,13 @@ def test_pattern_missing_error(built, oracle):
     prob.colptr = prob.colptr.copy()
     prob.colptr[col + 1:] -= 1
     h = make_handle(fg, O, prob)
-    with pytest.raises(fg.FEError) as ei:
-        h.assemble(np.zeros(prob.nnz), np.zeros(prob.ndofs), physics=fg.HEAT, p0=1.0, p1=1.0)
-    assert ei.value.name == "PATTERN_MISSING"
-    assert (ei.value.row, ei.value.col) in [(dropped_row, col + 1)]
-    # zero contributions to the missing entry are fine (k = 0)
-    h.assemble(np.zeros(prob.nnz), np.zeros(prob.ndofs), physics=fg.HEAT, p0=0.0, p1=1.0)
+    for form in ("fused", "two_phase"):
+        with pytest.raises(fg.FEError) as ei:
+            h.assemble(np.zeros(prob.nnz), np.zeros(prob.ndofs), physics=fg.HEAT, p0=1.0, p1=1.0, form=form)
+        assert ei.value.name == "PATTERN_MISSING"
+        assert (ei.value.row, ei.value.col) in [(dropped_row, col + 1)]
+        # zero contributions to the missing entry are fine (k = 0)
+        h.assemble(np.zeros(prob.nnz), np.zeros(prob.ndofs), physics=fg.HEAT, p0=0.0, p1=1.0, form=form)
 
 
 def test_distorted_cells_use_fp64_jacobians(built, oracle):
@@ -256,3 +259,59 @@ def test_unaligned_device_output(built, oracle, torch_cuda):
     h.assemble(b, f, **args)
     torch.cuda.synchronize()
     assert torch.equal(a, b)
+
+
+def _forms_bitwise(fg, O, prob, element_args):
+    """Element matrices first (two-phase) and in-tile (fused) give the same bits: the same FP32
+    element math feeds the same per-entry sums in cell order."""
+    h = make_handle(fg, O, prob)
+    out = {}
+    for form in ("fused", "two_phase"):
+        for prec in (0, 1):
+            nz = np.full(prob.nnz, np.nan)
+            f = np.full(prob.ndofs, np.nan)
+            h.assemble(nz, f, precision=prec, form=form, **element_args)
+            out[form, prec] = (nz, f)
+    for prec in (0, 1):
+        assert np.array_equal(out["fused", prec][0], out["two_phase", prec][0]), prec
+        assert np.array_equal(out["fused", prec][1], out["two_phase", prec][1]), prec
+    return h
+
+
+@pytest.mark.parametrize("case", ["hex_q1_elastic", "hex_q2_elastic", "hex_q2_heat", "quad_q2_heat", "tet_elastic"])
+def test_two_phase_matches_fused_bitwise(built, oracle, case):
+    fg, O = built, oracle
+    E, nu, b = 200e3, 0.3, (0.0, 0.0, -1.0)
+    el = dict(physics=fg.LINEAR_ELASTIC, p0=E, p1=nu, body=b)
+    ht = dict(physics=fg.HEAT, p0=1.0, p1=1.0)
+    if case == "hex_q1_elastic":
+        prob = O.box_problem(O.HEXAHEDRON, (7, 6, 5), ip_order=1, ncomp=3, qr_order=2, perturb=0.2, seed=21)
+        args = el
+    elif case == "hex_q2_elastic":
+        prob = O.box_problem(O.HEXAHEDRON, (4, 3, 3), ip_order=2, ncomp=3, qr_order=3, perturb=0.2, seed=22)
+        args = dict(el, cell_scale=np.random.default_rng(3).lognormal(0.0, 0.5, prob.n_cells))
+    elif case == "hex_q2_heat":
+        prob = O.box_problem(O.HEXAHEDRON, (4, 4, 3), ip_order=2, ncomp=1, qr_order=3, perturb=0.2, seed=23)
+        args = ht
+    elif case == "quad_q2_heat":
+        prob = O.box_problem(O.QUADRILATERAL, (12, 9), ip_order=2, ncomp=1, qr_order=3, perturb=0.2, seed=24)
+        args = ht
+    else:
+        prob = O.box_problem(O.TETRAHEDRON, (4, 3, 3), ip_order=1, ncomp=3, qr_order=1, perturb=0.15, seed=25)
+        args = el
+    _forms_bitwise(fg, O, prob, args)
+
+
+def test_two_phase_neo_hooke_mixed_cells(built, oracle):
+    fg, O = built, oracle
+    prob = mixed_problem(O)
+    u = 0.05 * np.random.default_rng(7).uniform(-1, 1, prob.ndofs)
+    _forms_bitwise(fg, O, prob, dict(physics=fg.NEO_HOOKE, p0=1.0, p1=10.0, u=u))
+
+
+def test_two_phase_q2_against_oracle(built, oracle):
+    """The default form of quadratic elements (two-phase) against the oracle."""
+    fg, O = built, oracle
+    prob = O.box_problem(O.HEXAHEDRON, (3, 3, 2), ip_order=2, ncomp=3, qr_order=3, perturb=0.2, seed=26)
+    E, nu = 200e3, 0.3
+    check(fg, O, prob, dict(physics=fg.LINEAR_ELASTIC, p0=E, p1=nu), dict(physics=O.LINEAR_ELASTIC, p0=E, p1=nu))
