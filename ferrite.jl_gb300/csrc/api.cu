@@ -216,10 +216,11 @@ void set_plan_caps(KernelArgs& A, const Plan& pl) {
     A.out_cap = std::max(pl.max_out, 2);
 }
 
-// The kernel compiled for this problem's subdomains, physics and precision (nullptr: none)
-const KernelEntry* find_kernel(const HostProblem& hp, int phys, bool fp64) {
+// The kernel compiled for this problem's subdomains, physics and precision (nullptr: none);
+// ea_only picks the gather-only form (every subdomain two-phase)
+const KernelEntry* find_kernel(const HostProblem& hp, int phys, bool fp64, bool ea_only = false) {
     for (const KernelEntry& e : registry()) {
-        if (e.phys != phys || e.fp64 != (int)fp64) continue;
+        if (e.phys != phys || e.fp64 != (int)fp64 || e.ea_only != (int)ea_only) continue;
         bool ok = true;
         for (int s = 0; s < MAX_SUB; ++s) {
             if (s < (int)hp.subs.size()) {
@@ -250,6 +251,7 @@ int tile_shape_bytes(const fe_handle* h, const KernelArgs& A, bool fp64) {
 }
 
 int tile_smem(fe_handle* h, const KernelEntry* ke, KernelArgs& A, bool fp64) {
+    if (ke->ea_only) A.node_cap = 0;  // no coordinates in the gather-only form
     const int fixed = smem_layout(A, tile_shape_bytes(h, A, fp64), fp64 ? 8 : 4).chunk;
     device_attributes(h);
     const int budget = h->max_smem - 1024;  // static shared (mbarriers) headroom
@@ -317,10 +319,10 @@ cudaError_t status_reset(fe_handle* h, cudaStream_t st) {
     return e;
 }
 
-// Two CTAs per SM hide each other's record and coordinate waits. The plan's tiles are sized
-// from the staging capacity, but its largest record and node list follow from the mesh (on a
-// lattice-aligned mesh more tiles snap to their upper size), so kernel ke may land just past
-// the two-CTA line. Then re-plan with a slightly smaller capacity, once per kernel; a kernel
+// Two CTAs per SM (three for the gather-only form) hide each other's record and coordinate
+// waits. The plan's tiles are sized from the staging capacity, but its largest record and
+// node list follow from the mesh (on a lattice-aligned mesh more tiles snap to their upper
+// size), so kernel ke may land just past that line. Then re-plan with a slightly smaller capacity, once per kernel; a kernel
 // far past the line (more than a tenth) keeps the plan: smaller tiles would cost more visits
 // than the second CTA wins. Returns FE_OK or a CUDA failure of the upload.
 int fit_plan(fe_handle* h, const KernelEntry* ke, cudaStream_t st, unsigned ea_mask) {
@@ -337,7 +339,7 @@ int fit_plan(fe_handle* h, const KernelEntry* ke, cudaStream_t st, unsigned ea_m
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ke->fn, THREADS, smem) != cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n0, ke->fn, THREADS, 0) != cudaSuccess)
         return FE_OK;
-    const int want = std::min(n0, 2);
+    const int want = std::min(n0, ke->ea_only ? 3 : 2);
     if (n >= want) return FE_OK;
     int per_sm = 0, reserved = 0;
     cudaFuncAttributes fa{};
@@ -664,14 +666,19 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
     const bool do_k = !(p->flags & FE_NO_K), do_f = !(p->flags & FE_NO_F);
     if (do_k && !nzval) return set_error(h, FE_ERR_ARG, "nzval is NULL");
     if (do_f && !f) return set_error(h, FE_ERR_ARG, "f is NULL");
-    const KernelEntry* ke = find_kernel(hp, phys, fp64);
-    if (!ke) return set_error(h, FE_ERR_UNSUPPORTED, "no kernel compiled for this element / quadrature / physics combination");
     // two-phase form per subdomain: quadratic elements by default (their geometry would be
     // recomputed in every tile that owns one of their ~27 dof entities)
     unsigned ea_mask = 0;
-    for (int s = 0; s < (int)hp.subs.size(); ++s)
+    bool all_ea = true;
+    for (int s = 0; s < (int)hp.subs.size(); ++s) {
         if (hp.subs[s].n_cells > 0 && ((p->flags & FE_TWO_PHASE) || (!(p->flags & FE_FUSED) && hp.subs[s].nb > 16)))
             ea_mask |= 1u << s;
+        else if (hp.subs[s].n_cells > 0)
+            all_ea = false;
+    }
+    const KernelEntry* ke = all_ea && ea_mask ? find_kernel(hp, phys, fp64, true) : nullptr;
+    if (!ke) ke = find_kernel(hp, phys, fp64);
+    if (!ke) return set_error(h, FE_ERR_UNSUPPORTED, "no kernel compiled for this element / quadrature / physics combination");
     if (!fp64 && !h->capturing && !h->plan_pinned && (h->fitted_fn != ke->fn || h->fitted_mask != ea_mask)) {
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         if (cudaStreamIsCapturing((cudaStream_t)p->stream, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone) {

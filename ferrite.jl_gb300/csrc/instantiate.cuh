@@ -18,14 +18,15 @@ constexpr int groups_or0() {
     else return THREADS / ElemT<K>::GS;
 }
 
-template <int K0, int Q0, int K1, int Q1, int K2, int Q2, int PH, typename R>
+template <int K0, int Q0, int K1, int Q1, int K2, int Q2, int PH, typename R, bool EAK = false>
 KernelEntry make_entry() {
     KernelEntry e;
+    e.ea_only = EAK ? 1 : 0;
     e.kind[0] = K0; e.kind[1] = K1; e.kind[2] = K2;
     e.nq[0] = Q0; e.nq[1] = Q1; e.nq[2] = Q2;
     e.phys = PH;
     e.fp64 = std::is_same<R, double>::value ? 1 : 0;
-    e.fn = (const void*)&tile_kernel<K0, Q0, K1, Q1, K2, Q2, PH, R>;
+    e.fn = (const void*)&tile_kernel<K0, Q0, K1, Q1, K2, Q2, PH, R, EAK>;
     e.table_bytes[0] = table_bytes_or0<K0, Q0, PH, R>();
     e.table_bytes[1] = table_bytes_or0<K1, Q1, PH, R>();
     e.table_bytes[2] = table_bytes_or0<K2, Q2, PH, R>();
@@ -53,5 +54,10 @@ ElemEntry make_elem_entry() {
     out.push_back(make_entry<K, Q, -1, 0, -1, 0, PH, double>());          \
     eout.push_back(make_elem_entry<K, Q, PH, float>());                   \
     eout.push_back(make_elem_entry<K, Q, PH, double>());
+
+// the gather-only tile kernel of a kind whose default form is two-phase
+#define FE_EA(K, Q, PH)                                                   \
+    out.push_back(make_entry<K, Q, -1, 0, -1, 0, PH, float, true>());     \
+    out.push_back(make_entry<K, Q, -1, 0, -1, 0, PH, double, true>());
 
 }  // namespace fe

@@ -6,6 +6,7 @@ namespace fe {
 void register_elastic(std::vector<KernelEntry>& out, std::vector<ElemEntry>& eout) {
     FE_ONE(KIND_HEX8, 8, PHYS_ELASTIC)
     FE_ONE(KIND_HEX27, 27, PHYS_ELASTIC)
+    FE_EA(KIND_HEX27, 27, PHYS_ELASTIC)
     FE_ONE(KIND_TET4, 1, PHYS_ELASTIC)
     FE_ONE(KIND_TET4, 4, PHYS_ELASTIC)
     FE_ONE(KIND_WEDGE6, 5, PHYS_ELASTIC)

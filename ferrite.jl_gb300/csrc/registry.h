@@ -14,6 +14,7 @@ struct KernelEntry {
     const void* fn;      // __global__ tile_kernel<...>
     int table_bytes[MAX_SUB];  // cell-table bytes per lane group of each slot
     int groups[MAX_SUB];       // lane groups per CTA of each slot
+    int ea_only;               // gather-only form: every subdomain two-phase
 };
 
 // adjoint kernels: one instantiation per (kind, quadrature points, physics, precision)

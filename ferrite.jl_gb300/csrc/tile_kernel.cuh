@@ -800,7 +800,7 @@ __device__ __forceinline__ void gather_blocks(const KernelArgs& a, const SubDev&
 // ---------------------------------------------------------------------------------------
 // the cells of one subdomain in a tile
 // ---------------------------------------------------------------------------------------
-template <int K, int NQ, int PHYS, typename Real>
+template <int K, int NQ, int PHYS, typename Real, bool EAK = false>
 __device__ __forceinline__ void process_segment(const KernelArgs& a, const SubDev& sd, const Real* shp, const RecSeg& g,
                                                 const char* R, const char* xs, Real* stage, char* chunk) {
     using E = ElemT<K>;
@@ -823,7 +823,7 @@ __device__ __forceinline__ void process_segment(const KernelArgs& a, const SubDe
     const uint16_t* gt = (const uint16_t*)(R + g.gt_off);
     const RecTask* tasks = (const RecTask*)(R + H->off_tasks);
     const Real* ea = (const Real*)a.ea[g.sub];
-    if (ea) {
+    if (EAK || ea) {
         // two-phase form: no geometry here, the blocks are loaded
         const int64_t es = a.ea_stride[g.sub];
         for (int pg = grp; grp < ngrp && pg < g.n_grp; pg += ngrp) {
@@ -838,6 +838,7 @@ __device__ __forceinline__ void process_segment(const KernelArgs& a, const SubDe
         }
         return;
     }
+    if constexpr (!EAK) {
     // the plan's groups run on this CTA's groups round robin (the same when the counts agree)
     for (int pg = grp; grp < ngrp && pg < g.n_grp; pg += ngrp) {
         const int t1 = gt[pg + 1];
@@ -852,6 +853,7 @@ __device__ __forceinline__ void process_segment(const KernelArgs& a, const SubDe
                                                lane, tk.item_begin, tk.item_end);
             __syncwarp(gmask);  // the next task overwrites the table
         }
+    }
     }
 }
 
@@ -1118,8 +1120,10 @@ __device__ __forceinline__ void gather_nodes(const KernelArgs& a, const char* R,
 // ---------------------------------------------------------------------------------------
 // the kernel: persistent CTAs, tiles blockIdx.x + it * gridDim.x
 // ---------------------------------------------------------------------------------------
-template <int K0, int Q0, int K1, int Q1, int K2, int Q2, int PHYS, typename Real>
-__global__ void __launch_bounds__(THREADS, 2) tile_kernel(const KernelArgs a, const Real* __restrict__ shape_g, int shape_bytes,
+// EAK: the gather-only form for subdomains whose element matrices all come precomputed (no
+// geometry code, no coordinates; fewer registers, so three CTAs share an SM)
+template <int K0, int Q0, int K1, int Q1, int K2, int Q2, int PHYS, typename Real, bool EAK = false>
+__global__ void __launch_bounds__(THREADS, EAK ? 3 : 2) tile_kernel(const KernelArgs a, const Real* __restrict__ shape_g, int shape_bytes,
                                                            int shape_off1, int shape_off2) {
     extern __shared__ __align__(128) char smem_raw[];
     __shared__ __align__(8) unsigned long long bars[1 + REC_RING];  // shape tables, record ring
@@ -1161,7 +1165,8 @@ __global__ void __launch_bounds__(THREADS, 2) tile_kernel(const KernelArgs a, co
     __syncthreads();  // the initialised barriers are visible to every thread
     // node coordinates are needed unless every subdomain's element matrices come precomputed
     bool geo = false;
-    for (int s = 0; s < a.n_sub; ++s) geo |= a.ea[s] == nullptr;
+    if constexpr (!EAK)
+        for (int s = 0; s < a.n_sub; ++s) geo |= a.ea[s] == nullptr;
     bool failed = false;
     if (t < a.n_tiles) {
         if (!mbar_wait(rec_bar(0), 0, WAIT_LIMIT)) failed = true;
@@ -1193,13 +1198,13 @@ __global__ void __launch_bounds__(THREADS, 2) tile_kernel(const KernelArgs a, co
             const RecSeg g = ((const RecSeg*)(R + sizeof(RecHead)))[gi];
             static_assert(sizeof(RecSeg) % 16 == 0, "segment entries are 16-byte multiples");
             if (g.sub == 0) {
-                process_segment<K0, Q0, PHYS, Real>(a, a.sub[0], shape, g, R, xs, stage, chunk);
+                process_segment<K0, Q0, PHYS, Real, EAK>(a, a.sub[0], shape, g, R, xs, stage, chunk);
             } else if constexpr (K1 >= 0) {
                 if (g.sub == 1) {
-                    process_segment<K1, Q1, PHYS, Real>(a, a.sub[1], (const Real*)((const char*)shape + shape_off1), g, R, xs,
+                    process_segment<K1, Q1, PHYS, Real, EAK>(a, a.sub[1], (const Real*)((const char*)shape + shape_off1), g, R, xs,
                                                         stage, chunk);
                 } else if constexpr (K2 >= 0) {
-                    process_segment<K2, Q2, PHYS, Real>(a, a.sub[2], (const Real*)((const char*)shape + shape_off2), g, R, xs,
+                    process_segment<K2, Q2, PHYS, Real, EAK>(a, a.sub[2], (const Real*)((const char*)shape + shape_off2), g, R, xs,
                                                         stage, chunk);
                 }
             }
