@@ -204,15 +204,18 @@ struct KernelArgs {
     int32_t chunk_bytes;     // bytes of the per-group cell table buffers of the launched kernel
     int32_t groups[MAX_SUB]; // lane groups (cells in flight) per CTA, per subdomain
     // two-phase form: per-cell element matrices of each subdomain (nullptr: computed in the
-    // tiles), [cell][j][t][i] then fe [x][i], ea_stride values per cell (ea_layout below)
+    // tiles), [cell][j][t][i] (column stride ea_col_values) then fe [x][i], ea_stride values
+    // per cell (ea_cell_values)
     const void* ea[MAX_SUB];
     int64_t ea_stride[MAX_SUB];
 };
 
-// values per cell of the element-matrix scratch: nb*nb blocks of nc*nc entries, then nb*nc
-// load entries, rounded up to 16 bytes of FP32
+// values of one column j (nb rows of nc*nc entries) of a cell's element matrix in the
+// two-phase scratch, rounded up to 16 bytes of FP32 so that every column is one aligned copy
+__host__ __device__ constexpr int ea_col_values(int nb, int nc) { return (nb * nc * nc + 3) / 4 * 4; }
+// values per cell: nb columns, then nb*nc load entries, rounded up to 16 bytes of FP32
 __host__ __device__ constexpr int64_t ea_cell_values(int nb, int nc) {
-    return ((int64_t)nb * nb * nc * nc + (int64_t)nb * nc + 3) / 4 * 4;
+    return ((int64_t)nb * ea_col_values(nb, nc) + (int64_t)nb * nc + 3) / 4 * 4;
 }
 
 }  // namespace fe

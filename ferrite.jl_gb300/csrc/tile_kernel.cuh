@@ -618,16 +618,16 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
     // cell's element matrix, [j][t][i] with t = y nc + x, then the load entries [x][i]
     auto store_block = [&](int j, int fslot, int slot, const Real* Kb, const Real* fe) {
         if constexpr (EA) {
-            constexpr int NCC = nc * nc;
+            constexpr int JS = ea_col_values(NB, nc);
             if (a.do_k) {
                 #pragma unroll
                 for (int y = 0; y < nc; ++y)
                     #pragma unroll
-                    for (int x = 0; x < nc; ++x) ea_out[(j * NCC + y * nc + x) * NB + i] = Kb[x * NC_MAX + y];
+                    for (int x = 0; x < nc; ++x) ea_out[j * JS + (y * nc + x) * NB + i] = Kb[x * NC_MAX + y];
             }
             if (a.do_f && i == j) {
                 #pragma unroll
-                for (int x = 0; x < nc; ++x) ea_out[NB * NB * NCC + x * NB + i] = fe[x];
+                for (int x = 0; x < nc; ++x) ea_out[NB * JS + x * NB + i] = fe[x];
             }
         } else {
             stage_block<NC_MAX, nc, Real>(a, sd, stage, f_off, cell, i, j, fslot, slot, Kb, fe);
@@ -771,7 +771,7 @@ __device__ __forceinline__ void gather_blocks(const KernelArgs& a, const SubDev&
     using E = ElemT<K>;
     constexpr int NB = E::NB, NC_MAX = E::DIM;
     constexpr int nc = PHYS == PHYS_HEAT ? 1 : E::DIM;
-    constexpr int NCC = nc * nc;
+    constexpr int JS = ea_col_values(NB, nc);
     const uint32_t* items = (const uint32_t*)(R + ((const RecHead*)R)->off_items);
     #pragma unroll 2
     for (int it = it0; it < it1; ++it) {
@@ -786,11 +786,11 @@ __device__ __forceinline__ void gather_blocks(const KernelArgs& a, const SubDev&
             #pragma unroll
             for (int y = 0; y < nc; ++y)
                 #pragma unroll
-                for (int x = 0; x < nc; ++x) Kb[x * NC_MAX + y] = __ldcs(ea + (j * NCC + y * nc + x) * NB + i);
+                for (int x = 0; x < nc; ++x) Kb[x * NC_MAX + y] = __ldcs(ea + j * JS + (y * nc + x) * NB + i);
         }
         if (a.do_f && i == j) {
             #pragma unroll
-            for (int x = 0; x < nc; ++x) fe[x] = __ldcs(ea + NB * NB * NCC + x * NB + i);
+            for (int x = 0; x < nc; ++x) fe[x] = __ldcs(ea + NB * JS + x * NB + i);
         }
         stage_block<NC_MAX, nc, Real>(a, sd, stage, f_off, cell, i, j, (int)(word >> 16), slot_rows[(it - it0) * NB + i], Kb,
                                       fe);
@@ -1190,6 +1190,7 @@ __global__ void __launch_bounds__(THREADS, EAK ? 3 : 2) tile_kernel(const Kernel
                 failed = true;
             else if (geo)
                 gather_nodes<Real>(a, rec_ring + nb * rec_stride, xs_ring + ((it + 1) & 1) * xs_stride);
+
         }
         const RecHead* H = (const RecHead*)R;
         const int n_seg = H->n_seg;
