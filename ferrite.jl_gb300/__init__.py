@@ -42,7 +42,7 @@ _FORMS = {None: 0, "two_phase": TWO_PHASE, "fused": FUSED}
 EXPORTED = ["fe_abi_version", "fe_create", "fe_assemble", "fe_sync", "fe_last_error", "fe_get_info",
             "fe_get_index_map", "fe_plan_dry_run", "fe_distribute_dofs", "fe_sparsity_pattern", "fe_kernel_time", "fe_assemble_noalloc",
             "fe_assemble_adjoint", "fe_graph_capture", "fe_graph_replay", "fe_graph_destroy",
-            "fe_autotune", "fe_destroy"]
+            "fe_autotune", "fe_assemble_elements", "fe_destroy"]
 
 i64p = ctypes.POINTER(ctypes.c_int64)
 f64p = ctypes.POINTER(ctypes.c_double)
@@ -71,6 +71,11 @@ class AssembleParams(ctypes.Structure):
                 ("p0", ctypes.c_double), ("p1", ctypes.c_double), ("body", ctypes.c_double * 3),
                 ("cell_scale", ctypes.c_void_p), ("u", ctypes.c_void_p), ("cond_threshold", ctypes.c_double),
                 ("stream", ctypes.c_void_p)]
+
+
+class ElementLayout(ctypes.Structure):
+    """fe_element_layout: element strides of Ke(cell, I, J) and fe(cell, I)."""
+    _fields_ = [("ke_stride", ctypes.c_int64 * 3), ("fe_stride", ctypes.c_int64 * 2)]
 
 
 class AdjointParams(ctypes.Structure):
@@ -138,6 +143,8 @@ def lib():
                                           ctypes.POINTER(DofDesc), i64p, i64p, i64p]
         L.fe_kernel_time.argtypes = [ctypes.c_void_p, f64p, i64p]
         L.fe_assemble_noalloc.argtypes = [ctypes.c_void_p, ctypes.POINTER(AssembleParams), ctypes.c_void_p, ctypes.c_void_p]
+        L.fe_assemble_elements.argtypes = [ctypes.c_void_p, ctypes.POINTER(AssembleParams), ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.POINTER(ElementLayout)]
         L.fe_assemble_adjoint.argtypes = [ctypes.c_void_p, ctypes.POINTER(AdjointParams), ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p, ctypes.c_void_p]
         L.fe_graph_capture.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(AssembleParams),
@@ -326,6 +333,32 @@ class Handle:
         if rc != FE_OK:
             self._raise(rc)
         return nzval, f
+
+    def assemble_elements(self, ke, fe, physics: int, p0: float, p1: float, ke_stride=None, fe_stride=None,
+                          stream=None, sync: bool = True, **kw):
+        """fe_assemble_elements: every cell's Ke and fe into device arrays (torch CUDA tensors,
+        float32 for mixed precision, float64 for FP64). Default layout: ke[n_cells, nbf, nbf] and
+        fe[n_cells, nbf] row-major, i.e. ke[c, I, J] (the strides of ke.stride() / fe.stride())."""
+        if stream is not None and hasattr(stream, "cuda_stream"):
+            stream = stream.cuda_stream
+        p = self._params(physics, p0, p1, stream=stream, **kw)
+        if ke is None:
+            p.flags |= NO_K
+        if fe is None:
+            p.flags |= NO_F
+        if not sync:
+            p.flags |= ASYNC
+        lay = ElementLayout()
+        ks = ke_stride if ke_stride is not None else (tuple(ke.stride()) if ke is not None else (0, 0, 0))
+        fs = fe_stride if fe_stride is not None else (tuple(fe.stride()) if fe is not None else (0, 0))
+        for k in range(3):
+            lay.ke_stride[k] = int(ks[k])
+        for k in range(2):
+            lay.fe_stride[k] = int(fs[k])
+        rc = lib().fe_assemble_elements(self._h, ctypes.byref(p), _ptr(ke), _ptr(fe), ctypes.byref(lay))
+        if rc != FE_OK:
+            self._raise(rc)
+        return ke, fe
 
     def adjoint(self, u, lam, d_rho, d_X, physics: int, p0: float, p1: float, body=(0.0, 0.0, 0.0), cell_scale=None,
                 dscale=None, precision: int = PREC_MIXED, stream=None, sync: bool = True):

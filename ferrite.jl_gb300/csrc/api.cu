@@ -381,6 +381,40 @@ int fit_plan(fe_handle* h, const KernelEntry* ke, cudaStream_t st, unsigned ea_m
     return FE_OK;
 }
 
+// One element_kernel launch over the cells of subdomain s: into the two-phase scratch, or
+// (to_caller) into the caller's element arrays
+int launch_elements(fe_handle* h, const KernelArgs& A, int s, int phys, bool fp64, cudaStream_t st, const EaOut& eo,
+                    bool to_caller) {
+    cudaError_t e;
+    const SubDev& sd = A.sub[s];
+    const ElemEntry* ee = find_elem(sd.kind, sd.nq, phys, fp64);
+    if (!ee) return set_error(h, FE_ERR_UNSUPPORTED, "no element kernel compiled for this element / physics");
+    const void* fn = to_caller ? ee->fn_out : ee->fn;
+    const int pi = fp64 ? 1 : 0;
+    const int o1 = h->shape_off1[pi], o2 = h->shape_off2[pi], sb = h->shape_bytes[pi];
+    const int off = s == 0 ? 0 : (s == 1 ? o1 : o2);
+    const int end = s + 1 < A.n_sub ? (s == 0 ? o1 : o2) : sb;
+    int sub_bytes = end - off;
+    device_attributes(h);
+    const int esmem = ((sub_bytes + 15) & ~15) + ee->groups * ee->group_bytes;
+    if (esmem > h->max_smem - 1024) return set_error(h, FE_ERR_UNSUPPORTED, "element tables do not fit in shared memory");
+    if ((e = ensure_smem_attribute(fn, esmem)) != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute");
+    int per_sm = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, THREADS, esmem)) != cudaSuccess)
+        return cuda_fail(h, e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    const int64_t need = (sd.n_cells + ee->groups - 1) / ee->groups;
+    const int64_t egrid = std::min<int64_t>(need, (int64_t)std::max(per_sm, 1) * std::max(h->n_sm, 1));
+    if (egrid <= 0) return FE_OK;
+    SubDev sdv = sd;
+    const void* eshp = (const char*)(fp64 ? (const void*)h->shape_d : (const void*)h->shape_f) + off;
+    EaOut eov = eo;
+    KernelArgs Av = A;
+    void* eargs[] = {(void*)&Av, (void*)&sdv, (void*)&eshp, (void*)&sub_bytes, (void*)&eov};
+    e = cudaLaunchKernel(fn, dim3((unsigned)egrid), dim3(THREADS), eargs, (size_t)esmem, st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "element kernel launch");
+    return FE_OK;
+}
+
 // Shared-memory sizing, status reset and the launch of one assembly: persistent CTAs, as
 // many as fit on the device at once (never more than there are tiles).
 int launch_assembly(fe_handle* h, const KernelEntry* ke, KernelArgs& A, bool fp64, cudaStream_t st,
@@ -410,28 +444,9 @@ int launch_assembly(fe_handle* h, const KernelEntry* ke, KernelArgs& A, bool fp6
     // two-phase form: the element matrices of those subdomains first
     for (int s = 0; s < A.n_sub; ++s) {
         if (!A.ea[s]) continue;
-        const SubDev& sd = A.sub[s];
-        const ElemEntry* ee = find_elem(sd.kind, sd.nq, ke->phys, fp64);
-        if (!ee) return set_error(h, FE_ERR_UNSUPPORTED, "no element kernel compiled for this element / physics");
-        const int off = s == 0 ? 0 : (s == 1 ? o1 : o2);
-        const int end = s + 1 < A.n_sub ? (s == 0 ? o1 : o2) : sb;
-        int sub_bytes = end - off;
-        const int esmem = ((sub_bytes + 15) & ~15) + ee->groups * ee->group_bytes;
-        if (esmem > h->max_smem - 1024) return set_error(h, FE_ERR_UNSUPPORTED, "element tables do not fit in shared memory");
-        if ((e = ensure_smem_attribute(ee->fn, esmem)) != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute");
-        int per_sm = 0;
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ee->fn, THREADS, esmem)) != cudaSuccess)
-            return cuda_fail(h, e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
-        const int64_t need = (sd.n_cells + ee->groups - 1) / ee->groups;
-        const int64_t egrid = std::min<int64_t>(need, (int64_t)std::max(per_sm, 1) * std::max(n_sm, 1));
-        if (egrid <= 0) continue;
-        SubDev sdv = sd;
-        const void* eshp = (const char*)shp + off;
-        void* out = const_cast<void*>(A.ea[s]);
-        int64_t stride = A.ea_stride[s];
-        void* eargs[] = {(void*)&A, (void*)&sdv, (void*)&eshp, (void*)&sub_bytes, (void*)&out, (void*)&stride};
-        e = cudaLaunchKernel(ee->fn, dim3((unsigned)egrid), dim3(THREADS), eargs, (size_t)esmem, st);
-        if (e != cudaSuccess) return cuda_fail(h, e, "element kernel launch");
+        EaOut eo{const_cast<void*>(A.ea[s]), nullptr, {A.ea_stride[s], 0, 0}, {0, 0}};
+        const int rc = launch_elements(h, A, s, ke->phys, fp64, st, eo, false);
+        if (rc != FE_OK) return rc;
     }
     if (grid > 0) {
         e = cudaLaunchKernel(ke->fn, dim3((unsigned)grid), dim3(THREADS), args, (size_t)smem, st);
@@ -639,7 +654,9 @@ int fe_sync(fe_handle* h) {
     return finish_status(h);
 }
 
-int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double* f) {
+// fe_assemble, or with eo the element assembly of fe_assemble_elements (no global matrix:
+// every cell's Ke and fe into the caller's device arrays)
+static int assemble_common(fe_handle* h, const fe_assemble_params* p, double* nzval, double* f, const EaOut* eo) {
     if (!h || !p) return FE_ERR_ARG;
     const HostProblem& hp = h->hp;
     const int nc = hp.nc;
@@ -664,13 +681,20 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
     if (p->precision != FE_PREC_MIXED && p->precision != FE_PREC_FP64) return set_error(h, FE_ERR_ARG, "unknown precision");
     const bool fp64 = p->precision == FE_PREC_FP64;
     const bool do_k = !(p->flags & FE_NO_K), do_f = !(p->flags & FE_NO_F);
-    if (do_k && !nzval) return set_error(h, FE_ERR_ARG, "nzval is NULL");
-    if (do_f && !f) return set_error(h, FE_ERR_ARG, "f is NULL");
+    if (eo) {
+        if (do_k && !eo->ke) return set_error(h, FE_ERR_ARG, "ke is NULL");
+        if (do_f && !eo->fe) return set_error(h, FE_ERR_ARG, "fe is NULL");
+        if ((do_k && !is_device_ptr(eo->ke)) || (do_f && !is_device_ptr(eo->fe)))
+            return set_error(h, FE_ERR_ARG, "element arrays must be device memory");
+    } else {
+        if (do_k && !nzval) return set_error(h, FE_ERR_ARG, "nzval is NULL");
+        if (do_f && !f) return set_error(h, FE_ERR_ARG, "f is NULL");
+    }
     // two-phase form per subdomain: quadratic elements by default (their geometry would be
     // recomputed in every tile that owns one of their ~27 dof entities)
     unsigned ea_mask = 0;
     bool all_ea = true;
-    for (int s = 0; s < (int)hp.subs.size(); ++s) {
+    for (int s = 0; s < (int)hp.subs.size() && !eo; ++s) {
         if (hp.subs[s].n_cells > 0 && ((p->flags & FE_TWO_PHASE) || (!(p->flags & FE_FUSED) && hp.subs[s].nb > 16)))
             ea_mask |= 1u << s;
         else if (hp.subs[s].n_cells > 0)
@@ -679,7 +703,7 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
     const KernelEntry* ke = all_ea && ea_mask ? find_kernel(hp, phys, fp64, true) : nullptr;
     if (!ke) ke = find_kernel(hp, phys, fp64);
     if (!ke) return set_error(h, FE_ERR_UNSUPPORTED, "no kernel compiled for this element / quadrature / physics combination");
-    if (!fp64 && !h->capturing && !h->plan_pinned && (h->fitted_fn != ke->fn || h->fitted_mask != ea_mask)) {
+    if (!eo && !fp64 && !h->capturing && !h->plan_pinned && (h->fitted_fn != ke->fn || h->fitted_mask != ea_mask)) {
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         if (cudaStreamIsCapturing((cudaStream_t)p->stream, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone) {
             const int rc = fit_plan(h, ke, (cudaStream_t)p->stream, ea_mask);
@@ -690,15 +714,15 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
         // inside fe_graph_capture: device buffers only, the capture stream, no host work
         if ((cudaStream_t)p->stream != h->cap_stream) return set_error(h, FE_ERR_STATE, "capture: steps run on the capture stream");
         if (p->flags & FE_PROFILE) return set_error(h, FE_ERR_STATE, "capture: FE_PROFILE is not capturable");
-        if ((do_k && !is_device_ptr(nzval)) || (do_f && !is_device_ptr(f)) || (p->u && !is_device_ptr(p->u)) ||
+        if ((!eo && ((do_k && !is_device_ptr(nzval)) || (do_f && !is_device_ptr(f)))) || (p->u && !is_device_ptr(p->u)) ||
             (p->cell_scale && !is_device_ptr(p->cell_scale)))
             return set_error(h, FE_ERR_STATE, "capture: nzval, f, u and cell_scale must be device memory");
     } else if (h->pending) {
         // An FE_ASYNC assembly on the same stream with device outputs is still running: keep
         // its status and let this one add to it (fe_sync reports both), without waiting.
         // Anything else waits for it first.
-        const bool chain = (cudaStream_t)p->stream == h->last_stream && (!do_k || is_device_ptr(nzval)) &&
-                           (!do_f || is_device_ptr(f));
+        const bool chain = (cudaStream_t)p->stream == h->last_stream &&
+                           (eo || ((!do_k || is_device_ptr(nzval)) && (!do_f || is_device_ptr(f))));
         if (chain) {
             h->accumulate_status = 1;
         } else {
@@ -710,8 +734,8 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
     cudaError_t e;
     KernelArgs A = h->base;
     // outputs: device pointers are written in place, host pointers are staged
-    const bool nz_dev = do_k && is_device_ptr(nzval);
-    const bool f_dev = do_f && is_device_ptr(f);
+    const bool nz_dev = eo || (do_k && is_device_ptr(nzval));
+    const bool f_dev = eo || (do_f && is_device_ptr(f));
     const bool fill = (p->flags & FE_FILLZERO) != 0;
     if (do_k && !nz_dev) {
         if (!h->nz_stage && (e = h->alloc(&h->nz_stage, hp.nnz)) != cudaSuccess) return cuda_fail(h, e, "alloc nzval");
@@ -723,8 +747,8 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
         if (!fill && (e = cudaMemcpyAsync(h->f_stage, f, hp.ndofs * 8, cudaMemcpyHostToDevice, st)) != cudaSuccess)
             return cuda_fail(h, e, "copy f");
     }
-    A.nzval = do_k ? (nz_dev ? nzval : h->nz_stage) : nullptr;
-    A.f = do_f ? (f_dev ? f : h->f_stage) : nullptr;
+    A.nzval = do_k && !eo ? (nz_dev ? nzval : h->nz_stage) : nullptr;
+    A.f = do_f && !eo ? (f_dev ? f : h->f_stage) : nullptr;
     A.do_k = do_k;
     A.do_f = do_f;
     A.fillzero = fill;
@@ -811,7 +835,20 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
             return cuda_fail(h, e, "cudaEventCreate");
         }
     }
-    {
+    if (eo) {
+        // element assembly: status reset, then the element kernels of every subdomain
+        if (!h->capturing && !h->accumulate_status && (e = status_reset(h, st)) != cudaSuccess)
+            return cuda_fail(h, e, "status reset");
+        A.status = h->status_d;
+        if (prof) cudaEventRecord(ev.first, st);
+        int rc = FE_OK;
+        for (int s = 0; s < A.n_sub && rc == FE_OK; ++s) rc = launch_elements(h, A, s, ke->phys, fp64, st, *eo, true);
+        if (prof) {
+            cudaEventRecord(ev.second, st);
+            (rc == FE_OK ? h->prof_events : h->prof_pool).push_back(ev);
+        }
+        if (rc != FE_OK) return rc;
+    } else {
         const int rc = launch_assembly(h, ke, A, fp64, st, prof ? &ev : nullptr);
         if (prof) (rc == FE_OK ? h->prof_events : h->prof_pool).push_back(ev);
         if (rc != FE_OK) return rc;
@@ -828,6 +865,17 @@ int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double
     const bool host_out = (do_k && !nz_dev) || (do_f && !f_dev);
     if ((p->flags & FE_ASYNC) && !host_out) return FE_OK;
     return fe_sync(h);
+}
+
+int fe_assemble(fe_handle* h, const fe_assemble_params* p, double* nzval, double* f) {
+    return assemble_common(h, p, nzval, f, nullptr);
+}
+
+int fe_assemble_elements(fe_handle* h, const fe_assemble_params* p, void* ke, void* fe, const fe_element_layout* layout) {
+    if (!h || !p || !layout) return FE_ERR_ARG;
+    EaOut eo{ke, fe, {layout->ke_stride[0], layout->ke_stride[1], layout->ke_stride[2]},
+             {layout->fe_stride[0], layout->fe_stride[1]}};
+    return assemble_common(h, p, nullptr, nullptr, &eo);
 }
 
 int fe_assemble_adjoint(fe_handle* h, const fe_adjoint_params* p, const double* u, const double* lambda, double* d_rho,

@@ -210,6 +210,16 @@ struct KernelArgs {
     int64_t ea_stride[MAX_SUB];
 };
 
+// where element_kernel writes: the two-phase scratch (ke = base, ks[0] = values per cell) or
+// the caller's arrays, Ke(cell, I, J) at ke[cell ks[0] + I ks[1] + J ks[2]] and fe(cell, I) at
+// fe[cell fs[0] + I fs[1]] (cell = Ferrite cell id - 1, I = nc * base function + component)
+struct EaOut {
+    void* ke;
+    void* fe;
+    int64_t ks[3];
+    int64_t fs[2];
+};
+
 // values of one column j (nb rows of nc*nc entries) of a cell's element matrix in the
 // two-phase scratch, rounded up to 16 bytes of FP32 so that every column is one aligned copy
 __host__ __device__ constexpr int ea_col_values(int nb, int nc) { return (nb * nc * nc + 3) / 4 * 4; }

@@ -43,7 +43,8 @@ ElemEntry make_elem_entry() {
     e.nq = Q;
     e.phys = PH;
     e.fp64 = std::is_same<R, double>::value ? 1 : 0;
-    e.fn = (const void*)&element_kernel<K, Q, PH, R>;
+    e.fn = (const void*)&element_kernel<K, Q, PH, R, 1>;
+    e.fn_out = (const void*)&element_kernel<K, Q, PH, R, 2>;
     e.group_bytes = EaGroup<K, Q, PH, R>::BYTES;
     e.groups = THREADS / ElemT<K>::GS;
     return e;

@@ -577,10 +577,10 @@ __device__ __forceinline__ void stage_block(const KernelArgs& a, const SubDev& s
     }
 }
 
-template <int K, int NQ, int PHYS, typename Real, bool EA = false>
+template <int K, int NQ, int PHYS, typename Real, int EA = 0>
 __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& sd, const char* R, const uint16_t* slot_rows,
                                             Real* stage, int f_off, const Real* tb, const Real* shp, int cell, int i, int it0,
-                                            int it1, Real* ea_out = nullptr) {
+                                            int it1, Real* ea_out = nullptr, const EaOut* eo = nullptr) {
     using E = ElemT<K>;
     using CT = CellTable<K, NQ, PHYS, Real>;
     using P = typename Pair<Real>::type;
@@ -595,7 +595,7 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
     const Real* cellp = sq + CT::SQ;
     const Real* neo = cellp + 4;
     const uint32_t* items = nullptr;
-    if constexpr (!EA) items = (const uint32_t*)(R + ((const RecHead*)R)->off_items);
+    if constexpr (EA == 0) items = (const uint32_t*)(R + ((const RecHead*)R)->off_items);
     P gi[CACHE ? NQP : 1][3];
     if constexpr (CACHE) {
         #pragma unroll
@@ -614,10 +614,25 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
             }
         }
     }
-    // phase B: the block goes to the tile's staging slot; element-assembly form (EA): to the
-    // cell's element matrix, [j][t][i] with t = y nc + x, then the load entries [x][i]
+    // EA 0: the block goes to the tile's staging slot; EA 1: to the cell's element matrix in
+    // the two-phase scratch, [j][t][i] with t = y nc + x, then the load entries [x][i]; EA 2:
+    // to the caller's element arrays (strides in eo)
     auto store_block = [&](int j, int fslot, int slot, const Real* Kb, const Real* fe) {
-        if constexpr (EA) {
+        if constexpr (EA == 2) {
+            const int64_t cid = sd.cellid[cell];
+            if (a.do_k) {
+                Real* ko = (Real*)eo->ke + cid * eo->ks[0];
+                #pragma unroll
+                for (int y = 0; y < nc; ++y)
+                    #pragma unroll
+                    for (int x = 0; x < nc; ++x) ko[(i * nc + x) * eo->ks[1] + (j * nc + y) * eo->ks[2]] = Kb[x * NC_MAX + y];
+            }
+            if (a.do_f && i == j) {
+                Real* fo = (Real*)eo->fe + cid * eo->fs[0];
+                #pragma unroll
+                for (int x = 0; x < nc; ++x) fo[(i * nc + x) * eo->fs[1]] = fe[x];
+            }
+        } else if constexpr (EA == 1) {
             constexpr int JS = ea_col_values(NB, nc);
             if (a.do_k) {
                 #pragma unroll
@@ -641,7 +656,7 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
             int jm[M], fsm[M], slm[M];
             #pragma unroll
             for (int m = 0; m < M; ++m) {
-                if constexpr (EA) {
+                if constexpr (EA != 0) {
                     jm[m] = it + m;  // every column of the cell
                     fsm[m] = slm[m] = 0;
                 } else {
@@ -714,7 +729,7 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
     } else {  // PHYS_NEO: per item and point, scalar
         for (int it = it0; it < it1; ++it) {
             int j = it, fslot = 0, slot = 0;
-            if constexpr (!EA) {
+            if constexpr (EA == 0) {
                 const uint32_t word = items[it];
                 j = (int)(word & 0xFF);
                 fslot = (int)(word >> 16);
@@ -1253,9 +1268,10 @@ __host__ __device__ constexpr int element_smem_bytes(int shape_bytes) {
     return pad16(shape_bytes) + (THREADS / ElemT<K>::GS) * EaGroup<K, NQ, PHYS, Real>::BYTES;
 }
 
-template <int K, int NQ, int PHYS, typename Real>
+// MODE 1: into the two-phase scratch; MODE 2: into the caller's arrays (EaOut strides)
+template <int K, int NQ, int PHYS, typename Real, int MODE>
 __global__ void __launch_bounds__(THREADS, 2) element_kernel(const KernelArgs a, const SubDev sd, const Real* __restrict__ shape_g,
-                                                              int shape_bytes, Real* __restrict__ out, int64_t stride) {
+                                                              int shape_bytes, const EaOut eo) {
     using E = ElemT<K>;
     using EG = EaGroup<K, NQ, PHYS, Real>;
     constexpr int NB = E::NB, NG = E::NG, GS = E::GS, NGRP = THREADS / GS;
@@ -1298,8 +1314,8 @@ __global__ void __launch_bounds__(THREADS, 2) element_kernel(const KernelArgs a,
         geometry_lanes<K, NQ, PHYS, Real>(a, sd, shape, (int)c, cn, xs, nodes, lane, gmask, gbase, tb);
         __syncwarp(gmask);
         if (lane < NB)
-            cell_blocks<K, NQ, PHYS, Real, true>(a, sd, nullptr, nullptr, nullptr, 0, tb, shape, (int)c, lane, 0, NB,
-                                                 out + c * stride);
+            cell_blocks<K, NQ, PHYS, Real, MODE>(a, sd, nullptr, nullptr, nullptr, 0, tb, shape, (int)c, lane, 0, NB,
+                                                 (Real*)eo.ke + c * eo.ks[0], &eo);
         __syncwarp(gmask);  // the next cell overwrites the table and the coordinates
     }
 }

@@ -174,6 +174,27 @@ int fe_create(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain
  */
 int fe_assemble(fe_handle* h, const fe_assemble_params* params, double* nzval, double* f);
 
+/*
+ * fe_assemble_elements: element assembly without the global matrix, the "Element Assembly"
+ * kernel of docs/src/literate-howto/gpu_assembly.jl:270-303 (per cell reinit!, fill!(Ke, 0),
+ * assemble_element!(Ke, fe, cv) into Kes[cellid, :, :] and fes[cellid, :]). Every cell's Ke and
+ * fe go to the caller's DEVICE arrays: Ke(c, I, J) at ke[c*ke_stride[0] + I*ke_stride[1] +
+ * J*ke_stride[2]], fe(c, I) at fe[c*fe_stride[0] + I*fe_stride[1]], with c = cell id - 1 and
+ * I, J = local dof index - 1 (Ferrite's order: vector dofs interleaved, I = n_components *
+ * base function + component). Elements are float for FE_PREC_MIXED and double for
+ * FE_PREC_FP64; strides count elements. The how-to's Kes = zeros(Float32, ncells, nbf, nbf)
+ * (column-major) has ke_stride = {1, ncells, ncells*nbf} and fe_stride = {1, ncells}.
+ * Physics, flags (FE_NO_K, FE_NO_F, FE_ASYNC, FE_PROFILE), cell_scale, u and errors (detJ) are
+ * those of fe_assemble; entries of cells not in any subdomain are left untouched.
+ */
+typedef struct {
+    int64_t ke_stride[3];
+    int64_t fe_stride[2];
+} fe_element_layout;
+
+int fe_assemble_elements(fe_handle* h, const fe_assemble_params* params, void* ke, void* fe,
+                         const fe_element_layout* layout);
+
 /* Wait for queued work of the handle and return the status of the last assembly. */
 int fe_sync(fe_handle* h);
 
