@@ -304,7 +304,7 @@ def run_ours(args):
     if rank == 0 and not args.skip_configs:
         configs = {}
         for name, fn in (("heat", config_heat), ("q2", config_q2), ("adjoint", config_adjoint),
-                         ("mixed_graph", config_mixed_graph)):
+                         ("mixed_graph", config_mixed_graph), ("elements", config_elements)):
             try:
                 configs[name] = fn(fg, stream)
             except Exception as exc:  # reported, not fatal: the headline line still prints
@@ -465,6 +465,31 @@ def config_q2(fg, stream, nel=64, reps=5):
            "tiles": info["n_tiles"], "cell_visits_per_cell": info["n_cell_visits"] / dh.n_cells,
            "setup_s": {"host": t1 - t0, "fe_create": t2 - t1},
            "path": "CUDA cores (FP32 element math, per-tile geometry recompute); no tensor-core path"}
+    h.close()
+    return out
+
+
+def config_elements(fg, stream, nel=64, reps=10):
+    """Element assembly (fe_assemble_elements, the GPU how-to's Kes/fes) of Q1 hex elasticity
+    on the perturbed unit cube: FP32 Ke per cell, per-cell contiguous (Kes[c, I, J] row-major)
+    and the how-to's cell-fastest layout (Julia Kes[ncells, nbf, nbf])."""
+    import torch
+    host = __import__("ferrite_gb300.host", fromlist=["host"])
+    n3 = (nel, nel, nel)
+    g = host.generate_grid(host.HEXAHEDRON, n3, (0, 0, 0), (1, 1, 1))
+    g = host.perturb_interior(g, n3, 0.2, SEED, (0, 0, 0), (1, 1, 1))
+    dh = host.DofHandler.from_grid(g, ip_order=1, n_components=3).close()
+    colptr, rowval = dh.allocate_matrix()
+    h = dh.handle([host.CellValues(host.HEXAHEDRON, 1, 2)], colptr, rowval)
+    n, nbf = dh.n_cells, 24
+    ke = torch.empty((n, nbf, nbf), dtype=torch.float32, device="cuda")
+    fe = torch.empty((n, nbf), dtype=torch.float32, device="cuda")
+    kw = dict(physics=fg.LINEAR_ELASTIC, p0=E_MOD, p1=NU, body=BODY, stream=stream, sync=False)
+    out = {"workload": f"hex{nel}_q1_elasticity_elements", "cells": n, "bytes_out": (ke.numel() + fe.numel()) * 4}
+    for name, ks, fs in (("cell_major", None, None), ("cell_fastest", (1, n, n * nbf), (1, n))):
+        ms = _timed(stream, lambda: h.assemble_elements(ke, fe, ke_stride=ks, fe_stride=fs, **kw), reps)
+        h.sync()
+        out[name] = {"ms": ms, "Melem_s": n / (ms * 1e-3) / 1e6, "write_GBs": out["bytes_out"] / (ms * 1e-3) / 1e9}
     h.close()
     return out
 

@@ -42,7 +42,8 @@ _FORMS = {None: 0, "two_phase": TWO_PHASE, "fused": FUSED}
 EXPORTED = ["fe_abi_version", "fe_create", "fe_assemble", "fe_sync", "fe_last_error", "fe_get_info",
             "fe_get_index_map", "fe_plan_dry_run", "fe_distribute_dofs", "fe_sparsity_pattern", "fe_kernel_time", "fe_assemble_noalloc",
             "fe_assemble_adjoint", "fe_graph_capture", "fe_graph_replay", "fe_graph_destroy",
-            "fe_autotune", "fe_assemble_elements", "fe_destroy"]
+            "fe_autotune", "fe_assemble_elements", "fe_dirichlet_create", "fe_apply", "fe_dirichlet_destroy",
+            "fe_destroy"]
 
 i64p = ctypes.POINTER(ctypes.c_int64)
 f64p = ctypes.POINTER(ctypes.c_double)
@@ -143,6 +144,11 @@ def lib():
                                           ctypes.POINTER(DofDesc), i64p, i64p, i64p]
         L.fe_kernel_time.argtypes = [ctypes.c_void_p, f64p, i64p]
         L.fe_assemble_noalloc.argtypes = [ctypes.c_void_p, ctypes.POINTER(AssembleParams), ctypes.c_void_p, ctypes.c_void_p]
+        L.fe_dirichlet_create.argtypes = [ctypes.c_void_p, i64p, ctypes.c_int64, i64p, ctypes.POINTER(ctypes.c_void_p)]
+        L.fe_apply.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                               ctypes.c_void_p]
+        L.fe_dirichlet_destroy.argtypes = [ctypes.c_void_p]
+        L.fe_dirichlet_destroy.restype = None
         L.fe_assemble_elements.argtypes = [ctypes.c_void_p, ctypes.POINTER(AssembleParams), ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.POINTER(ElementLayout)]
         L.fe_assemble_adjoint.argtypes = [ctypes.c_void_p, ctypes.POINTER(AdjointParams), ctypes.c_void_p, ctypes.c_void_p,
@@ -360,6 +366,18 @@ class Handle:
             self._raise(rc)
         return ke, fe
 
+    def dirichlet(self, rowval, prescribed):
+        """fe_dirichlet_create: Dirichlet constraints of this handle's pattern (K.rowval, host,
+        1-based) on the 1-based ascending prescribed dofs (ch.prescribed_dofs)."""
+        rv = np.ascontiguousarray(rowval, np.int64)
+        pd = np.ascontiguousarray(prescribed, np.int64)
+        out = ctypes.c_void_p()
+        rc = lib().fe_dirichlet_create(self._h, rv.ctypes.data_as(i64p), len(pd), pd.ctypes.data_as(i64p),
+                                       ctypes.byref(out))
+        if rc != FE_OK:
+            self._raise(rc)
+        return Dirichlet(self, out, len(pd))
+
     def adjoint(self, u, lam, d_rho, d_X, physics: int, p0: float, p1: float, body=(0.0, 0.0, 0.0), cell_scale=None,
                 dscale=None, precision: int = PREC_MIXED, stream=None, sync: bool = True):
         """fe_assemble_adjoint: d_rho[n_cells] = dscale * lam^T (dK/ds) u and d_X[n_nodes*dim] =
@@ -529,3 +547,41 @@ def assemble(asm: GPUAssembler, element, sync: bool = True):
 
 def finish_assemble(asm: GPUAssembler):
     return asm.nzval, asm.f
+
+
+class Dirichlet:
+    """Dirichlet constraints on a handle's pattern: apply!(K, f, ch) / apply_zero!(K, f, ch)
+    on device buffers (torch CUDA tensors). Close it before its handle."""
+
+    def __init__(self, handle, ptr, n_prescribed):
+        self._handle = handle
+        self._c = ptr
+        self.n_prescribed = n_prescribed
+
+    def apply(self, nzval, f=None, inhomogeneities=None, applyzero: bool = False, stream=None, sync: bool = True):
+        if stream is not None and hasattr(stream, "cuda_stream"):
+            stream = stream.cuda_stream
+        g = inhomogeneities
+        if isinstance(g, np.ndarray):
+            g = np.ascontiguousarray(g, np.float64)
+        rc = lib().fe_apply(self._c, _ptr(nzval), _ptr(f), _ptr(g), 1 if applyzero else 0, stream)
+        if rc != FE_OK:
+            self._handle._raise(rc)
+        if sync:
+            import torch
+            torch.cuda.synchronize()
+        return nzval, f
+
+    def apply_zero(self, nzval, f=None, stream=None, sync: bool = True):
+        return self.apply(nzval, f, None, True, stream, sync)
+
+    def close(self):
+        if self._c:
+            lib().fe_dirichlet_destroy(self._c)
+            self._c = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

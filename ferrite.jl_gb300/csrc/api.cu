@@ -13,6 +13,7 @@
 #include "plan.h"
 #include "registry.h"
 #include "adjoint.cuh"
+#include "dirichlet.cuh"
 #include "tile_kernel.cuh"
 
 using namespace fe;
@@ -457,6 +458,37 @@ int launch_assembly(fe_handle* h, const KernelEntry* ke, KernelArgs& A, bool fp6
 }
 
 }  // namespace
+
+// Dirichlet constraints of a handle (fe_dirichlet_create / fe_apply)
+struct fe_dirichlet {
+    fe_handle* h = nullptr;
+    int64_t n = 0, np = 0, n_rows = 0, n_zero = 0;
+    int64_t* pd0 = nullptr;    // [np] prescribed dofs, 0-based ascending
+    int64_t* diag = nullptr;   // [n] nzval index of K[i, i], -1 if the pattern has none
+    int64_t* pdiag = nullptr;  // [np] nzval index of K[d, d]
+    int64_t* zero = nullptr;   // [n_zero] entries of the prescribed columns and rows
+    int64_t* rptr = nullptr;   // [n_rows + 1] per row with prescribed-column entries:
+    int64_t* rows = nullptr;   // [n_rows]     the row,
+    int64_t* epos = nullptr;   //              its entries' nzval indices and
+    int32_t* epi = nullptr;    //              prescribed-dof numbers, in prescribed order
+    double* g = nullptr;       // [np] inhomogeneities of the current call
+    double* part = nullptr;    // [DIAG_BLOCKS] meandiag partial sums
+    double* m = nullptr;       // meandiag
+    std::vector<void*> allocs;
+    int64_t device_bytes = 0;
+    template <typename T>
+    cudaError_t upload(T** p, const T* src, size_t count) {
+        cudaError_t e = cudaMalloc((void**)p, (count ? count : 1) * sizeof(T));
+        if (e != cudaSuccess) return e;
+        allocs.push_back((void*)*p);
+        device_bytes += (int64_t)(count * sizeof(T));
+        if (src && count) e = cudaMemcpy(*p, src, count * sizeof(T), cudaMemcpyHostToDevice);
+        return e;
+    }
+    ~fe_dirichlet() {
+        for (void* p : allocs) cudaFree(p);
+    }
+};
 
 extern "C" {
 
@@ -1256,6 +1288,143 @@ int fe_get_index_map(const fe_handle* h, int64_t cell, int64_t* positions) {
     }
     return FE_OK;
 }
+
+// ---------------------------------------------------------------------------------------
+// Dirichlet constraints (apply!, apply_zero!)
+// ---------------------------------------------------------------------------------------
+int fe_dirichlet_create(fe_handle* h, const int64_t* rowval, int64_t n_prescribed, const int64_t* prescribed,
+                        fe_dirichlet** out) {
+    if (!h || !out || (n_prescribed > 0 && (!prescribed || !rowval)) || n_prescribed < 0) return FE_ERR_ARG;
+    *out = nullptr;
+    const HostProblem& hp = h->hp;
+    const int64_t n = hp.ndofs;
+    const int64_t* cp = hp.colptr.data();
+    // the prescribed dofs of a closed ConstraintHandler: ascending, unique, in range
+    for (int64_t i = 0; i < n_prescribed; ++i) {
+        if (prescribed[i] < 1 || prescribed[i] > n) return set_error(h, FE_ERR_BOUNDS, "prescribed dof out of range");
+        if (i && prescribed[i] <= prescribed[i - 1]) return set_error(h, FE_ERR_ARG, "prescribed dofs must be ascending and unique");
+    }
+    std::vector<char> isc((size_t)n, 0);
+    for (int64_t i = 0; i < n_prescribed; ++i) isc[prescribed[i] - 1] = 1;
+    // diagonal positions (binary search: rowval ascending within a column), row bounds
+    std::vector<int64_t> diag((size_t)n, -1);
+    int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+    for (int64_t c = 0; c < n; ++c) {
+        int64_t lo = cp[c] - 1, hi = cp[c + 1] - 1;
+        for (int64_t j = lo; j < hi; ++j)
+            if (rowval[j] < 1 || rowval[j] > n || (j > lo && rowval[j] <= rowval[j - 1])) bad = 1;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi) / 2;
+            if (rowval[mid] < c + 1) lo = mid + 1;
+            else hi = mid;
+        }
+        if (lo < cp[c + 1] - 1 && rowval[lo] == c + 1) diag[c] = lo;
+    }
+    if (bad) return set_error(h, FE_ERR_BOUNDS, "rowval out of range or not ascending within a column");
+    std::vector<int64_t> pd0((size_t)n_prescribed), pdiag((size_t)n_prescribed);
+    for (int64_t i = 0; i < n_prescribed; ++i) {
+        const int64_t d = prescribed[i] - 1;
+        pd0[i] = d;
+        pdiag[i] = diag[d];
+        if (diag[d] < 0) {
+            char buf[200];
+            std::snprintf(buf, sizeof buf, "You are trying to assemble values in to K[%lld, %lld], but K[%lld, %lld] is missing in the sparsity pattern.",
+                          (long long)(d + 1), (long long)(d + 1), (long long)(d + 1), (long long)(d + 1));
+            return set_error(h, FE_ERR_PATTERN_MISSING, buf, 0, 0, d + 1, d + 1);
+        }
+    }
+    // entries to zero: every entry of a prescribed column, and the prescribed rows elsewhere
+    std::vector<int64_t> zero;
+    {
+        std::vector<int64_t> cnt((size_t)n + 1, 0);
+#pragma omp parallel for schedule(static)
+        for (int64_t c = 0; c < n; ++c) {
+            int64_t k = 0;
+            for (int64_t j = cp[c] - 1; j < cp[c + 1] - 1; ++j) k += isc[c] || isc[rowval[j] - 1];
+            cnt[c + 1] = k;
+        }
+        for (int64_t c = 0; c < n; ++c) cnt[c + 1] += cnt[c];
+        zero.resize((size_t)cnt[n]);
+#pragma omp parallel for schedule(static)
+        for (int64_t c = 0; c < n; ++c) {
+            int64_t k = cnt[c];
+            for (int64_t j = cp[c] - 1; j < cp[c + 1] - 1; ++j)
+                if (isc[c] || isc[rowval[j] - 1]) zero[k++] = j;
+        }
+    }
+    // f -= K g: per row, its entries in the prescribed columns, in prescribed order
+    std::vector<int64_t> rcount((size_t)n + 1, 0);
+    for (int64_t i = 0; i < n_prescribed; ++i)
+        for (int64_t j = cp[pd0[i]] - 1; j < cp[pd0[i] + 1] - 1; ++j) ++rcount[rowval[j]];
+    std::vector<int64_t> rows, rptr(1, 0);
+    std::vector<int64_t> slot((size_t)n, -1);
+    for (int64_t r = 0; r < n; ++r)
+        if (rcount[r + 1]) {
+            slot[r] = (int64_t)rows.size();
+            rows.push_back(r);
+            rptr.push_back(rptr.back() + rcount[r + 1]);
+        }
+    std::vector<int64_t> epos((size_t)rptr.back());
+    std::vector<int32_t> epi((size_t)rptr.back());
+    {
+        std::vector<int64_t> fill(rptr.begin(), rptr.end() - 1);
+        for (int64_t i = 0; i < n_prescribed; ++i)
+            for (int64_t j = cp[pd0[i]] - 1; j < cp[pd0[i] + 1] - 1; ++j) {
+                const int64_t k = fill[slot[rowval[j] - 1]]++;
+                epos[k] = j;
+                epi[k] = (int32_t)i;
+            }
+    }
+    fe_dirichlet* ch = new (std::nothrow) fe_dirichlet();
+    if (!ch) return FE_ERR_OOM;
+    ch->h = h;
+    ch->n = n;
+    ch->np = n_prescribed;
+    ch->n_rows = (int64_t)rows.size();
+    ch->n_zero = (int64_t)zero.size();
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e == cudaSuccess) e = ch->upload(&ch->pd0, pd0.data(), pd0.size());
+    if (e == cudaSuccess) e = ch->upload(&ch->diag, diag.data(), diag.size());
+    if (e == cudaSuccess) e = ch->upload(&ch->pdiag, pdiag.data(), pdiag.size());
+    if (e == cudaSuccess) e = ch->upload(&ch->zero, zero.data(), zero.size());
+    if (e == cudaSuccess) e = ch->upload(&ch->rptr, rptr.data(), rptr.size());
+    if (e == cudaSuccess) e = ch->upload(&ch->rows, rows.data(), rows.size());
+    if (e == cudaSuccess) e = ch->upload(&ch->epos, epos.data(), epos.size());
+    if (e == cudaSuccess) e = ch->upload(&ch->epi, epi.data(), epi.size());
+    if (e == cudaSuccess) e = ch->upload<double>(&ch->g, nullptr, (size_t)n_prescribed);
+    if (e == cudaSuccess) e = ch->upload<double>(&ch->part, nullptr, DIAG_BLOCKS);
+    if (e == cudaSuccess) e = ch->upload<double>(&ch->m, nullptr, 1);
+    if (e != cudaSuccess) {
+        delete ch;
+        return cuda_fail(h, e, "dirichlet upload");
+    }
+    *out = ch;
+    return FE_OK;
+}
+
+int fe_apply(fe_dirichlet* ch, double* nzval, double* f, const double* inhomogeneities, int32_t applyzero, void* stream) {
+    if (!ch || !nzval) return FE_ERR_ARG;
+    fe_handle* h = ch->h;
+    if (!is_device_ptr(nzval) || (f && !is_device_ptr(f))) return set_error(h, FE_ERR_ARG, "nzval and f must be device memory");
+    if (ch->np == 0) return FE_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e;
+    const bool inhom = f && !applyzero && inhomogeneities;
+    if (inhom && (e = cudaMemcpyAsync(ch->g, inhomogeneities, ch->np * 8, cudaMemcpyDefault, st)) != cudaSuccess)
+        return cuda_fail(h, e, "copy inhomogeneities");
+    device_attributes(h);
+    const unsigned grid = (unsigned)std::max(1, h->n_sm * 4);
+    meandiag_partial<<<DIAG_BLOCKS, 256, 0, st>>>(nzval, ch->diag, ch->n, ch->part);
+    meandiag_final<<<1, 256, 0, st>>>(ch->part, DIAG_BLOCKS, ch->n, ch->m);
+    if (inhom && ch->n_rows) apply_rows<<<grid, 256, 0, st>>>(f, nzval, ch->rptr, ch->rows, ch->epos, ch->epi, ch->g, ch->n_rows);
+    if (ch->n_zero) apply_zero_entries<<<grid, 256, 0, st>>>(nzval, ch->zero, ch->n_zero);
+    apply_diag<<<grid, 256, 0, st>>>(nzval, f, ch->pdiag, ch->pd0, ch->g, ch->m, ch->np, applyzero || !inhomogeneities ? 1 : 0);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(h, e, "apply kernels");
+    return FE_OK;
+}
+
+void fe_dirichlet_destroy(fe_dirichlet* ch) { delete ch; }
 
 }  // extern "C"
 

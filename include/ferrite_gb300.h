@@ -195,6 +195,26 @@ typedef struct {
 int fe_assemble_elements(fe_handle* h, const fe_assemble_params* params, void* ke, void* fe,
                          const fe_element_layout* layout);
 
+/*
+ * Dirichlet constraints on the assembled matrix: apply!(K, f, ch) and apply_zero!(K, f, ch)
+ * (src/Dofs/ConstraintHandler.jl:711-744; device form ext/FerriteKAExt/constraints.jl:40-148).
+ * fe_dirichlet_create takes the closed handler's prescribed dofs (ch.prescribed_dofs: 1-based,
+ * ascending, unique) and K.rowval (host, 1-based, the pattern of fe_create), and works out once
+ * which nzval entries each step touches. fe_apply, on DEVICE nzval and f (f may be NULL, as in
+ * apply!(K, ch)), in the reference's order: m = meandiag(K); unless applyzero,
+ * f -= K * g over the prescribed columns (g = inhomogeneities, host or device, ch.inhomogeneities;
+ * NULL: all zero); zero the prescribed columns and rows; K[d, d] = m; f[d] = g_d * m (0 for
+ * apply_zero!). Asynchronous on `stream`; deterministic (no atomics); f -= K g is bitwise the
+ * reference's per-row operation order, m is a fixed-order parallel sum. A prescribed dof
+ * without a diagonal entry in the pattern is FE_ERR_PATTERN_MISSING at creation. Destroy the
+ * constraints before their handle.
+ */
+typedef struct fe_dirichlet fe_dirichlet;
+int fe_dirichlet_create(fe_handle* h, const int64_t* rowval, int64_t n_prescribed, const int64_t* prescribed_dofs,
+                        fe_dirichlet** out);
+int fe_apply(fe_dirichlet* ch, double* nzval, double* f, const double* inhomogeneities, int32_t applyzero, void* stream);
+void fe_dirichlet_destroy(fe_dirichlet* ch);
+
 /* Wait for queued work of the handle and return the status of the last assembly. */
 int fe_sync(fe_handle* h);
 

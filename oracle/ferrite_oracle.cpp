@@ -1199,4 +1199,52 @@ int or_adjoint(const or_problem* p, const or_physics* ph, const double* u, const
     return OR_OK;
 }
 
+// apply! for Dirichlet constraints, ConstraintHandler.jl:711-744 step by step (no affine
+// constraints: _condense! returns early for them, 803-805)
+int or_apply(int64_t n, const int64_t* colptr, const int64_t* rowval, double* nzval, double* f, int64_t np,
+             const int64_t* pd, const double* g, int32_t applyzero) {
+    auto diag = [&](int64_t c) -> int64_t {  // nzval index of K[c, c] (0-based c), -1 if absent
+        for (int64_t j = colptr[c] - 1; j < colptr[c + 1] - 1; ++j)
+            if (rowval[j] == c + 1) return j;
+        return -1;
+    };
+    // meandiag (944-955): sum of |K[i, i]| in order, divided by the size
+    double z = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t j = diag(i);
+        z += j >= 0 ? std::fabs(nzval[j]) : 0.0;
+    }
+    const double m = z / (double)n;
+    // f -= K * g (add_inhomogeneities_csc!, 752-767)
+    if (f && !applyzero)
+        for (int64_t i = 0; i < np; ++i) {
+            const int64_t d = pd[i] - 1;
+            const double v = g[i];
+            if (v != 0)
+                for (int64_t j = colptr[d] - 1; j < colptr[d + 1] - 1; ++j) {
+                    const double kv = nzval[j];
+                    const double t = v * kv;
+                    f[rowval[j] - 1] = f[rowval[j] - 1] - t;
+                }
+        }
+    // zero_out_columns! (931-938), zero_out_rows! (940-949)
+    std::vector<char> isc((size_t)n, 0);
+    for (int64_t i = 0; i < np; ++i) isc[pd[i] - 1] = 1;
+    for (int64_t i = 0; i < np; ++i) {
+        const int64_t d = pd[i] - 1;
+        for (int64_t j = colptr[d] - 1; j < colptr[d + 1] - 1; ++j) nzval[j] = 0.0;
+    }
+    for (int64_t j = 0; j < colptr[n] - 1; ++j)
+        if (isc[rowval[j] - 1]) nzval[j] = 0.0;
+    // meandiag on the constrained diagonals, f[d] = g_d m (735-742)
+    for (int64_t i = 0; i < np; ++i) {
+        const int64_t d = pd[i] - 1;
+        const int64_t j = diag(d);
+        if (j < 0) return OR_ERR_PATTERN_MISSING;
+        nzval[j] = m;
+        if (f) f[d] = (applyzero ? 0.0 : g[i]) * m;
+    }
+    return OR_OK;
+}
+
 }  // extern "C"

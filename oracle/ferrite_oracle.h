@@ -20,6 +20,7 @@
  *                        docs/src/literate-gallery/topology_optimization.jl:347-383
  *   CSC assembler        src/assembler.jl:287-291, 322-457, 513-576; src/arrayutils.jl:100-152
  *   greedy coloring      src/Grid/coloring.jl:47-143
+ *   Dirichlet apply!     src/Dofs/ConstraintHandler.jl:711-767, 931-955
  *
  * Conventions follow Ferrite's memory layout: node coordinates AoS [n_nodes][dim],
  * connectivity, cell_dofs, cell_dofs_offset, colptr and rowval are 1-based Int64, nzval is
@@ -96,6 +97,15 @@ int or_assemble(const or_problem* p, const or_physics* phys, int32_t nthreads, i
 int or_element_matrix(const or_problem* p, const or_physics* phys, int64_t cell, double* Ke,
                       double* fe, or_error* err);
 int or_index_map(const or_problem* p, int64_t cell, int64_t* positions);
+
+/* apply!(K, f, ch, applyzero) for Dirichlet constraints (src/Dofs/ConstraintHandler.jl:711-744):
+ * m = meandiag(K) (944-955, before any change); unless applyzero, f -= K * g over the prescribed
+ * columns (add_inhomogeneities_csc!, 752-767, prescribed dofs in ascending order, v != 0 only);
+ * zero the prescribed columns (931-938) and rows (940-949); K[d, d] = m and f[d] = g_d m (0 for
+ * apply_zero!). prescribed: 1-based, ascending, unique; f may be NULL (apply!(K, ch)).
+ * Returns OR_ERR_PATTERN_MISSING if a prescribed diagonal is not in the pattern. */
+int or_apply(int64_t n, const int64_t* colptr, const int64_t* rowval, double* nzval, double* f,
+             int64_t n_prescribed, const int64_t* prescribed, const double* inhomogeneities, int32_t applyzero);
 int or_greedy_coloring(const or_problem* p, int32_t* cell_color, int32_t* n_colors);
 
 /* Adjoint of the assembly (heat, linear elasticity): for Phi = lambda^T (K(X, s) u - f(X)),

@@ -88,6 +88,7 @@ def lib():
                                             ctypes.c_int64, f64p, f64p, ctypes.POINTER(_Error)]
             L.or_index_map.argtypes = [ctypes.POINTER(_Problem), ctypes.c_int64, i64p]
             L.or_greedy_coloring.argtypes = [ctypes.POINTER(_Problem), i32p, i32p]
+            L.or_apply.argtypes = [ctypes.c_int64, i64p, i64p, f64p, f64p, ctypes.c_int64, i64p, f64p, ctypes.c_int32]
             L.or_adjoint.argtypes = [ctypes.POINTER(_Problem), ctypes.POINTER(_Physics), f64p, f64p, f64p, f64p, f64p,
                                      ctypes.POINTER(_Error)]
             _lib = L
@@ -365,6 +366,18 @@ class Problem:
         if rc:
             raise OracleError(rc, err)
         return d_cell, d_X
+
+    def apply(self, nzval, f, prescribed, inhomogeneities=None, applyzero=False):
+        """apply!(K, f, ch) / apply_zero!(K, f, ch) for Dirichlet constraints, in place
+        (ConstraintHandler.jl:711-744). prescribed: 1-based, ascending; f may be None."""
+        pd = np.ascontiguousarray(prescribed, np.int64)
+        g = np.ascontiguousarray(inhomogeneities if inhomogeneities is not None else np.zeros(len(pd)), np.float64)
+        rc = lib().or_apply(self.ndofs, _p(self.colptr, i64p), _p(self.rowval, i64p), _p(nzval, f64p),
+                            _p(f, f64p) if f is not None else None, len(pd), _p(pd, i64p), _p(g, f64p),
+                            1 if applyzero else 0)
+        if rc:
+            raise OracleError(rc, _Error())
+        return nzval, f
 
     def index_map(self, c0: int):
         """1-based nzval positions of Ke entries of cell c0 ([ld, ld], Ke[I, J])."""

@@ -47,6 +47,49 @@ def test_heat_equation_golden(oracle):
     assert np.linalg.norm(u) == pytest.approx(g["value"], rel=g["rtol"])
 
 
+def test_heat_equation_golden_with_apply(oracle):
+    """The tutorial's own sequence: assemble, apply!(K, f, ch), u = K \\ f (heat_equation.jl:
+    215-234), with the oracle's apply! (ConstraintHandler.jl:711-744) on the full system."""
+    O = oracle
+    p = O.box_problem(O.QUADRILATERAL, (20, 20), qr_order=2)
+    nz, f = p.assemble(O.HEAT, 1.0, 1.0)
+    x = p.nodes
+    n2d = node_to_dofs(p, 1)[:, 0]
+    bnd = np.where((np.abs(np.abs(x[:, 0]) - 1) < 1e-12) | (np.abs(np.abs(x[:, 1]) - 1) < 1e-12))[0]
+    pd = np.sort(n2d[bnd]) + 1
+    p.apply(nz, f, pd, np.zeros(len(pd)))
+    K = p.to_scipy(nz)
+    # constrained rows and columns are zero apart from the mean diagonal
+    m = K.diagonal()[pd[0] - 1]
+    assert np.all(K.diagonal()[pd - 1] == m) and m > 0
+    assert np.all(f[pd - 1] == 0)
+    u = spla.spsolve(K.tocsc(), f)
+    g = GOLDEN["heat_equation_norm_u"]
+    assert np.linalg.norm(u) == pytest.approx(g["value"], rel=g["rtol"])
+
+
+def test_apply_inhomogeneous_semantics(oracle):
+    """apply! with g != 0 leaves K u = f solved by u = g on the constrained dofs, and the free
+    rows see f - K g (the condensed system); apply_zero! sets f[d] = 0."""
+    O = oracle
+    p = O.box_problem(O.QUADRILATERAL, (6, 5), qr_order=2, perturb=0.2, seed=2)
+    nz0, f0 = p.assemble(O.HEAT, 1.0, 1.0)
+    rng = np.random.default_rng(3)
+    pd = np.sort(rng.choice(p.ndofs, 9, replace=False)) + 1
+    g = rng.normal(size=len(pd))
+    nz, f = nz0.copy(), f0.copy()
+    p.apply(nz, f, pd, g)
+    u = spla.spsolve(p.to_scipy(nz).tocsc(), f)
+    assert np.allclose(u[pd - 1], g, rtol=1e-12, atol=1e-12)
+    free = np.setdiff1d(np.arange(p.ndofs), pd - 1)
+    K0 = p.to_scipy(nz0).tocsr()
+    r = K0 @ u - f0
+    assert np.abs(r[free]).max() < 1e-10 * np.abs(f0).max()
+    nz, f = nz0.copy(), f0.copy()
+    p.apply(nz, f, pd, g, applyzero=True)
+    assert np.all(f[pd - 1] == 0) and np.array_equal(f[free], f0[free])
+
+
 def test_hyperelasticity_golden(oracle):
     O = oracle
     N, L = 10, 1.0
