@@ -516,7 +516,8 @@ def config_q2(fg, stream, nel=64, reps=5):
            "mixed_vs_fp64_rel_frobenius": {"K": rel_k, "f": rel_f},
            "tiles": info["n_tiles"], "cell_visits_per_cell": info["n_cell_visits"] / dh.n_cells,
            "setup_s": {"host": t1 - t0, "fe_create": t2 - t1},
-           "path": "CUDA cores (FP32 element math, per-tile geometry recompute); no tensor-core path"}
+           "path": "two-phase: element matrices once per cell (CUDA cores), then the gather-only owner-tile "
+                   "reduce; no tensor-core path"}
     h.close()
     return out
 
@@ -609,7 +610,19 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-configs", action="store_true", help="skip the heat / Q2 / adjoint / mixed-graph configurations")
     ap.add_argument("--nel", type=int, default=128, help="cells per axis (128 = the benchmark workload)")
+    ap.add_argument("--config", choices=["heat", "q2", "adjoint", "mixed_graph", "elements"],
+                    help="run only this configuration and print its JSON (profiling runs)")
+    ap.add_argument("--q2-nel", type=int, default=64, help="cells per axis of the Q2 configuration")
     args = ap.parse_args()
+    if args.config:
+        import torch
+        fg = _package()
+        fg.build()
+        stream = torch.cuda.Stream()
+        fn = {"heat": config_heat, "q2": lambda g, s: config_q2(g, s, nel=args.q2_nel), "adjoint": config_adjoint,
+              "mixed_graph": config_mixed_graph, "elements": config_elements}[args.config]
+        print(json.dumps({"config": args.config, "result": fn(fg, stream)}))
+        return
     if args.warmup < 3:
         args.warmup = 3
     global NEL, WORKLOAD
