@@ -158,4 +158,62 @@ function assemble_csc!(K::SparseMatrixCSC{Float64,Int}, f::Vector{Float64}, h::H
     return K, f
 end
 
+struct ElementLayout
+    ke_stride::NTuple{3,Int64}
+    fe_stride::NTuple{2,Int64}
+end
+
+"""
+    assemble_elements!(Kes, fes, h; physics, p0, p1, ...)
+
+The GPU how-to's element assembly (gpu_assembly.jl:270-303): `Kes[cellid, :, :]` and
+`fes[cellid, :]` for every cell, in the how-to's arrays `Kes = CUDA.zeros(Float32, ncells, nbf,
+nbf)`, `fes = CUDA.zeros(Float32, ncells, nbf)` (Float64 arrays with FE_PREC_FP64).
+"""
+function assemble_elements!(Kes, fes, h::Handle; physics=FE_LINEAR_ELASTIC, p0=1.0, p1=0.3,
+                            body=(0.0, 0.0, 0.0), cell_scale=nothing, u=nothing, precision=FE_PREC_MIXED)
+    n, nbf = size(Kes, 1), size(Kes, 2)
+    lay = Ref(ElementLayout((1, n, n * nbf), (1, n)))
+    cs = cell_scale === nothing ? Ptr{Float64}(C_NULL) : pointer(cell_scale)
+    up = u === nothing ? Ptr{Float64}(C_NULL) : pointer(u)
+    par = Ref(AssembleParams(physics, precision, UInt32(0), p0, p1, Tuple(Float64.(body)), cs, up, 0.0, C_NULL))
+    rc = GC.@preserve Kes fes cell_scale u ccall((:fe_assemble_elements, LIB), Cint,
+        (Ptr{Cvoid}, Ptr{AssembleParams}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{ElementLayout}),
+        h.ptr, par, pointer(Kes), pointer(fes), lay)
+    check(rc, h.ptr)
+    return Kes, fes
+end
+
+# Dirichlet constraints of a closed ConstraintHandler on the handle's pattern
+mutable struct Constraints
+    ptr::Ptr{Cvoid}
+    h::Handle
+    inhomogeneities::Vector{Float64}
+end
+
+function Constraints(h::Handle, K::SparseMatrixCSC{Float64,Int}, ch::ConstraintHandler)
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    pd = Vector{Int64}(ch.prescribed_dofs)
+    rc = GC.@preserve K pd ccall((:fe_dirichlet_create, LIB), Cint,
+        (Ptr{Cvoid}, Ptr{Int64}, Int64, Ptr{Int64}, Ptr{Ptr{Cvoid}}), h.ptr, K.rowval, length(pd), pd, out)
+    check(rc, h.ptr)
+    c = Constraints(out[], h, Vector{Float64}(ch.inhomogeneities))
+    finalizer(x -> ccall((:fe_dirichlet_destroy, LIB), Cvoid, (Ptr{Cvoid},), x.ptr), c)
+    return c
+end
+
+"""
+    apply!(nzval, f, c::Constraints; applyzero=false)
+
+`Ferrite.apply!(K, f, ch)` / `apply_zero!(K, f, ch)` (ConstraintHandler.jl:711-744) on device
+arrays (`nzval = nonzeros(K_gpu)`, `f` a CuArray); asynchronous on the default stream.
+"""
+function apply!(nzval, f, c::Constraints; applyzero::Bool=false)
+    rc = GC.@preserve nzval f c ccall((:fe_apply, LIB), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int32, Ptr{Cvoid}),
+        c.ptr, pointer(nzval), f === nothing ? C_NULL : pointer(f), c.inhomogeneities, Int32(applyzero), C_NULL)
+    check(rc, c.h.ptr)
+    return nzval, f
+end
+
 end # module
