@@ -66,6 +66,19 @@ bool is_device_ptr(const void* p) {
     return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
 }
 
+// Page-locked host memory: the device address the kernels reach it by (its mapping), else
+// nullptr. Kernels then store into host memory directly, overlapping the transfer with the
+// assembly instead of staging it and copying afterwards.
+void* pinned_device_alias(void* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 }  // namespace
 
 struct fe_handle {
@@ -765,9 +778,12 @@ static int assemble_common(fe_handle* h, const fe_assemble_params* p, double* nz
     cudaStream_t st = (cudaStream_t)p->stream;
     cudaError_t e;
     KernelArgs A = h->base;
-    // outputs: device pointers are written in place, host pointers are staged
-    const bool nz_dev = eo || (do_k && is_device_ptr(nzval));
-    const bool f_dev = eo || (do_f && is_device_ptr(f));
+    // outputs: device pointers are written in place, page-locked host memory through its
+    // mapping (plain stores), other host memory is staged
+    double* nz_map = !eo && do_k && !h->capturing && !is_device_ptr(nzval) ? (double*)pinned_device_alias(nzval) : nullptr;
+    double* f_map = !eo && do_f && !h->capturing && !is_device_ptr(f) ? (double*)pinned_device_alias(f) : nullptr;
+    const bool nz_dev = eo || (do_k && (nz_map || is_device_ptr(nzval)));
+    const bool f_dev = eo || (do_f && (f_map || is_device_ptr(f)));
     const bool fill = (p->flags & FE_FILLZERO) != 0;
     if (do_k && !nz_dev) {
         if (!h->nz_stage && (e = h->alloc(&h->nz_stage, hp.nnz)) != cudaSuccess) return cuda_fail(h, e, "alloc nzval");
@@ -779,8 +795,9 @@ static int assemble_common(fe_handle* h, const fe_assemble_params* p, double* nz
         if (!fill && (e = cudaMemcpyAsync(h->f_stage, f, hp.ndofs * 8, cudaMemcpyHostToDevice, st)) != cudaSuccess)
             return cuda_fail(h, e, "copy f");
     }
-    A.nzval = do_k && !eo ? (nz_dev ? nzval : h->nz_stage) : nullptr;
-    A.f = do_f && !eo ? (f_dev ? f : h->f_stage) : nullptr;
+    A.nzval = do_k && !eo ? (nz_map ? nz_map : nz_dev ? nzval : h->nz_stage) : nullptr;
+    A.f = do_f && !eo ? (f_map ? f_map : f_dev ? f : h->f_stage) : nullptr;
+    A.host_out = nz_map != nullptr;
     A.do_k = do_k;
     A.do_f = do_f;
     A.fillzero = fill;

@@ -947,7 +947,8 @@ __device__ __forceinline__ void reduce_tile(const KernelArgs& a, const char* R, 
     const RecRun* runs = (const RecRun*)(R + H->off_runs);
     const RecPass* passes = (const RecPass*)(R + H->off_pass);
     const RecRng* rngs = (const RecRng*)(R + H->off_rng);
-    const bool bulk = ((uintptr_t)a.nzval & 15) == 0;
+    // TMA bulk stores into device memory; plain stores into host memory or unaligned nzval
+    const bool bulk = !a.host_out && ((uintptr_t)a.nzval & 15) == 0;
     const uint32_t outb_s = (uint32_t)__cvta_generic_to_shared(outb);
     const int n_pass = H->n_pass;
     for (int p = 0; p < n_pass; ++p) {

@@ -315,3 +315,29 @@ def test_two_phase_q2_against_oracle(built, oracle):
     prob = O.box_problem(O.HEXAHEDRON, (3, 3, 2), ip_order=2, ncomp=3, qr_order=3, perturb=0.2, seed=26)
     E, nu = 200e3, 0.3
     check(fg, O, prob, dict(physics=fg.LINEAR_ELASTIC, p0=E, p1=nu), dict(physics=O.LINEAR_ELASTIC, p0=E, p1=nu))
+
+
+def test_pinned_host_outputs_written_directly(built, oracle, torch_cuda):
+    """Page-locked host nzval/f are written by the kernels through their mapping (no staging
+    copy): the same bits as device outputs, including accumulation without fill-zero."""
+    torch = torch_cuda
+    fg, O = built, oracle
+    prob = O.box_problem(O.HEXAHEDRON, (6, 5, 4), ncomp=3, perturb=0.2, seed=51)
+    h = make_handle(fg, O, prob)
+    kw = dict(physics=fg.LINEAR_ELASTIC, p0=200e3, p1=0.3, body=(0.0, 0.0, -1.0))
+    nz_d = torch.zeros(prob.nnz, dtype=torch.float64, device="cuda")
+    f_d = torch.zeros(prob.ndofs, dtype=torch.float64, device="cuda")
+    h.assemble(nz_d, f_d, **kw)
+    nz_p = torch.full((prob.nnz,), float("nan"), dtype=torch.float64).pin_memory()
+    f_p = torch.full((prob.ndofs,), float("nan"), dtype=torch.float64).pin_memory()
+    h.assemble(nz_p, f_p, **kw)
+    assert torch.equal(nz_p, nz_d.cpu()) and torch.equal(f_p, f_d.cpu())
+    h.assemble(nz_p, f_p, fillzero=False, **kw)
+    h.assemble(nz_d, f_d, fillzero=False, **kw)
+    assert torch.equal(nz_p, nz_d.cpu()) and torch.equal(f_p, f_d.cpu())
+    s = torch.cuda.Stream()
+    nz_p.fill_(float("nan"))
+    h.assemble(nz_p, f_p, stream=s, sync=False, **kw)
+    h.sync()
+    h.assemble(nz_d, f_d, **kw)
+    assert torch.equal(nz_p, nz_d.cpu())
