@@ -36,8 +36,8 @@ ERROR_NAMES = {0: "OK", 1: "ARG", 2: "BOUNDS", 3: "DETJ", 4: "PATTERN_MISSING", 
 TRIANGLE, QUADRILATERAL, TETRAHEDRON, HEXAHEDRON, WEDGE = 1, 2, 3, 4, 5
 HEAT, LINEAR_ELASTIC, NEO_HOOKE = 1, 2, 3
 PREC_MIXED, PREC_FP64 = 0, 1
-FILLZERO, NO_K, NO_F, ASYNC, PROFILE, COMPENSATED, TWO_PHASE, FUSED = 1, 2, 4, 8, 16, 32, 64, 128
-_FORMS = {None: 0, "two_phase": TWO_PHASE, "fused": FUSED}
+FILLZERO, NO_K, NO_F, ASYNC, PROFILE, COMPENSATED, TWO_PHASE, FUSED, NO_TENSOR = 1, 2, 4, 8, 16, 32, 64, 128, 256
+_FORMS = {None: 0, "two_phase": TWO_PHASE, "fused": FUSED, "two_phase_cuda_cores": TWO_PHASE | NO_TENSOR}
 
 EXPORTED = ["fe_abi_version", "fe_create", "fe_assemble", "fe_sync", "fe_last_error", "fe_get_info",
             "fe_get_index_map", "fe_plan_dry_run", "fe_distribute_dofs", "fe_sparsity_pattern", "fe_kernel_time", "fe_assemble_noalloc",
@@ -310,7 +310,8 @@ class Handle:
                  cond_threshold: float = 0.0, profile: bool = False, compensated: bool = False, form=None):
         """One fe_assemble call. ``stream`` is a torch.cuda.Stream, a raw handle or None.
         ``compensated`` (mixed precision): sum each entry as a compensated FP32 pair.
-        ``form``: None (the engine's choice), "two_phase" (element matrices first) or "fused"."""
+        ``form``: None (the engine's choice), "two_phase" (element matrices first; on the tensor
+        cores where a kernel exists), "two_phase_cuda_cores" or "fused"."""
         p = AssembleParams()
         p.physics, p.precision = physics, precision
         flags = FILLZERO if fillzero else 0

@@ -403,20 +403,27 @@ int launch_elements(fe_handle* h, const KernelArgs& A, int s, int phys, bool fp6
     const SubDev& sd = A.sub[s];
     const ElemEntry* ee = find_elem(sd.kind, sd.nq, phys, fp64);
     if (!ee) return set_error(h, FE_ERR_UNSUPPORTED, "no element kernel compiled for this element / physics");
-    const void* fn = to_caller ? ee->fn_out : ee->fn;
+    // the tensor-core form (128 threads, one cell at a time per CTA) where one exists
+    const bool tc = !to_caller && ee->fn_tc && A.tensor;
+    const void* fn = tc ? ee->fn_tc : to_caller ? ee->fn_out : ee->fn;
+    const int threads = tc ? 128 : THREADS;
     const int pi = fp64 ? 1 : 0;
     const int o1 = h->shape_off1[pi], o2 = h->shape_off2[pi], sb = h->shape_bytes[pi];
     const int off = s == 0 ? 0 : (s == 1 ? o1 : o2);
     const int end = s + 1 < A.n_sub ? (s == 0 ? o1 : o2) : sb;
     int sub_bytes = end - off;
     device_attributes(h);
-    const int esmem = ((sub_bytes + 15) & ~15) + ee->groups * ee->group_bytes;
+    const int esmem = tc ? tc_layout(sub_bytes).bytes : ((sub_bytes + 15) & ~15) + ee->groups * ee->group_bytes;
     if (esmem > h->max_smem - 1024) return set_error(h, FE_ERR_UNSUPPORTED, "element tables do not fit in shared memory");
     if ((e = ensure_smem_attribute(fn, esmem)) != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute");
     int per_sm = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, THREADS, esmem)) != cudaSuccess)
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, esmem)) != cudaSuccess)
         return cuda_fail(h, e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
-    const int64_t need = (sd.n_cells + ee->groups - 1) / ee->groups;
+    const int64_t cells_per_cta = tc ? 1 : ee->groups;
+    const int64_t need = (sd.n_cells + cells_per_cta - 1) / cells_per_cta;
+    // the tensor-core form: three CTAs per SM by its launch bounds (three TMEM allocations of
+    // 128 columns fit an SM's 512; a CTA that does not fit waits for one to finish)
+    if (tc) per_sm = std::max(per_sm, 3);
     const int64_t egrid = std::min<int64_t>(need, (int64_t)std::max(per_sm, 1) * std::max(h->n_sm, 1));
     if (egrid <= 0) return FE_OK;
     SubDev sdv = sd;
@@ -424,7 +431,7 @@ int launch_elements(fe_handle* h, const KernelArgs& A, int s, int phys, bool fp6
     EaOut eov = eo;
     KernelArgs Av = A;
     void* eargs[] = {(void*)&Av, (void*)&sdv, (void*)&eshp, (void*)&sub_bytes, (void*)&eov};
-    e = cudaLaunchKernel(fn, dim3((unsigned)egrid), dim3(THREADS), eargs, (size_t)esmem, st);
+    e = cudaLaunchKernel(fn, dim3((unsigned)egrid), dim3(threads), eargs, (size_t)esmem, st);
     if (e != cudaSuccess) return cuda_fail(h, e, "element kernel launch");
     return FE_OK;
 }
@@ -798,6 +805,7 @@ static int assemble_common(fe_handle* h, const fe_assemble_params* p, double* nz
     A.nzval = do_k && !eo ? (nz_map ? nz_map : nz_dev ? nzval : h->nz_stage) : nullptr;
     A.f = do_f && !eo ? (f_map ? f_map : f_dev ? f : h->f_stage) : nullptr;
     A.host_out = nz_map != nullptr;
+    A.tensor = (p->flags & FE_NO_TENSOR) ? 0 : 1;
     A.do_k = do_k;
     A.do_f = do_f;
     A.fillzero = fill;

@@ -196,6 +196,7 @@ struct KernelArgs {
     int32_t do_k, do_f, fillzero;
     int32_t compensated;     // mixed precision: compensated FP32 pair sums
     int32_t host_out;        // nzval is page-locked host memory (its mapping): plain stores only
+    int32_t tensor;          // element matrices on the tensor cores where a kernel exists
     Physics phys;
     DevStatus* status;
     int32_t rec_cap;         // record bytes per ring buffer (max over tiles)

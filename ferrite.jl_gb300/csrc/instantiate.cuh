@@ -45,6 +45,9 @@ ElemEntry make_elem_entry() {
     e.fp64 = std::is_same<R, double>::value ? 1 : 0;
     e.fn = (const void*)&element_kernel<K, Q, PH, R, 1>;
     e.fn_out = (const void*)&element_kernel<K, Q, PH, R, 2>;
+    e.fn_tc = nullptr;
+    if constexpr (K == KIND_HEX27 && Q == 27 && PH == PHYS_ELASTIC && std::is_same<R, float>::value)
+        e.fn_tc = (const void*)&element_kernel_tc<PHYS_ELASTIC>;
     e.group_bytes = EaGroup<K, Q, PH, R>::BYTES;
     e.groups = THREADS / ElemT<K>::GS;
     return e;

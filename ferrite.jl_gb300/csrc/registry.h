@@ -30,6 +30,7 @@ struct ElemEntry {
     int kind, nq, phys, fp64;
     const void* fn;      // __global__ element_kernel<..., 1>: into the two-phase scratch
     const void* fn_out;  // __global__ element_kernel<..., 2>: into the caller's element arrays
+    const void* fn_tc;   // tensor-core form into the two-phase scratch (nullptr: none)
     int group_bytes;     // shared memory per lane group (the shape tables come on top)
     int groups;          // lane groups per CTA
 };

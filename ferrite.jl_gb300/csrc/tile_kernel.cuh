@@ -354,7 +354,10 @@ __device__ __forceinline__ void lds16(const Real* p, Real* out) {
 template <int K, int NQ, int PHYS, typename Real>
 __device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev& sd, const Real* shp, int cell,
                                                const uint16_t* cn, const char* xs, const int32_t* nodes, int lane,
-                                               unsigned gmask, int gbase, Real* tb) {
+                                               unsigned gmask, int gbase, Real* tb, int i0 = 0,
+                                               int i1 = ElemT<K>::NB, bool lead = true) {
+    // [i0, i1): the base functions whose gradients this group writes (groups sharing a cell
+    // split them); lead: the group that also writes the cell's point weights and factors
     using E = ElemT<K>;
     using CT = CellTable<K, NQ, PHYS, Real>;
     constexpr int NB = E::NB, NG = E::NG, DIM = E::DIM;
@@ -448,7 +451,7 @@ __device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev
                 s = (float)sd_;
             }
             dt = (float)dtd;
-            if (q == 0) atomicAdd(&a.status->flagged, 1u);
+            if (q == 0 && lead) atomicAdd(&a.status->flagged, 1u);
         } else {
             const float r = rsqrtf(dt);
             const float sc = Q[SQL.w + 1] * r;  // sqrt(w) / sqrt(detJ)
@@ -474,13 +477,16 @@ __device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev
     if constexpr (DN_REG) lds16<Real, round_up(NB * DIM, V)>(Q + SQL.dn, dN);
     const int p = q >> 1, hh = q & 1;
     const bool pad = (NQ & 1) && q == NQ - 1;
-    sq[2 * p + hh] = s;
-    if (pad) sq[2 * p + 1] = Real(0);
+    if (lead) {
+        sq[2 * p + hh] = s;
+        if (pad) sq[2 * p + 1] = Real(0);
+    }
     Real H[9];
     #pragma unroll
     for (int t = 0; t < 9; ++t) H[t] = Real(0);
     #pragma unroll
     for (int i = 0; i < NB; ++i) {
+        if (i < i0 || i >= i1) continue;
         Real g[3] = {0, 0, 0};
         #pragma unroll
         for (int b = 0; b < DIM; ++b)
@@ -508,7 +514,7 @@ __device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev
             }
         }
     }
-    if (q == 0) {
+    if (q == 0 && lead) {
         Real scale = Real(1);
         if (a.phys.scale_f) {
             if constexpr (sizeof(Real) == 4) scale = a.phys.scale_f[sd.cellid[cell]];
@@ -1319,6 +1325,257 @@ __global__ void __launch_bounds__(THREADS, 2) element_kernel(const KernelArgs a,
                                                  (Real*)eo.ke + c * eo.ks[0], &eo);
         __syncwarp(gmask);  // the next cell overwrites the table and the coordinates
     }
+}
+
+// ---------------------------------------------------------------------------------------
+// element matrices of 27-node hexahedra (isotropic elasticity) on the tensor cores
+// (tcgen05, kind::tf32). Per cell the blocks need only the Gram matrix of the scaled
+// gradients, G[(i,a),(j,b)] = sum_q g_ia(q) g_jb(q) (g = sqrt(detJ w) grad N), since
+// Ke[(i,a),(j,b)] = lam G[(i,a),(j,b)] + mu G[(i,b),(j,a)] + mu delta_ab sum_c G[(i,c),(j,c)]
+// (threaded_assembly.jl:105-132 with C isotropic). G = A A^T with A the 81 x 27 matrix of
+// gradient components (row m = 32 a + i, column = point): one M=128, N=96 MMA chain per
+// product, K = 32 (27 points padded), accumulated in TMEM in FP32. TF32 keeps 10 mantissa
+// bits, so A = hi + lo is split and G = hi hi^T + hi lo^T + lo hi^T (the lo lo^T term is
+// below FP32 rounding). Operands live in shared memory in the K-major core-matrix layout
+// without swizzle: (m, k) at (m%8)*16 + (k%4)*4 + (k/4)*128 + (m/8)*1024 bytes.
+// 128 threads: the four warps split the geometry (functions), convert the operands, read
+// back the rows of G (warp a = component a, lane = function i: TMEM lane 32 a + i) and
+// write the element matrix columns [j][t][i] of the two-phase scratch.
+// ---------------------------------------------------------------------------------------
+constexpr int TC_OPERAND_BYTES = 128 * 32 * 4;  // one 128 x 32 tf32 operand
+constexpr int TC_GS = 81;                        // row stride (floats) of the G exchange (odd: no bank conflicts)
+
+struct TcLayout {
+    int shape, tb, xs, nodes, cn, hi, lo, bytes;
+};
+__host__ __device__ inline TcLayout tc_layout(int shape_bytes) {
+    using CT = CellTable<KIND_HEX27, 27, PHYS_ELASTIC, float>;
+    TcLayout L;
+    int o = 0;
+    L.shape = o; o += pad16i(shape_bytes);
+    L.tb = o; o += CT::BYTES;
+    L.xs = o; o += 8 * NODE_BYTES;
+    L.nodes = o; o += 32;
+    L.cn = o; o += 16;
+    o = (o + 127) & ~127;
+    L.hi = o; o += TC_OPERAND_BYTES;
+    L.lo = o; o += TC_OPERAND_BYTES;
+    L.bytes = o;
+    return L;
+}
+
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
+    // start address, leading byte offset (next core matrix along K) 128, stride byte offset
+    // (next 8-row group) 1024, all in 16-byte units; bits 46-48 = 0b001; no swizzle
+    return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46);
+}
+
+__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity, long long limit) {
+    for (long long it = 0; it < limit; ++it) {
+        uint32_t ok;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(ok)
+                     : "r"(bar), "r"(parity)
+                     : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, float* r) {
+    uint32_t v[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,"
+        "%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]),
+          "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]),
+          "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]),
+          "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr));
+    #pragma unroll
+    for (int k = 0; k < 32; ++k) r[k] = __uint_as_float(v[k]);
+}
+
+template <int PHYS>
+__global__ void __launch_bounds__(128, 3) element_kernel_tc(const KernelArgs a, const SubDev sd, const float* __restrict__ shape_g,
+                                                             int shape_bytes, const EaOut eo) {
+    static_assert(PHYS == PHYS_ELASTIC, "the Gram-matrix form is isotropic elasticity");
+    constexpr int K = KIND_HEX27, NQ = 27, NB = 27, NG = 8;
+    using CT = CellTable<K, NQ, PHYS_ELASTIC, float>;
+    constexpr ShapeQ SQL = shape_q(NB, NG, 3, 4);
+    constexpr int JS = ea_col_values(NB, 3);
+    extern __shared__ __align__(128) char smem_raw[];
+    __shared__ __align__(8) unsigned long long bar;
+    __shared__ uint32_t tmem_base;
+    const TcLayout L = tc_layout(shape_bytes);
+    const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+    {
+        // the host sized the allocation from the same layout; refuse to run past it
+        uint32_t dyn;
+        asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+        if ((uint32_t)L.bytes > dyn) {
+            if (tid == 0) atomicAdd(&a.status->timeout, 1u);
+            return;
+        }
+    }
+    float* shape = (float*)(smem_raw + L.shape);
+    float* tb = (float*)(smem_raw + L.tb);
+    char* xs = smem_raw + L.xs;
+    int32_t* nodes = (int32_t*)(smem_raw + L.nodes);
+    uint16_t* cn = (uint16_t*)(smem_raw + L.cn);
+    float* G = (float*)(smem_raw + L.hi);  // the G exchange reuses the operands (96 x 81 floats)
+    for (int k = tid; k < shape_bytes / 16; k += 128) ((int4*)shape)[k] = ((const int4*)shape_g)[k];
+    if (tid < NG) cn[tid] = (uint16_t)tid;
+    const uint32_t barp = (uint32_t)__cvta_generic_to_shared(&bar);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(barp) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"((uint32_t)__cvta_generic_to_shared(&tmem_base))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tm = tmem_base;
+    const uint32_t hi_s = (uint32_t)__cvta_generic_to_shared(smem_raw + L.hi);
+    const uint32_t lo_s = (uint32_t)__cvta_generic_to_shared(smem_raw + L.lo);
+    // D f32, A and B tf32, both K-major, N = 96, M = 128
+    constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(96 >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+    const char* src = (const char*)a.xf6;
+    bool failed = false;
+    int it = 0;
+    for (int64_t c = blockIdx.x; c < sd.n_cells; c += gridDim.x, ++it) {
+        // node ids and coordinates
+        if (tid < NG) {
+            const int nd = sd.conn[c * NG + tid];
+            nodes[tid] = nd;
+            const uint2* p = (const uint2*)(src + (int64_t)nd * NODE_BYTES);
+            uint2* d = (uint2*)(xs + tid * NODE_BYTES);
+            d[0] = p[0];
+            d[1] = p[1];
+            d[2] = p[2];
+        }
+        __syncthreads();
+        // geometry: every warp maps the 27 points, warp w writes the gradients of functions
+        // [7w, 7w + 7); warp 0 also the point weights and the cell's factors
+        geometry_lanes<K, NQ, PHYS_ELASTIC, float>(a, sd, shape, (int)c, cn, xs, nodes, lane, 0xFFFFFFFFu, 0, tb, 7 * warp,
+                                                    7 * warp + 7, warp == 0);
+        __syncthreads();
+        // operands: (m, k) = (32 a + i, point), zero outside a < 3, i < 27, k < 27
+        for (int e = tid; e < 128 * 8; e += 128) {
+            const int m = e & 127, kq = e >> 7;
+            const int ca = m >> 5, ci = m & 31;
+            float x[4] = {0.f, 0.f, 0.f, 0.f};
+            if (ca < 3 && ci < NB) {
+                #pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int pp = 2 * kq + h;  // point pair: points 2 pp, 2 pp + 1 (the pad point is zero)
+                    if (pp < CT::NQP) {
+                        const float2 v = *(const float2*)(tb + pp * CT::SP + ci * 6 + 2 * ca);
+                        x[2 * h] = v.x;
+                        x[2 * h + 1] = v.y;
+                    }
+                }
+            }
+            float4 hv, lv;
+            float* hp = &hv.x;
+            float* lp = &lv.x;
+            #pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                uint32_t hb;
+                asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hb) : "f"(x[r]));
+                hp[r] = __uint_as_float(hb);
+                lp[r] = x[r] - hp[r];
+            }
+            const int off = (m & 7) * 16 + kq * 128 + (m >> 3) * 1024;
+            *(float4*)(smem_raw + L.hi + off) = hv;
+            *(float4*)(smem_raw + L.lo + off) = lv;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // operand writes -> tensor core reads
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            #pragma unroll
+            for (int prod = 0; prod < 3; ++prod) {
+                const uint32_t as = prod == 2 ? lo_s : hi_s, bs = prod == 1 ? lo_s : hi_s;
+                #pragma unroll
+                for (int s = 0; s < 4; ++s) {
+                    const uint64_t da = tc_desc(as + s * 256), db = tc_desc(bs + s * 256);
+                    const uint32_t acc = (prod | s) ? 1u : 0u;
+                    asm volatile(
+                        "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tm),
+                        "l"(da), "l"(db), "r"(IDESC), "r"(acc)
+                        : "memory");
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(barp) : "memory");
+        }
+        const bool ok = tc_wait(barp, (uint32_t)(it & 1), WAIT_LIMIT);
+        if (__syncthreads_or(!ok)) {  // the whole CTA leaves together
+            failed = true;
+            break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // rows of G: warp a reads TMEM lanes 32 a .. 32 a + 31 (lane = function i)
+        float g[96];
+        if (warp < 3) {
+            #pragma unroll
+            for (int c0 = 0; c0 < 3; ++c0) tc_ld32(tm + ((uint32_t)(32 * warp) << 16) + (uint32_t)(32 * c0), g + 32 * c0);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (lane < NB) {
+                #pragma unroll
+                for (int b = 0; b < 3; ++b)
+                    #pragma unroll
+                    for (int j = 0; j < NB; ++j) G[(32 * warp + lane) * TC_GS + 27 * b + j] = g[32 * b + j];
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        if (warp < 3 && lane < NB) {
+            const int aa = warp, i = lane;
+            const float lam = tb[CT::GRAD + CT::SQ], mu = tb[CT::GRAD + CT::SQ + 1];
+            float* out = (float*)eo.ke + c * eo.ks[0];
+            if (a.do_k) {
+                const float* Gi0 = G + (0 * 32 + i) * TC_GS;
+                const float* Gi1 = G + (1 * 32 + i) * TC_GS;
+                const float* Gi2 = G + (2 * 32 + i) * TC_GS;
+                const float* Gia[3] = {Gi0, Gi1, Gi2};
+                #pragma unroll
+                for (int j = 0; j < NB; ++j) {
+                    const float tr = Gi0[j] + Gi1[27 + j] + Gi2[54 + j];
+                    #pragma unroll
+                    for (int b = 0; b < 3; ++b) {
+                        const float gab = g[32 * b + j];
+                        const float gba = Gia[b][27 * aa + j];  // G[(i,b),(j,a)]
+                        float v = lam * gab + mu * gba;
+                        if (b == aa) v += mu * tr;
+                        out[j * JS + (b * 3 + aa) * NB + i] = v;
+                    }
+                }
+            }
+            if (a.do_f) {
+                const float* sq = tb + CT::GRAD;
+                float Fi = 0.f;
+                #pragma unroll
+                for (int q = 0; q < NQ; ++q) Fi += sq[q] * sq[q] * shape[q * SQL.qs + SQL.n + i];
+                out[NB * JS + aa * NB + i] = Fi * a.phys.body_f[aa];
+            }
+        }
+        __syncthreads();  // the next cell overwrites the table, the operands and G
+    }
+    if (failed) {
+        // the MMAs of this cell did not report back: record it and wait (bounded) once more
+        // before the operands and TMEM are released
+        if (tid == 0) atomicAdd(&a.status->timeout, 1u);
+        tc_wait(barp, (uint32_t)(it & 1), WAIT_LIMIT);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tm) : "memory");
 }
 
 }  // namespace fe

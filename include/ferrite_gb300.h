@@ -78,6 +78,10 @@ extern "C" {
                               cell's geometry in every tile that owns one of its dofs. The default for
                               quadratic elements; results are bitwise those of the fused form */
 #define FE_FUSED 128u      /* element math inside the owner tiles (the default for linear elements) */
+#define FE_NO_TENSOR 256u  /* two-phase form: element matrices on the CUDA cores even where a tensor-core
+                              kernel exists (27-node hexahedra, elasticity, mixed precision); the CUDA-core
+                              form gives the fused form's bits, the tensor-core form (split TF32 products,
+                              FP32 accumulation) differs from them by FP32 rounding */
 
 typedef struct fe_handle fe_handle;
 

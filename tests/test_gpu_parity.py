@@ -262,19 +262,19 @@ def test_unaligned_device_output(built, oracle, torch_cuda):
 
 
 def _forms_bitwise(fg, O, prob, element_args):
-    """Element matrices first (two-phase) and in-tile (fused) give the same bits: the same FP32
-    element math feeds the same per-entry sums in cell order."""
+    """Element matrices first (two-phase, CUDA cores) and in-tile (fused) give the same bits:
+    the same FP32 element math feeds the same per-entry sums in cell order."""
     h = make_handle(fg, O, prob)
     out = {}
-    for form in ("fused", "two_phase"):
+    for form in ("fused", "two_phase_cuda_cores"):
         for prec in (0, 1):
             nz = np.full(prob.nnz, np.nan)
             f = np.full(prob.ndofs, np.nan)
             h.assemble(nz, f, precision=prec, form=form, **element_args)
             out[form, prec] = (nz, f)
     for prec in (0, 1):
-        assert np.array_equal(out["fused", prec][0], out["two_phase", prec][0]), prec
-        assert np.array_equal(out["fused", prec][1], out["two_phase", prec][1]), prec
+        assert np.array_equal(out["fused", prec][0], out["two_phase_cuda_cores", prec][0]), prec
+        assert np.array_equal(out["fused", prec][1], out["two_phase_cuda_cores", prec][1]), prec
     return h
 
 
@@ -341,3 +341,39 @@ def test_pinned_host_outputs_written_directly(built, oracle, torch_cuda):
     h.sync()
     h.assemble(nz_d, f_d, **kw)
     assert torch.equal(nz_p, nz_d.cpu())
+
+
+@pytest.mark.parametrize("nel,scale", [((3, 3, 2), False), ((4, 3, 3), True), ((5, 4, 4), True)])
+def test_q2_tensor_core_elements(built, oracle, nel, scale):
+    """Q2 hexahedron elasticity with the element matrices on the tensor cores (tcgen05,
+    split-TF32 Gram products, FP32 accumulation; the default for this element) against the
+    FP64 oracle (1e-6) and against the CUDA-core element matrices (FP32-rounding apart)."""
+    fg, O = built, oracle
+    prob = O.box_problem(O.HEXAHEDRON, nel, ip_order=2, ncomp=3, qr_order=3, perturb=0.2, seed=61 + nel[0])
+    E, nu, b = 200e3, 0.3, (0.0, -1.0, 0.5)
+    sc = np.random.default_rng(6).lognormal(0.0, 0.5, prob.n_cells) if scale else None
+    h, out = check(fg, O, prob, dict(physics=fg.LINEAR_ELASTIC, p0=E, p1=nu, body=b, cell_scale=sc),
+                   dict(physics=O.LINEAR_ELASTIC, p0=E, p1=nu, body=b, cell_scale=sc), precisions=(0,))
+    nz_tc, f_tc = out[0]
+    nz_cc, f_cc = np.zeros(prob.nnz), np.zeros(prob.ndofs)
+    h.assemble(nz_cc, f_cc, physics=fg.LINEAR_ELASTIC, p0=E, p1=nu, body=b, cell_scale=sc, form="two_phase_cuda_cores")
+    assert rel_fro(nz_tc, nz_cc) <= 1e-6
+    assert np.array_equal(f_tc, f_cc)  # the loads are computed the same way on both paths
+    # no K / no f
+    nz1 = np.full(prob.nnz, 7.0)
+    f1 = np.zeros(prob.ndofs)
+    h.assemble(None, f1, physics=fg.LINEAR_ELASTIC, p0=E, p1=nu, body=b, cell_scale=sc)
+    assert np.array_equal(f1, f_tc)
+    h.assemble(nz1, None, physics=fg.LINEAR_ELASTIC, p0=E, p1=nu, body=b, cell_scale=sc)
+    assert np.array_equal(nz1, nz_tc)
+
+
+def test_q2_tensor_core_detj_error(built, oracle):
+    fg, O = built, oracle
+    nodes, cells = O.generate_grid(O.HEXAHEDRON, (2, 2, 2))
+    cells[3] = cells[3][[1, 0, 3, 2, 5, 4, 7, 6]]
+    prob = O.Problem.single(O.HEXAHEDRON, nodes, cells, ip_order=2, ncomp=3, qr_order=3).close().allocate_matrix()
+    h = make_handle(fg, O, prob)
+    with pytest.raises(fg.FEError) as ei:
+        h.assemble(np.zeros(prob.nnz), np.zeros(prob.ndofs), physics=fg.LINEAR_ELASTIC, p0=1.0, p1=0.3)
+    assert ei.value.name == "DETJ" and ei.value.cell == 4
