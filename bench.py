@@ -308,7 +308,8 @@ def run_ours(args):
         except Exception as exc:
             configs["apply"] = {"error": f"{type(exc).__name__}: {exc}"}
         for name, fn in (("heat", config_heat), ("q2", config_q2), ("adjoint", config_adjoint),
-                         ("mixed_graph", config_mixed_graph), ("elements", config_elements)):
+                         ("mixed_graph", config_mixed_graph), ("elements", config_elements),
+                         ("pattern", config_pattern)):
             try:
                 configs[name] = fn(fg, stream)
             except Exception as exc:  # reported, not fatal: the headline line still prints
@@ -547,6 +548,34 @@ def config_elements(fg, stream, nel=64, reps=10):
     return out
 
 
+def config_pattern(fg, stream, nel=128):
+    """allocate_matrix(dh) for 128^3 Q1 hex elasticity (6.4M dofs, nnz 513.6M): the host
+    fe_sparsity_pattern (threaded, all host cores) against fe_sparsity_pattern_device (GPU
+    kernels, outputs in device memory, inputs uploaded inside the timing); identical arrays."""
+    import torch
+    host = __import__("ferrite_gb300.host", fromlist=["host"])
+    n3 = (nel, nel, nel)
+    g = host.generate_grid(host.HEXAHEDRON, n3, (0, 0, 0), (1, 1, 1))
+    dh = host.DofHandler.from_grid(g, ip_order=1, n_components=3).close()
+    t0 = time.perf_counter()
+    cp_h, rv_h = dh.allocate_matrix()
+    host_s = time.perf_counter() - t0
+    dh.allocate_matrix(device=True)  # warm-up (module load, first allocations)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    cp_d, rv_d = dh.allocate_matrix(device=True)
+    torch.cuda.synchronize()
+    dev_s = time.perf_counter() - t0
+    same = bool(np.array_equal(cp_d.cpu().numpy(), cp_h) and np.array_equal(rv_d.cpu().numpy(), rv_h))
+    out = {"workload": f"hex{nel}_q1_vector_pattern", "ndofs": dh.ndofs, "nnz": int(len(rv_h)), "host_s": host_s,
+           "host_threads": os.cpu_count(), "device_s": dev_s, "identical": same,
+           "note": "device time includes the host pass over cell_dofs, the uploads and both passes "
+                   "(count, then fill); the two-call protocol of fe_sparsity_pattern"}
+    del rv_d, cp_d
+    torch.cuda.empty_cache()
+    return out
+
+
 def config_mixed_graph(fg, stream, steps=20):
     """~2M cells over three x-slabs sharing vertex nodes (Hex Q1 50%, Tet P1 25% as 6 per cube,
     Wedge P1 25% as 2 per cube), compressible Neo-Hooke (mu 1, lambda 10), u = 0.05 U(-1,1)
@@ -610,7 +639,7 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-configs", action="store_true", help="skip the heat / Q2 / adjoint / mixed-graph configurations")
     ap.add_argument("--nel", type=int, default=128, help="cells per axis (128 = the benchmark workload)")
-    ap.add_argument("--config", choices=["heat", "q2", "adjoint", "mixed_graph", "elements"],
+    ap.add_argument("--config", choices=["heat", "q2", "adjoint", "mixed_graph", "elements", "pattern"],
                     help="run only this configuration and print its JSON (profiling runs)")
     ap.add_argument("--q2-nel", type=int, default=64, help="cells per axis of the Q2 configuration")
     args = ap.parse_args()
@@ -620,7 +649,7 @@ def main():
         fg.build()
         stream = torch.cuda.Stream()
         fn = {"heat": config_heat, "q2": lambda g, s: config_q2(g, s, nel=args.q2_nel), "adjoint": config_adjoint,
-              "mixed_graph": config_mixed_graph, "elements": config_elements}[args.config]
+              "mixed_graph": config_mixed_graph, "elements": config_elements, "pattern": config_pattern}[args.config]
         print(json.dumps({"config": args.config, "result": fn(fg, stream)}))
         return
     if args.warmup < 3:

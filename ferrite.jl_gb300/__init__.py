@@ -42,7 +42,7 @@ _FORMS = {None: 0, "two_phase": TWO_PHASE, "fused": FUSED, "two_phase_cuda_cores
 EXPORTED = ["fe_abi_version", "fe_create", "fe_assemble", "fe_sync", "fe_last_error", "fe_get_info",
             "fe_get_index_map", "fe_plan_dry_run", "fe_distribute_dofs", "fe_sparsity_pattern", "fe_kernel_time", "fe_assemble_noalloc",
             "fe_assemble_adjoint", "fe_graph_capture", "fe_graph_replay", "fe_graph_destroy",
-            "fe_autotune", "fe_assemble_elements", "fe_dirichlet_create", "fe_apply", "fe_dirichlet_destroy",
+            "fe_autotune", "fe_assemble_elements", "fe_sparsity_pattern_device", "fe_dirichlet_create", "fe_apply", "fe_dirichlet_destroy",
             "fe_destroy"]
 
 i64p = ctypes.POINTER(ctypes.c_int64)
@@ -141,6 +141,8 @@ def lib():
         L.fe_distribute_dofs.argtypes = [ctypes.POINTER(GridDesc), ctypes.c_int32, ctypes.POINTER(SubdomainDesc),
                                          i64p, i64p, i64p]
         L.fe_sparsity_pattern.argtypes = [ctypes.POINTER(GridDesc), ctypes.c_int32, ctypes.POINTER(SubdomainDesc),
+                                          ctypes.POINTER(DofDesc), i64p, i64p, i64p]
+        L.fe_sparsity_pattern_device.argtypes = [ctypes.POINTER(GridDesc), ctypes.c_int32, ctypes.POINTER(SubdomainDesc),
                                           ctypes.POINTER(DofDesc), i64p, i64p, i64p]
         L.fe_kernel_time.argtypes = [ctypes.c_void_p, f64p, i64p]
         L.fe_assemble_noalloc.argtypes = [ctypes.c_void_p, ctypes.POINTER(AssembleParams), ctypes.c_void_p, ctypes.c_void_p]

@@ -281,20 +281,30 @@ class DofHandler:
         self.ndofs = nd.value
         return self
 
-    def allocate_matrix(self):
-        """``allocate_matrix(dh)`` via fe_sparsity_pattern: (colptr, rowval), 1-based Int64."""
+    def allocate_matrix(self, device: bool = False):
+        """``allocate_matrix(dh)`` via fe_sparsity_pattern: (colptr, rowval), 1-based Int64
+        numpy arrays. device=True builds it with fe_sparsity_pattern_device (GPU kernels) into
+        torch CUDA tensors."""
         g, d = self._descs()
         dd = DofDesc(self.ndofs, self.cell_dofs.ctypes.data_as(i64p), self.cell_dofs_offset.ctypes.data_as(i64p))
-        colptr = np.zeros(self.ndofs + 1, np.int64)
         nnz = ctypes.c_int64()
         L = lib()
-        rc = L.fe_sparsity_pattern(ctypes.byref(g), len(self.subs), d, ctypes.byref(dd),
-                                   colptr.ctypes.data_as(i64p), None, ctypes.byref(nnz))
+        fn = L.fe_sparsity_pattern_device if device else L.fe_sparsity_pattern
+        if device:
+            import torch
+            colptr = torch.zeros(self.ndofs + 1, dtype=torch.int64, device="cuda")
+            ptr = lambda t: ctypes.cast(t.data_ptr(), i64p)
+        else:
+            colptr = np.zeros(self.ndofs + 1, np.int64)
+            ptr = lambda t: t.ctypes.data_as(i64p)
+        rc = fn(ctypes.byref(g), len(self.subs), d, ctypes.byref(dd), ptr(colptr), None, ctypes.byref(nnz))
         if rc != FE_OK:
             raise FEError(rc)
-        rowval = np.empty(nnz.value, np.int64)
-        rc = L.fe_sparsity_pattern(ctypes.byref(g), len(self.subs), d, ctypes.byref(dd),
-                                   colptr.ctypes.data_as(i64p), rowval.ctypes.data_as(i64p), ctypes.byref(nnz))
+        if device:
+            rowval = torch.empty(nnz.value, dtype=torch.int64, device="cuda")
+        else:
+            rowval = np.empty(nnz.value, np.int64)
+        rc = fn(ctypes.byref(g), len(self.subs), d, ctypes.byref(dd), ptr(colptr), ptr(rowval), ctypes.byref(nnz))
         if rc != FE_OK:
             raise FEError(rc)
         return colptr, rowval

@@ -259,6 +259,11 @@ int fe_distribute_dofs(const fe_grid_desc* grid, int32_t n_subdomains, const fe_
                        int64_t* cell_dofs, int64_t* cell_dofs_offset, int64_t* ndofs);
 int fe_sparsity_pattern(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain_desc* subdomains,
                         const fe_dof_desc* dofs, int64_t* colptr, int64_t* rowval, int64_t* nnz);
+/* fe_sparsity_pattern on the device: the same arrays (bit for bit), built by GPU kernels; colptr
+ * and rowval may be host or device memory (device arrays are written in place, e.g. the
+ * colPtr/rowVal of a CuSparseMatrixCSC). Same two-call protocol. */
+int fe_sparsity_pattern_device(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain_desc* subdomains,
+                               const fe_dof_desc* dofs, int64_t* colptr, int64_t* rowval, int64_t* nnz);
 
 /* Device time of the assembly kernels launched with FE_PROFILE since the last call: waits
  * for them, returns the summed milliseconds and the number of launches, then resets. */
