@@ -42,11 +42,13 @@ _FORMS = {None: 0, "two_phase": TWO_PHASE, "fused": FUSED, "two_phase_cuda_cores
 EXPORTED = ["fe_abi_version", "fe_create", "fe_assemble", "fe_sync", "fe_last_error", "fe_get_info",
             "fe_get_index_map", "fe_plan_dry_run", "fe_distribute_dofs", "fe_sparsity_pattern", "fe_kernel_time", "fe_assemble_noalloc",
             "fe_assemble_adjoint", "fe_graph_capture", "fe_graph_replay", "fe_graph_destroy",
-            "fe_autotune", "fe_assemble_elements", "fe_sparsity_pattern_device", "fe_dirichlet_create", "fe_apply", "fe_dirichlet_destroy",
+            "fe_autotune", "fe_assemble_elements", "fe_sparsity_pattern_device", "fe_facet_set_create", "fe_assemble_facet_load",
+            "fe_facet_set_destroy", "fe_dirichlet_create", "fe_apply", "fe_dirichlet_destroy",
             "fe_destroy"]
 
 i64p = ctypes.POINTER(ctypes.c_int64)
 f64p = ctypes.POINTER(ctypes.c_double)
+i32p = ctypes.POINTER(ctypes.c_int32)
 
 
 class GridDesc(ctypes.Structure):
@@ -72,6 +74,12 @@ class AssembleParams(ctypes.Structure):
                 ("p0", ctypes.c_double), ("p1", ctypes.c_double), ("body", ctypes.c_double * 3),
                 ("cell_scale", ctypes.c_void_p), ("u", ctypes.c_void_p), ("cond_threshold", ctypes.c_double),
                 ("stream", ctypes.c_void_p)]
+
+
+class FacetDesc(ctypes.Structure):
+    """fe_facet_desc: FacetValues tables per reference facet and the set's (cell, facet) pairs."""
+    _fields_ = [("n_qp", ctypes.c_int32), ("n_ref_facets", ctypes.c_int32), ("qr_weights", f64p), ("N", f64p),
+                ("dMdxi", f64p), ("n_facets", ctypes.c_int64), ("cells", i64p), ("facets", i32p)]
 
 
 class ElementLayout(ctypes.Structure):
@@ -146,6 +154,11 @@ def lib():
                                           ctypes.POINTER(DofDesc), i64p, i64p, i64p]
         L.fe_kernel_time.argtypes = [ctypes.c_void_p, f64p, i64p]
         L.fe_assemble_noalloc.argtypes = [ctypes.c_void_p, ctypes.POINTER(AssembleParams), ctypes.c_void_p, ctypes.c_void_p]
+        L.fe_facet_set_create.argtypes = [ctypes.c_void_p, ctypes.POINTER(FacetDesc), ctypes.POINTER(ctypes.c_void_p)]
+        L.fe_assemble_facet_load.argtypes = [ctypes.c_void_p, ctypes.c_double, f64p, ctypes.c_uint32, ctypes.c_void_p,
+                                             ctypes.c_void_p]
+        L.fe_facet_set_destroy.argtypes = [ctypes.c_void_p]
+        L.fe_facet_set_destroy.restype = None
         L.fe_dirichlet_create.argtypes = [ctypes.c_void_p, i64p, ctypes.c_int64, i64p, ctypes.POINTER(ctypes.c_void_p)]
         L.fe_apply.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
                                ctypes.c_void_p]
@@ -369,6 +382,20 @@ class Handle:
             self._raise(rc)
         return ke, fe
 
+    def facet_set(self, cells, facets, tables):
+        """fe_facet_set_create: (cell, local facet) pairs (1-based) of one subdomain and the
+        FacetValues tables (n_ref_facets, n_qp, w, N, dM) per reference facet."""
+        nf, nq, w, N, dM = tables
+        keep = [np.ascontiguousarray(cells, np.int64), np.ascontiguousarray(facets, np.int32),
+                np.ascontiguousarray(w, np.float64), np.ascontiguousarray(N, np.float64), np.ascontiguousarray(dM, np.float64)]
+        d = FacetDesc(int(nq), int(nf), keep[2].ctypes.data_as(f64p), keep[3].ctypes.data_as(f64p), keep[4].ctypes.data_as(f64p),
+                      len(keep[0]), keep[0].ctypes.data_as(i64p), keep[1].ctypes.data_as(i32p))
+        out = ctypes.c_void_p()
+        rc = lib().fe_facet_set_create(self._h, ctypes.byref(d), ctypes.byref(out))
+        if rc != FE_OK:
+            self._raise(rc)
+        return FacetSet(self, out)
+
     def dirichlet(self, rowval, prescribed):
         """fe_dirichlet_create: Dirichlet constraints of this handle's pattern (K.rowval, host,
         1-based) on the 1-based ascending prescribed dofs (ch.prescribed_dofs)."""
@@ -581,6 +608,35 @@ class Dirichlet:
     def close(self):
         if self._c:
             lib().fe_dirichlet_destroy(self._c)
+            self._c = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class FacetSet:
+    """Facet loads over a facet set (fe_assemble_facet_load) into a device f (torch CUDA)."""
+
+    def __init__(self, handle, ptr):
+        self._handle = handle
+        self._c = ptr
+
+    def load(self, f, pressure: float, traction=(0.0, 0.0, 0.0), fillzero: bool = False, stream=None):
+        if stream is not None and hasattr(stream, "cuda_stream"):
+            stream = stream.cuda_stream
+        t = (ctypes.c_double * 3)(*[float(x) for x in list(traction) + [0.0] * (3 - len(traction))])
+        rc = lib().fe_assemble_facet_load(self._c, float(pressure), ctypes.cast(t, f64p), FILLZERO if fillzero else 0,
+                                          _ptr(f), stream)
+        if rc != FE_OK:
+            self._handle._raise(rc)
+        return f
+
+    def close(self):
+        if self._c:
+            lib().fe_facet_set_destroy(self._c)
             self._c = None
 
     def __del__(self):

@@ -14,6 +14,7 @@
 #include "registry.h"
 #include "adjoint.cuh"
 #include "dirichlet.cuh"
+#include "facet.cuh"
 #include "tile_kernel.cuh"
 
 using namespace fe;
@@ -478,6 +479,75 @@ int launch_assembly(fe_handle* h, const KernelEntry* ke, KernelArgs& A, bool fp6
 }
 
 }  // namespace
+
+// Facet sets of a handle (fe_facet_set_create / fe_assemble_facet_load)
+struct fe_facet_set {
+    fe_handle* h = nullptr;
+    FacetArgs args{};
+    int64_t n_rows = 0;
+    int64_t *rptr = nullptr, *rows = nullptr, *epos = nullptr;
+    DevStatus* status = nullptr;
+    DevStatus* status_h = nullptr;
+    std::vector<void*> allocs;
+    template <typename T>
+    cudaError_t upload(T** p, const T* src, size_t count) {
+        cudaError_t e = cudaMalloc((void**)p, (count ? count : 1) * sizeof(T));
+        if (e != cudaSuccess) return e;
+        allocs.push_back((void*)*p);
+        if (src && count) e = cudaMemcpy(*p, src, count * sizeof(T), cudaMemcpyHostToDevice);
+        return e;
+    }
+    ~fe_facet_set() {
+        for (void* p : allocs) cudaFree(p);
+        if (status_h) cudaFreeHost(status_h);
+    }
+};
+
+// Reference tangents u, v of a facet: the weighted normal is (J u) x (J v) in 3D and
+// ((J u)_2, -(J u)_1) in 2D, Ferrite's weighted_normal per reference shape and facet
+// (src/FEValues/facet_integrals.jl: quadrilateral 122-129, triangle 154-160, hexahedron
+// 190-199, tetrahedron 226-234, prism 264-273). Returns false for an unknown facet.
+bool facet_tangent_table(int32_t cell_type, int32_t facet, double* uv) {
+    for (int k = 0; k < 6; ++k) uv[k] = 0.0;
+    double* u = uv;
+    double* v = uv + 3;
+    switch (cell_type) {
+        case FE_QUADRILATERAL: {
+            static const double T[4][2] = {{1, 0}, {0, 1}, {-1, 0}, {0, -1}};
+            if (facet < 1 || facet > 4) return false;
+            u[0] = T[facet - 1][0];
+            u[1] = T[facet - 1][1];
+            return true;
+        }
+        case FE_TRIANGLE: {
+            static const double T[3][2] = {{-1, 1}, {0, -1}, {1, 0}};
+            if (facet < 1 || facet > 3) return false;
+            u[0] = T[facet - 1][0];
+            u[1] = T[facet - 1][1];
+            return true;
+        }
+        case FE_HEXAHEDRON: {
+            static const int T[6][2] = {{1, 0}, {0, 2}, {1, 2}, {2, 0}, {2, 1}, {0, 1}};
+            if (facet < 1 || facet > 6) return false;
+            u[T[facet - 1][0]] = 1;
+            v[T[facet - 1][1]] = 1;
+            return true;
+        }
+        case FE_TETRAHEDRON: {
+            static const double T[4][6] = {{0, 1, 0, 1, 0, 0}, {1, 0, 0, 0, 0, 1}, {1, 0, -1, 0, 1, -1}, {0, 0, 1, 0, 1, 0}};
+            if (facet < 1 || facet > 4) return false;
+            for (int k = 0; k < 6; ++k) uv[k] = T[facet - 1][k];
+            return true;
+        }
+        case FE_WEDGE: {
+            static const double T[5][6] = {{0, 1, 0, 1, 0, 0}, {1, 0, 0, 0, 0, 1}, {0, 0, 1, 0, 1, 0}, {-1, 1, 0, 0, 0, 1}, {1, 0, 0, 0, 1, 0}};
+            if (facet < 1 || facet > 5) return false;
+            for (int k = 0; k < 6; ++k) uv[k] = T[facet - 1][k];
+            return true;
+        }
+    }
+    return false;
+}
 
 // Dirichlet constraints of a handle (fe_dirichlet_create / fe_apply)
 struct fe_dirichlet {
@@ -1450,6 +1520,138 @@ int fe_apply(fe_dirichlet* ch, double* nzval, double* f, const double* inhomogen
 }
 
 void fe_dirichlet_destroy(fe_dirichlet* ch) { delete ch; }
+
+int fe_facet_set_create(fe_handle* h, const fe_facet_desc* d, fe_facet_set** out) {
+    if (!h || !d || !out || d->n_facets < 0 || (d->n_facets > 0 && (!d->cells || !d->facets))) return FE_ERR_ARG;
+    *out = nullptr;
+    const HostProblem& hp = h->hp;
+    if (d->n_qp < 1 || d->n_qp > 32 || d->n_ref_facets < 1 || !d->qr_weights || !d->N || !d->dMdxi)
+        return set_error(h, FE_ERR_ARG, "facet tables: 1 <= n_qp <= 32 points per facet and all tables required");
+    // every facet's cell in one subdomain
+    int sub = -1;
+    for (int64_t k = 0; k < d->n_facets; ++k) {
+        const int64_t c = d->cells[k] - 1;
+        if (c < 0 || c >= hp.n_cells || hp.cell_sub[c] < 0) return set_error(h, FE_ERR_BOUNDS, "facet cell out of range or in no subdomain");
+        if (d->facets[k] < 1 || d->facets[k] > d->n_ref_facets) return set_error(h, FE_ERR_BOUNDS, "local facet number out of range");
+        if (sub < 0) sub = hp.cell_sub[c];
+        else if (hp.cell_sub[c] != sub) return set_error(h, FE_ERR_UNSUPPORTED, "the facets' cells must belong to one subdomain");
+    }
+    if (sub < 0) sub = 0;
+    const HostSub& hs = hp.subs[sub];
+    fe_facet_set* fs = new (std::nothrow) fe_facet_set();
+    if (!fs) return FE_ERR_OOM;
+    FacetArgs& A = fs->args;
+    A.n = d->n_facets;
+    A.nf = d->n_ref_facets;
+    A.nqp = d->n_qp;
+    A.nb = hs.nb;
+    A.ng = hs.ng;
+    A.nc = hs.nc;
+    A.dim = hp.dim;
+    A.x = h->base.xd;
+    const int nbf = hs.nb * hs.nc;
+    std::vector<double> tang((size_t)A.nf * 6);
+    for (int f = 0; f < A.nf; ++f)
+        if (!facet_tangent_table(hs.cell_type, f + 1, tang.data() + (size_t)f * 6)) {
+            delete fs;
+            return set_error(h, FE_ERR_UNSUPPORTED, "no facet normals for this cell type / facet count");
+        }
+    std::vector<int32_t> nodes((size_t)A.n * A.ng), fnr((size_t)A.n), cid((size_t)A.n);
+    std::vector<int64_t> dofs((size_t)A.n * nbf);
+    for (int64_t k = 0; k < A.n; ++k) {
+        const int64_t c = d->cells[k] - 1;
+        const int64_t kk = hp.cell_local[c];
+        for (int j = 0; j < A.ng; ++j) nodes[k * A.ng + j] = hs.conn[kk * A.ng + j];
+        fnr[k] = d->facets[k] - 1;
+        cid[k] = (int32_t)c;
+        const int64_t* cd = hp.cell_dofs.data() + hp.cell_dofs_off[c] - 1;
+        for (int I = 0; I < nbf; ++I) dofs[k * nbf + I] = cd[I] - 1;
+    }
+    // per dof, its (facet, entry) positions in facet order
+    std::vector<int64_t> cnt((size_t)hp.ndofs + 1, 0);
+    for (int64_t t = 0; t < (int64_t)dofs.size(); ++t) ++cnt[dofs[t] + 1];
+    std::vector<int64_t> rows, rptr(1, 0), slot((size_t)hp.ndofs, -1);
+    for (int64_t r = 0; r < hp.ndofs; ++r)
+        if (cnt[r + 1]) {
+            slot[r] = (int64_t)rows.size();
+            rows.push_back(r);
+            rptr.push_back(rptr.back() + cnt[r + 1]);
+        }
+    std::vector<int64_t> epos((size_t)rptr.back());
+    {
+        std::vector<int64_t> fill(rptr.begin(), rptr.end() - 1);
+        for (int64_t t = 0; t < (int64_t)dofs.size(); ++t) epos[fill[slot[dofs[t]]]++] = t;
+    }
+    fs->h = h;
+    fs->n_rows = (int64_t)rows.size();
+    const size_t tq = (size_t)A.nf * A.nqp;
+    cudaError_t e = cudaSetDevice(h->device);
+    int32_t *dn = nullptr, *df = nullptr, *dc = nullptr;
+    double *dw = nullptr, *dN = nullptr, *dM = nullptr, *dt = nullptr, *dcon = nullptr;
+    if (e == cudaSuccess) e = fs->upload(&dn, nodes.data(), nodes.size());
+    if (e == cudaSuccess) e = fs->upload(&df, fnr.data(), fnr.size());
+    if (e == cudaSuccess) e = fs->upload(&dc, cid.data(), cid.size());
+    if (e == cudaSuccess) e = fs->upload(&dw, d->qr_weights, tq);
+    if (e == cudaSuccess) e = fs->upload(&dN, d->N, tq * A.nb);
+    if (e == cudaSuccess) e = fs->upload(&dM, d->dMdxi, tq * A.ng * A.dim);
+    if (e == cudaSuccess) e = fs->upload(&dt, tang.data(), tang.size());
+    if (e == cudaSuccess) e = fs->upload<double>(&dcon, nullptr, (size_t)A.n * nbf);
+    if (e == cudaSuccess) e = fs->upload(&fs->rptr, rptr.data(), rptr.size());
+    if (e == cudaSuccess) e = fs->upload(&fs->rows, rows.data(), rows.size());
+    if (e == cudaSuccess) e = fs->upload(&fs->epos, epos.data(), epos.size());
+    if (e == cudaSuccess) e = fs->upload<DevStatus>(&fs->status, nullptr, 1);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&fs->status_h, sizeof(DevStatus));
+    if (e != cudaSuccess) {
+        delete fs;
+        return cuda_fail(h, e, "facet set upload");
+    }
+    A.nodes = dn;
+    A.fnr = df;
+    A.cellid = dc;
+    A.w = dw;
+    A.N = dN;
+    A.dM = dM;
+    A.tang = dt;
+    A.contrib = dcon;
+    A.status = fs->status;
+    *out = fs;
+    return FE_OK;
+}
+
+int fe_assemble_facet_load(fe_facet_set* fs, double pressure, const double* traction, uint32_t flags, double* f, void* stream) {
+    if (!fs || !f) return FE_ERR_ARG;
+    fe_handle* h = fs->h;
+    if (!is_device_ptr(f)) return set_error(h, FE_ERR_ARG, "f must be device memory");
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e;
+    FacetArgs A = fs->args;
+    A.pressure = pressure;
+    for (int a = 0; a < 3; ++a) A.t[a] = traction ? traction[a] : 0.0;
+    if ((flags & FE_FILLZERO) && (e = cudaMemsetAsync(f, 0, h->hp.ndofs * 8, st)) != cudaSuccess) return cuda_fail(h, e, "fill zero");
+    if ((e = cudaMemsetAsync(fs->status, 0xFF, 2 * sizeof(unsigned long long), st)) != cudaSuccess ||
+        (e = cudaMemsetAsync(&fs->status->flagged, 0, 2 * sizeof(unsigned int), st)) != cudaSuccess)
+        return cuda_fail(h, e, "status reset");
+    device_attributes(h);
+    if (A.n > 0) {
+        const unsigned g1 = (unsigned)std::min<int64_t>((A.n + FACET_WARPS - 1) / FACET_WARPS, (int64_t)h->n_sm * 16);
+        facet_contrib<<<g1, 32 * FACET_WARPS, 0, st>>>(A);
+        const unsigned g2 = (unsigned)std::max<int64_t>(1, std::min<int64_t>((fs->n_rows + 255) / 256, (int64_t)h->n_sm * 8));
+        if (fs->n_rows) facet_gather<<<g2, 256, 0, st>>>(f, A.contrib, fs->rptr, fs->rows, fs->epos, fs->n_rows);
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(h, e, "facet kernels");
+    if ((e = cudaMemcpyAsync(fs->status_h, fs->status, sizeof(DevStatus), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return cuda_fail(h, e, "status read");
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(h, e, "cudaStreamSynchronize");
+    if (fs->status_h->detj_key != ~0ull) {
+        const int64_t cell = (int64_t)(fs->status_h->detj_key >> 32) + 1;
+        char buf[120];
+        std::snprintf(buf, sizeof buf, "det(J) is not positive on a facet of cell %lld", (long long)cell);
+        return set_error(h, FE_ERR_DETJ, buf, cell, 0.0);
+    }
+    return FE_OK;
+}
+
+void fe_facet_set_destroy(fe_facet_set* fs) { delete fs; }
 
 }  // extern "C"
 

@@ -213,6 +213,33 @@ int fe_assemble_elements(fe_handle* h, const fe_assemble_params* params, void* k
  * without a diagonal entry in the pattern is FE_ERR_PATTERN_MISSING at creation. Destroy the
  * constraints before their handle.
  */
+/*
+ * Facet (Neumann) loads: FacetValues on a facet set (src/FEValues/FacetValues.jl:129-155) and
+ * f[celldofs] += fe, fe[(i, a)] = sum_q (N_i t_a) dGamma with t = pressure n + traction (vector
+ * fields; the pressure load of benchmark/helper.jl:331-348, the traction of
+ * hyperelasticity.jl:278-290 with pressure = -tn), t = pressure for scalar fields (a flux).
+ * dGamma = |weighted normal| w and n its direction, the weighted normal being Ferrite's
+ * (src/FEValues/facet_integrals.jl) from the cell's Jacobian at the facet point. The caller
+ * passes the FacetValues tables per reference facet (pad a facet's rule with zero weights when
+ * the facets' rules differ in length) and the set's (cell, local facet) pairs, all of one
+ * subdomain. FP64; facets are added in the given order, so the result is that of a serial
+ * FP64 loop. fe_assemble_facet_load: f is DEVICE memory; flags FE_FILLZERO; synchronous.
+ */
+typedef struct {
+    int32_t n_qp;            /* points per facet (FacetQuadratureRule), <= 32 */
+    int32_t n_ref_facets;    /* nfacets of the reference shape */
+    const double* qr_weights;/* [n_ref_facets][n_qp] */
+    const double* N;         /* [n_ref_facets][n_qp][n_base] field shape values at the facet points */
+    const double* dMdxi;     /* [n_ref_facets][n_qp][n_geo][dim] geometric shape gradients there */
+    int64_t n_facets;
+    const int64_t* cells;    /* [n_facets] 1-based cell ids (FacetIndex) */
+    const int32_t* facets;   /* [n_facets] 1-based local facet numbers */
+} fe_facet_desc;
+typedef struct fe_facet_set fe_facet_set;
+int fe_facet_set_create(fe_handle* h, const fe_facet_desc* desc, fe_facet_set** out);
+int fe_assemble_facet_load(fe_facet_set* set, double pressure, const double* traction, uint32_t flags, double* f, void* stream);
+void fe_facet_set_destroy(fe_facet_set* set);
+
 typedef struct fe_dirichlet fe_dirichlet;
 int fe_dirichlet_create(fe_handle* h, const int64_t* rowval, int64_t n_prescribed, const int64_t* prescribed_dofs,
                         fe_dirichlet** out);

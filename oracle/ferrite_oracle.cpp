@@ -1199,6 +1199,110 @@ int or_adjoint(const or_problem* p, const or_physics* ph, const double* u, const
     return OR_OK;
 }
 
+// reference tangents u, v of facet `facet` (1-based): weighted_normal = (J u) x (J v) in 3D,
+// rot(J u) = ((J u)_2, -(J u)_1) in 2D (facet_integrals.jl: quadrilateral 122-129, triangle
+// 154-160, hexahedron 190-199, tetrahedron 226-234, prism 264-273)
+static bool facet_tangents(int32_t ct, int32_t facet, double u[3], double v[3]) {
+    for (int k = 0; k < 3; ++k) u[k] = v[k] = 0.0;
+    auto e = [](double* x, int k, double s) { x[k] += s; };
+    switch (ct) {
+        case OR_QUADRILATERAL:
+            if (facet == 1) e(u, 0, 1); else if (facet == 2) e(u, 1, 1); else if (facet == 3) e(u, 0, -1);
+            else if (facet == 4) e(u, 1, -1); else return false;
+            return true;
+        case OR_TRIANGLE:
+            if (facet == 1) { e(u, 0, -1); e(u, 1, 1); } else if (facet == 2) e(u, 1, -1); else if (facet == 3) e(u, 0, 1);
+            else return false;
+            return true;
+        case OR_HEXAHEDRON: {
+            static const int T[6][2] = {{1, 0}, {0, 2}, {1, 2}, {2, 0}, {2, 1}, {0, 1}};
+            if (facet < 1 || facet > 6) return false;
+            e(u, T[facet - 1][0], 1); e(v, T[facet - 1][1], 1);
+            return true;
+        }
+        case OR_TETRAHEDRON:
+            if (facet == 1) { e(u, 1, 1); e(v, 0, 1); }
+            else if (facet == 2) { e(u, 0, 1); e(v, 2, 1); }
+            else if (facet == 3) { e(u, 0, 1); e(u, 2, -1); e(v, 1, 1); e(v, 2, -1); }
+            else if (facet == 4) { e(u, 2, 1); e(v, 1, 1); }
+            else return false;
+            return true;
+        case OR_WEDGE:
+            if (facet == 1) { e(u, 1, 1); e(v, 0, 1); }
+            else if (facet == 2) { e(u, 0, 1); e(v, 2, 1); }
+            else if (facet == 3) { e(u, 2, 1); e(v, 1, 1); }
+            else if (facet == 4) { e(u, 1, 1); e(u, 0, -1); e(v, 2, 1); }
+            else if (facet == 5) { e(u, 0, 1); e(v, 1, 1); }
+            else return false;
+            return true;
+    }
+    return false;
+}
+
+int or_facet_load(const or_problem* p, int64_t n, const int64_t* cells, const int32_t* facets, int32_t nf, int32_t nqp,
+                  const double* w, const double* N, const double* dM, double pressure, const double* traction, double* f,
+                  or_error* err) {
+    const int dim = p->dim;
+    for (int64_t k = 0; k < n; ++k) {
+        const int64_t c = cells[k] - 1;
+        const int32_t fc = facets[k];
+        if (c < 0 || c >= p->n_cells || fc < 1 || fc > nf) return OR_ERR_BOUNDS;
+        const int32_t ct = p->cell_types[c];
+        int sdh = -1;
+        for (int s = 0; s < p->n_sdh && sdh < 0; ++s)
+            for (int64_t t = p->sdh_cellset_offset[s]; t < p->sdh_cellset_offset[s + 1]; ++t)
+                if (p->sdh_cellset[t] == c + 1) { sdh = s; break; }
+        if (sdh < 0) return OR_ERR_ARG;
+        const int nc = p->sdh_ncomp[sdh];
+        const int nb = or_nbase(ct, p->sdh_ip_order[sdh]);
+        const int64_t off = p->cell_nodes_offset[c];
+        const int ng = (int)(p->cell_nodes_offset[c + 1] - off);
+        double u[3], v[3];
+        if (!facet_tangents(ct, fc, u, v)) return OR_ERR_ARG;
+        std::vector<double> fe((size_t)nb * nc, 0.0);
+        for (int q = 0; q < nqp; ++q) {
+            const double* dMq = dM + ((size_t)(fc - 1) * nqp + q) * ng * dim;
+            double J[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+            for (int j = 0; j < ng; ++j) {
+                const double* x = p->nodes + (p->cell_nodes[off + j] - 1) * dim;
+                for (int a = 0; a < dim; ++a)
+                    for (int b = 0; b < dim; ++b) J[a * 3 + b] = J[a * 3 + b] + x[a] * dMq[j * dim + b];
+            }
+            double wn[3] = {0, 0, 0};
+            if (dim == 2) {
+                const double ju0 = J[0] * u[0] + J[1] * u[1], ju1 = J[3] * u[0] + J[4] * u[1];
+                wn[0] = ju1;
+                wn[1] = -ju0;
+            } else {
+                double ju[3], jv[3];
+                for (int a = 0; a < 3; ++a) {
+                    ju[a] = J[a * 3] * u[0] + J[a * 3 + 1] * u[1] + J[a * 3 + 2] * u[2];
+                    jv[a] = J[a * 3] * v[0] + J[a * 3 + 1] * v[1] + J[a * 3 + 2] * v[2];
+                }
+                wn[0] = ju[1] * jv[2] - ju[2] * jv[1];
+                wn[1] = ju[2] * jv[0] - ju[0] * jv[2];
+                wn[2] = ju[0] * jv[1] - ju[1] * jv[0];
+            }
+            const double nrm = std::sqrt(wn[0] * wn[0] + wn[1] * wn[1] + wn[2] * wn[2]);
+            if (!(nrm > 0.0)) {
+                if (err) { err->code = OR_ERR_DETJ; err->cell = c + 1; err->detJ = nrm; }
+                return OR_ERR_DETJ;
+            }
+            const double dG = nrm * w[(size_t)(fc - 1) * nqp + q];
+            const double* Nq = N + ((size_t)(fc - 1) * nqp + q) * nb;
+            for (int i = 0; i < nb; ++i)
+                for (int a = 0; a < nc; ++a) {
+                    const double t = nc == 1 ? pressure : pressure * (wn[a] / nrm) + traction[a];
+                    const double s = Nq[i] * t;
+                    fe[(size_t)i * nc + a] = fe[(size_t)i * nc + a] + s * dG;
+                }
+        }
+        const int64_t* cd = p->cell_dofs + p->cell_dofs_offset[c] - 1;
+        for (int I = 0; I < nb * nc; ++I) f[cd[I] - 1] = f[cd[I] - 1] + fe[I];
+    }
+    return OR_OK;
+}
+
 // apply! for Dirichlet constraints, ConstraintHandler.jl:711-744 step by step (no affine
 // constraints: _condense! returns early for them, 803-805)
 int or_apply(int64_t n, const int64_t* colptr, const int64_t* rowval, double* nzval, double* f, int64_t np,

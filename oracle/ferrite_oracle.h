@@ -21,6 +21,8 @@
  *   CSC assembler        src/assembler.jl:287-291, 322-457, 513-576; src/arrayutils.jl:100-152
  *   greedy coloring      src/Grid/coloring.jl:47-143
  *   Dirichlet apply!     src/Dofs/ConstraintHandler.jl:711-767, 931-955
+ *   facet loads          src/FEValues/FacetValues.jl:129-155, facet_integrals.jl:85-273,
+ *                        benchmark/helper.jl:331-348
  *
  * Conventions follow Ferrite's memory layout: node coordinates AoS [n_nodes][dim],
  * connectivity, cell_dofs, cell_dofs_offset, colptr and rowval are 1-based Int64, nzval is
@@ -97,6 +99,17 @@ int or_assemble(const or_problem* p, const or_physics* phys, int32_t nthreads, i
 int or_element_matrix(const or_problem* p, const or_physics* phys, int64_t cell, double* Ke,
                       double* fe, or_error* err);
 int or_index_map(const or_problem* p, int64_t cell, int64_t* positions);
+
+/* Facet (Neumann) loads: for each facet (cell, local facet number) of the set, in the given
+ * order, FacetValues reinit! (src/FEValues/FacetValues.jl:129-155: J = sum_k x_k (x) dM_k at the
+ * facet point, wn = weighted_normal(J, refshape, facet) (src/FEValues/facet_integrals.jl),
+ * dGamma = |wn| w, n = wn / |wn|, detJ = |wn| > 0) and f[celldofs] += fe with
+ * fe[(i, a)] = sum_q (N_i(q) t_a) dGamma, t = pressure n + traction (benchmark/helper.jl:331-348;
+ * hyperelasticity.jl:278-290 with pressure = -tn); scalar fields: t = pressure.
+ * Tables per reference facet: w [nf][nqp], N [nf][nqp][n_base], dM [nf][nqp][n_geo][rdim]. */
+int or_facet_load(const or_problem* p, int64_t n, const int64_t* cells, const int32_t* facets, int32_t n_ref_facets,
+                  int32_t n_qp, const double* w, const double* N, const double* dM, double pressure,
+                  const double* traction, double* f, or_error* err);
 
 /* apply!(K, f, ch, applyzero) for Dirichlet constraints (src/Dofs/ConstraintHandler.jl:711-744):
  * m = meandiag(K) (944-955, before any change); unless applyzero, f -= K * g over the prescribed

@@ -88,6 +88,8 @@ def lib():
                                             ctypes.c_int64, f64p, f64p, ctypes.POINTER(_Error)]
             L.or_index_map.argtypes = [ctypes.POINTER(_Problem), ctypes.c_int64, i64p]
             L.or_greedy_coloring.argtypes = [ctypes.POINTER(_Problem), i32p, i32p]
+            L.or_facet_load.argtypes = [ctypes.POINTER(_Problem), ctypes.c_int64, i64p, i32p, ctypes.c_int32, ctypes.c_int32,
+                                        f64p, f64p, f64p, ctypes.c_double, f64p, f64p, ctypes.POINTER(_Error)]
             L.or_apply.argtypes = [ctypes.c_int64, i64p, i64p, f64p, f64p, ctypes.c_int64, i64p, f64p, ctypes.c_int32]
             L.or_adjoint.argtypes = [ctypes.POINTER(_Problem), ctypes.POINTER(_Physics), f64p, f64p, f64p, f64p, f64p,
                                      ctypes.POINTER(_Error)]
@@ -366,6 +368,25 @@ class Problem:
         if rc:
             raise OracleError(rc, err)
         return d_cell, d_X
+
+    def facet_load(self, cells, facets, tables, pressure, traction=(0.0, 0.0, 0.0), f=None):
+        """Facet loads over (cell, local facet) pairs (1-based), f += (in place; zeros if None).
+        tables = (n_ref_facets, n_qp, w, N, dM) per reference facet."""
+        nf, nq, w, N, dM = tables
+        c = np.ascontiguousarray(cells, np.int64)
+        fc = np.ascontiguousarray(facets, np.int32)
+        if f is None:
+            f = np.zeros(self.ndofs)
+        t = np.ascontiguousarray(list(traction) + [0.0] * (3 - len(traction)), np.float64)
+        P = self._struct()
+        err = _Error()
+        rc = lib().or_facet_load(ctypes.byref(P), len(c), _p(c, i64p), _p(fc, i32p), nf, nq,
+                                 _p(np.ascontiguousarray(w, np.float64), f64p), _p(np.ascontiguousarray(N, np.float64), f64p),
+                                 _p(np.ascontiguousarray(dM, np.float64), f64p), float(pressure), _p(t, f64p),
+                                 _p(f, f64p), ctypes.byref(err))
+        if rc:
+            raise OracleError(rc, err)
+        return f
 
     def apply(self, nzval, f, prescribed, inhomogeneities=None, applyzero=False):
         """apply!(K, f, ch) / apply_zero!(K, f, ch) for Dirichlet constraints, in place

@@ -93,3 +93,30 @@ def test_autotune_keeps_fastest_plan_and_results(built, oracle, torch_cuda):
     h.assemble(nz, f, **kw)
     # summation order is cell order whatever the tiles: bitwise the same
     assert torch.equal(nz, nz0) and torch.equal(f, f0)
+
+
+def test_graph_replay_two_phase_tensor_core(built, oracle, torch_cuda):
+    """Q2 hexahedra (two-phase form, element matrices on the tensor cores) captured as a
+    graph: the element kernel, the gather-only tile kernel and the scratch they share."""
+    torch = torch_cuda
+    fg, O = built, oracle
+    prob = O.box_problem(O.HEXAHEDRON, (3, 3, 2), ip_order=2, ncomp=3, qr_order=3, perturb=0.2, seed=8)
+    h = make_handle(fg, O, prob)
+    rng = np.random.default_rng(2)
+    scales = [torch.as_tensor(rng.lognormal(0.0, 0.5, prob.n_cells), device="cuda") for _ in range(2)]
+    nz = torch.zeros(prob.nnz, dtype=torch.float64, device="cuda")
+    f = torch.zeros(prob.ndofs, dtype=torch.float64, device="cuda")
+    kw = dict(physics=fg.LINEAR_ELASTIC, p0=200e3, p1=0.3, body=(0.0, 0.0, -1.0))
+    stream = torch.cuda.Stream()
+    nz2 = torch.zeros_like(nz)
+    gid = h.graph_capture([dict(cell_scale=scales[0], **kw), dict(cell_scale=scales[1], **kw)], [nz, nz2], [f, f], stream)
+    nz.zero_()
+    nz2.zero_()
+    h.graph_replay(gid, stream)
+    ref1 = torch.zeros_like(nz)
+    ref2 = torch.zeros_like(nz)
+    fr = torch.zeros_like(f)
+    h.assemble(ref1, fr, cell_scale=scales[0], **kw)
+    h.assemble(ref2, fr, cell_scale=scales[1], **kw)
+    assert torch.equal(nz, ref1) and torch.equal(nz2, ref2) and torch.equal(f, fr)
+    h.graph_destroy(gid)

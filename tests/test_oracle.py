@@ -329,3 +329,51 @@ def test_index_map_matches_binary_search(oracle):
             a, b = p.colptr[d[J] - 1] - 1, p.colptr[d[J]] - 1
             expect = a + np.searchsorted(p.rowval[a:b], d) + 1
             assert np.array_equal(pos[:, J], expect)
+
+
+def test_facet_load_matches_tutorial_traction(oracle):
+    """The oracle's facet loads (FacetValues.jl:129-155, 1-point facet rule on tetrahedra)
+    reproduce the traction the hyperelasticity golden above is computed with (-tn n area/3 per
+    facet node, hyperelasticity.jl:278-290)."""
+    from helpers import boundary_facets, facet_tables
+    O = oracle
+    N, L = 4, 1.0
+    p = O.box_problem(O.TETRAHEDRON, (N, N, N), [0, 0, 0], [L, L, L], ip_order=1, ncomp=3, qr_order=1)
+    x = p.nodes
+    n2d = node_to_dofs(p, 3)
+    gt = np.zeros(p.ndofs)
+    faces = [(0, 2, 1), (0, 1, 3), (1, 2, 3), (0, 3, 2)]
+    sides = [(2, L, (0, 0, 1)), (2, 0, (0, 0, -1)), (1, 0, (0, -1, 0)), (1, L, (0, 1, 0))]
+    for c in range(p.n_cells):
+        cn = p.cells_of(c) - 1
+        for fc in faces:
+            nd = cn[list(fc)]
+            P = x[nd]
+            for ax, val, nrm in sides:
+                if np.all(np.abs(P[:, ax] - val) < 1e-12):
+                    area = 0.5 * np.linalg.norm(np.cross(P[1] - P[0], P[2] - P[0]))
+                    for n in nd:
+                        gt[n2d[n]] -= 0.1 * np.array(nrm) * area / 3
+    sel = [boundary_facets(p, O.TETRAHEDRON, lambda X, ax=ax, val=val: abs(X[ax] - val) < 1e-12) for ax, val, _ in sides]
+    cells = np.concatenate([c for c, _ in sel])
+    facets = np.concatenate([f for _, f in sel])
+    f = p.facet_load(cells, facets, facet_tables(O, O.TETRAHEDRON, 1, 1), pressure=-0.1)
+    assert np.allclose(f, gt, rtol=1e-13, atol=1e-16)
+
+
+@pytest.mark.parametrize("ct,ip", [(4, 1), (4, 2), (2, 1)])
+def test_facet_load_integrates_pressure(oracle, ct, ip):
+    """sum of f over a flat face's dofs = pressure * area * n + traction * area (partition of
+    unity of the shape functions)."""
+    from helpers import boundary_facets, facet_tables
+    O = oracle
+    d = 3 if ct == O.HEXAHEDRON else 2
+    nel = (3, 4, 2) if d == 3 else (5, 4)
+    p = O.box_problem(ct, nel, [0.0] * d, [2.0, 1.0, 3.0][:d], ip_order=ip, ncomp=d, qr_order=2, perturb=0.2, seed=9)
+    cells, facets = boundary_facets(p, ct, lambda X: abs(X[0] - 2.0) < 1e-12)
+    t = (0.5, -0.25, 1.0)[:d]
+    f = p.facet_load(cells, facets, facet_tables(O, ct, ip, 2), pressure=1.5, traction=t)
+    area = 3.0 if d == 3 else 1.0
+    sums = [f[a::d].sum() for a in range(d)]
+    expect = [1.5 * area + t[0] * area] + [t[a] * area for a in range(1, d)]
+    assert np.allclose(sums, expect, rtol=1e-13, atol=1e-13)
