@@ -414,7 +414,27 @@ def config_apply(fg, stream, P, nz, f, kw, reps=20):
            "note": "fe_apply touches the prescribed columns, rows and diagonals only; the CPU reference "
                    "(oracle restatement of ConstraintHandler.jl apply!) also scans every rowval entry"}
     ch.close()
+    # facet loads on the same system: pressure on the x = 1 face (local facet 3 of the cells
+    # with i = n-1), a traction on the z = 1 face (facet 6 of the cells with k = n-1)
+    n = NEL[0]
+    ids = np.arange(n ** 3, dtype=np.int64)
+    i, k = ids % n, ids // (n * n)
+    cells = np.concatenate([ids[i == n - 1], ids[k == n - 1]]) + 1
+    facets = np.concatenate([np.full(n * n, 3, np.int32), np.full(n * n, 6, np.int32)])
+    fs = h.facet_set(cells, facets, host_module().facet_values(host_module().HEXAHEDRON, 1, 2))
+    f.zero_()
+    fs.load(f, pressure=-1.0, traction=(0.0, 0.0, -0.5), stream=stream)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        fs.load(f, pressure=-1.0, traction=(0.0, 0.0, -0.5), stream=stream)
+    out["facet_load"] = {"facets": int(len(cells)), "ms": (time.perf_counter() - t0) * 1e3 / reps,
+                         "note": "fe_assemble_facet_load, synchronous (host wall time per call)"}
+    fs.close()
     return out
+
+
+def host_module():
+    return __import__("ferrite_gb300.host", fromlist=["host"])
 
 
 def config_heat(fg, stream):

@@ -227,6 +227,42 @@ class CellValues:
         self.M, self.dMdxi = shape_tables(self.cell_type, 1, self.points)
 
 
+def _facet_points(cell_type: int, order: int):
+    """FacetQuadratureRule{RefShape}(order) (src/Quadrature/quadrature.jl:214-245): per reference
+    facet, (weights [nq], points [nq, rdim] in cell reference coordinates), the facet rule
+    mapped by Ferrite's facet_to_element_transformation (src/FEValues/facet_integrals.jl)."""
+    if cell_type in (QUADRILATERAL, TRIANGLE):
+        x, w = np.polynomial.legendre.leggauss(order)
+        if cell_type == QUADRILATERAL:
+            maps = [lambda p: (p, -1.0), lambda p: (1.0, p), lambda p: (-p, 1.0), lambda p: (-1.0, -p)]
+            return [(w, np.array([m(p) for p in x])) for m in maps]
+        h = (x + 1) / 2  # the facet parameter on (0, 1): half the length, half the weights
+        maps = [lambda t: (1 - t, t), lambda t: (0.0, 1 - t), lambda t: (t, 0.0)]
+        return [(w / 2, np.array([m(t) for t in h])) for m in maps]
+    if cell_type == HEXAHEDRON:
+        w, q = quadrature_rule(QUADRILATERAL, order)
+        maps = [lambda a, b: (b, a, -1.0), lambda a, b: (a, -1.0, b), lambda a, b: (1.0, a, b),
+                lambda a, b: (-a, 1.0, b), lambda a, b: (-1.0, b, a), lambda a, b: (a, b, 1.0)]
+        return [(w, np.array([m(a, b) for a, b in q])) for m in maps]
+    if cell_type == TETRAHEDRON:
+        w, q = quadrature_rule(TRIANGLE, order)
+        maps = [lambda a, b: (1 - a - b, b, 0.0), lambda a, b: (b, 0.0, 1 - a - b), lambda a, b: (a, b, 1 - a - b),
+                lambda a, b: (0.0, 1 - a - b, b)]
+        return [(w, np.array([m(a, b) for a, b in q])) for m in maps]
+    raise ValueError(f"no facet rule for cell type {cell_type}")
+
+
+def facet_values(cell_type: int, ip_order: int, qr_order: int):
+    """``FacetValues(FacetQuadratureRule(qr_order), ip)``: the tables fe_facet_set_create takes,
+    (n_ref_facets, n_qp, w [nf, nq], N [nf, nq, nb], dMdxi [nf, nq, ng, rdim])."""
+    rules = _facet_points(cell_type, qr_order)
+    nf, nq = len(rules), len(rules[0][0])
+    W = np.stack([np.asarray(w, float) for w, _ in rules])
+    N = np.stack([shape_tables(cell_type, ip_order, p)[0] for _, p in rules])
+    dM = np.stack([shape_tables(cell_type, 1, p)[1] for _, p in rules])
+    return nf, nq, np.ascontiguousarray(W), np.ascontiguousarray(N), np.ascontiguousarray(dM)
+
+
 # ---------------------------------------------------------------------------------------
 # DofHandler + pattern (native)
 # ---------------------------------------------------------------------------------------

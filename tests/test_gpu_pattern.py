@@ -1,6 +1,6 @@
 """allocate_matrix(dh) on the device (fe_sparsity_pattern_device) against the host
 fe_sparsity_pattern (itself checked bit for bit against the oracle's restatement of
-sparsity_pattern.jl in tests/test_host_setup.py): identical colptr and rowval."""
+sparsity_pattern.jl in tests/test_host.py): identical colptr and rowval."""
 import numpy as np
 import pytest
 

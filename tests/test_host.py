@@ -60,3 +60,16 @@ def test_tables_match_oracle(host, oracle, ct, orders):
             N, dN = host.shape_tables(ct, ip, p2)
             N2, dN2 = oracle.shape_tables(ct, ip, p2)
             assert np.allclose(N, N2, atol=1e-15) and np.allclose(dN, dN2, atol=1e-15)
+
+
+@pytest.mark.parametrize("ct,ip,qo", [(2, 1, 2), (2, 2, 3), (1, 1, 2), (4, 1, 2), (4, 2, 3), (3, 1, 1), (3, 1, 2)])
+def test_facet_values_tables(fg, oracle, ct, ip, qo):
+    """The product's FacetValues tables (host.facet_values) equal the oracle-side ones built
+    from the reference's facet rules and shape functions."""
+    from helpers import facet_tables
+    host = __import__("ferrite_gb300.host", fromlist=["host"])
+    a = host.facet_values(ct, ip, qo)
+    b = facet_tables(oracle, ct, ip, qo)
+    assert a[0] == b[0] and a[1] == b[1]
+    for x, y in zip(a[2:], b[2:]):
+        assert x.shape == y.shape and np.allclose(x, y, rtol=1e-14, atol=1e-15)
