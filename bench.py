@@ -537,8 +537,8 @@ def config_q2(fg, stream, nel=64, reps=5):
            "mixed_vs_fp64_rel_frobenius": {"K": rel_k, "f": rel_f},
            "tiles": info["n_tiles"], "cell_visits_per_cell": info["n_cell_visits"] / dh.n_cells,
            "setup_s": {"host": t1 - t0, "fe_create": t2 - t1},
-           "path": "two-phase: element matrices once per cell (CUDA cores), then the gather-only owner-tile "
-                   "reduce; no tensor-core path"}
+           "path": "two-phase: element matrices once per cell on the tensor cores (tcgen05 kind::tf32, split-TF32 "
+                   "Gram products), then the gather-only owner-tile reduce"}
     h.close()
     return out
 
