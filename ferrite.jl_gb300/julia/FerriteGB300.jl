@@ -216,4 +216,71 @@ function apply!(nzval, f, c::Constraints; applyzero::Bool=false)
     return nzval, f
 end
 
+"""
+    allocate_matrix_device(dh_desc...) -> (colPtr, rowVal)
+
+`allocate_matrix(dh)` by GPU kernels (fe_sparsity_pattern_device) into device arrays, e.g.
+for a `CuSparseMatrixCSC` (the same colptr/rowval as `allocate_matrix(dh)`). `grid`, `subs`
+and `dofs` are the descriptors `Handle` builds.
+"""
+function sparsity_pattern_device!(colptr, grid::Ref{GridDesc}, subs::Vector{SubdomainDesc}, dofs::Ref{DofDesc}, rowval=nothing)
+    nnz = Ref{Int64}(0)
+    rc = GC.@preserve colptr rowval subs ccall((:fe_sparsity_pattern_device, LIB), Cint,
+        (Ptr{GridDesc}, Int32, Ptr{SubdomainDesc}, Ptr{DofDesc}, Ptr{Int64}, Ptr{Int64}, Ptr{Int64}),
+        grid, length(subs), subs, dofs, pointer(colptr), rowval === nothing ? C_NULL : pointer(rowval), nnz)
+    rc == 0 || error("fe_sparsity_pattern_device failed with code $rc")
+    return nnz[]
+end
+
+struct FacetDesc
+    n_qp::Int32
+    n_ref_facets::Int32
+    qr_weights::Ptr{Float64}
+    N::Ptr{Float64}
+    dMdxi::Ptr{Float64}
+    n_facets::Int64
+    cells::Ptr{Int64}
+    facets::Ptr{Int32}
+end
+
+mutable struct FacetSet
+    ptr::Ptr{Cvoid}
+    h::Handle
+end
+
+"""
+    FacetSet(h, facetset, fv)
+
+A facet set (`getfacetset(grid, name)`: FacetIndex(cell, facet) pairs) with its FacetValues
+tables (`fv.fun_values.Nξ`, `fv.geo_mapping.dMdξ`, `getweights(fv.fqr, f)` per reference facet).
+"""
+function FacetSet(h::Handle, facetset, w::Array{Float64,2}, N::Array{Float64,3}, dM::Array{Float64,4})
+    cells = Int64[first(fi) for fi in facetset]
+    facets = Int32[last(fi) for fi in facetset]
+    d = Ref(FacetDesc(Int32(size(w, 1)), Int32(size(w, 2)), pointer(w), pointer(N), pointer(dM),
+                      length(cells), pointer(cells), pointer(facets)))
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    rc = GC.@preserve w N dM cells facets ccall((:fe_facet_set_create, LIB), Cint,
+        (Ptr{Cvoid}, Ptr{FacetDesc}, Ptr{Ptr{Cvoid}}), h.ptr, d, out)
+    check(rc, h.ptr)
+    fs = FacetSet(out[], h)
+    finalizer(x -> ccall((:fe_facet_set_destroy, LIB), Cvoid, (Ptr{Cvoid},), x.ptr), fs)
+    return fs
+end
+
+"""
+    assemble_facet_load!(f, fs; pressure, traction)
+
+`f += ∫ N_i ⋅ (pressure n + traction) dΓ` over the set (benchmark/helper.jl:331-348,
+hyperelasticity.jl:278-290 with pressure = -tn); f a CuArray.
+"""
+function assemble_facet_load!(f, fs::FacetSet; pressure=0.0, traction=(0.0, 0.0, 0.0), fillzero::Bool=false)
+    t = collect(Float64.(traction))
+    rc = GC.@preserve f t ccall((:fe_assemble_facet_load, LIB), Cint,
+        (Ptr{Cvoid}, Float64, Ptr{Float64}, UInt32, Ptr{Float64}, Ptr{Cvoid}),
+        fs.ptr, pressure, t, fillzero ? FE_FILLZERO : UInt32(0), pointer(f), C_NULL)
+    check(rc, fs.h.ptr)
+    return f
+end
+
 end # module

@@ -262,19 +262,26 @@ def test_unaligned_device_output(built, oracle, torch_cuda):
 
 
 def _forms_bitwise(fg, O, prob, element_args):
-    """Element matrices first (two-phase, CUDA cores) and in-tile (fused) give the same bits:
-    the same FP32 element math feeds the same per-entry sums in cell order."""
+    """Element matrices first (two-phase, CUDA cores) and in-tile (fused) give the same bits,
+    with fill-zero and accumulating: the same FP32 element math feeds the same per-entry sums
+    in cell order."""
     h = make_handle(fg, O, prob)
     out = {}
-    for form in ("fused", "two_phase_cuda_cores"):
+    forms = ("fused", "two_phase_cuda_cores")
+    for form in forms:
         for prec in (0, 1):
             nz = np.full(prob.nnz, np.nan)
             f = np.full(prob.ndofs, np.nan)
             h.assemble(nz, f, precision=prec, form=form, **element_args)
             out[form, prec] = (nz, f)
+            # accumulation without fill-zero follows the same sums
+            h.assemble(nz, f, precision=prec, form=form, fillzero=False, **element_args)
+            out[form, prec, "acc"] = (nz.copy(), f.copy())
     for prec in (0, 1):
-        assert np.array_equal(out["fused", prec][0], out["two_phase_cuda_cores", prec][0]), prec
-        assert np.array_equal(out["fused", prec][1], out["two_phase_cuda_cores", prec][1]), prec
+        for form in forms[1:]:
+            for key in ((prec,), (prec, "acc")):
+                a, b = out[("fused",) + key], out[(form,) + key]
+                assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]), (form, key)
     return h
 
 
