@@ -217,11 +217,14 @@ function apply!(nzval, f, c::Constraints; applyzero::Bool=false)
 end
 
 """
-    allocate_matrix_device(dh_desc...) -> (colPtr, rowVal)
+    sparsity_pattern_device!(colptr, grid, subs, dofs, rowval=nothing) -> nnz
 
-`allocate_matrix(dh)` by GPU kernels (fe_sparsity_pattern_device) into device arrays, e.g.
-for a `CuSparseMatrixCSC` (the same colptr/rowval as `allocate_matrix(dh)`). `grid`, `subs`
-and `dofs` are the descriptors `Handle` builds.
+`allocate_matrix(dh)` by GPU kernels (fe_sparsity_pattern_device) into device arrays, e.g. the
+`colPtr`/`rowVal` of a `CuSparseMatrixCSC` (the same arrays as `allocate_matrix(dh)`): call
+once with `rowval === nothing` for colptr and nnz, then with a `CuArray{Int64}(undef, nnz)`.
+`grid`, `subs` and `dofs` are the descriptors `Handle` builds. The facet tables below are
+`[nf][nqp]...` row-major, i.e. Julia arrays of size (nqp, nf), (nbase, nqp, nf), (dim, ngeo,
+nqp, nf).
 """
 function sparsity_pattern_device!(colptr, grid::Ref{GridDesc}, subs::Vector{SubdomainDesc}, dofs::Ref{DofDesc}, rowval=nothing)
     nnz = Ref{Int64}(0)
