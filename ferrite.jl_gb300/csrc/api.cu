@@ -86,6 +86,7 @@ struct fe_handle {
     HostProblem hp;
     Plan plan;
     std::vector<void*> allocs;
+    std::vector<int64_t> alloc_bytes;  // size of each allocation in allocs
     int64_t device_bytes = 0;
     KernelArgs base{};
     // staged reference tables (one block per subdomain), float and double
@@ -141,6 +142,7 @@ struct fe_handle {
         cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
         if (e == cudaSuccess) {
             allocs.push_back((void*)*p);
+            alloc_bytes.push_back((int64_t)(count * sizeof(T)));
             device_bytes += (int64_t)(count * sizeof(T));
         }
         return e;
@@ -149,7 +151,9 @@ struct fe_handle {
         for (size_t k = 0; k < allocs.size(); ++k)
             if (allocs[k] == p) {
                 cudaFree(p);
+                device_bytes -= alloc_bytes[k];
                 allocs.erase(allocs.begin() + (long)k);
+                alloc_bytes.erase(alloc_bytes.begin() + (long)k);
                 return;
             }
     }
