@@ -185,6 +185,31 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def dist_setup(world: int):
+    """Replicas only: one process per GPU, NCCL between them (gloo when CUDA is absent, e.g.
+    the CPU tests of this logic); nothing but the timing crosses ranks."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+
+
+def max_over_ranks(ms: float, world: int, device=None) -> float:
+    """The step time of the slowest rank (all ranks receive it)."""
+    if world <= 1:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(world: int, cells_per_rank: int, ms: float) -> float:
+    """Whole-job throughput in Melem/s: every rank assembles its own copy of the workload."""
+    return world * cells_per_rank / (ms * 1e-3) / 1e6
+
+
 def run_ours(args):
     import torch
 
@@ -194,9 +219,7 @@ def run_ours(args):
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    dist_setup(world)
     P = setup_problem(fg, NEL)
     h, dh = P["handle"], P["dh"]
     info = h.info()
@@ -231,12 +254,8 @@ def run_ours(args):
             barrier()
         total_ms = start.elapsed_time(end)
         kern_ms, kern_n = h.kernel_time()
-    ms = total_ms / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * n_cells / (ms * 1e-3) / 1e6
+    ms = max_over_ranks(total_ms / args.steps, world, dev)
+    value = replica_value(world, n_cells, ms)
     kernel_ms = kern_ms / max(kern_n, 1)
 
     # ---- correctness at full size: rigid-body modes annihilated, body force integrates to -1 ----
