@@ -119,3 +119,18 @@ def test_apply_errors(built, oracle, torch_cuda):
     with pytest.raises(fg.FEError) as e:
         h.dirichlet(prob.rowval, np.array([1, prob.ndofs + 1], np.int64))
     assert e.value.name == "BOUNDS"
+
+
+def test_apply_without_prescribed_dofs(built, oracle, torch_cuda):
+    torch = torch_cuda
+    fg, O = built, oracle
+    prob = O.box_problem(O.QUADRILATERAL, (4, 3), qr_order=2)
+    h = make_handle(fg, O, prob)
+    nz = torch.zeros(prob.nnz, dtype=torch.float64, device="cuda")
+    f = torch.zeros(prob.ndofs, dtype=torch.float64, device="cuda")
+    h.assemble(nz, f, physics=fg.HEAT, p0=1.0, p1=1.0)
+    nz0, f0 = nz.clone(), f.clone()
+    ch = h.dirichlet(prob.rowval, np.zeros(0, np.int64))
+    ch.apply(nz, f, None)
+    assert torch.equal(nz, nz0) and torch.equal(f, f0)
+    ch.close()

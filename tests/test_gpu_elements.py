@@ -116,3 +116,21 @@ def test_elements_detj_error(built, oracle, torch_cuda):
     with pytest.raises(fg.FEError) as ei:
         h.assemble_elements(ke, fe, physics=fg.HEAT, p0=1.0, p1=1.0)
     assert ei.value.name == "DETJ" and ei.value.cell == 5
+
+
+def test_elements_without_k_or_f(built, oracle, torch_cuda):
+    torch = torch_cuda
+    fg, O = built, oracle
+    prob = O.box_problem(O.HEXAHEDRON, (2, 2, 1), ncomp=3, perturb=0.2, seed=36)
+    h = make_handle(fg, O, prob)
+    n, nbf = prob.n_cells, prob.ndofs_per_cell(0)
+    kw = dict(physics=fg.LINEAR_ELASTIC, p0=1.0, p1=0.3, body=(0.0, 0.0, -1.0))
+    ke = torch.zeros((n, nbf, nbf), dtype=torch.float32, device="cuda")
+    fe = torch.zeros((n, nbf), dtype=torch.float32, device="cuda")
+    h.assemble_elements(ke, fe, **kw)
+    ke2 = torch.full_like(ke, 7.0)
+    h.assemble_elements(ke2, None, fe_stride=(0, 0), **kw)
+    assert torch.equal(ke2, ke)
+    fe2 = torch.full_like(fe, 7.0)
+    h.assemble_elements(None, fe2, ke_stride=(0, 0, 0), **kw)
+    assert torch.equal(fe2, fe)

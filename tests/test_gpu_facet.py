@@ -81,3 +81,16 @@ def test_facet_set_errors(built, oracle, torch_cuda):
     with pytest.raises(fg.FEError) as e:
         h.facet_set(np.array([prob.n_cells + 1], np.int64), np.array([1], np.int32), tabs)
     assert e.value.name == "BOUNDS"
+
+
+def test_empty_facet_set(built, oracle, torch_cuda):
+    torch = torch_cuda
+    fg, O = built, oracle
+    prob = O.box_problem(O.HEXAHEDRON, (2, 2, 2), ncomp=3)
+    h = make_handle(fg, O, prob)
+    fs = h.facet_set(np.zeros(0, np.int64), np.zeros(0, np.int32), facet_tables(O, O.HEXAHEDRON, 1, 2))
+    f = torch.ones(prob.ndofs, dtype=torch.float64, device="cuda")
+    fs.load(f, pressure=1.0)
+    assert bool((f == 1).all())
+    fs.load(f, pressure=1.0, fillzero=True)
+    assert bool((f == 0).all())
