@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include "device_buffers.h"
 #include "ferrite_gb300.h"
 #include "plan.h"
 #include "registry.h"
@@ -85,9 +86,7 @@ void* pinned_device_alias(void* p) {
 struct fe_handle {
     HostProblem hp;
     Plan plan;
-    std::vector<void*> allocs;
-    std::vector<int64_t> alloc_bytes;  // size of each allocation in allocs
-    int64_t device_bytes = 0;
+    DeviceBuffers mem;  // every device buffer of the handle
     KernelArgs base{};
     // staged reference tables (one block per subdomain), float and double
     float* shape_f = nullptr;
@@ -138,31 +137,12 @@ struct fe_handle {
 
     template <typename T>
     cudaError_t alloc(T** p, size_t count) {
-        if (count == 0) count = 1;
-        cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
-        if (e == cudaSuccess) {
-            allocs.push_back((void*)*p);
-            alloc_bytes.push_back((int64_t)(count * sizeof(T)));
-            device_bytes += (int64_t)(count * sizeof(T));
-        }
-        return e;
+        return mem.alloc(p, count);
     }
-    void release(void* p) {  // free one allocation made by alloc()
-        for (size_t k = 0; k < allocs.size(); ++k)
-            if (allocs[k] == p) {
-                cudaFree(p);
-                device_bytes -= alloc_bytes[k];
-                allocs.erase(allocs.begin() + (long)k);
-                alloc_bytes.erase(alloc_bytes.begin() + (long)k);
-                return;
-            }
-    }
+    void release(void* p) { mem.release(p); }
     template <typename T>
     cudaError_t upload(T** p, const T* src, size_t count) {
-        cudaError_t e = alloc(p, count);
-        if (e != cudaSuccess) return e;
-        if (count) e = cudaMemcpy(*p, src, count * sizeof(T), cudaMemcpyHostToDevice);
-        return e;
+        return mem.upload(p, src, count);
     }
     ~fe_handle() {
         for (auto& g : graphs) {
@@ -171,7 +151,6 @@ struct fe_handle {
         }
         for (auto& e : prof_events) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
         for (auto& e : prof_pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
-        for (void* p : allocs) cudaFree(p);
         if (status_h) cudaFreeHost(status_h);
     }
 };
@@ -492,17 +471,12 @@ struct fe_facet_set {
     int64_t *rptr = nullptr, *rows = nullptr, *epos = nullptr;
     DevStatus* status = nullptr;
     DevStatus* status_h = nullptr;
-    std::vector<void*> allocs;
+    DeviceBuffers mem;
     template <typename T>
     cudaError_t upload(T** p, const T* src, size_t count) {
-        cudaError_t e = cudaMalloc((void**)p, (count ? count : 1) * sizeof(T));
-        if (e != cudaSuccess) return e;
-        allocs.push_back((void*)*p);
-        if (src && count) e = cudaMemcpy(*p, src, count * sizeof(T), cudaMemcpyHostToDevice);
-        return e;
+        return mem.upload(p, src, count);
     }
     ~fe_facet_set() {
-        for (void* p : allocs) cudaFree(p);
         if (status_h) cudaFreeHost(status_h);
     }
 };
@@ -568,19 +542,10 @@ struct fe_dirichlet {
     double* g = nullptr;       // [np] inhomogeneities of the current call
     double* part = nullptr;    // [DIAG_BLOCKS] meandiag partial sums
     double* m = nullptr;       // meandiag
-    std::vector<void*> allocs;
-    int64_t device_bytes = 0;
+    DeviceBuffers mem;
     template <typename T>
     cudaError_t upload(T** p, const T* src, size_t count) {
-        cudaError_t e = cudaMalloc((void**)p, (count ? count : 1) * sizeof(T));
-        if (e != cudaSuccess) return e;
-        allocs.push_back((void*)*p);
-        device_bytes += (int64_t)(count * sizeof(T));
-        if (src && count) e = cudaMemcpy(*p, src, count * sizeof(T), cudaMemcpyHostToDevice);
-        return e;
-    }
-    ~fe_dirichlet() {
-        for (void* p : allocs) cudaFree(p);
+        return mem.upload(p, src, count);
     }
 };
 
@@ -1359,7 +1324,7 @@ int fe_get_info(const fe_handle* h, fe_info* out) {
     out->max_out_doubles = h->plan.max_out;
     out->stage_cap = h->stage_cap;
     out->flagged_cells = h->flagged;
-    out->device_bytes = h->device_bytes;
+    out->device_bytes = h->mem.bytes();
     out->create_seconds = h->create_seconds;
     return FE_OK;
 }

@@ -14,6 +14,7 @@
 #include <cstdint>
 #include <vector>
 
+#include "device_buffers.h"
 #include "ferrite_gb300.h"
 #include "plan.h"
 
@@ -204,23 +205,10 @@ bool device_memory(const void* p) {
     return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
 }
 
-struct DevBufs {
-    std::vector<void*> ptrs;
-    template <typename T>
-    cudaError_t get(T** p, size_t n) {
-        cudaError_t e = cudaMalloc((void**)p, (n ? n : 1) * sizeof(T));
-        if (e == cudaSuccess) ptrs.push_back((void*)*p);
-        return e;
-    }
-    ~DevBufs() {
-        for (void* p : ptrs) cudaFree(p);
-    }
-};
-
-cudaError_t scan(const int32_t* in, int64_t n, int64_t* out, DevBufs& B) {
+cudaError_t scan(const int32_t* in, int64_t n, int64_t* out, fe::DeviceBuffers& B) {
     const int64_t nb = std::max<int64_t>(1, (n + SCAN_CHUNK - 1) / SCAN_CHUNK);
     int64_t* bsum = nullptr;
-    cudaError_t e = B.get(&bsum, (size_t)nb + 1);
+    cudaError_t e = B.alloc(&bsum, (size_t)nb + 1);
     if (e != cudaSuccess) return e;
     scan_blocks<<<(unsigned)nb, 256>>>(in, n, bsum);
     scan_sums<<<1, 1>>>(bsum, nb);
@@ -282,7 +270,7 @@ int fe_sparsity_pattern_device(const fe_grid_desc* grid, int32_t n_sub, const fe
         }
     }
     if (bad) return FE_ERR_UNSUPPORTED;
-    DevBufs B;
+    fe::DeviceBuffers B;
     int32_t *d_ents, *d_slot_cell, *d_cnb, *d_cnt, *d_ecell, *d_nnb;
     int64_t *d_cstart, *d_eptr, *d_cursor, *d_roff, *d_colptr;
     int* d_over;
@@ -291,17 +279,17 @@ int fe_sparsity_pattern_device(const fe_grid_desc* grid, int32_t n_sub, const fe
     do {                                      \
         if ((e = (x)) != cudaSuccess) return FE_ERR_CUDA; \
     } while (0)
-    PK(B.get(&d_ents, (size_t)n_slots));
-    PK(B.get(&d_slot_cell, (size_t)n_slots));
-    PK(B.get(&d_cnb, (size_t)n_cells));
-    PK(B.get(&d_cstart, (size_t)n_cells));
-    PK(B.get(&d_cnt, (size_t)ne));
-    PK(B.get(&d_eptr, (size_t)ne + 1));
-    PK(B.get(&d_cursor, (size_t)ne + 1));
-    PK(B.get(&d_ecell, (size_t)n_slots));
-    PK(B.get(&d_nnb, (size_t)ne));
-    PK(B.get(&d_roff, (size_t)ne + 1));
-    PK(B.get(&d_over, 1));
+    PK(B.alloc(&d_ents, (size_t)n_slots));
+    PK(B.alloc(&d_slot_cell, (size_t)n_slots));
+    PK(B.alloc(&d_cnb, (size_t)n_cells));
+    PK(B.alloc(&d_cstart, (size_t)n_cells));
+    PK(B.alloc(&d_cnt, (size_t)ne));
+    PK(B.alloc(&d_eptr, (size_t)ne + 1));
+    PK(B.alloc(&d_cursor, (size_t)ne + 1));
+    PK(B.alloc(&d_ecell, (size_t)n_slots));
+    PK(B.alloc(&d_nnb, (size_t)ne));
+    PK(B.alloc(&d_roff, (size_t)ne + 1));
+    PK(B.alloc(&d_over, 1));
     PK(cudaMemcpy(d_ents, ents.data(), ents.size() * 4, cudaMemcpyHostToDevice));
     PK(cudaMemcpy(d_slot_cell, slot_cell.data(), slot_cell.size() * 4, cudaMemcpyHostToDevice));
     PK(cudaMemcpy(d_cnb, cnb.data(), cnb.size() * 4, cudaMemcpyHostToDevice));
@@ -325,7 +313,7 @@ int fe_sparsity_pattern_device(const fe_grid_desc* grid, int32_t n_sub, const fe
     // colptr (1-based), in place if the caller's array is device memory
     const bool cp_dev = device_memory(colptr);
     if (cp_dev) d_colptr = colptr;
-    else PK(B.get(&d_colptr, (size_t)nd + 1));
+    else PK(B.alloc(&d_colptr, (size_t)nd + 1));
     make_colptr<<<grid1, 256>>>(ne, nc, d_roff, d_nnb, d_colptr);
     int64_t total = 0;
     PK(cudaMemcpy(&total, d_colptr + nd, 8, cudaMemcpyDeviceToHost));
@@ -334,7 +322,7 @@ int fe_sparsity_pattern_device(const fe_grid_desc* grid, int32_t n_sub, const fe
     if (!rowval) return FE_OK;
     const bool rv_dev = device_memory(rowval);
     int64_t* d_rowval = rowval;
-    if (!rv_dev) PK(B.get(&d_rowval, (size_t)*nnz));
+    if (!rv_dev) PK(B.alloc(&d_rowval, (size_t)*nnz));
     fill_rows<<<grid2, 32 * PAT_WARPS>>>(ne, nc, d_eptr, d_ecell, d_cstart, d_cnb, d_ents, d_roff, d_rowval, d_over);
     PK(cudaGetLastError());
     if (!rv_dev) PK(cudaMemcpy(rowval, d_rowval, (size_t)*nnz * 8, cudaMemcpyDeviceToHost));
