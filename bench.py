@@ -287,7 +287,11 @@ def run_ours(args):
     if rank == 0 and not args.skip_fp64:
         k64 = max(1, min(args.steps, 10))
         with torch.cuda.stream(stream):
+            h.assemble(nz, f, **kw)  # the mixed result, against the FP64 one below
+            nz_mixed, f_mixed = nz.clone(), f.clone()
             h.assemble(nz, f, precision=fg.PREC_FP64, **kw)
+            err = {"K": rel_fro_t(nz_mixed, nz), "f": rel_fro_t(f_mixed, f)}
+            del nz_mixed, f_mixed
             h.kernel_time()
             torch.cuda.synchronize()
             s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -299,7 +303,9 @@ def run_ours(args):
             torch.cuda.synchronize()
         ms64 = s2.elapsed_time(e2) / k64
         fp64 = {"value": n_cells / (ms64 * 1e-3) / 1e6, "unit": "Melem/s", "ms_per_step": ms64, "steps": k64,
-                "speedup_mixed_over_fp64": ms64 / ms}
+                "speedup_mixed_over_fp64": ms64 / ms, "mixed_vs_fp64_rel_frobenius": err,
+                "note": "the FP64 form equals the CPU oracle (FP64 restatement of Ferrite's assembly) to 1e-12 "
+                        "in the parity tests, so this is the mixed form's error against it"}
         h.kernel_time()
 
     # ---- e2e: public API with pinned host buffers (D2H of nzval and f each step) ----
@@ -371,6 +377,13 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def rel_fro_t(a, b) -> float:
+    """relative Frobenius norm |a - b| / |b| of two device vectors"""
+    import torch
+    nb = float(torch.linalg.vector_norm(b))
+    return float(torch.linalg.vector_norm(a - b)) / (nb if nb > 0 else 1.0)
 
 
 def _timed(stream, fn, reps, warmup=2):
@@ -467,11 +480,15 @@ def config_heat(fg, stream):
     nz = torch.empty(h.nnz, dtype=torch.float64, device="cuda")
     f = torch.empty(dh.ndofs, dtype=torch.float64, device="cuda")
     out = {"workload": "heat_quad100x100", "cells": dh.n_cells, "ndofs": dh.ndofs, "nnz": h.nnz}
+    res = {}
     for name, prec in (("mixed", fg.PREC_MIXED), ("fp64", fg.PREC_FP64)):
         ms = _timed(stream, lambda: h.assemble(nz, f, physics=fg.HEAT, p0=1.0, p1=1.0, precision=prec, stream=stream,
                                                sync=False), 200)
         h.sync()
         out[name] = {"us_per_assembly": ms * 1e3, "Melem_s": dh.n_cells / (ms * 1e-3) / 1e6}
+        res[name] = (nz.clone(), f.clone())
+    out["mixed_vs_fp64_rel_frobenius"] = {"K": rel_fro_t(res["mixed"][0], res["fp64"][0]),
+                                          "f": rel_fro_t(res["mixed"][1], res["fp64"][1])}
     out["note"] = "launch-bound (10,000 cells); one kernel launch per assembly"
     h.close()
     return out
@@ -583,6 +600,14 @@ def config_elements(fg, stream, nel=64, reps=10):
         ms = _timed(stream, lambda: h.assemble_elements(ke, fe, ke_stride=ks, fe_stride=fs, **kw), reps)
         h.sync()
         out[name] = {"ms": ms, "Melem_s": n / (ms * 1e-3) / 1e6, "write_GBs": out["bytes_out"] / (ms * 1e-3) / 1e9}
+    h.assemble_elements(ke, fe, **kw)
+    h.sync()
+    ke64 = torch.empty((n, nbf, nbf), dtype=torch.float64, device="cuda")
+    fe64 = torch.empty((n, nbf), dtype=torch.float64, device="cuda")
+    h.assemble_elements(ke64, fe64, precision=fg.PREC_FP64, **kw)
+    h.sync()
+    out["fp32_vs_fp64_rel_frobenius"] = {"Ke": rel_fro_t(ke.double(), ke64), "fe": rel_fro_t(fe.double(), fe64)}
+    del ke64, fe64
     h.close()
     return out
 
@@ -617,8 +642,9 @@ def config_pattern(fg, stream, nel=128):
 
 def config_mixed_graph(fg, stream, steps=20):
     """~2M cells over three x-slabs sharing vertex nodes (Hex Q1 50%, Tet P1 25% as 6 per cube,
-    Wedge P1 25% as 2 per cube), compressible Neo-Hooke (mu 1, lambda 10), u = 0.05 U(-1,1)
-    seeded per step; the tile plan autotuned, then `steps` re-assemblies with updated u captured
+    Wedge P1 25% as 2 per cube), compressible Neo-Hooke (mu 1, lambda 10), displacement
+    amplitude 0.05 of the cell size h = 0.01 (u = 0.05 h U(-1,1), seeded per step: an absolute
+    0.05 is five cells wide and inverts cells, where log J is undefined in any precision); the tile plan autotuned, then `steps` re-assemblies with updated u captured
     as one CUDA graph and replayed."""
     import torch
     host = __import__("ferrite_gb300.host", fromlist=["host"])
@@ -644,7 +670,8 @@ def config_mixed_graph(fg, stream, steps=20):
     cvs = [host.CellValues(host.HEXAHEDRON, 1, 2), host.CellValues(host.TETRAHEDRON, 1, 1), host.CellValues(host.WEDGE, 1, 2)]
     h = dh.handle(cvs, colptr, rowval)
     rng = np.random.default_rng(SEED + 6)
-    us = [torch.as_tensor(0.05 * rng.uniform(-1, 1, dh.ndofs), device="cuda") for _ in range(steps)]
+    cell_h = 0.01
+    us = [torch.as_tensor(0.05 * cell_h * rng.uniform(-1, 1, dh.ndofs), device="cuda") for _ in range(steps)]
     nz = torch.empty(h.nnz, dtype=torch.float64, device="cuda")
     f = torch.empty(dh.ndofs, dtype=torch.float64, device="cuda")
     kw = dict(physics=fg.NEO_HOOKE, p0=1.0, p1=10.0, body=(0.0, 0.0, 0.0))
@@ -654,6 +681,11 @@ def config_mixed_graph(fg, stream, steps=20):
     gid = h.graph_capture([dict(u=u, **kw) for u in us], [nz] * steps, [f] * steps, stream)
     replay = _timed(stream, lambda: h.graph_replay(gid, stream, sync=False), 3, warmup=1)
     h.sync()
+    h.assemble(nz, f, u=us[-1], stream=stream, **kw)
+    nz_m, f_m = nz.clone(), f.clone()
+    h.assemble(nz, f, u=us[-1], stream=stream, precision=fg.PREC_FP64, **kw)
+    err = {"K": rel_fro_t(nz_m, nz), "f": rel_fro_t(f_m, f)}
+    del nz_m, f_m
     info = h.info()
     out = {"workload": "mixed_hex_tet_wedge_neo_hooke_2M", "cells": n_cells, "hex": len(hexes), "tet": len(tets),
            "wedge": len(wedges), "ndofs": dh.ndofs, "nnz": h.nnz, "steps_per_graph": steps,
@@ -662,6 +694,7 @@ def config_mixed_graph(fg, stream, steps=20):
            "autotune": {"best_stage_cap": tune["best_stage_cap"],
                         "candidates": [{"stage_cap": c, "ms": ms, "tiles": t} for c, ms, t, _ in tune["candidates"]]},
            "tiles": info["n_tiles"], "cell_visits_per_cell": info["n_cell_visits"] / n_cells,
+           "mixed_vs_fp64_rel_frobenius": err, "u": "0.05 * 0.01 * U(-1,1) per dof (amplitude 0.05 of the cell size)",
            "quadrature": "hex 2x2x2 Gauss, tet 1 point, wedge 5-point order-2 rule"}
     h.close()
     return out
