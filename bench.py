@@ -356,7 +356,7 @@ def run_ours(args):
         return
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
-    peak = peaks.get("hbm_gbs", 6800.0)
+    peak = hbm_peak_gbs()
     balg = algorithmic_bytes(nnz, ndofs, n_nodes, n_cells)
     achieved = balg / (kernel_ms * 1e-3) / 1e9
     traffic = read_profile_traffic()
@@ -384,6 +384,12 @@ def rel_fro_t(a, b) -> float:
     import torch
     nb = float(torch.linalg.vector_norm(b))
     return float(torch.linalg.vector_norm(a - b)) / (nb if nb > 0 else 1.0)
+
+
+def hbm_peak_gbs():
+    """Measured copy bandwidth of this GPU model (MEASURED_PEAKS.json), else 6800 GB/s."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    return json.load(open(path)).get("hbm_gbs", 6800.0) if os.path.exists(path) else 6800.0
 
 
 def _timed(stream, fn, reps, warmup=2):
@@ -607,9 +613,62 @@ def config_elements(fg, stream, nel=64, reps=10):
     h.assemble_elements(ke64, fe64, precision=fg.PREC_FP64, **kw)
     h.sync()
     out["fp32_vs_fp64_rel_frobenius"] = {"Ke": rel_fro_t(ke.double(), ke64), "fe": rel_fro_t(fe.double(), fe64)}
+    out["matvec"] = matvec_leg(fg, h, stream, dh, colptr, rowval, ke, ke64, kw, reps)
     del ke64, fe64
     h.close()
     return out
+
+
+def matvec_leg(fg, h, stream, dh, colptr, rowval, ke, ke64, kw, reps):
+    """Matrix-free product y = sum_c A_c^T Ke_c A_c u (fe_element_matvec) with the element
+    matrices just assembled (row-major Kes[c, I, J]), float and double, against y = K u of the
+    assembled FP64 K as a CSR product (torch.sparse, a library SpMV; K is symmetric, so its CSC
+    arrays are its CSR arrays)."""
+    import torch
+    n, nbf = ke.shape[0], ke.shape[1]
+    rng = np.random.default_rng(SEED + 9)
+    u = torch.as_tensor(rng.standard_normal(dh.ndofs), device="cuda")
+    y = torch.empty(dh.ndofs, dtype=torch.float64, device="cuda")
+    res = {"what": "y = sum_c A_c^T Ke_c A_c u, two kernels (per-cell products, per-dof gather in cell order); "
+                   "cell_major = Kes[c, I, J] row-major (a warp per cell), cell_fastest = the how-to's "
+                   "Kes[ncells, nbf, nbf] column-major (a thread per cell)"}
+    ys = {}
+    for name, kk, prec in (("float", ke, fg.PREC_MIXED), ("double", ke64, fg.PREC_FP64)):
+        res[name] = {}
+        alg = kk.numel() * kk.element_size() + 4 * 8 * n + 16 * dh.ndofs
+        for layout in ("cell_major", "cell_fastest"):
+            kl = kk if layout == "cell_major" else kk.permute(2, 1, 0).contiguous()
+            ks = kk.stride() if layout == "cell_major" else (1, n, n * nbf)
+            op = h.element_operator(ks, prec)
+            ms = _timed(stream, lambda: op.matvec(kl, u, y, stream=stream, sync=False), reps)
+            torch.cuda.synchronize()
+            if layout == "cell_major":
+                ys[name] = y.clone()
+            else:
+                res[name]["layouts_bitwise_equal"] = bool(torch.equal(y, ys[name]))
+            res[name][layout] = {"ms": ms, "GBs": alg / (ms * 1e-3) / 1e9,
+                                 "frac_of_measured_hbm": alg / (ms * 1e-3) / 1e9 / hbm_peak_gbs()}
+            op.close()
+            del kl
+        res[name]["algorithmic_bytes"] = alg
+    nz = torch.empty(h.nnz, dtype=torch.float64, device="cuda")
+    f = torch.empty(dh.ndofs, dtype=torch.float64, device="cuda")
+    h.assemble(nz, f, **dict(kw, precision=fg.PREC_FP64, sync=True))
+    try:
+        K = torch.sparse_csr_tensor(torch.as_tensor(colptr - 1, device="cuda"), torch.as_tensor(rowval - 1, device="cuda"),
+                                    nz, size=(dh.ndofs, dh.ndofs))
+        uc = u.unsqueeze(1)
+        with torch.cuda.stream(stream):
+            ms = _timed(stream, lambda: torch.sparse.mm(K, uc), reps)
+            Ku = torch.sparse.mm(K, uc).squeeze(1)
+        torch.cuda.synchronize()
+        res["csr_spmv_fp64"] = {"ms": ms, "nnz": h.nnz}
+        res["rel_error_vs_Ku"] = {k: rel_fro_t(v, Ku) for k, v in ys.items()}
+        del K, Ku
+    except Exception as e:  # the library SpMV is a comparison only
+        res["csr_spmv_fp64"] = {"error": str(e)[:200]}
+    del nz, f
+    return res
 
 
 def config_pattern(fg, stream, nel=128):

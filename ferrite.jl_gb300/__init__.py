@@ -44,7 +44,7 @@ EXPORTED = ["fe_abi_version", "fe_create", "fe_assemble", "fe_sync", "fe_last_er
             "fe_assemble_adjoint", "fe_graph_capture", "fe_graph_replay", "fe_graph_destroy",
             "fe_autotune", "fe_assemble_elements", "fe_sparsity_pattern_device", "fe_facet_set_create", "fe_assemble_facet_load",
             "fe_facet_set_destroy", "fe_dirichlet_create", "fe_apply", "fe_dirichlet_destroy",
-            "fe_destroy"]
+            "fe_element_operator_create", "fe_element_matvec", "fe_element_operator_destroy", "fe_destroy"]
 
 i64p = ctypes.POINTER(ctypes.c_int64)
 f64p = ctypes.POINTER(ctypes.c_double)
@@ -164,6 +164,12 @@ def lib():
                                ctypes.c_void_p]
         L.fe_dirichlet_destroy.argtypes = [ctypes.c_void_p]
         L.fe_dirichlet_destroy.restype = None
+        L.fe_element_operator_create.argtypes = [ctypes.c_void_p, ctypes.POINTER(ElementLayout), ctypes.c_int32,
+                                                 ctypes.POINTER(ctypes.c_void_p)]
+        L.fe_element_matvec.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                        ctypes.c_void_p]
+        L.fe_element_operator_destroy.argtypes = [ctypes.c_void_p]
+        L.fe_element_operator_destroy.restype = None
         L.fe_assemble_elements.argtypes = [ctypes.c_void_p, ctypes.POINTER(AssembleParams), ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.POINTER(ElementLayout)]
         L.fe_assemble_adjoint.argtypes = [ctypes.c_void_p, ctypes.POINTER(AdjointParams), ctypes.c_void_p, ctypes.c_void_p,
@@ -408,6 +414,19 @@ class Handle:
             self._raise(rc)
         return Dirichlet(self, out, len(pd))
 
+    def element_operator(self, ke_stride, precision: int = PREC_MIXED):
+        """fe_element_operator_create: the matrix-free product y (+)= sum_c A_c^T Ke_c A_c u over
+        element matrices laid out with ke_stride (elements, Ke(c, I, J) at c*s0 + I*s1 + J*s2;
+        float32 for PREC_MIXED, float64 for PREC_FP64)."""
+        lay = ElementLayout()
+        for k in range(3):
+            lay.ke_stride[k] = int(ke_stride[k])
+        out = ctypes.c_void_p()
+        rc = lib().fe_element_operator_create(self._h, ctypes.byref(lay), int(precision), ctypes.byref(out))
+        if rc != FE_OK:
+            self._raise(rc)
+        return ElementOperator(self, out, precision)
+
     def adjoint(self, u, lam, d_rho, d_X, physics: int, p0: float, p1: float, body=(0.0, 0.0, 0.0), cell_scale=None,
                 dscale=None, precision: int = PREC_MIXED, stream=None, sync: bool = True):
         """fe_assemble_adjoint: d_rho[n_cells] = dscale * lam^T (dK/ds) u and d_X[n_nodes*dim] =
@@ -608,6 +627,38 @@ class Dirichlet:
     def close(self):
         if self._c:
             lib().fe_dirichlet_destroy(self._c)
+            self._c = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class ElementOperator:
+    """y (+)= sum_c A_c^T Ke_c A_c u with element matrices (fe_element_matvec) on device buffers
+    (torch CUDA tensors). Close it before its handle."""
+
+    def __init__(self, handle, ptr, precision):
+        self._handle = handle
+        self._c = ptr
+        self.precision = precision
+
+    def matvec(self, ke, u, y, fillzero: bool = True, stream=None, sync: bool = True):
+        if stream is not None and hasattr(stream, "cuda_stream"):
+            stream = stream.cuda_stream
+        rc = lib().fe_element_matvec(self._c, _ptr(ke), _ptr(u), _ptr(y), FILLZERO if fillzero else 0, stream)
+        if rc != FE_OK:
+            self._handle._raise(rc)
+        if sync:
+            import torch
+            torch.cuda.synchronize()
+        return y
+
+    def close(self):
+        if self._c:
+            lib().fe_element_operator_destroy(self._c)
             self._c = None
 
     def __del__(self):

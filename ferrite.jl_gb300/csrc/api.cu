@@ -16,6 +16,7 @@
 #include "adjoint.cuh"
 #include "dirichlet.cuh"
 #include "facet.cuh"
+#include "matvec.cuh"
 #include "tile_kernel.cuh"
 
 using namespace fe;
@@ -548,6 +549,66 @@ struct fe_dirichlet {
         return mem.upload(p, src, count);
     }
 };
+
+// Element-matrix operator of a handle (fe_element_operator_create / fe_element_matvec)
+struct fe_element_operator {
+    fe_handle* h = nullptr;
+    int fp64 = 0;
+    bool rows = false;  // a cell's matrix is one block (cell stride != 1): a warp per cell
+    int64_t ks[3] = {0, 0, 0};
+    int64_t ndofs = 0;
+    struct Sub {
+        int32_t n = 0;              // dofs per cell
+        int64_t n_cells = 0, off = 0;  // cells, first scratch value
+        int32_t* cells = nullptr;   // [n_cells] 0-based cell ids
+        int32_t* dofs = nullptr;    // 0-based dofs, [n][n_cells] (rows: [n_cells][n])
+    };
+    std::vector<Sub> subs;
+    int64_t* ptr = nullptr;  // [ndofs + 1] incidences of each dof
+    int32_t* inc = nullptr;  //   their scratch positions, in ascending cell order
+    void* ye = nullptr;      // scratch: per subdomain [n][n_cells] element products
+    DeviceBuffers mem;
+    template <typename T>
+    cudaError_t upload(T** p, const T* src, size_t count) {
+        return mem.upload(p, src, count);
+    }
+};
+
+namespace {
+
+template <typename T>
+cudaError_t launch_products(int n, bool rows, unsigned grid, cudaStream_t st, const T* ke, const int64_t* ks,
+                            const int32_t* cells, const int32_t* dofs, int64_t n_cells, const double* u, T* ye) {
+#define FE_PRODUCTS(N)                                                                                               \
+    case N:                                                                                                          \
+        if (rows)                                                                                                    \
+            element_products_rows<T, N><<<grid, 256, 0, st>>>(ke, ks[0], ks[1], ks[2], cells, dofs, n_cells, u, ye); \
+        else                                                                                                         \
+            element_products<T, N><<<grid, 128, 0, st>>>(ke, ks[0], ks[1], ks[2], cells, dofs, n_cells, u, ye);      \
+        break;
+    switch (n) {
+        FE_PRODUCTS(3)
+        FE_PRODUCTS(4)
+        FE_PRODUCTS(6)
+        FE_PRODUCTS(8)
+        FE_PRODUCTS(9)
+        FE_PRODUCTS(12)
+        FE_PRODUCTS(18)
+        FE_PRODUCTS(24)
+        FE_PRODUCTS(27)
+        FE_PRODUCTS(81)
+        default:
+            return cudaErrorInvalidValue;
+    }
+#undef FE_PRODUCTS
+    return cudaGetLastError();
+}
+
+bool matvec_supported(int n) {
+    return n == 3 || n == 4 || n == 6 || n == 8 || n == 9 || n == 12 || n == 18 || n == 24 || n == 27 || n == 81;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -1489,6 +1550,123 @@ int fe_apply(fe_dirichlet* ch, double* nzval, double* f, const double* inhomogen
 }
 
 void fe_dirichlet_destroy(fe_dirichlet* ch) { delete ch; }
+
+int fe_element_operator_create(fe_handle* h, const fe_element_layout* layout, int32_t precision, fe_element_operator** out) {
+    if (!h || !layout || !out) return FE_ERR_ARG;
+    *out = nullptr;
+    if (precision != FE_PREC_MIXED && precision != FE_PREC_FP64) return set_error(h, FE_ERR_ARG, "unknown precision");
+    const HostProblem& hp = h->hp;
+    if (hp.ndofs >= INT32_MAX || hp.n_cells >= INT32_MAX) return set_error(h, FE_ERR_UNSUPPORTED, "more than 2^31 - 1 dofs or cells");
+    fe_element_operator* op = new (std::nothrow) fe_element_operator();
+    if (!op) return FE_ERR_OOM;
+    op->h = h;
+    op->fp64 = precision == FE_PREC_FP64;
+    for (int k = 0; k < 3; ++k) op->ks[k] = layout->ke_stride[k];
+    op->rows = op->ks[0] != 1;
+    op->ndofs = hp.ndofs;
+    int64_t total = 0;
+    op->subs.resize(hp.subs.size());
+    for (size_t s = 0; s < hp.subs.size(); ++s) {
+        fe_element_operator::Sub& os = op->subs[s];
+        os.n = hp.subs[s].nb * hp.subs[s].nc;
+        os.n_cells = hp.subs[s].n_cells;
+        os.off = total;
+        if (os.n_cells && !matvec_supported(os.n)) {
+            delete op;
+            return set_error(h, FE_ERR_UNSUPPORTED, "no element product compiled for this number of dofs per cell");
+        }
+        total += (int64_t)os.n * os.n_cells;
+    }
+    if (total >= INT32_MAX) {
+        delete op;
+        return set_error(h, FE_ERR_UNSUPPORTED, "more than 2^31 - 1 (cell, dof) pairs");
+    }
+    // dof -> scratch positions, in ascending cell order (a counting sort over the cells)
+    std::vector<int64_t> ptr((size_t)hp.ndofs + 1, 0);
+    for (int64_t c = 0; c < hp.n_cells; ++c) {
+        const int s = hp.cell_sub[c];
+        if (s < 0) continue;
+        const int64_t* cd = hp.cell_dofs.data() + hp.cell_dofs_off[c] - 1;
+        for (int I = 0; I < op->subs[s].n; ++I) ++ptr[cd[I]];
+    }
+    for (int64_t d = 0; d < hp.ndofs; ++d) ptr[d + 1] += ptr[d];
+    std::vector<int32_t> inc((size_t)ptr[hp.ndofs]);
+    {
+        std::vector<int64_t> fill(ptr.begin(), ptr.end() - 1);
+        for (int64_t c = 0; c < hp.n_cells; ++c) {
+            const int s = hp.cell_sub[c];
+            if (s < 0) continue;
+            const fe_element_operator::Sub& os = op->subs[s];
+            const int64_t k = hp.cell_local[c];
+            const int64_t* cd = hp.cell_dofs.data() + hp.cell_dofs_off[c] - 1;
+            for (int I = 0; I < os.n; ++I)
+                inc[fill[cd[I] - 1]++] = (int32_t)(os.off + (op->rows ? k * os.n + I : I * os.n_cells + k));
+        }
+    }
+    cudaError_t e = cudaSetDevice(h->device);
+    for (size_t s = 0; s < hp.subs.size() && e == cudaSuccess; ++s) {
+        fe_element_operator::Sub& os = op->subs[s];
+        const HostSub& hs = hp.subs[s];
+        std::vector<int32_t> dofs((size_t)os.n * os.n_cells);
+        for (int64_t k = 0; k < os.n_cells; ++k) {
+            const int64_t* cd = hp.cell_dofs.data() + hp.cell_dofs_off[hs.cellid[k]] - 1;
+            for (int I = 0; I < os.n; ++I)
+                dofs[op->rows ? (size_t)k * os.n + I : (size_t)I * os.n_cells + k] = (int32_t)(cd[I] - 1);
+        }
+        e = op->upload(&os.cells, hs.cellid.data(), (size_t)os.n_cells);
+        if (e == cudaSuccess) e = op->upload(&os.dofs, dofs.data(), dofs.size());
+    }
+    if (e == cudaSuccess) e = op->upload(&op->ptr, ptr.data(), ptr.size());
+    if (e == cudaSuccess) e = op->upload(&op->inc, inc.data(), inc.size());
+    if (e == cudaSuccess) {
+        if (op->fp64)
+            e = op->upload<double>((double**)&op->ye, nullptr, (size_t)total);
+        else
+            e = op->upload<float>((float**)&op->ye, nullptr, (size_t)total);
+    }
+    if (e != cudaSuccess) {
+        delete op;
+        return cuda_fail(h, e, "element operator upload");
+    }
+    *out = op;
+    return FE_OK;
+}
+
+int fe_element_matvec(fe_element_operator* op, const void* ke, const double* u, double* y, uint32_t flags, void* stream) {
+    if (!op || !ke || !u || !y) return FE_ERR_ARG;
+    fe_handle* h = op->h;
+    if (!is_device_ptr(ke) || !is_device_ptr(u) || !is_device_ptr(y)) return set_error(h, FE_ERR_ARG, "ke, u and y must be device memory");
+    cudaStream_t st = (cudaStream_t)stream;
+    device_attributes(h);
+    cudaError_t e = cudaSuccess;
+    for (const fe_element_operator::Sub& os : op->subs) {
+        if (!os.n_cells) continue;
+        // threads per cell: 1 (128-thread blocks), or a warp (256-thread blocks, 8 cells each)
+        const int64_t blocks = op->rows ? (os.n_cells + 7) / 8 : (os.n_cells + 127) / 128;
+        const int64_t cap = (int64_t)h->n_sm * (op->rows ? 8 : 16);
+        const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(blocks, cap));
+        if (op->fp64)
+            e = launch_products<double>(os.n, op->rows, grid, st, (const double*)ke, op->ks, os.cells, os.dofs, os.n_cells, u,
+                                        (double*)op->ye + os.off);
+        else
+            e = launch_products<float>(os.n, op->rows, grid, st, (const float*)ke, op->ks, os.cells, os.dofs, os.n_cells, u,
+                                       (float*)op->ye + os.off);
+        if (e != cudaSuccess) return cuda_fail(h, e, "element products");
+    }
+    if (op->ndofs) {
+        const int64_t blocks = (op->ndofs + 255) / 256;
+        const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)h->n_sm * 8));
+        const int fz = (flags & FE_FILLZERO) ? 1 : 0;
+        if (op->fp64)
+            dof_gather<double><<<grid, 256, 0, st>>>((const double*)op->ye, op->ptr, op->inc, op->ndofs, fz, y);
+        else
+            dof_gather<float><<<grid, 256, 0, st>>>((const float*)op->ye, op->ptr, op->inc, op->ndofs, fz, y);
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(h, e, "dof gather");
+    }
+    return FE_OK;
+}
+
+void fe_element_operator_destroy(fe_element_operator* op) { delete op; }
 
 int fe_facet_set_create(fe_handle* h, const fe_facet_desc* d, fe_facet_set** out) {
     if (!h || !d || !out || d->n_facets < 0 || (d->n_facets > 0 && (!d->cells || !d->facets))) return FE_ERR_ARG;

@@ -99,7 +99,11 @@ end
 fe_create for a closed DofHandler, one scalar-interpolation CellValues per SubDofHandler (the
 field is `ip^n_components`), and the pattern of `K = allocate_matrix(dh)`.
 """
-function Handle(dh::DofHandler, cvs::Vector, K::SparseMatrixCSC{Float64,Int})
+Handle(dh::DofHandler, cvs::Vector, K::SparseMatrixCSC{Float64,Int}) = Handle(dh, cvs, K.colptr, K.rowval)
+
+# A SparseMatrixCSR{1} of allocate_matrix(SparseMatrixCSR, dh) (ext/FerriteSparseMatrixCSR.jl):
+# Handle(dh, cvs, K.rowptr, K.colval); its arrays equal the CSC ones (symmetric pattern).
+function Handle(dh::DofHandler, cvs::Vector, colptr::Vector{Int64}, rowval::Vector{Int64})
     grid = Ferrite.get_grid(dh)
     nodes = reinterpret(Float64, grid.nodes)            # AoS Vec{dim} memory
     keep = Any[nodes]
@@ -128,9 +132,9 @@ function Handle(dh::DofHandler, cvs::Vector, K::SparseMatrixCSC{Float64,Int})
     append!(keep, (offs, cd))
     g = Ref(GridDesc(Int32(Ferrite.getspatialdim(grid)), length(grid.nodes), pointer(nodes), length(grid.cells)))
     d = Ref(DofDesc(ndofs(dh), pointer(cd), pointer(offs)))
-    p = Ref(CscDesc(size(K, 2), nnz(K), pointer(K.colptr), pointer(K.rowval)))
+    p = Ref(CscDesc(length(colptr) - 1, length(rowval), pointer(colptr), pointer(rowval)))
     out = Ref{Ptr{Cvoid}}(C_NULL)
-    rc = GC.@preserve keep subs ccall((:fe_create, LIB), Cint,
+    rc = GC.@preserve keep subs colptr rowval ccall((:fe_create, LIB), Cint,
         (Ptr{GridDesc}, Int32, Ptr{SubdomainDesc}, Ptr{DofDesc}, Ptr{CscDesc}, Ptr{Ptr{Cvoid}}),
         g, Int32(length(subs)), subs, d, p, out)
     check(rc, C_NULL)
@@ -148,6 +152,26 @@ host arrays or device arrays (CuArray pointers).
 function assemble_csc!(K::SparseMatrixCSC{Float64,Int}, f::Vector{Float64}, h::Handle;
                        physics=FE_LINEAR_ELASTIC, p0=1.0, p1=0.3, body=(0.0, 0.0, 0.0),
                        cell_scale=nothing, u=nothing, precision=FE_PREC_MIXED, fillzero=true)
+    cs = cell_scale === nothing ? Ptr{Float64}(C_NULL) : pointer(cell_scale)
+    up = u === nothing ? Ptr{Float64}(C_NULL) : pointer(u)
+    par = Ref(AssembleParams(physics, precision, fillzero ? FE_FILLZERO : UInt32(0), p0, p1,
+                             Tuple(Float64.(body)), cs, up, 0.0, C_NULL))
+    rc = GC.@preserve K f cell_scale u ccall((:fe_assemble, LIB), Cint,
+        (Ptr{Cvoid}, Ptr{AssembleParams}, Ptr{Float64}, Ptr{Float64}), h.ptr, par, K.nzval, f)
+    check(rc, h.ptr)
+    return K, f
+end
+
+"""
+    assemble_csr!(K, f, h; ...)
+
+`start_assemble(K::SparseMatrixCSR, f)` + the cell loop + `assemble!` of
+ext/FerriteSparseMatrixCSR.jl for a handle made with `Handle(dh, cvs, K.rowptr, K.colval)`:
+every physics here has a symmetric K, so the CSC values of the same arrays are the CSR values
+(up to the rounding of Ke(I, J) against Ke(J, I)).
+"""
+function assemble_csr!(K, f::Vector{Float64}, h::Handle; physics=FE_LINEAR_ELASTIC, p0=1.0, p1=0.3,
+                       body=(0.0, 0.0, 0.0), cell_scale=nothing, u=nothing, precision=FE_PREC_MIXED, fillzero=true)
     cs = cell_scale === nothing ? Ptr{Float64}(C_NULL) : pointer(cell_scale)
     up = u === nothing ? Ptr{Float64}(C_NULL) : pointer(u)
     par = Ref(AssembleParams(physics, precision, fillzero ? FE_FILLZERO : UInt32(0), p0, p1,
@@ -182,6 +206,45 @@ function assemble_elements!(Kes, fes, h::Handle; physics=FE_LINEAR_ELASTIC, p0=1
         h.ptr, par, pointer(Kes), pointer(fes), lay)
     check(rc, h.ptr)
     return Kes, fes
+end
+
+# Matrix-free product with the element matrices of assemble_elements!
+mutable struct ElementOperator
+    ptr::Ptr{Cvoid}
+    h::Handle
+end
+
+"""
+    ElementOperator(h, Kes; precision=FE_PREC_MIXED)
+
+The operator u -> sum_c A_c' Kes[c, :, :] A_c u for the how-to's `Kes` (column-major
+`CUDA.zeros(Float32, ncells, nbf, nbf)`; Float64 with FE_PREC_FP64), which the how-to leaves
+to the user (gpu_assembly.jl:265-311).
+"""
+function ElementOperator(h::Handle, Kes; precision=FE_PREC_MIXED)
+    n, nbf = size(Kes, 1), size(Kes, 2)
+    lay = Ref(ElementLayout((1, n, n * nbf), (0, 0)))
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    rc = ccall((:fe_element_operator_create, LIB), Cint, (Ptr{Cvoid}, Ptr{ElementLayout}, Int32, Ptr{Ptr{Cvoid}}),
+               h.ptr, lay, Int32(precision), out)
+    check(rc, h.ptr)
+    op = ElementOperator(out[], h)
+    finalizer(x -> ccall((:fe_element_operator_destroy, LIB), Cvoid, (Ptr{Cvoid},), x.ptr), op)
+    return op
+end
+
+"""
+    element_mul!(y, op::ElementOperator, Kes, u; fillzero=true)
+
+y = sum_c A_c' Ke_c A_c u (y += ... with fillzero=false) on device arrays; asynchronous on the
+default stream.
+"""
+function element_mul!(y, op::ElementOperator, Kes, u; fillzero::Bool=true)
+    rc = GC.@preserve y Kes u op ccall((:fe_element_matvec, LIB), Cint,
+        (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, UInt32, Ptr{Cvoid}),
+        op.ptr, pointer(Kes), pointer(u), pointer(y), fillzero ? FE_FILLZERO : UInt32(0), C_NULL)
+    check(rc, op.h.ptr)
+    return y
 end
 
 # Dirichlet constraints of a closed ConstraintHandler on the handle's pattern

@@ -120,6 +120,12 @@ typedef struct {
     const int64_t* colptr; /* [n+1] 1-based (K.colptr) */
     const int64_t* rowval; /* [nnz] 1-based (K.rowval); read during fe_create only */
 } fe_csc_desc;
+/* A SparseMatrixCSR{1} (ext/FerriteSparseMatrixCSR.jl:9-160) goes in as (K.rowptr, K.colval)
+ * in place of (colptr, rowval), with its nzval as the output. Ferrite's pattern (cell
+ * couplings plus the diagonal) is structurally symmetric, so its CSR arrays are its CSC
+ * arrays, and every physics here has a symmetric K: the value written at row c of "column" r
+ * is K[c, r], which is K[r, c] up to the rounding of Ke(I, J) against Ke(J, I). A pattern
+ * miss is then reported with row and col swapped relative to the CSR (row, col). */
 
 typedef struct {
     int32_t physics;       /* FE_HEAT, FE_LINEAR_ELASTIC, FE_NEO_HOOKE */
@@ -198,6 +204,28 @@ typedef struct {
 
 int fe_assemble_elements(fe_handle* h, const fe_assemble_params* params, void* ke, void* fe,
                          const fe_element_layout* layout);
+
+/*
+ * Matrix-free product with the element matrices of fe_assemble_elements (the element-assembly
+ * technique of docs/src/literate-howto/gpu_assembly.jl:265-303, whose Kes the how-to leaves to
+ * a user-written product): y (+)= sum over the cells of the handle's subdomains, in ascending
+ * cell order, of A_c^T (Ke_c (A_c u)), A_c the gather of the cell's dofs.
+ * fe_element_operator_create takes the element layout (ke_stride as in fe_assemble_elements;
+ * fe_stride is ignored) and the precision: FE_PREC_MIXED for float Ke, FE_PREC_FP64 for double
+ * Ke. It builds once the dof -> (cell, local dof) incidence in cell order and a scratch of one
+ * value per (cell, local dof). fe_element_matvec, on DEVICE ke, u and y, asynchronous on
+ * `stream`: per cell ye_I = sum_J Ke(I, J) u_J as fused multiply-adds in the element precision
+ * (J ascending; u rounded to float for FE_PREC_MIXED), then y[dof_I] += (double) ye_I in FP64
+ * in cell order; flags FE_FILLZERO sets y = 0 first. Deterministic, no atomics: bitwise the
+ * serial loop over cells. The caller keeps ke covering every cell the strides address.
+ * Destroy the operator before its handle.
+ */
+typedef struct fe_element_operator fe_element_operator;
+int fe_element_operator_create(fe_handle* h, const fe_element_layout* layout, int32_t precision,
+                               fe_element_operator** out);
+int fe_element_matvec(fe_element_operator* op, const void* ke, const double* u, double* y, uint32_t flags,
+                      void* stream);
+void fe_element_operator_destroy(fe_element_operator* op);
 
 /*
  * Dirichlet constraints on the assembled matrix: apply!(K, f, ch) and apply_zero!(K, f, ch)

@@ -938,6 +938,98 @@ int or_index_map(const or_problem* p, int64_t cell, int64_t* positions) {
     return OR_OK;
 }
 
+// CSR assembler of ext/FerriteSparseMatrixCSR.jl:9-96 (start_assemble for SparseMatrixCSR and
+// its _assemble_inner!): per sorted row dof, a walk over the row's sorted columns (dense row and
+// binary-search fast paths as for CSC), K[row, col] += Ke[row_local, col_local] with zeros
+// skipped, a non-zero without a pattern entry reported as (row, col). The row walk is the CSC
+// column walk on (rowptr, colval) with the element matrix read transposed.
+int or_assemble_csr(const or_problem* p, const or_physics* ph, int32_t fillzero, const int64_t* rowptr,
+                    const int64_t* colval, double* nzval, double* f, or_error* err) {
+    Setup S;
+    int rc = S.init(p);
+    err->code = OR_OK;
+    err->cell = 0;
+    if (rc) { err->code = rc; return rc; }
+    const int64_t nnz = rowptr[p->ndofs] - 1;
+    if (fillzero) {
+        if (nzval) std::memset(nzval, 0, nnz * sizeof(double));
+        if (f) std::memset(f, 0, p->ndofs * sizeof(double));
+    }
+    CSCView rows{p->ndofs, rowptr, colval};
+    std::vector<double> Ke, fe, x, ue;
+    std::vector<int64_t> sorted;
+    std::vector<int> perm;
+    for (int s = 0; s < p->n_sdh; ++s)
+        for (int64_t k = p->sdh_cellset_offset[s]; k < p->sdh_cellset_offset[s + 1]; ++k) {
+            const int64_t c = p->sdh_cellset[k] - 1;
+            const int ld = S.ndpc[s];
+            Ke.resize(ld * ld);
+            fe.resize(ld);
+            int r = element(S, S.cvs[s], s, c, ph, Ke.data(), fe.data(), x, ue, err);
+            if (r) return r;
+            const int64_t* dofs = p->cell_dofs + p->cell_dofs_offset[c] - 1;
+            if (f)
+                for (int i = 0; i < ld; ++i) f[dofs[i] - 1] += fe[i];
+            if (!nzval) continue;
+            int miss_code = OR_OK;
+            // walk row dofs[kerow]; kecol is the local index of the column found at R
+            merge_walk(rows, dofs, ld, sorted, perm,
+                       [&](int64_t R, int kecol, int kerow) {
+                           const double v = Ke[kecol * ld + kerow];  // Ke[kerow, kecol], column-major
+                           if (v != 0.0) nzval[R] += v;
+                       },
+                       [&](int64_t col, int64_t row, int kecol, int kerow) {
+                           if (Ke[kecol * ld + kerow] != 0.0 && miss_code == OR_OK) {
+                               miss_code = OR_ERR_PATTERN_MISSING;
+                               err->code = OR_ERR_PATTERN_MISSING;
+                               err->row = row;
+                               err->col = col;
+                               err->cell = c + 1;
+                           }
+                       });
+            if (miss_code) return miss_code;
+        }
+    return OR_OK;
+}
+
+// Element-matrix product y (+)= sum_c A_c^T Ke_c A_c u in ascending cell order: the consumer
+// of the element-assembly output of docs/src/literate-howto/gpu_assembly.jl:265-303 (Kes per
+// cell, FP32 there), with explicit fused multiply-adds so the operation order is exact.
+extern "C++" {
+template <typename T>
+static void element_matvec(const or_problem* p, const Setup& S, const T* ke, const int64_t* ks, const double* u,
+                           double* y) {
+    std::vector<T> ue, ye;
+    for (int64_t c = 0; c < p->n_cells; ++c) {
+        const int s = S.cell_sdh[c];
+        if (s < 0) continue;
+        const int n = S.ndpc[s];
+        const int64_t* dofs = p->cell_dofs + p->cell_dofs_offset[c] - 1;
+        ue.assign(n, T(0));
+        ye.assign(n, T(0));
+        for (int J = 0; J < n; ++J) ue[J] = (T)u[dofs[J] - 1];
+        const T* kc = ke + c * ks[0];
+        for (int J = 0; J < n; ++J)
+            for (int I = 0; I < n; ++I) ye[I] = std::fma(kc[I * ks[1] + J * ks[2]], ue[J], ye[I]);
+        for (int I = 0; I < n; ++I) y[dofs[I] - 1] += (double)ye[I];
+    }
+}
+}
+
+int or_element_matvec(const or_problem* p, int32_t fp64, const void* ke, const int64_t* ks, const double* u,
+                      int32_t fillzero, double* y) {
+    Setup S;
+    int rc = S.init(p);
+    if (rc) return rc;
+    if (fillzero)
+        for (int64_t i = 0; i < p->ndofs; ++i) y[i] = 0.0;
+    if (fp64)
+        element_matvec(p, S, (const double*)ke, ks, u, y);
+    else
+        element_matvec(p, S, (const float*)ke, ks, u, y);
+    return OR_OK;
+}
+
 // Greedy node-sharing coloring in cell order (coloring.jl:47-143).
 int or_greedy_coloring(const or_problem* p, int32_t* cell_color, int32_t* n_colors) {
     std::vector<int64_t> nptr(p->n_nodes + 1, 0);

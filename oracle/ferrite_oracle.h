@@ -121,6 +121,22 @@ int or_apply(int64_t n, const int64_t* colptr, const int64_t* rowval, double* nz
              int64_t n_prescribed, const int64_t* prescribed, const double* inhomogeneities, int32_t applyzero);
 int or_greedy_coloring(const or_problem* p, int32_t* cell_color, int32_t* n_colors);
 
+/* CSR assembly (ext/FerriteSparseMatrixCSR.jl:9-96, SparseMatrixCSR{1}): as or_assemble (serial,
+ * cell order) into a CSR matrix with 1-based rowptr[ndofs+1] / colval[nnz] (columns ascending
+ * within a row): K[row, col] += Ke[row_local, col_local]; a pattern miss reports (row, col). */
+int or_assemble_csr(const or_problem* p, const or_physics* phys, int32_t fillzero, const int64_t* rowptr,
+                    const int64_t* colval, double* nzval, double* f, or_error* err);
+
+/* Matrix-free product with element matrices (the element-assembly technique of
+ * docs/src/literate-howto/gpu_assembly.jl:265-303, Kes[cell, i, j]):
+ *   y (+)= sum over cells c in ascending order, c in a SubDofHandler, of A_c^T (Ke_c (A_c u)).
+ * Ke_c(I, J) = ke[c*ks[0] + I*ks[1] + J*ks[2]] (c, I, J 0-based; float if fp64 == 0, else
+ * double). Per cell, u_e = u[celldofs] (rounded to float when fp64 == 0) and
+ * ye_I = fma(Ke(I, n-1), u_{n-1}, ... fma(Ke(I, 0), u_0, 0)) in the element precision, J
+ * ascending; then y[celldofs[I]] += (double) ye_I in FP64, I ascending. fillzero: y = 0 first. */
+int or_element_matvec(const or_problem* p, int32_t fp64, const void* ke, const int64_t* ks, const double* u,
+                      int32_t fillzero, double* y);
+
 /* Adjoint of the assembly (heat, linear elasticity): for Phi = lambda^T (K(X, s) u - f(X)),
  *   d_cell[c] = dscale[c] * dPhi/ds_c   (s_c = cell_scale[c], the factor on the material;
  *                                        dscale NULL = 1: the derivative w.r.t. s_c itself)

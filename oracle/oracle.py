@@ -93,6 +93,10 @@ def lib():
             L.or_apply.argtypes = [ctypes.c_int64, i64p, i64p, f64p, f64p, ctypes.c_int64, i64p, f64p, ctypes.c_int32]
             L.or_adjoint.argtypes = [ctypes.POINTER(_Problem), ctypes.POINTER(_Physics), f64p, f64p, f64p, f64p, f64p,
                                      ctypes.POINTER(_Error)]
+            L.or_assemble_csr.argtypes = [ctypes.POINTER(_Problem), ctypes.POINTER(_Physics), ctypes.c_int32, i64p, i64p,
+                                          f64p, f64p, ctypes.POINTER(_Error)]
+            L.or_element_matvec.argtypes = [ctypes.POINTER(_Problem), ctypes.c_int32, ctypes.c_void_p, i64p, f64p,
+                                            ctypes.c_int32, f64p]
             _lib = L
     return _lib
 
@@ -337,6 +341,31 @@ class Problem:
             raise OracleError(rc, err)
         return nzval, f
 
+    def csr_pattern(self):
+        """allocate_matrix(SparseMatrixCSR, dh) (ext/FerriteSparseMatrixCSR.jl:124-160): the
+        pattern's rows, columns ascending -- the transpose of the CSC pattern; returns 1-based
+        (rowptr, colval)."""
+        import scipy.sparse as sp
+        A = sp.csc_matrix((np.ones(self.nnz), self.rowval - 1, self.colptr - 1), shape=(self.ndofs, self.ndofs)).tocsr()
+        A.sort_indices()
+        return A.indptr.astype(np.int64) + 1, A.indices.astype(np.int64) + 1
+
+    def assemble_csr(self, rowptr, colval, physics, p0, p1, body=None, cell_scale=None, u=None, fillzero=True):
+        """start_assemble(K::SparseMatrixCSR, f) + cell loop + assemble! (serial, cell order);
+        returns (nzval, f) of the CSR matrix."""
+        rowptr = np.ascontiguousarray(rowptr, np.int64)
+        colval = np.ascontiguousarray(colval, np.int64)
+        nzval = np.zeros(len(colval))
+        f = np.zeros(self.ndofs)
+        P = self._struct()
+        ph = self._physics(physics, p0, p1, body, cell_scale, u)
+        err = _Error()
+        rc = lib().or_assemble_csr(ctypes.byref(P), ctypes.byref(ph), int(fillzero), _p(rowptr, i64p), _p(colval, i64p),
+                                   _p(nzval, f64p), _p(f, f64p), ctypes.byref(err))
+        if rc:
+            raise OracleError(rc, err)
+        return nzval, f
+
     def element(self, c0: int, physics, p0, p1, body=None, cell_scale=None, u=None):
         s = self._sdh_of(c0)
         ld = self.ndofs_per_cell(s)
@@ -399,6 +428,26 @@ class Problem:
         if rc:
             raise OracleError(rc, _Error())
         return nzval, f
+
+    def element_matvec(self, ke, u, y=None, fillzero=True):
+        """y (+)= sum over cells in ascending order of A_c^T Ke_c A_c u, Ke_c = ke[c] (an array
+        [n_cells, n, n], float32 or float64, any strides), with the operation order of
+        or_element_matvec (fused multiply-adds in the element precision, FP64 sums)."""
+        ke = np.asarray(ke)
+        if ke.dtype not in (np.float32, np.float64) or ke.ndim != 3:
+            raise ValueError("ke must be a float32 or float64 array [n_cells, n, n]")
+        ks = np.array([st // ke.itemsize for st in ke.strides], np.int64)
+        u = np.ascontiguousarray(u, np.float64)
+        if y is None:
+            y = np.zeros(self.ndofs, np.float64)
+            fillzero = True
+        P = self._struct()
+        rc = lib().or_element_matvec(ctypes.byref(P), 1 if ke.dtype == np.float64 else 0,
+                                     ctypes.c_void_p(ke.ctypes.data), _p(ks, i64p), _p(u, f64p),
+                                     1 if fillzero else 0, _p(y, f64p))
+        if rc:
+            raise OracleError(rc, _Error())
+        return y
 
     def index_map(self, c0: int):
         """1-based nzval positions of Ke entries of cell c0 ([ld, ld], Ke[I, J])."""

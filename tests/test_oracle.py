@@ -377,3 +377,86 @@ def test_facet_load_integrates_pressure(oracle, ct, ip):
     sums = [f[a::d].sum() for a in range(d)]
     expect = [1.5 * area + t[0] * area] + [t[a] * area for a in range(1, d)]
     assert np.allclose(sums, expect, rtol=1e-13, atol=1e-13)
+
+
+def _element_stack(p, physics, p0, p1, dtype=np.float64):
+    """Ke of every cell from the oracle's element routine, as [n_cells, n, n]."""
+    return np.stack([p.element(c, physics, p0, p1)[0] for c in range(p.n_cells)]).astype(dtype)
+
+
+@pytest.mark.parametrize("ct,nel,ip,nc", [("QUADRILATERAL", (5, 4), 1, 1), ("HEXAHEDRON", (3, 2, 2), 1, 3),
+                                          ("TETRAHEDRON", (2, 2, 1), 1, 3), ("HEXAHEDRON", (2, 1, 1), 2, 3)])
+def test_element_matvec_equals_assembled_product(oracle, ct, nel, ip, nc):
+    """sum_c A_c^T Ke_c A_c u with FP64 element matrices equals K u of the assembled K."""
+    O = oracle
+    ctype = getattr(O, ct)
+    phys, p0, p1 = (O.HEAT, 1.0, 1.0) if nc == 1 else (O.LINEAR_ELASTIC, 200e3, 0.3)
+    p = O.box_problem(ctype, nel, ip_order=ip, ncomp=nc, qr_order=3 if ip == 2 else 2, perturb=0.15, seed=11)
+    nz, _ = p.assemble(phys, p0, p1)
+    ke = _element_stack(p, phys, p0, p1)
+    u = np.random.default_rng(4).standard_normal(p.ndofs)
+    y = p.element_matvec(ke, u)
+    ref = p.to_scipy(nz) @ u
+    assert np.abs(y - ref).max() <= 1e-13 * np.abs(ke).max() * np.abs(u).max() * 8
+    # accumulation: y0 + product
+    y0 = np.random.default_rng(5).standard_normal(p.ndofs)
+    y2 = p.element_matvec(ke, u, y=y0.copy(), fillzero=False)
+    assert np.abs(y2 - (y0 + y)).max() <= 1e-12 * np.abs(y).max()
+
+
+def test_element_matvec_layouts_and_float_order(oracle):
+    """Any strides address the same matrices (the how-to's column-major Kes included), and the
+    float form is the fused multiply-add chain of its definition, checked against a numpy loop."""
+    O = oracle
+    p = O.box_problem(O.HEXAHEDRON, (2, 2, 1), ip_order=1, ncomp=3, perturb=0.1, seed=2)
+    ke = _element_stack(p, O.LINEAR_ELASTIC, 200e3, 0.3, np.float32)
+    u = np.random.default_rng(6).standard_normal(p.ndofs)
+    y_row = p.element_matvec(ke, u)
+    y_col = p.element_matvec(np.asfortranarray(ke), u)      # Kes[cell, i, j], column-major
+    assert np.array_equal(y_row, y_col)
+    # numpy restatement of the fma chain: the float32 product is exact in float64 and so is its
+    # sum with a float32 addend of nearby exponent, then one rounding to float32 (a double
+    # rounding could only differ for far-apart exponents, which these seeded values do not have)
+    y = np.zeros(p.ndofs)
+    for c in range(p.n_cells):
+        dofs = p.celldofs(c) - 1
+        ue = u[dofs].astype(np.float32)
+        acc = np.zeros(len(dofs), np.float32)
+        for J in range(len(dofs)):
+            acc = (ke[c, :, J].astype(np.float64) * np.float64(ue[J]) + acc.astype(np.float64)).astype(np.float32)
+        y[dofs] += acc.astype(np.float64)
+    assert np.array_equal(y, y_row)
+
+
+def test_csr_assembly_pins(oracle):
+    """CSR assembly (ext/FerriteSparseMatrixCSR.jl): its pattern is the transpose of the CSC
+    pattern, which Ferrite's cell-coupling pattern makes the same arrays; K_csr is the
+    transpose of K_csc entry by entry (symmetric physics: equal to rounding); a missing entry
+    is reported as the CSR (row, col)."""
+    O = oracle
+    p = O.box_problem(O.HEXAHEDRON, (3, 2, 2), ncomp=3, perturb=0.2, seed=12)
+    rowptr, colval = p.csr_pattern()
+    assert np.array_equal(rowptr, p.colptr) and np.array_equal(colval, p.rowval)
+    for phys, p0, p1 in ((O.LINEAR_ELASTIC, 200e3, 0.3), (O.HEAT, 1.0, 1.0)):
+        if phys == O.HEAT:
+            p = O.box_problem(O.QUADRILATERAL, (4, 3), perturb=0.2, seed=13)
+            rowptr, colval = p.csr_pattern()
+        nz_csc, f_csc = p.assemble(phys, p0, p1)
+        nz_csr, f_csr = p.assemble_csr(rowptr, colval, phys, p0, p1)
+        import scipy.sparse as sp
+        Kr = sp.csr_matrix((nz_csr, colval - 1, rowptr - 1), shape=(p.ndofs, p.ndofs))
+        Kc = p.to_scipy(nz_csc)
+        assert abs(Kr - Kc).max() <= 1e-14 * abs(Kc).max()
+        assert np.array_equal(f_csr, f_csc)
+    # a pattern without K[r, c] for some coupled pair: the CSR error names row r, column c
+    rp, cv = rowptr.copy(), colval.copy()
+    r = 0
+    lo, hi = rp[r] - 1, rp[r + 1] - 1
+    c = int(cv[hi - 1])                     # last column of row 1
+    keep = np.ones(len(cv), bool)
+    keep[hi - 1] = False
+    cv = cv[keep]
+    rp[r + 1:] -= 1
+    with pytest.raises(O.OracleError) as ei:
+        p.assemble_csr(rp, cv, O.HEAT, 1.0, 1.0)
+    assert ei.value.row == r + 1 and ei.value.col == c
