@@ -576,15 +576,36 @@ struct fe_element_operator {
 
 namespace {
 
+// the vector form of element_products_rows: J contiguous, every row start 16-byte aligned
+template <typename T>
+bool rows_vectorizable(int n, const T* ke, const int64_t* ks) {
+    constexpr int W = Vec16<T>::W;
+    return ks[2] == 1 && ks[1] % W == 0 && ks[0] % W == 0 && n % W == 0 && ((uintptr_t)ke & 15u) == 0;
+}
+
+template <typename T, int N>
+void launch_rows(bool vec, unsigned grid, cudaStream_t st, const T* ke, const int64_t* ks, const int32_t* cells,
+                 const int32_t* dofs, int64_t n_cells, const double* u, T* ye) {
+    if constexpr (N % Vec16<T>::W == 0) {
+        if (vec) {
+            element_products_rows<T, N, true><<<grid, 256, 0, st>>>(ke, ks[0], ks[1], ks[2], cells, dofs, n_cells, u, ye);
+            return;
+        }
+    }
+    element_products_rows<T, N, false><<<grid, 256, 0, st>>>(ke, ks[0], ks[1], ks[2], cells, dofs, n_cells, u, ye);
+}
+
 template <typename T>
 cudaError_t launch_products(int n, bool rows, unsigned grid, cudaStream_t st, const T* ke, const int64_t* ks,
                             const int32_t* cells, const int32_t* dofs, int64_t n_cells, const double* u, T* ye) {
-#define FE_PRODUCTS(N)                                                                                               \
-    case N:                                                                                                          \
-        if (rows)                                                                                                    \
-            element_products_rows<T, N><<<grid, 256, 0, st>>>(ke, ks[0], ks[1], ks[2], cells, dofs, n_cells, u, ye); \
-        else                                                                                                         \
-            element_products<T, N><<<grid, 128, 0, st>>>(ke, ks[0], ks[1], ks[2], cells, dofs, n_cells, u, ye);      \
+    const bool vec = rows && rows_vectorizable(n, ke, ks);
+#define FE_PRODUCTS(N)                                                                                          \
+    case N:                                                                                                     \
+        if (rows)                                                                                               \
+            launch_rows<T, N>(vec, grid, st, ke, ks, cells, dofs, n_cells, u, ye);                              \
+        else                                                                                                    \
+            element_products<T, N, products_split<T>(N)>                                                        \
+                <<<grid, 128, 0, st>>>(ke, ks[0], ks[1], ks[2], cells, dofs, n_cells, u, ye);                   \
         break;
     switch (n) {
         FE_PRODUCTS(3)
@@ -1641,8 +1662,10 @@ int fe_element_matvec(fe_element_operator* op, const void* ke, const double* u, 
     cudaError_t e = cudaSuccess;
     for (const fe_element_operator::Sub& os : op->subs) {
         if (!os.n_cells) continue;
-        // threads per cell: 1 (128-thread blocks), or a warp (256-thread blocks, 8 cells each)
-        const int64_t blocks = op->rows ? (os.n_cells + 7) / 8 : (os.n_cells + 127) / 128;
+        // threads per cell: products_split(n) (128-thread blocks of 128 / split cells), or a warp
+        // (256-thread blocks, 8 cells each)
+        const int64_t per_block = op->rows ? 8 : 128 / (op->fp64 ? products_split<double>(os.n) : products_split<float>(os.n));
+        const int64_t blocks = (os.n_cells + per_block - 1) / per_block;
         const int64_t cap = (int64_t)h->n_sm * (op->rows ? 8 : 16);
         const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(blocks, cap));
         if (op->fp64)
