@@ -48,15 +48,21 @@ __global__ void __launch_bounds__(128) element_products(const T* __restrict__ ke
         T acc[RP];
 #pragma unroll
         for (int i = 0; i < RP; ++i) acc[i] = T(0);
-        // four J per step: their u and Ke loads are independent of the chains, so they issue
-        // together
-#pragma unroll 4
-        for (int J = 0; J < N; ++J) {
+        auto step = [&](int J) {
             const T uj = MatvecPrec<T>::from(u[dofs[(int64_t)J * n_cells + k]]);
             const T* col = kc + (int64_t)J * ks2;
 #pragma unroll
             for (int i = 0; i < RP; ++i)
                 if (i0 + i < N) acc[i] = MatvecPrec<T>::fma(__ldg(col + (int64_t)(i0 + i) * ks1), uj, acc[i]);
+        };
+        if constexpr (sizeof(T) == 8) {
+            // the FP64 pipe is the bound; the unrolled form measured slower
+#pragma unroll 1
+            for (int J = 0; J < N; ++J) step(J);
+        } else {
+            // four J per step: their u and Ke loads do not depend on the chains, so they issue together
+#pragma unroll 4
+            for (int J = 0; J < N; ++J) step(J);
         }
 #pragma unroll
         for (int i = 0; i < RP; ++i)
