@@ -224,6 +224,48 @@ def _ptr(x):
     raise TypeError(f"unsupported buffer type {type(x)}")
 
 
+def _dtype(x) -> str:
+    return str(x.dtype).replace("torch.", "")
+
+
+def _numel(x) -> int:
+    return int(x.size) if isinstance(x, np.ndarray) else int(x.numel())
+
+
+def _check(x, name: str, dtype: str, n: int):
+    """A buffer the library reads or writes n elements of: its element type and length. The C
+    ABI takes bare pointers, so a wrong type or a short buffer would be accessed past its end."""
+    if x is None:
+        return
+    if not isinstance(x, np.ndarray) and not hasattr(x, "data_ptr"):
+        raise TypeError(f"{name}: unsupported buffer type {type(x)}")
+    if _dtype(x) != dtype:
+        raise TypeError(f"{name} must be {dtype}, got {_dtype(x)}")
+    if _numel(x) < n:
+        raise ValueError(f"{name} has {_numel(x)} elements; the call accesses {n}")
+
+
+def _extent(n_cells: int, m: int, strides) -> int:
+    """Elements spanned by per-cell arrays X(c, I[, J]) at c*s0 + I*s1 (+ J*s2), m dofs per cell."""
+    st = [int(v) for v in strides]
+    if any(v < 0 for v in st):
+        raise ValueError("element strides must be non-negative")
+    if n_cells == 0 or m == 0:
+        return 0
+    return (n_cells - 1) * st[0] + sum((m - 1) * v for v in st[1:]) + 1
+
+
+def _max_dofs_per_cell(subdomains) -> int:
+    """Most dofs of one cell over the subdomains: base functions (N is [n_qp, n_base]) times
+    components."""
+    return max(((np.asarray(sd.N).size // max(len(np.asarray(sd.qr_weights)), 1)) * int(sd.n_components)
+                for sd in subdomains), default=0)
+
+
+def _elem_dtype(precision: int) -> str:
+    return "float64" if precision == PREC_FP64 else "float32"
+
+
 @dataclass
 class Subdomain:
     """One SubDofHandler + its CellValues data (the arrays a Julia caller extracts from
@@ -303,8 +345,18 @@ class Handle:
         self.ndofs = int(ndofs)
         self.nnz = int(len(rv))
         self.n_cells = int(n_cells)
+        self.n_nodes, self.dim = int(nodes.shape[0]), int(nodes.shape[1])
         self.ndofs_per_cell = {}
         self._subdomains = list(subdomains)
+        self.max_dofs_per_cell = _max_dofs_per_cell(subdomains)
+
+    def _check_fields(self, u=None, cell_scale=None):
+        _check(u, "u", "float64", self.ndofs)
+        _check(cell_scale, "cell_scale", "float64", self.n_cells)
+
+    def _check_outputs(self, nzval, f):
+        _check(nzval, "nzval", "float64", self.nnz)
+        _check(f, "f", "float64", self.ndofs)
 
     @property
     def ptr(self):
@@ -333,6 +385,8 @@ class Handle:
         ``compensated`` (mixed precision): sum each entry as a compensated FP32 pair.
         ``form``: None (the engine's choice), "two_phase" (element matrices first; on the tensor
         cores where a kernel exists), "two_phase_cuda_cores" or "fused"."""
+        self._check_outputs(nzval, f)
+        self._check_fields(u, cell_scale)
         p = AssembleParams()
         p.physics, p.precision = physics, precision
         flags = FILLZERO if fillzero else 0
@@ -383,6 +437,13 @@ class Handle:
             lay.ke_stride[k] = int(ks[k])
         for k in range(2):
             lay.fe_stride[k] = int(fs[k])
+        dt = _elem_dtype(kw.get("precision", PREC_MIXED))
+        m = self.max_dofs_per_cell
+        if ke is not None:
+            _check(ke, "ke", dt, _extent(self.n_cells, m, ks))
+        if fe is not None:
+            _check(fe, "fe", dt, _extent(self.n_cells, m, fs))
+        self._check_fields(kw.get("u"), kw.get("cell_scale"))
         rc = lib().fe_assemble_elements(self._h, ctypes.byref(p), _ptr(ke), _ptr(fe), ctypes.byref(lay))
         if rc != FE_OK:
             self._raise(rc)
@@ -425,12 +486,18 @@ class Handle:
         rc = lib().fe_element_operator_create(self._h, ctypes.byref(lay), int(precision), ctypes.byref(out))
         if rc != FE_OK:
             self._raise(rc)
-        return ElementOperator(self, out, precision)
+        return ElementOperator(self, out, precision, tuple(int(v) for v in ke_stride))
 
     def adjoint(self, u, lam, d_rho, d_X, physics: int, p0: float, p1: float, body=(0.0, 0.0, 0.0), cell_scale=None,
                 dscale=None, precision: int = PREC_MIXED, stream=None, sync: bool = True):
         """fe_assemble_adjoint: d_rho[n_cells] = dscale * lam^T (dK/ds) u and d_X[n_nodes*dim] =
         lam^T d(K u - f)/dX, written in place (numpy or torch CUDA buffers; d_X may be None)."""
+        _check(u, "u", "float64", self.ndofs)
+        _check(lam, "lam", "float64", self.ndofs)
+        _check(d_rho, "d_rho", "float64", self.n_cells)
+        _check(d_X, "d_X", "float64", self.n_nodes * self.dim)
+        _check(cell_scale, "cell_scale", "float64", self.n_cells)
+        _check(dscale, "dscale", "float64", self.n_cells)
         p = AdjointParams()
         p.physics, p.precision = physics, precision
         p.flags = 0 if sync else ASYNC
@@ -467,6 +534,8 @@ class Handle:
         Returns {"best_stage_cap", "best_ms", "candidates": [(cap, ms, tiles, visits), ...]}."""
         if stream is not None and hasattr(stream, "cuda_stream"):
             stream = stream.cuda_stream
+        self._check_outputs(nzval, f)
+        self._check_fields(assemble_kw.get("u"), assemble_kw.get("cell_scale"))
         p = self._params(stream=stream, **assemble_kw)
         caps = None
         n = 0
@@ -486,6 +555,11 @@ class Handle:
         n = len(steps)
         if stream is not None and hasattr(stream, "cuda_stream"):
             stream = stream.cuda_stream
+        if len(nzvals) != n or len(fs) != n:
+            raise ValueError("one nzval and one f per step")
+        for st, nz, fv in zip(steps, nzvals, fs):
+            self._check_outputs(nz, fv)
+            self._check_fields(st.get("u"), st.get("cell_scale"))
         arr = (AssembleParams * n)(*[self._params(stream=stream, **st) for st in steps])
         nz = (ctypes.c_void_p * n)(*[_ptr(x) for x in nzvals])
         ff = (ctypes.c_void_p * n)(*[_ptr(x) for x in fs])
@@ -613,6 +687,8 @@ class Dirichlet:
         g = inhomogeneities
         if isinstance(g, np.ndarray):
             g = np.ascontiguousarray(g, np.float64)
+        self._handle._check_outputs(nzval, f)
+        _check(g, "inhomogeneities", "float64", self.n_prescribed)
         rc = lib().fe_apply(self._c, _ptr(nzval), _ptr(f), _ptr(g), 1 if applyzero else 0, stream)
         if rc != FE_OK:
             self._handle._raise(rc)
@@ -640,14 +716,19 @@ class ElementOperator:
     """y (+)= sum_c A_c^T Ke_c A_c u with element matrices (fe_element_matvec) on device buffers
     (torch CUDA tensors). Close it before its handle."""
 
-    def __init__(self, handle, ptr, precision):
+    def __init__(self, handle, ptr, precision, ke_stride):
         self._handle = handle
         self._c = ptr
         self.precision = precision
+        self.ke_stride = ke_stride
 
     def matvec(self, ke, u, y, fillzero: bool = True, stream=None, sync: bool = True):
         if stream is not None and hasattr(stream, "cuda_stream"):
             stream = stream.cuda_stream
+        h = self._handle
+        _check(ke, "ke", _elem_dtype(self.precision), _extent(h.n_cells, h.max_dofs_per_cell, self.ke_stride))
+        _check(u, "u", "float64", h.ndofs)
+        _check(y, "y", "float64", h.ndofs)
         rc = lib().fe_element_matvec(self._c, _ptr(ke), _ptr(u), _ptr(y), FILLZERO if fillzero else 0, stream)
         if rc != FE_OK:
             self._handle._raise(rc)
@@ -678,6 +759,7 @@ class FacetSet:
     def load(self, f, pressure: float, traction=(0.0, 0.0, 0.0), fillzero: bool = False, stream=None):
         if stream is not None and hasattr(stream, "cuda_stream"):
             stream = stream.cuda_stream
+        _check(f, "f", "float64", self._handle.ndofs)
         t = (ctypes.c_double * 3)(*[float(x) for x in list(traction) + [0.0] * (3 - len(traction))])
         rc = lib().fe_assemble_facet_load(self._c, float(pressure), ctypes.cast(t, f64p), FILLZERO if fillzero else 0,
                                           _ptr(f), stream)

@@ -73,3 +73,34 @@ def test_facet_values_tables(fg, oracle, ct, ip, qo):
     assert a[0] == b[0] and a[1] == b[1]
     for x, y in zip(a[2:], b[2:]):
         assert x.shape == y.shape and np.allclose(x, y, rtol=1e-14, atol=1e-15)
+
+
+def test_buffer_checks(fg, oracle):
+    """The Python layer checks element types and lengths before passing bare pointers to the
+    C ABI (a float32 buffer where float64 is read, or a short one, would be accessed past its
+    end)."""
+    import numpy as np
+    from helpers import subdomain_specs
+    O = oracle
+    for ct, nel, ip, nc, want in [(O.HEXAHEDRON, (2, 2, 1), 1, 3, 24), (O.HEXAHEDRON, (1, 1, 1), 2, 3, 81),
+                                  (O.QUADRILATERAL, (2, 2), 1, 1, 4), (O.TETRAHEDRON, (1, 1, 1), 1, 3, 12)]:
+        prob = O.box_problem(ct, nel, ip_order=ip, ncomp=nc, qr_order=3 if ip == 2 else 2)
+        assert fg._max_dofs_per_cell(subdomain_specs(fg, O, prob)) == want
+    fg._check(np.zeros(10), "x", "float64", 10)
+    with pytest.raises(TypeError):
+        fg._check(np.zeros(10, np.float32), "x", "float64", 10)
+    with pytest.raises(ValueError):
+        fg._check(np.zeros(9), "x", "float64", 10)
+    with pytest.raises(TypeError):
+        fg._check([0.0] * 10, "x", "float64", 10)
+    # extents: row-major [n, m, m], the how-to's column-major, and a per-cell vector
+    n, m = 5, 24
+    assert fg._extent(n, m, (m * m, m, 1)) == n * m * m
+    assert fg._extent(n, m, (1, n, n * m)) == n * m * m
+    assert fg._extent(n, m, (1, n)) == n * m
+    with pytest.raises(ValueError):
+        fg._extent(n, m, (-1, n, n * m))
+    torch = pytest.importorskip("torch")
+    fg._check(torch.zeros(n * m * m, dtype=torch.float32), "ke", fg._elem_dtype(fg.PREC_MIXED), n * m * m)
+    with pytest.raises(TypeError):
+        fg._check(torch.zeros(n * m * m, dtype=torch.float32), "ke", fg._elem_dtype(fg.PREC_FP64), n * m * m)
