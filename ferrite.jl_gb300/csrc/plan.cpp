@@ -16,7 +16,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <numeric>
+#include <type_traits>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -177,39 +179,45 @@ int build_problem(const CreateInput& in, HostProblem& hp, Error& err) {
         err.col = bad_col;
         return fail(err, FE_ERR_UNSUPPORTED, "sparsity pattern is not blocked by dof entity (all components coupled)");
     }
-    // ranks (the index map)
+    // ranks (the index map): rank of row entity e[i] in column entity e[j]'s row list, by one
+    // merge walk per (cell, j) over the column's ascending row entities against the cell's
+    // entities in ascending order; 8-bit ranks unless some rank exceeds 254
     for (int s = 0; s < in.n_sub; ++s) {
         HostSub& hs = hp.subs[s];
         const int nb = hs.nb;
-        std::vector<uint16_t> r16((size_t)hs.n_cells * nb * nb);
-        int maxr = 0;
-#pragma omp parallel for schedule(static) reduction(max : maxr)
-        for (int64_t k = 0; k < hs.n_cells; ++k) {
-            const int32_t* e = &hs.ents[k * nb];
-            for (int j = 0; j < nb; ++j) {
-                const int64_t n = e[j];
-                const int64_t c0 = cp[nc * n] - 1;
-                const int64_t Le = (cp[nc * n + 1] - cp[nc * n]) / nc;
-                for (int i = 0; i < nb; ++i) {
-                    const int64_t want = (int64_t)e[i] * nc + 1;
-                    int64_t lo = 0, hi = Le;
-                    while (lo < hi) {
-                        const int64_t mid = (lo + hi) >> 1;
-                        if (rv[c0 + nc * mid] < want) lo = mid + 1; else hi = mid;
+        auto fill_ranks = [&](auto* out, const int64_t miss, const int64_t limit) -> bool {
+            int over = 0;
+#pragma omp parallel for schedule(static) reduction(| : over)
+            for (int64_t k = 0; k < hs.n_cells; ++k) {
+                const int32_t* e = &hs.ents[k * nb];
+                int32_t srt[MAX_NB];  // local indices by entity (ties by index)
+                for (int i = 0; i < nb; ++i) srt[i] = i;
+                std::sort(srt, srt + nb, [&](int32_t a, int32_t b) { return e[a] < e[b] || (e[a] == e[b] && a < b); });
+                for (int j = 0; j < nb; ++j) {
+                    const int64_t n = e[j];
+                    const int64_t c0 = cp[nc * n] - 1;
+                    const int64_t Le = (cp[nc * n + 1] - cp[nc * n]) / nc;
+                    int64_t m = 0;
+                    for (int q = 0; q < nb; ++q) {
+                        const int i = srt[q];
+                        const int64_t want = (int64_t)e[i] * nc + 1;
+                        while (m < Le && rv[c0 + nc * m] < want) ++m;
+                        int64_t r = miss;
+                        if (m < Le && rv[c0 + nc * m] == want && m < 0xFFFF) r = m;
+                        if (r != miss && r >= limit) over = 1;
+                        out[((size_t)k * nb + j) * nb + i] = (typename std::remove_pointer<decltype(out)>::type)(r >= limit ? miss : r);
                     }
-                    uint16_t r = 0xFFFF;
-                    if (lo < Le && rv[c0 + nc * lo] == want && lo < 0xFFFF) r = (uint16_t)lo;
-                    r16[((size_t)k * nb + j) * nb + i] = r;
-                    if (r != 0xFFFF) maxr = std::max(maxr, (int)r);
                 }
             }
-        }
-        if (maxr < 255) {
-            hs.rank8.resize(r16.size());
-            for (size_t t = 0; t < r16.size(); ++t) hs.rank8[t] = r16[t] == 0xFFFF ? 255 : (uint8_t)r16[t];
+            return over == 0;
+        };
+        hs.rank8.resize((size_t)hs.n_cells * nb * nb);
+        if (fill_ranks(hs.rank8.data(), 255, 255)) {
             hs.wide_rank = false;
         } else {
-            hs.rank16.swap(r16);
+            std::vector<uint8_t>().swap(hs.rank8);
+            hs.rank16.resize((size_t)hs.n_cells * nb * nb);
+            fill_ranks(hs.rank16.data(), 0xFFFF, 0xFFFF);
             hs.wide_rank = true;
         }
     }
@@ -602,55 +610,49 @@ int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error&
     const double target = std::max(1.0, std::min({std::floor(opt.stage_cap / max_stage), std::floor(opt.red_cap / max_nnb),
                                                   std::floor(out_cap / max_out), (double)opt.ent_cap,
                                                   (double)MAX_TILE_ENTS}));
-    std::vector<int32_t> order(n_ent);
-    for (int64_t n = 0; n < n_ent; ++n) order[n] = (int32_t)n;
-    std::vector<int32_t> tile_of(n_ent), tile_local(n_ent);
-    std::vector<int32_t> eids;              // owned entities, tile after tile
-    std::vector<int64_t> tent = {0};        // tile t owns eids[tent[t] .. tent[t+1])
-    eids.reserve(n_ent);
+    // The entities with their positions, permuted together, so the selections and bounding
+    // boxes below read memory in order.
+    struct EntPos {
+        double p[3];
+        int32_t id;
+    };
+    std::vector<EntPos> ep(n_ent);
+#pragma omp parallel for schedule(static)
+    for (int64_t n = 0; n < n_ent; ++n) {
+        for (int x = 0; x < 3; ++x) ep[n].p[x] = pos[n * 3 + x];
+        ep[n].id = (int32_t)n;
+    }
     auto fits = [&](int64_t lo, int64_t hi) {
         if (hi - lo > opt.ent_cap || hi - lo > MAX_TILE_ENTS) return false;
         int64_t st = 0, rd = 0, ot = 0;
         for (int64_t q = lo; q < hi; ++q) {
-            st += stage_of(order[q]);
-            rd += nnb_of(order[q]);
-            ot += out_of(order[q]);
+            st += stage_of(ep[q].id);
+            rd += nnb_of(ep[q].id);
+            ot += out_of(ep[q].id);
         }
         return st <= opt.stage_cap && rd <= opt.red_cap && ot <= out_cap;
     };
-    auto emit = [&](int64_t lo, int64_t hi) {
-        std::sort(order.begin() + lo, order.begin() + hi);
-        const int32_t tid = (int32_t)(tent.size() - 1);
-        for (int64_t q = lo; q < hi; ++q) {
-            tile_of[order[q]] = tid;
-            tile_local[order[q]] = (int32_t)(q - lo);
-            eids.push_back(order[q]);
-        }
-        tent.push_back((int64_t)eids.size());
-    };
-    // explicit stack (depth ~ log2 of the tile count): (lo, hi, parts)
-    struct Part { int64_t lo, hi, k; };
-    std::vector<Part> stack;
-    // leaves average 88 % of the target: the layer-snapped cuts vary part sizes by up to 15 %
-    stack.push_back({0, n_ent, std::max<int64_t>(1, (int64_t)std::ceil((double)n_ent / (0.88 * target)))});
-    while (!stack.empty()) {
-        Part P = stack.back();
-        stack.pop_back();
-        const int64_t n = P.hi - P.lo;
-        if (n == 0) continue;
-        int64_t k = std::min(P.k, n);
+    // Recursive bisection of ep[lo, hi) into k parts. The parts are disjoint ranges, so the
+    // leaves in depth-first (left first) order are the leaves by ascending start; large parts
+    // are split in parallel and the leaves sorted afterwards.
+    std::vector<std::pair<int64_t, int64_t>> leaves;
+    std::function<void(int64_t, int64_t, int64_t)> split = [&](int64_t lo, int64_t hi, int64_t k) {
+        const int64_t n = hi - lo;
+        if (n == 0) return;
+        k = std::min(k, n);
         if (k == 1) {
-            if (fits(P.lo, P.hi) || n == 1) {
-                emit(P.lo, P.hi);
-                continue;
+            if (fits(lo, hi) || n == 1) {
+#pragma omp critical(fe_plan_leaves)
+                leaves.emplace_back(lo, hi);
+                return;
             }
             k = 2;
         }
         double lo_[3] = {1e300, 1e300, 1e300}, hi_[3] = {-1e300, -1e300, -1e300};
-        for (int64_t q = P.lo; q < P.hi; ++q)
+        for (int64_t q = lo; q < hi; ++q)
             for (int x = 0; x < dim; ++x) {
-                lo_[x] = std::min(lo_[x], pos[(int64_t)order[q] * 3 + x]);
-                hi_[x] = std::max(hi_[x], pos[(int64_t)order[q] * 3 + x]);
+                lo_[x] = std::min(lo_[x], ep[q].p[x]);
+                hi_[x] = std::max(hi_[x], ep[q].p[x]);
             }
         int ax = 0;
         for (int x = 1; x < dim; ++x)
@@ -660,35 +662,69 @@ int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error&
         // order along the axis (ties by the other coordinates, then id) and move the cut to the
         // nearest change of the axis coordinate within 15 %, so cuts follow element layers
         const int ax1 = (ax + 1) % dim, ax2 = (ax + 2) % dim;
-        auto less = [&](int32_t x, int32_t y) {
-            const double* px = &pos[(int64_t)x * 3];
-            const double* py = &pos[(int64_t)y * 3];
-            if (px[ax] != py[ax]) return px[ax] < py[ax];
-            if (px[ax1] != py[ax1]) return px[ax1] < py[ax1];
-            if (dim > 2 && px[ax2] != py[ax2]) return px[ax2] < py[ax2];
-            return x < y;
+        auto less = [&](const EntPos& x, const EntPos& y) {
+            if (x.p[ax] != y.p[ax]) return x.p[ax] < y.p[ax];
+            if (x.p[ax1] != y.p[ax1]) return x.p[ax1] < y.p[ax1];
+            if (dim > 2 && x.p[ax2] != y.p[ax2]) return x.p[ax2] < y.p[ax2];
+            return x.id < y.id;
         };
-        std::sort(order.begin() + P.lo, order.begin() + P.hi, less);
+        const int64_t slack = std::max<int64_t>(1, (int64_t)(0.15 * (double)nl));
+        // Only the ranks around the cut need their order: place ranks [w0, w1) sorted with every
+        // smaller rank before them and every larger one after (two selections and a short sort).
+        // `less` is a strict total order, so the parts hold the same entities as after a full
+        // sort, and each part is ordered again before it is split or emitted.
         {
-            const int64_t slack = std::max<int64_t>(1, (int64_t)(0.15 * (double)nl));
-            int64_t best = nl;
-            for (int64_t d = 0; d <= slack; ++d) {
-                bool hit = false;
-                for (const int64_t c : {nl - d, nl + d}) {
-                    if (c <= 0 || c >= n) continue;
-                    if (pos[(int64_t)order[P.lo + c - 1] * 3 + ax] != pos[(int64_t)order[P.lo + c] * 3 + ax]) {
-                        best = c;
-                        hit = true;
-                        break;
-                    }
-                }
-                if (hit) break;
-            }
-            nl = best;
+            const int64_t w0 = std::max<int64_t>(0, nl - slack - 1), w1 = std::min<int64_t>(n, nl + slack + 1);
+            auto b = ep.begin() + lo;
+            std::nth_element(b, b + w0, b + n, less);
+            if (w1 < n) std::nth_element(b + w0 + 1, b + w1, b + n, less);
+            std::sort(b + w0 + 1, b + w1, less);
         }
-        // right part first on the stack so the left part is emitted first (spatial order)
-        stack.push_back({P.lo + nl, P.hi, k - kl});
-        stack.push_back({P.lo, P.lo + nl, kl});
+        int64_t best = nl;
+        for (int64_t d = 0; d <= slack; ++d) {
+            bool hit = false;
+            for (const int64_t c : {nl - d, nl + d}) {
+                if (c <= 0 || c >= n) continue;
+                if (ep[lo + c - 1].p[ax] != ep[lo + c].p[ax]) {
+                    best = c;
+                    hit = true;
+                    break;
+                }
+            }
+            if (hit) break;
+        }
+        nl = best;
+        if (n >= (1 << 16)) {
+#pragma omp task default(shared) firstprivate(lo, nl, kl)
+            split(lo, lo + nl, kl);
+            split(lo + nl, hi, k - kl);
+#pragma omp taskwait
+        } else {
+            split(lo, lo + nl, kl);
+            split(lo + nl, hi, k - kl);
+        }
+    };
+    // leaves average 88 % of the target: the layer-snapped cuts vary part sizes by up to 15 %
+    const int64_t k0 = std::max<int64_t>(1, (int64_t)std::ceil((double)n_ent / (0.88 * target)));
+#pragma omp parallel
+#pragma omp single
+    split(0, n_ent, k0);
+    std::sort(leaves.begin(), leaves.end());
+    // tiles in leaf order; within a tile entities by id, so its nzval is a few contiguous ranges
+    const int64_t n_leaves = (int64_t)leaves.size();
+    std::vector<int32_t> tile_of(n_ent), tile_local(n_ent);
+    std::vector<int32_t> eids(n_ent);  // owned entities, tile after tile
+    std::vector<int64_t> tent(n_leaves + 1, 0);  // tile t owns eids[tent[t] .. tent[t+1])
+    for (int64_t t = 0; t < n_leaves; ++t) tent[t + 1] = leaves[t].second;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t t = 0; t < n_leaves; ++t) {
+        const int64_t lo = leaves[t].first, hi = leaves[t].second;
+        for (int64_t q = lo; q < hi; ++q) eids[q] = ep[q].id;
+        std::sort(eids.begin() + lo, eids.begin() + hi);
+        for (int64_t q = lo; q < hi; ++q) {
+            tile_of[eids[q]] = (int32_t)t;
+            tile_local[eids[q]] = (int32_t)(q - lo);
+        }
     }
     const int64_t n_tiles = (int64_t)tent.size() - 1;
     // (sub, cell, j) triples per tile, in (sub, cell, j) order
