@@ -114,7 +114,7 @@ class Info(ctypes.Structure):
                 ("flagged_cells", ctypes.c_int64), ("device_bytes", ctypes.c_int64),
                 ("create_seconds", ctypes.c_double), ("max_record_bytes", ctypes.c_int32),
                 ("max_tile_nodes", ctypes.c_int32), ("max_stage_values", ctypes.c_int32),
-                ("max_out_doubles", ctypes.c_int32), ("stage_cap", ctypes.c_int32), ("pad", ctypes.c_int32)]
+                ("max_out_doubles", ctypes.c_int32), ("stage_cap", ctypes.c_int32), ("plan_checksum", ctypes.c_uint32)]
 
 
 _lib = None

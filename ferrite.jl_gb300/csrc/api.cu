@@ -775,6 +775,28 @@ int fe_create(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain
     return FE_OK;
 }
 
+// digest of a plan: FNV-1a 64 of each tile record (in parallel), then of those in tile order
+static uint32_t plan_digest(const Plan& pl) {
+    constexpr uint64_t basis = 1469598103934665603ull, prime = 1099511628211ull;
+    std::vector<uint64_t> th((size_t)pl.n_tiles);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t t = 0; t < pl.n_tiles; ++t) {
+        uint64_t h = basis;
+        for (int64_t b = pl.rec_off[t]; b < pl.rec_off[t + 1]; ++b) {
+            h ^= pl.rec[(size_t)b];
+            h *= prime;
+        }
+        th[(size_t)t] = h;
+    }
+    uint64_t h = basis;
+    for (const uint64_t v : th)
+        for (int k = 0; k < 8; ++k) {
+            h ^= (v >> (8 * k)) & 0xFFu;
+            h *= prime;
+        }
+    return (uint32_t)(h ^ (h >> 32));
+}
+
 int fe_plan_dry_run(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain_desc* subdomains,
                     const fe_dof_desc* dofs, const fe_csc_desc* pattern, fe_info* out) {
     if (!out) return FE_ERR_ARG;
@@ -809,6 +831,7 @@ int fe_plan_dry_run(const fe_grid_desc* grid, int32_t n_subdomains, const fe_sub
     out->max_stage_values = pl.max_stage;
     out->max_out_doubles = pl.max_out;
     out->stage_cap = opt.stage_cap;
+    out->plan_checksum = plan_digest(pl);
     out->create_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return FE_OK;
 }

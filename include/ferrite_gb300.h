@@ -162,7 +162,9 @@ typedef struct {
     int32_t max_stage_values;   /* most staging values of one tile */
     int32_t max_out_doubles;    /* largest reduce output buffer of one tile */
     int32_t stage_cap;          /* staging capacity the plan was built with */
-    int32_t pad;
+    uint32_t plan_checksum;     /* fe_plan_dry_run: digest of the tile records (FNV-1a 64 of each record,
+                                   then of those in tile order, folded to 32 bits); equal plans, equal
+                                   digests, whatever the host thread count. 0 from fe_get_info */
 } fe_info;
 
 /*
