@@ -37,6 +37,7 @@ TRIANGLE, QUADRILATERAL, TETRAHEDRON, HEXAHEDRON, WEDGE = 1, 2, 3, 4, 5
 HEAT, LINEAR_ELASTIC, NEO_HOOKE = 1, 2, 3
 PREC_MIXED, PREC_FP64 = 0, 1
 FILLZERO, NO_K, NO_F, ASYNC, PROFILE, COMPENSATED, TWO_PHASE, FUSED, NO_TENSOR = 1, 2, 4, 8, 16, 32, 64, 128, 256
+STAGED_OUTPUT = 512
 _FORMS = {None: 0, "two_phase": TWO_PHASE, "fused": FUSED, "two_phase_cuda_cores": TWO_PHASE | NO_TENSOR}
 
 EXPORTED = ["fe_abi_version", "fe_create", "fe_assemble", "fe_sync", "fe_last_error", "fe_get_info",
@@ -380,9 +381,12 @@ class Handle:
 
     def assemble(self, nzval, f, physics: int, p0: float, p1: float, body=(0.0, 0.0, 0.0), cell_scale=None, u=None,
                  precision: int = PREC_MIXED, fillzero: bool = True, stream=None, sync: bool = True,
-                 cond_threshold: float = 0.0, profile: bool = False, compensated: bool = False, form=None):
+                 cond_threshold: float = 0.0, profile: bool = False, compensated: bool = False, form=None,
+                 staged_output: bool = False):
         """One fe_assemble call. ``stream`` is a torch.cuda.Stream, a raw handle or None.
         ``compensated`` (mixed precision): sum each entry as a compensated FP32 pair.
+        ``staged_output``: host outputs through a device buffer and the copy engine, also when
+        they are page-locked (default there: written by the kernels through the mapping).
         ``form``: None (the engine's choice), "two_phase" (element matrices first; on the tensor
         cores where a kernel exists), "two_phase_cuda_cores" or "fused"."""
         self._check_outputs(nzval, f)
@@ -400,6 +404,8 @@ class Handle:
             flags |= PROFILE
         if compensated:
             flags |= COMPENSATED
+        if staged_output:
+            flags |= STAGED_OUTPUT
         flags |= _FORMS[form]
         p.flags = flags
         p.p0, p.p1 = float(p0), float(p1)

@@ -930,9 +930,10 @@ static int assemble_common(fe_handle* h, const fe_assemble_params* p, double* nz
     cudaError_t e;
     KernelArgs A = h->base;
     // outputs: device pointers are written in place, page-locked host memory through its
-    // mapping (plain stores), other host memory is staged
-    double* nz_map = !eo && do_k && !h->capturing && !is_device_ptr(nzval) ? (double*)pinned_device_alias(nzval) : nullptr;
-    double* f_map = !eo && do_f && !h->capturing && !is_device_ptr(f) ? (double*)pinned_device_alias(f) : nullptr;
+    // mapping (plain stores) unless FE_STAGED_OUTPUT, other host memory is staged
+    const bool mapped_out = !eo && !h->capturing && !(p->flags & FE_STAGED_OUTPUT);
+    double* nz_map = mapped_out && do_k && !is_device_ptr(nzval) ? (double*)pinned_device_alias(nzval) : nullptr;
+    double* f_map = mapped_out && do_f && !is_device_ptr(f) ? (double*)pinned_device_alias(f) : nullptr;
     const bool nz_dev = eo || (do_k && (nz_map || is_device_ptr(nzval)));
     const bool f_dev = eo || (do_f && (f_map || is_device_ptr(f)));
     const bool fill = (p->flags & FE_FILLZERO) != 0;

@@ -78,6 +78,9 @@ extern "C" {
                               cell's geometry in every tile that owns one of its dofs. The default for
                               quadratic elements; results are bitwise those of the fused form */
 #define FE_FUSED 128u      /* element math inside the owner tiles (the default for linear elements) */
+#define FE_STAGED_OUTPUT 512u /* host nzval / f: assemble into a device buffer held by the handle and copy it back
+                                 with the copy engine, also for page-locked memory (which by default the kernels
+                                 write through its mapping); pageable memory is always staged */
 #define FE_NO_TENSOR 256u  /* two-phase form: element matrices on the CUDA cores even where a tensor-core
                               kernel exists (27-node hexahedra, elasticity, mixed precision); the CUDA-core
                               form gives the fused form's bits, the tensor-core form (split TF32 products,
