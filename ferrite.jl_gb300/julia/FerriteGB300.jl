@@ -14,6 +14,7 @@ const LIB = get(ENV, "FERRITE_GB300_LIB", joinpath(@__DIR__, "..", "lib", "libfe
 const FE_HEAT, FE_LINEAR_ELASTIC, FE_NEO_HOOKE = Int32(1), Int32(2), Int32(3)
 const FE_PREC_MIXED, FE_PREC_FP64 = Int32(0), Int32(1)
 const FE_FILLZERO = UInt32(1)
+const FE_STAGED_OUTPUT = UInt32(512)
 
 struct GridDesc
     dim::Int32
@@ -147,14 +148,17 @@ end
     assemble_csc!(K, f, h; physics, p0, p1, body, cell_scale, u, precision, fillzero)
 
 The whole `start_assemble(K, f)` + cell loop + `assemble!` in one call. K.nzval and f may be
-host arrays or device arrays (CuArray pointers).
+host arrays or device arrays (CuArray pointers). `staged_output=true`: host arrays go through
+a device buffer and the copy engine even when page-locked.
 """
 function assemble_csc!(K::SparseMatrixCSC{Float64,Int}, f::Vector{Float64}, h::Handle;
                        physics=FE_LINEAR_ELASTIC, p0=1.0, p1=0.3, body=(0.0, 0.0, 0.0),
-                       cell_scale=nothing, u=nothing, precision=FE_PREC_MIXED, fillzero=true)
+                       cell_scale=nothing, u=nothing, precision=FE_PREC_MIXED, fillzero=true,
+                       staged_output=false)
     cs = cell_scale === nothing ? Ptr{Float64}(C_NULL) : pointer(cell_scale)
     up = u === nothing ? Ptr{Float64}(C_NULL) : pointer(u)
-    par = Ref(AssembleParams(physics, precision, fillzero ? FE_FILLZERO : UInt32(0), p0, p1,
+    flags = (fillzero ? FE_FILLZERO : UInt32(0)) | (staged_output ? FE_STAGED_OUTPUT : UInt32(0))
+    par = Ref(AssembleParams(physics, precision, flags, p0, p1,
                              Tuple(Float64.(body)), cs, up, 0.0, C_NULL))
     rc = GC.@preserve K f cell_scale u ccall((:fe_assemble, LIB), Cint,
         (Ptr{Cvoid}, Ptr{AssembleParams}, Ptr{Float64}, Ptr{Float64}), h.ptr, par, K.nzval, f)
