@@ -334,8 +334,21 @@ class Handle:
         subs = (SubdomainDesc * len(subdomains))(*[s.desc() for s in subdomains])
         cd, co = _as_i64(cell_dofs), _as_i64(cell_dofs_offset)
         dd = DofDesc(int(ndofs), cd.ctypes.data_as(i64p), co.ctypes.data_as(i64p))
-        cp, rv = _as_i64(colptr), _as_i64(rowval)
-        pd = CscDesc(int(ndofs), int(len(rv)), cp.ctypes.data_as(i64p), rv.ctypes.data_as(i64p))
+        if getattr(colptr, "is_cuda", False) or getattr(rowval, "is_cuda", False):
+            # a device pattern (allocate_matrix(device=True)): fe_create copies it to the host
+            for x, name, n in ((colptr, "colptr", int(ndofs) + 1), (rowval, "rowval", 0)):
+                if not getattr(x, "is_cuda", False):
+                    raise TypeError("colptr and rowval must both be CUDA tensors or both host arrays")
+                _check(x, name, "int64", n)
+                if not x.is_contiguous():
+                    raise ValueError(f"{name} must be contiguous")
+            cp, rv = colptr, rowval
+            nnz = int(rowval.numel())
+            pd = CscDesc(int(ndofs), nnz, ctypes.cast(colptr.data_ptr(), i64p), ctypes.cast(rowval.data_ptr(), i64p))
+        else:
+            cp, rv = _as_i64(colptr), _as_i64(rowval)
+            nnz = int(len(rv))
+            pd = CscDesc(int(ndofs), nnz, cp.ctypes.data_as(i64p), rv.ctypes.data_as(i64p))
         h = ctypes.c_void_p()
         rc = L.fe_create(ctypes.byref(g), len(subdomains), subs, ctypes.byref(dd), ctypes.byref(pd), ctypes.byref(h))
         if rc != FE_OK:
@@ -344,7 +357,7 @@ class Handle:
             raise FEError(rc, info)
         self._h = h
         self.ndofs = int(ndofs)
-        self.nnz = int(len(rv))
+        self.nnz = nnz
         self.n_cells = int(n_cells)
         self.n_nodes, self.dim = int(nodes.shape[0]), int(nodes.shape[1])
         self.ndofs_per_cell = {}

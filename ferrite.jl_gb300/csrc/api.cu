@@ -640,6 +640,27 @@ int fe_create(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain
     if (!out) return FE_ERR_ARG;
     *out = nullptr;
     const auto t0 = std::chrono::steady_clock::now();
+    // A device-resident pattern (fe_sparsity_pattern_device, or a CuSparseMatrixCSC's colPtr /
+    // rowVal) is read on the host, like a host one: copy it first.
+    std::vector<int64_t> cp_host, rv_host;
+    fe_csc_desc pattern_host{};
+    if (pattern && pattern->n > 0 && pattern->nnz >= 0 && pattern->colptr && pattern->rowval &&
+        (is_device_ptr(pattern->colptr) || is_device_ptr(pattern->rowval))) {
+        cp_host.resize((size_t)pattern->n + 1);
+        rv_host.resize((size_t)pattern->nnz);
+        cudaError_t ce = cudaMemcpy(cp_host.data(), pattern->colptr, cp_host.size() * 8, cudaMemcpyDefault);
+        if (ce == cudaSuccess && pattern->nnz > 0)
+            ce = cudaMemcpy(rv_host.data(), pattern->rowval, rv_host.size() * 8, cudaMemcpyDefault);
+        if (ce != cudaSuccess) {
+            g_create_error = fe_error_info{};
+            g_create_error.code = FE_ERR_CUDA;
+            std::snprintf(g_create_error.message, sizeof(g_create_error.message), "copy of the device pattern: %s",
+                          cudaGetErrorString(ce));
+            return FE_ERR_CUDA;
+        }
+        pattern_host = fe_csc_desc{pattern->n, pattern->nnz, cp_host.data(), rv_host.data()};
+        pattern = &pattern_host;
+    }
     fe_handle* h = new (std::nothrow) fe_handle();
     if (!h) return FE_ERR_OOM;
     Error err;

@@ -121,7 +121,10 @@ typedef struct {
     int64_t n;             /* number of columns (= ndofs) */
     int64_t nnz;
     const int64_t* colptr; /* [n+1] 1-based (K.colptr) */
-    const int64_t* rowval; /* [nnz] 1-based (K.rowval); read during fe_create only */
+    const int64_t* rowval; /* [nnz] 1-based (K.rowval); read during fe_create only. Host or DEVICE
+                              memory for fe_create (a device pattern from fe_sparsity_pattern_device or a
+                              CuSparseMatrixCSC's colPtr / rowVal is copied to the host first); host
+                              memory for fe_plan_dry_run */
 } fe_csc_desc;
 /* A SparseMatrixCSR{1} (ext/FerriteSparseMatrixCSR.jl:9-160) goes in as (K.rowptr, K.colval)
  * in place of (colptr, rowval), with its nzval as the output. Ferrite's pattern (cell
