@@ -249,7 +249,34 @@ def _facet_points(cell_type: int, order: int):
         maps = [lambda a, b: (1 - a - b, b, 0.0), lambda a, b: (b, 0.0, 1 - a - b), lambda a, b: (a, b, 1 - a - b),
                 lambda a, b: (0.0, 1 - a - b, b)]
         return [(w, np.array([m(a, b) for a, b in q])) for m in maps]
+    if cell_type == WEDGE:
+        # triangle facets 1 and 5 take the triangle rule; quadrilateral facets 2-4 the Gauss rule
+        # on (-1, 1)^2 mapped to (0, 1)^2, a quarter of the area, so a quarter of the weights
+        # (src/Quadrature/quadrature.jl:240-249)
+        wt, qt = quadrature_rule(TRIANGLE, order)
+        wq, qq = quadrature_rule(QUADRILATERAL, order)
+        tri = {1: lambda x, y: (1 - x - y, y, 0.0), 5: lambda x, y: (y, 1 - x - y, 1.0)}
+        quad = {2: lambda x, y: ((1 + x) / 2, 0.0, (1 + y) / 2), 3: lambda x, y: (0.0, 1 - (1 + x) / 2, (1 + y) / 2),
+                4: lambda x, y: (1 - (1 + x) / 2, (1 + x) / 2, (1 + y) / 2)}
+        rules = []
+        for fct in range(1, 6):
+            if fct in tri:
+                rules.append((np.asarray(wt, float), np.array([tri[fct](a, b) for a, b in qt])))
+            else:
+                rules.append((np.asarray(wq, float) / 4, np.array([quad[fct](a, b) for a, b in qq])))
+        return _pad_rules(rules)
     raise ValueError(f"no facet rule for cell type {cell_type}")
+
+
+def _pad_rules(rules):
+    """Rules of different lengths padded to the longest with zero weights (the last point
+    repeated), as fe_facet_set_create takes them."""
+    nq = max(len(w) for w, _ in rules)
+    out = []
+    for w, p in rules:
+        k = nq - len(w)
+        out.append((np.concatenate([w, np.zeros(k)]), np.concatenate([p, np.repeat(p[-1:], k, axis=0)])))
+    return out
 
 
 def facet_values(cell_type: int, ip_order: int, qr_order: int):

@@ -74,6 +74,7 @@ FACET_NODES = {
     1: ((1, 2), (2, 3), (3, 1)),                                                            # triangle
     4: ((1, 4, 3, 2), (1, 2, 6, 5), (2, 3, 7, 6), (3, 4, 8, 7), (1, 5, 8, 4), (5, 6, 7, 8)),  # hexahedron
     3: ((1, 3, 2), (1, 2, 4), (2, 3, 4), (1, 4, 3)),                                        # tetrahedron
+    5: ((1, 3, 2), (1, 2, 5, 4), (3, 1, 4, 6), (2, 3, 6, 5), (4, 5, 6)),                    # wedge
 }
 
 

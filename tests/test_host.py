@@ -104,3 +104,35 @@ def test_buffer_checks(fg, oracle):
     fg._check(torch.zeros(n * m * m, dtype=torch.float32), "ke", fg._elem_dtype(fg.PREC_MIXED), n * m * m)
     with pytest.raises(TypeError):
         fg._check(torch.zeros(n * m * m, dtype=torch.float32), "ke", fg._elem_dtype(fg.PREC_FP64), n * m * m)
+
+
+@pytest.mark.parametrize("qo", [1, 2])
+def test_wedge_facet_values_integrate_loads(host, oracle, qo):
+    """Wedge (RefPrism) facet tables: triangle facets (1, 5) with the triangle rule, quadrilateral
+    facets (2-4) with a quarter of the Gauss weights, padded to one length. Through the oracle's
+    facet loads they integrate pressure and traction exactly over the box's x, y and z faces,
+    so every facet's normal, orientation and dGamma scale is Ferrite's."""
+    import numpy as np
+    from helpers import boundary_facets
+    O = oracle
+    tables = host.facet_values(host.WEDGE, 1, qo)
+    nf, nq, W, N, dM = tables
+    assert nf == 5 and np.allclose(W.sum(axis=1), [0.5, 1.0, 1.0, 1.0, 0.5])
+    p = O.box_problem(O.WEDGE, (3, 2, 2), [0.0, 0.0, 0.0], [2.0, 1.0, 3.0], ip_order=1, ncomp=3, qr_order=2,
+                      perturb=0.2, seed=9)
+    t = np.array([0.5, -0.25, 1.0])
+    seen = set()
+    for on_face, normal, area, kinds in (
+            (lambda X: abs(X[0]) < 1e-12, (-1, 0, 0), 3.0, {2, 3, 4}),
+            (lambda X: abs(X[0] - 2.0) < 1e-12, (1, 0, 0), 3.0, {2, 3, 4}),
+            (lambda X: abs(X[1]) < 1e-12, (0, -1, 0), 6.0, {2, 3, 4}),
+            (lambda X: abs(X[1] - 1.0) < 1e-12, (0, 1, 0), 6.0, {2, 3, 4}),
+            (lambda X: abs(X[2]) < 1e-12, (0, 0, -1), 2.0, {1}),
+            (lambda X: abs(X[2] - 3.0) < 1e-12, (0, 0, 1), 2.0, {5})):
+        cells, facets = boundary_facets(p, O.WEDGE, on_face)
+        assert len(cells) > 0 and set(facets.tolist()) <= kinds
+        seen |= set(facets.tolist())
+        f = p.facet_load(cells, facets, tables, pressure=1.5, traction=tuple(t))
+        sums = np.array([f[a::3].sum() for a in range(3)])
+        assert np.allclose(sums, 1.5 * area * np.array(normal) + t * area, rtol=1e-13, atol=1e-13), (normal, sums)
+    assert seen == {1, 2, 3, 4, 5}
