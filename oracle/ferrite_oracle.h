@@ -19,6 +19,9 @@
  *                        docs/src/literate-tutorials/hyperelasticity.jl:157-276,
  *                        docs/src/literate-gallery/topology_optimization.jl:347-383
  *   CSC assembler        src/assembler.jl:287-291, 322-457, 513-576; src/arrayutils.jl:100-152
+ *   CSR assembler        ext/FerriteSparseMatrixCSR.jl:9-96
+ *   element product      y = sum_c A_c^T Ke_c A_c u over the element matrices of
+ *                        docs/src/literate-howto/gpu_assembly.jl:265-303 (no reference code)
  *   greedy coloring      src/Grid/coloring.jl:47-143
  *   Dirichlet apply!     src/Dofs/ConstraintHandler.jl:711-767, 931-955
  *   facet loads          src/FEValues/FacetValues.jl:129-155, facet_integrals.jl:85-273,
