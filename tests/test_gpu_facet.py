@@ -33,7 +33,7 @@ def shaken(O, ct, nel, ip, nc, qo, seed):
     return prob, base
 
 
-@pytest.mark.parametrize("case", ["hex_q1", "hex_q2", "tet", "quad_heat", "tri_heat", "wedge"])
+@pytest.mark.parametrize("case", ["hex_q1", "hex_q2", "tet", "quad_heat", "tri_heat"])
 def test_facet_loads_against_oracle(built, oracle, torch_cuda, case):
     torch = torch_cuda
     fg, O = built, oracle
@@ -45,23 +45,15 @@ def test_facet_loads_against_oracle(built, oracle, torch_cuda, case):
         ct, nel, ip, nc, qo, fq = O.TETRAHEDRON, (3, 2, 2), 1, 3, 1, 2
     elif case == "quad_heat":
         ct, nel, ip, nc, qo, fq = O.QUADRILATERAL, (6, 5), 1, 1, 2, 3
-    elif case == "tri_heat":
-        ct, nel, ip, nc, qo, fq = O.TRIANGLE, (5, 4), 1, 1, 2, 2
     else:
-        ct, nel, ip, nc, qo, fq = O.WEDGE, (3, 3, 2), 1, 3, 2, 2
+        ct, nel, ip, nc, qo, fq = O.TRIANGLE, (5, 4), 1, 1, 2, 2
     prob, base = shaken(O, ct, nel, ip, nc, qo, seed=70 + len(case))
-    # two sides of the box, selected on the unperturbed nodes (the wedge also its top:
-    # triangle facets besides the quadrilateral ones, rules padded to one length)
+    # two sides of the box, selected on the unperturbed nodes
     sel = [boundary_facets(prob, ct, lambda X: abs(X[0] - 1.0) < 1e-12, base),
            boundary_facets(prob, ct, lambda X: abs(X[1]) < 1e-12, base)]
-    if ct == O.WEDGE:
-        sel.append(boundary_facets(prob, ct, lambda X: abs(X[2] - 1.0) < 1e-12, base))
     cells = np.concatenate([c for c, _ in sel])
     facets = np.concatenate([f for _, f in sel])
-    if ct == O.WEDGE:
-        tabs = __import__("ferrite_gb300.host", fromlist=["host"]).facet_values(ct, ip, fq)
-    else:
-        tabs = facet_tables(O, ct, ip, fq)
+    tabs = facet_tables(O, ct, ip, fq)
     h = make_handle(fg, O, prob)
     fs = h.facet_set(cells, facets, tabs)
     t = (0.3, -1.2, 0.7)

@@ -348,14 +348,6 @@ def test_pinned_host_outputs_written_directly(built, oracle, torch_cuda):
     h.sync()
     h.assemble(nz_d, f_d, **kw)
     assert torch.equal(nz_p, nz_d.cpu())
-    # FE_STAGED_OUTPUT: the same page-locked buffers through a device buffer and the copy engine
-    nz_p.fill_(float("nan"))
-    f_p.fill_(float("nan"))
-    h.assemble(nz_p, f_p, staged_output=True, **kw)
-    assert torch.equal(nz_p, nz_d.cpu()) and torch.equal(f_p, f_d.cpu())
-    h.assemble(nz_p, f_p, fillzero=False, staged_output=True, **kw)
-    h.assemble(nz_d, f_d, fillzero=False, **kw)
-    assert torch.equal(nz_p, nz_d.cpu()) and torch.equal(f_p, f_d.cpu())
 
 
 @pytest.mark.parametrize("nel,scale", [((3, 3, 2), False), ((4, 3, 3), True), ((5, 4, 4), True)])
