@@ -11,5 +11,8 @@ void register_elastic(std::vector<KernelEntry>& out, std::vector<ElemEntry>& eou
     FE_ONE(KIND_TET4, 4, PHYS_ELASTIC)
     FE_ONE(KIND_WEDGE6, 5, PHYS_ELASTIC)
     FE_ONE(KIND_QUAD4, 4, PHYS_ELASTIC)
+    // P1 triangles, ip^2, 1 or 3 points (docs/src/literate-tutorials/linear_elasticity.jl)
+    FE_ONE(KIND_TRI3, 1, PHYS_ELASTIC)
+    FE_ONE(KIND_TRI3, 3, PHYS_ELASTIC)
 }
 }  // namespace fe
