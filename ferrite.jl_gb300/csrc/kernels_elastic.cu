@@ -14,5 +14,7 @@ void register_elastic(std::vector<KernelEntry>& out, std::vector<ElemEntry>& eou
     // P1 triangles, ip^2, 1 or 3 points (docs/src/literate-tutorials/linear_elasticity.jl)
     FE_ONE(KIND_TRI3, 1, PHYS_ELASTIC)
     FE_ONE(KIND_TRI3, 3, PHYS_ELASTIC)
+    // Q2 quadrilaterals, ip^2, 3x3 Gauss (fused form: 9 base functions)
+    FE_ONE(KIND_QUAD9, 9, PHYS_ELASTIC)
 }
 }  // namespace fe

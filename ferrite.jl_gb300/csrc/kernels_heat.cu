@@ -11,6 +11,8 @@ void register_heat(std::vector<KernelEntry>& out, std::vector<ElemEntry>& eout) 
     FE_ONE(KIND_HEX8, 8, PHYS_HEAT)
     FE_ONE(KIND_TET4, 1, PHYS_HEAT)
     FE_ONE(KIND_TET4, 4, PHYS_HEAT)
+    FE_ONE(KIND_WEDGE6, 1, PHYS_HEAT)
+    FE_ONE(KIND_WEDGE6, 5, PHYS_HEAT)
     FE_ONE(KIND_HEX27, 27, PHYS_HEAT)
     FE_EA(KIND_HEX27, 27, PHYS_HEAT)
     FE_EA(KIND_QUAD9, 9, PHYS_HEAT)
