@@ -872,7 +872,18 @@ int check_plan(const HostProblem& hp, const Plan& pl, Error& err) {
         // pass that one range maps to that entry's nzval index, and every range position is written once
         {
             std::vector<std::vector<int32_t>> writes(H.n_pass);
-            for (int32_t p = 0; p < H.n_pass; ++p) writes[p].assign(PS[p].out_len, 0);
+            // per pass and buffer position: how many ranges cover it, and the last one that does
+            std::vector<std::vector<int32_t>> cover(H.n_pass), owner(H.n_pass);
+            for (int32_t p = 0; p < H.n_pass; ++p) {
+                writes[p].assign(PS[p].out_len, 0);
+                cover[p].assign(PS[p].out_len, 0);
+                owner[p].assign(PS[p].out_len, -1);
+                for (int32_t g = PS[p].rng_begin; g < PS[p].rng_end; ++g)
+                    for (int32_t i = RG[g].buf_off; i < RG[g].buf_off + RG[g].len; ++i) {
+                        ++cover[p][i];
+                        owner[p][i] = g;
+                    }
+            }
             for (int32_t q = 0; q < H.n_red && !bad; ++q) {
                 const int32_t e = (int32_t)(RED[q] >> RED_RANK_BITS), r = (int32_t)(RED[q] & ((1u << RED_RANK_BITS) - 1));
                 const int32_t p = blk_pass[q];
@@ -883,13 +894,9 @@ int check_plan(const HostProblem& hp, const Plan& pl, Error& err) {
                         const int64_t i = (int64_t)E[e].out_off + (int64_t)b * E[e].L + (int64_t)nc * r + x;
                         if (E[e].out_off < 0 || i >= P.out_len) { bad = 1; break; }
                         const int64_t want = E[e].colbase + (int64_t)b * E[e].L + (int64_t)nc * r + x;
-                        int hits = 0;
-                        for (int32_t g = P.rng_begin; g < P.rng_end; ++g)
-                            if (i >= RG[g].buf_off && i < RG[g].buf_off + RG[g].len) {
-                                ++hits;
-                                if (RG[g].nz0 + (i - RG[g].buf_off) != want) bad = 1;
-                            }
-                        if (hits != 1) bad = 1;
+                        // exactly one range covers i, and it maps i to this entry's nzval index
+                        const int32_t g = owner[p][i];
+                        if (cover[p][i] != 1 || RG[g].nz0 + (i - RG[g].buf_off) != want) bad = 1;
                         writes[p][i]++;
                     }
             }
