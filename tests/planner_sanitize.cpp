@@ -3,6 +3,7 @@
 // library's own host set-up (fe_distribute_dofs, fe_sparsity_pattern), then validation, the
 // owner-tile plan and the record check (build_problem, build_plan, check_plan).
 #include <cstdio>
+#include <cstring>
 #include <vector>
 #include <cmath>
 #include "plan.h"
@@ -65,5 +66,29 @@ int main(int argc, char** argv) {
     if (!rc) rc = check_plan(hp, pl, err);
     printf("n=%d nc=%d cells=%lld ndofs=%lld nnz=%lld rc=%d tiles=%lld msg=%s\n", n, nc, (long long)c, (long long)ndofs,
            (long long)nnz, rc, (long long)pl.n_tiles, err.msg.c_str());
-    return rc;
+    if (rc) return rc;
+    // the record check rejects a corrupted record: a range's nzval start, a node id, the size
+    int rejected = 0;
+    for (int kind = 0; kind < 3; ++kind) {
+        Plan bad = pl;
+        uint8_t* B = bad.rec.data() + bad.rec_off[pl.n_tiles / 2];
+        RecHead H;
+        std::memcpy(&H, B, sizeof H);
+        if (kind == 0 && H.n_rng > 0) {
+            RecRng R;
+            std::memcpy(&R, B + H.off_rng, sizeof R);
+            R.nz0 += 2;  // keeps the parity of buf_off - nz0, so only the mapping check can see it
+            std::memcpy(B + H.off_rng, &R, sizeof R);
+        } else if (kind == 1 && H.n_nodes > 0) {
+            const int32_t v = (int32_t)hp.n_nodes;
+            std::memcpy(B + H.off_nodes, &v, sizeof v);
+        } else if (kind == 2) {
+            H.bytes += 16;
+            std::memcpy(B, &H, sizeof H);
+        }
+        Error e2;
+        if (check_plan(hp, bad, e2) != 0) ++rejected;
+    }
+    printf("corrupted records rejected: %d of 3\n", rejected);
+    return rejected == 3 ? 0 : 3;
 }

@@ -1,6 +1,7 @@
 """The host planner (validation, ranks, bisection with OpenMP tasks, records, record check)
 built with AddressSanitizer and UndefinedBehaviorSanitizer and run on grids up to 85k
-entities, so the parallel bisection path runs too. No GPU needed."""
+entities, so the parallel bisection path runs too; the record check must also reject three
+kinds of corrupted record. No GPU needed."""
 import os
 import shutil
 import subprocess
@@ -31,3 +32,4 @@ def test_planner_clean_under_sanitizers(tmp_path):
         p = subprocess.run([exe] + args, capture_output=True, text=True, timeout=900, env=env)
         assert p.returncode == 0, (args, p.stdout[-500:], p.stderr[-3000:])
         assert "rc=0" in p.stdout and "ERROR" not in p.stderr and "runtime error" not in p.stderr, (args, p.stderr[-3000:])
+        assert "corrupted records rejected: 3 of 3" in p.stdout, p.stdout[-500:]
