@@ -139,19 +139,39 @@ def test_hyperelasticity_golden(oracle):
 
 
 @pytest.mark.parametrize("ct,orders,vol", [(2, [1, 2, 3, 4], 4.0), (4, [1, 2, 3, 4], 8.0),
-                                           (3, [1, 2, 3], 1 / 6), (5, [1, 2], 0.5)])
+                                           (3, [1, 2, 3], 1 / 6), (5, [1, 2], 0.5), (1, [1, 2], 0.5)])
 def test_quadrature_exactness(oracle, ct, orders, vol):
+    """Gauss rules on (-1, 1)^d integrate degree 2n-1 per coordinate exactly; the simplex and
+    prism rules of order n integrate every monomial of total degree <= n exactly, against the
+    closed forms a! b! / (a+b+2)! (triangle), a! b! c! / (a+b+c+3)! (tetrahedron) and
+    a! b! / (a+b+2)! / (c+1) (prism = triangle x (0, 1))."""
+    from math import factorial
     O = oracle
     for order in orders:
         w, pts = O.quadrature(ct, order)
         assert w.sum() == pytest.approx(vol, abs=1e-14)
+        d = pts.shape[1]
         if ct in (O.QUADRILATERAL, O.HEXAHEDRON):
             deg = 2 * order - 1
-            d = pts.shape[1]
             for exps in itertools.product(range(deg + 1), repeat=d):
                 exact = np.prod([(1 - (-1) ** (e + 1)) / (e + 1) for e in exps])
                 num = np.sum(w * np.prod(pts ** np.array(exps), axis=1))
                 assert num == pytest.approx(exact, abs=1e-13)
+            continue
+        for exps in itertools.product(range(order + 1), repeat=d):
+            if sum(exps) > order:
+                continue
+            if ct == O.TRIANGLE:
+                a, b = exps
+                exact = factorial(a) * factorial(b) / factorial(a + b + 2)
+            elif ct == O.TETRAHEDRON:
+                a, b, c = exps
+                exact = factorial(a) * factorial(b) * factorial(c) / factorial(a + b + c + 3)
+            else:
+                a, b, c = exps
+                exact = factorial(a) * factorial(b) / factorial(a + b + 2) / (c + 1)
+            num = np.sum(w * np.prod(pts ** np.array(exps), axis=1))
+            assert num == pytest.approx(exact, abs=1e-14), (ct, order, exps)
 
 
 @pytest.mark.parametrize("ct,nel,ip,nc", [(2, (3, 4), 1, 1), (4, (3, 2, 2), 1, 3), (4, (2, 2, 2), 2, 3),
