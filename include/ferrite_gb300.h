@@ -78,13 +78,13 @@ extern "C" {
                               cell's geometry in every tile that owns one of its dofs. The default for
                               quadratic elements; results are bitwise those of the fused form */
 #define FE_FUSED 128u      /* element math inside the owner tiles (the default for linear elements) */
-#define FE_STAGED_OUTPUT 512u /* host nzval / f: assemble into a device buffer held by the handle and copy it back
-                                 with the copy engine, also for page-locked memory (which by default the kernels
-                                 write through its mapping); pageable memory is always staged */
 #define FE_NO_TENSOR 256u  /* two-phase form: element matrices on the CUDA cores even where a tensor-core
                               kernel exists (27-node hexahedra, elasticity, mixed precision); the CUDA-core
                               form gives the fused form's bits, the tensor-core form (split TF32 products,
                               FP32 accumulation) differs from them by FP32 rounding */
+#define FE_STAGED_OUTPUT 512u /* host nzval / f: assemble into a device buffer held by the handle and copy it back
+                                 with the copy engine, also for page-locked memory (which by default the kernels
+                                 write through its mapping); pageable memory is always staged */
 
 typedef struct fe_handle fe_handle;
 
@@ -225,7 +225,9 @@ int fe_assemble_elements(fe_handle* h, const fe_assemble_params* params, void* k
  * `stream`: per cell ye_I = sum_J Ke(I, J) u_J as fused multiply-adds in the element precision
  * (J ascending; u rounded to float for FE_PREC_MIXED), then y[dof_I] += (double) ye_I in FP64
  * in cell order; flags FE_FILLZERO sets y = 0 first. Deterministic, no atomics: bitwise the
- * serial loop over cells. The caller keeps ke covering every cell the strides address.
+ * serial loop over cells. fe_element_matvec only launches kernels (no host work, no
+ * allocation), so a Krylov loop can capture it in a CUDA graph. The caller keeps ke covering
+ * every cell the strides address.
  * Destroy the operator before its handle.
  */
 typedef struct fe_element_operator fe_element_operator;
