@@ -13,7 +13,8 @@ def host(fg):
 
 
 CASES = [(2, (7, 5), 1, 1), (2, (4, 3), 2, 1), (1, (5, 4), 1, 1), (4, (5, 4, 3), 1, 3), (4, (3, 3, 2), 2, 3),
-         (3, (3, 2, 2), 1, 3), (5, (3, 3, 2), 1, 3), (4, (4, 4, 4), 1, 1)]
+         (3, (3, 2, 2), 1, 3), (5, (3, 3, 2), 1, 3), (4, (4, 4, 4), 1, 1),
+         (1, (4, 3), 1, 2), (2, (3, 3), 2, 2), (5, (3, 2, 2), 1, 1)]
 
 
 @pytest.mark.parametrize("ct,nel,ip,nc", CASES)
