@@ -13,7 +13,8 @@ def dry(fg, O, prob):
 
 @pytest.mark.parametrize("ct,nel,ip,nc,qo", [(2, (13, 9), 1, 1, 2), (2, (6, 5), 1, 2, 2), (4, (7, 6, 5), 1, 3, 2),
                                              (4, (4, 3, 3), 2, 3, 3), (3, (4, 4, 3), 1, 3, 1), (5, (4, 3, 3), 1, 3, 2),
-                                             (1, (5, 4), 1, 1, 1)])
+                                             (1, (5, 4), 1, 1, 1), (1, (6, 5), 1, 2, 1), (2, (4, 3), 2, 2, 3),
+                                             (5, (4, 3, 3), 1, 1, 2)])
 def test_dry_run_plans(fg, oracle, ct, nel, ip, nc, qo):
     fg.build()
     O = oracle
