@@ -1885,9 +1885,14 @@ constexpr int NOALLOC_MAX_DEVICES = 64;
 std::mutex g_noalloc_mutex;
 float* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
 
-// Device address of g_noalloc_scratch on the current device (resolved once per device).
+// Device address of g_noalloc_scratch on `device`, which must be the current device (the
+// symbol resolves on whichever device is current); looked up once per device.
 cudaError_t noalloc_scratch(int device, float** out) {
     if (device < 0 || device >= NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
+    int cur = -1;
+    const cudaError_t ce = cudaGetDevice(&cur);
+    if (ce != cudaSuccess) return ce;
+    if (cur != device) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
     if (!g_noalloc_ptr[device]) {
         float* ptr = nullptr;
@@ -1946,11 +1951,24 @@ extern "C" int fe_assemble_noalloc(fe_handle* h, const fe_assemble_params* p, do
                       (long long)need, (long long)NOALLOC_SCRATCH_FLOATS);
         return set_error(h, FE_ERR_ARG, buf);
     }
-    if (h->pending) fe_sync(h);
+    if (h->capturing) return set_error(h, FE_ERR_STATE, "fe_assemble_noalloc: fe_graph_capture is open on this handle");
+    cudaStream_t st = (cudaStream_t)p->stream;
+    if (!(p->flags & FE_ASYNC)) {
+        // a synchronous call ends by waiting for its stream, which a capturing stream refuses
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone)
+            return set_error(h, FE_ERR_STATE, "fe_assemble_noalloc: the stream is capturing; a synchronous call would wait on it");
+    }
+    if (h->pending) {
+        // an earlier FE_ASYNC assembly's error is reported here, before this call replaces it
+        const int rc = fe_sync(h);
+        if (rc != FE_OK) return rc;
+    }
     const KernelEntry* ke = find_kernel(hp, phys, fp64);
     if (!ke) return set_error(h, FE_ERR_UNSUPPORTED, "no kernel compiled for this element / quadrature / physics combination");
-    cudaStream_t st = (cudaStream_t)p->stream;
     cudaError_t e;
+    // the scratch address and every launch below belong to the handle's device
+    if ((e = cudaSetDevice(h->device)) != cudaSuccess) return cuda_fail(h, e, "cudaSetDevice");
     float* scratch = nullptr;
     if ((e = noalloc_scratch(h->device, &scratch)) != cudaSuccess) return cuda_fail(h, e, "cudaGetSymbolAddress");
     KernelArgs A = h->base;

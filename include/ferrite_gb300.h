@@ -344,10 +344,14 @@ int fe_kernel_time(fe_handle* h, double* total_ms, int64_t* launches);
  * copies of u and of cell_scale that mixed precision uses live in one static device array of
  * 4,194,304 floats (16 MiB) that every GPU loading this library holds until exit. Problems
  * needing more (ndofs for FE_NEO_HOOKE plus n_cells when cell_scale is given) are rejected
- * with FE_ERR_ARG. The first call on a device looks up that array's address
- * (cudaGetSymbolAddress); make that first call before any stream capture. All calls share the
- * array, which keeps the last call's values: calls that overlap on the GPU (other streams,
- * other handles) race on it. FE_PROFILE is not supported here.
+ * with FE_ERR_ARG. The call makes the handle's device current (cudaSetDevice); the first call
+ * on a device looks up that array's address there (cudaGetSymbolAddress), so make that first
+ * call before any stream capture. All calls share the array, which keeps the last call's
+ * values (each call overwrites what it reads): calls that overlap on the GPU (other streams,
+ * other handles) race on it. Without FE_ASYNC the call waits for its stream, so it returns
+ * FE_ERR_STATE on a stream that is capturing; with FE_ASYNC its status is read at the next
+ * fe_sync. An earlier FE_ASYNC assembly on the handle that failed returns its error here
+ * before anything is launched. FE_PROFILE is not supported here.
  */
 int fe_assemble_noalloc(fe_handle* h, const fe_assemble_params* params, double* nzval, double* f);
 
