@@ -37,7 +37,13 @@ SEED = 20261203
 E_MOD, NU, BODY = 200e3, 0.3, (0.0, 0.0, -1.0)
 METRIC = "K+f assembly Melem/s (3D Q1 hex elasticity, mixed FP32/FP64-accumulate)"
 WORKLOAD = "hex128_q1_elasticity"
+# accumulation of the timed mixed-precision form: "compensated" (TwoSum FP32 pairs per entry,
+# FP64-class, rounded exactly to FP64) or "plain_fp32" (one FP32 sum per entry)
+DEFAULT_ACCUMULATION = "compensated"
+DTYPE = {"compensated": "f32 element math, FP64-class accumulation (compensated FP32 pairs, exact FP64 rounding)",
+         "plain_fp32": "f32 element math, FP32 sums per entry (exact FP64 rounding)"}
 PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "tile_kernel_hex8_q1_elastic.md")
+Q2_PROFILE = os.path.join(ROOT, "profiles", "q2_two_phase_hex64.md")
 
 
 def _package():
@@ -111,6 +117,17 @@ class ClockSampler:
                 "reasons": reasons, "n_samples": len(self.samples)}
 
 
+def read_profile_value(path, key):
+    """A `key: value` line of a committed ncu summary (None when absent)."""
+    try:
+        for line in open(path):
+            if line.startswith(key + ":"):
+                return float(line.split(":")[1].split()[0])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
 def read_profile_traffic():
     """DRAM bytes per launch of the tile kernel from the committed ncu summary, if any."""
     try:
@@ -136,18 +153,75 @@ def setup_problem(fg, nel=NEL):
     return dict(grid=g, dh=dh, colptr=colptr, rowval=rowval, handle=h, setup_s=t1 - t0, create_s=t2 - t1)
 
 
-def cpu_rate(O, nslab, nthreads, repeats=1):
-    """Melem/s of the oracle's colored threaded assembly on a 128x128xnslab slab."""
-    prob = O.box_problem(O.HEXAHEDRON, (NEL[0], NEL[1], nslab), [0, 0, 0], [1, 1, nslab / NEL[2]], ip_order=1,
+def oracle_view(O, dh, colptr, rowval, qr_orders):
+    """The oracle's Problem over the product's own host arrays (grid, cell_dofs, colptr /
+    rowval), which the CPU tests check bit for bit against the oracle's set-up; qr_orders per
+    SubDofHandler."""
+    n = dh.n_cells
+    types = np.zeros(n, np.int32)
+    npc = np.zeros(n, np.int64)
+    for s in dh.subs:
+        types[s["cellset"] - 1] = s["cell_type"]
+        npc[s["cellset"] - 1] = s["cell_nodes"].shape[1]
+    off = np.zeros(n + 1, np.int64)
+    off[1:] = np.cumsum(npc)
+    cn = np.zeros(int(off[-1]), np.int64)
+    for s in dh.subs:
+        k = s["cell_nodes"].shape[1]
+        cn[(off[s["cellset"] - 1][:, None] + np.arange(k)[None, :]).ravel()] = s["cell_nodes"].ravel()
+    subs = [O.Subdomain(s["cellset"], s["ip_order"], s["n_components"], q) for s, q in zip(dh.subs, qr_orders)]
+    prob = O.Problem(dh.nodes, types, off, cn, subs)
+    prob.cell_dofs, prob.cell_dofs_offset, prob.ndofs = dh.cell_dofs, dh.cell_dofs_offset, dh.ndofs
+    prob.colptr, prob.rowval = colptr, rowval
+    return prob
+
+
+def rel_fro_np(a, b, chunk=1 << 26):
+    """|a - b| / |b| over host vectors, in chunks (no full-size temporaries)."""
+    num = den = 0.0
+    for k in range(0, len(b), chunk):
+        d = a[k:k + chunk] - b[k:k + chunk]
+        num += float(np.dot(d, d))
+        den += float(np.dot(b[k:k + chunk], b[k:k + chunk]))
+    return (num ** 0.5) / (den ** 0.5 if den > 0 else 1.0)
+
+
+def oracle_parity(O, prob, dev_nz, dev_f, nthreads, **phys):
+    """Relative Frobenius error of the engine's K and f (device tensors) against the oracle's
+    FP64 threaded assembly of the same problem (outside every timed region)."""
+    t = time.perf_counter()
+    T = prob.threaded(nthreads)
+    nz_o, f_o = T.assemble(**phys)
+    T.close()
+    cpu_s = time.perf_counter() - t
+    out = {"K": rel_fro_np(dev_nz.cpu().numpy(), nz_o), "f": rel_fro_np(dev_f.cpu().numpy(), f_o),
+           "oracle_s": cpu_s, "oracle_threads": nthreads,
+           "oracle": "FP64 C++ restatement of Ferrite's threaded colored assembly (WorkStream coloring)"}
+    del nz_o, f_o
+    return out
+
+
+def slab_problem(O, nslab):
+    return O.box_problem(O.HEXAHEDRON, (NEL[0], NEL[1], nslab), [0, 0, 0], [1, 1, nslab / NEL[2]], ip_order=1,
                          ncomp=3, qr_order=2, perturb=0.2, seed=SEED)
+
+
+def cpu_rate(O, nslab, nthreads, repeats=1):
+    """Melem/s of the oracle's threaded colored assembly on a 128x128xnslab slab: the
+    CellValues and the WorkStream coloring are built once (threaded_assembly.jl:134-141); each
+    timed call is one assemble_global! (start_assemble + the colored loop, 232-265)."""
+    prob = slab_problem(O, nslab)
+    T = prob.threaded(nthreads)
     nz = np.zeros(prob.nnz)
     f = np.zeros(prob.ndofs)
     times = []
     for _ in range(repeats):
         t = time.perf_counter()
-        prob.assemble(O.LINEAR_ELASTIC, E_MOD, NU, body=list(BODY), nthreads=nthreads, nzval=nz, f=f)
+        T.assemble(O.LINEAR_ELASTIC, E_MOD, NU, body=list(BODY), nzval=nz, f=f)
         times.append(time.perf_counter() - t)
-    return prob.n_cells, times
+    info = {"n_colors": T.n_colors, "coloring_setup_s": T.setup_s}
+    T.close()
+    return prob.n_cells, times, info
 
 
 def run_reference(args):
@@ -158,21 +232,24 @@ def run_reference(args):
     O = _oracle()
     cores = os.cpu_count() or 1
     # size the per-step slab so warmup + steps take about a minute
-    n0, t0 = cpu_rate(O, 2, cores)
+    n0, t0, _ = cpu_rate(O, 2, cores)
     rate = n0 / t0[0]
     per_step = 60.0 / max(1, args.steps + args.warmup)
     nslab = int(max(1, min(NEL[2], round(per_step * rate / (NEL[0] * NEL[1])))))
-    prob = O.box_problem(O.HEXAHEDRON, (NEL[0], NEL[1], nslab), [0, 0, 0], [1, 1, nslab / NEL[2]], ip_order=1,
-                         ncomp=3, qr_order=2, perturb=0.2, seed=SEED)
+    prob = slab_problem(O, nslab)
+    T = prob.threaded(cores)
     nz, f = np.zeros(prob.nnz), np.zeros(prob.ndofs)
     for _ in range(args.warmup):
-        prob.assemble(O.LINEAR_ELASTIC, E_MOD, NU, body=list(BODY), nthreads=cores, nzval=nz, f=f)
+        T.assemble(O.LINEAR_ELASTIC, E_MOD, NU, body=list(BODY), nzval=nz, f=f)
     t = time.perf_counter()
     for _ in range(args.steps):
-        prob.assemble(O.LINEAR_ELASTIC, E_MOD, NU, body=list(BODY), nthreads=cores, nzval=nz, f=f)
+        T.assemble(O.LINEAR_ELASTIC, E_MOD, NU, body=list(BODY), nzval=nz, f=f)
     dt = time.perf_counter() - t
     value = prob.n_cells * args.steps / dt / 1e6
-    sample = f"128x128x{nslab} slab of the 128^3 grid ({prob.n_cells} cells) per step"
+    sample = (f"128x128x{nslab} slab of the 128^3 grid ({prob.n_cells} cells) per step; WorkStream coloring "
+              f"({T.n_colors} colors) and CellValues built once at set-up, not timed; each step = start_assemble + "
+              f"the colored loop on {cores} threads")
+    T.close()
     line = {"metric": METRIC, "value": value, "unit": "Melem/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -229,7 +306,8 @@ def run_ours(args):
     stream = torch.cuda.Stream(device=dev)
     nz = torch.empty(nnz, dtype=torch.float64, device=dev)
     f = torch.empty(ndofs, dtype=torch.float64, device=dev)
-    kw = dict(physics=fg.LINEAR_ELASTIC, p0=E_MOD, p1=NU, body=BODY, stream=stream)
+    kw = dict(physics=fg.LINEAR_ELASTIC, p0=E_MOD, p1=NU, body=BODY, stream=stream,
+              compensated=DEFAULT_ACCUMULATION == "compensated")
 
     def barrier():
         if world > 1:
@@ -281,6 +359,36 @@ def run_ours(args):
         checks = {"rigid_body_residual_rel": worst, "sum_f_z": float(fh[2::3].sum()),
                   "finite": bool(np.isfinite(nzh).all() and np.isfinite(fh).all())}
         del K, nzh, fh
+
+    # ---- parity at full size: the oracle's FP64 threaded assembly of the same 128^3 problem,
+    # against the default (timed) result and the plain-FP32-sum form ----
+    parity = None
+    accumulation = None
+    if rank == 0 and not args.skip_oracle:
+        O = _oracle()
+        prob_o = oracle_view(O, dh, P["colptr"], P["rowval"], [2])
+        t0 = time.perf_counter()
+        T = prob_o.threaded(os.cpu_count() or 1)
+        nz_o, f_o = T.assemble(O.LINEAR_ELASTIC, E_MOD, NU, body=list(BODY))
+        T.close()
+        oracle_s = time.perf_counter() - t0
+        parity = {"oracle_rel_frobenius": {"K": rel_fro_np(nz.cpu().numpy(), nz_o), "f": rel_fro_np(f.cpu().numpy(), f_o)},
+                  "oracle_s": oracle_s, "oracle_threads": os.cpu_count(),
+                  "oracle": "FP64 C++ restatement of Ferrite's threaded colored assembly, full 128^3 grid",
+                  "accumulation": DEFAULT_ACCUMULATION}
+        # the other accumulation: its time and its error against the same oracle result
+        other = "plain_fp32" if DEFAULT_ACCUMULATION == "compensated" else "compensated"
+        with torch.cuda.stream(stream):
+            kw_other = dict(kw, compensated=(other == "compensated"))
+            ms_other = _timed(stream, lambda: h.assemble(nz, f, sync=False, **kw_other), max(3, min(args.steps, 10)))
+            h.sync()
+        accumulation = {"default": DEFAULT_ACCUMULATION, "default_ms": ms, other + "_ms": ms_other,
+                        other + "_oracle_rel_frobenius": {"K": rel_fro_np(nz.cpu().numpy(), nz_o),
+                                                          "f": rel_fro_np(f.cpu().numpy(), f_o)},
+                        "what": "compensated = TwoSum pairs of FP32 per nzval/f entry (FP64-class), rounded exactly "
+                                "to FP64; plain_fp32 = one FP32 sum per entry, rounded exactly to FP64"}
+        del nz_o, f_o, T
+        h.assemble(nz, f, **kw)  # the default result again (the legs below reuse nz / f)
 
     # ---- plain FP64 GPU form of the same engine ----
     fp64 = None
@@ -360,9 +468,11 @@ def run_ours(args):
     if rank == 0 and not args.skip_cpu:
         O = _oracle()
         cores = os.cpu_count() or 1
-        ncell, times = cpu_rate(O, 16, cores, repeats=3)
+        ncell, times, cinfo = cpu_rate(O, 16, cores, repeats=3)
         cpu = {"value": ncell / statistics.median(times) / 1e6, "unit": "Melem/s", "cores": cores, "kind": "port",
-               "sample": f"128x128x16 slab ({ncell} cells) of the 128^3 grid, median of 3, colored OpenMP"}
+               "sample": f"128x128x16 slab ({ncell} cells) of the 128^3 grid, median of 3; WorkStream coloring "
+                         f"({cinfo['n_colors']} colors) and CellValues built once at set-up (not timed); each call = "
+                         f"start_assemble + the colored loop on {cores} OpenMP threads"}
 
     if rank != 0:
         if world > 1:
@@ -376,7 +486,7 @@ def run_ours(args):
     traffic = read_profile_traffic()
     line = {"metric": METRIC, "value": value, "unit": "Melem/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32+f64acc", "data": "synthetic",
+            "vs_baseline": None, "dtype": DTYPE[DEFAULT_ACCUMULATION], "data": "synthetic",
             "config": {"workload": WORKLOAD, "nel": list(NEL), "cells": n_cells, "ndofs": ndofs, "nnz": nnz, "seed": SEED,
                        "perturbation": "interior nodes +-0.2h uniform", "E": E_MOD, "nu": NU, "body": BODY,
                        "l2": f"outputs ({8 * (nnz + ndofs) / 1e9:.2f} GB) and inputs larger than the 129 MB L2; no flush",
@@ -386,7 +496,7 @@ def run_ours(args):
                          "traffic": traffic, "algorithmic_bytes": balg, "kernel_ms": kernel_ms,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy)" if peaks else "fallback"},
             "clocks": clk.summary(), "gpu_launches": args.steps, "e2e": e2e, "fp64_gpu": fp64,
-            "cpu_baseline": cpu, "checks": checks, "configs": configs,
+            "cpu_baseline": cpu, "checks": checks, "parity": parity, "accumulation": accumulation, "configs": configs,
             "setup_s": {"host_setup": P["setup_s"], "fe_create": P["create_s"]}}
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -514,7 +624,68 @@ def config_heat(fg, stream):
     return out
 
 
-def config_adjoint(fg, stream):
+# FLOPs of the adjoint per Q1 hexahedron, counted from the formula per quadrature point (8
+# points): Jacobian (7 node offsets x 9 FMA = 126 flops), adjugate and determinant (~45),
+# gradient table dN/dx (8 x 9 FMA = 144), grad u and grad lambda (2 x 8 x 9 FMA = 288), the
+# two stresses (2 x ~15), psi (18), Sigma (2 x 27 FMA = 108) and dPhi/dx_k (8 x 9 FMA = 144),
+# plus the load density (~30): ~935 per point
+ADJ_FLOPS_PER_CELL = 8 * 935
+
+
+def ADJ_BYTES(n_cells, n_nodes, ndofs):
+    """compulsory bytes of one adjoint: coordinates, connectivity, rho, u, lambda read; d_rho,
+    d_X written (FP64, int32 ids)"""
+    return 24 * n_nodes + 32 * n_cells + 8 * n_cells + 16 * ndofs + 8 * n_cells + 24 * n_nodes
+
+
+def adjoint_fd_check(dh, colptr, rowval, rho, u, lam, adj, h=1e-6, ndir=3):
+    """Central finite differences (step h) of Phi = lambda^T (K(X, rho^3) u - f(X)) from the
+    oracle's FP64 threaded assembly, along `ndir` seeded random directions in rho and in X,
+    against the engine's adjoint (mixed and FP64) projected on the same directions. The
+    difference Phi(+) - Phi(-) is taken entry-wise (K+ - K-, f+ - f-) before the products, so
+    cancellation stays at the entry level."""
+    import scipy.sparse as sp
+    O = _oracle()
+    prob = oracle_view(O, dh, colptr, rowval, [2])
+    prob.nodes = dh.nodes.copy()
+    X0 = prob.nodes.copy()
+    T = prob.threaded(os.cpu_count() or 1)
+    rng = np.random.default_rng(SEED + 11)
+    t0 = time.perf_counter()
+
+    def dphi(s_plus, s_minus):
+        kp, fp = T.assemble(O.LINEAR_ELASTIC, 1.0, NU, body=list(BODY), cell_scale=s_plus)
+        km, fm = T.assemble(O.LINEAR_ELASTIC, 1.0, NU, body=list(BODY), cell_scale=s_minus)
+        dK = sp.csc_matrix((kp - km, rowval - 1, colptr - 1), shape=(dh.ndofs, dh.ndofs))
+        return float(lam @ (dK @ u) - lam @ (fp - fm)) / (2 * h)
+
+    out = {"h": h, "directions": ndir, "rho": [], "X": []}
+    for _ in range(ndir):
+        v = rng.standard_normal(dh.n_cells)
+        fd = dphi((rho + h * v) ** 3, (rho - h * v) ** 3)
+        out["rho"].append({"fd": fd, **{k: float(a[0] @ v) for k, a in adj.items()}})
+    s = rho ** 3
+    for _ in range(ndir):
+        w = rng.standard_normal(X0.shape)
+        prob.nodes[:] = X0 + h * w
+        kp, fp = T.assemble(O.LINEAR_ELASTIC, 1.0, NU, body=list(BODY), cell_scale=s)
+        prob.nodes[:] = X0 - h * w
+        km, fm = T.assemble(O.LINEAR_ELASTIC, 1.0, NU, body=list(BODY), cell_scale=s)
+        dK = sp.csc_matrix((kp - km, rowval - 1, colptr - 1), shape=(dh.ndofs, dh.ndofs))
+        fd = float(lam @ (dK @ u) - lam @ (fp - fm)) / (2 * h)
+        out["X"].append({"fd": fd, **{k: float(a[1] @ w.reshape(-1)) for k, a in adj.items()}})
+    prob.nodes[:] = X0
+    T.close()
+    for key in ("rho", "X"):
+        for name in adj:
+            out[f"max_rel_err_{key}_{name}"] = max(abs(d[name] - d["fd"]) / abs(d["fd"]) for d in out[key])
+    out["oracle_s"] = time.perf_counter() - t0
+    out["what"] = ("directional derivatives d/dt Phi(rho + t v) and d/dt Phi(X + t w): FD of the oracle's FP64 "
+                   "assembly vs the engine's adjoint (d_rho . v, d_X . w); mixed and fp64 = the engine's precisions")
+    return out
+
+
+def config_adjoint(fg, stream, oracle=True):
     """SIMP cantilever (96,48,48) on [0,2]x[0,1]^2: rho ~ U(0.01,1), E = rho^3, nu = 0.3, u and
     lambda ~ N(0, 1e-3^2); adjoint (d/d rho, d/dX) against the forward K+f assembly."""
     import torch
@@ -547,13 +718,22 @@ def config_adjoint(fg, stream):
     out["adjoint_over_forward"] = out["adjoint_mixed_ms"] / fwd
     rel = lambda a, b: float((a - b).abs().max() / b.abs().max())
     out["mixed_vs_fp64_rel_max"] = {"d_rho": rel(res["mixed"][0], res["fp64"][0]), "d_X": rel(res["mixed"][1], res["fp64"][1])}
+    # work of one adjoint: FLOPs counted from the formula per quadrature point (8 per cell)
+    out["roofline"] = {"bound": "fp32 issue (compute)", "flops_per_cell": ADJ_FLOPS_PER_CELL,
+                       "achieved_tflops": dh.n_cells * ADJ_FLOPS_PER_CELL / (out["adjoint_mixed_ms"] * 1e-3) / 1e12,
+                       "algorithmic_bytes": ADJ_BYTES(dh.n_cells, g.nodes.shape[0], dh.ndofs),
+                       "achieved_GBs": ADJ_BYTES(dh.n_cells, g.nodes.shape[0], dh.ndofs) / (out["adjoint_mixed_ms"] * 1e-3) / 1e9,
+                       "bar": "adjoint <= 2x one forward assembly of the same grid"}
+    if oracle:
+        out["fd_check"] = adjoint_fd_check(dh, colptr, rowval, rho, u.cpu().numpy(), lam.cpu().numpy(),
+                                           {k: (v[0].cpu().numpy(), v[1].cpu().numpy()) for k, v in res.items()})
     out["note"] = ("forward = mixed K+f assembly with E_e = rho^3; adjoint recomputes the geometry; "
                    "finite-difference checks of the formulas are in the tests")
     h.close()
     return out
 
 
-def config_q2(fg, stream, nel=64, reps=5):
+def config_q2(fg, stream, nel=64, reps=5, oracle=True):
     """Q2 hexahedra (27 nodes, 81 dofs per cell) on the perturbed unit cube, 3x3x3 Gauss,
     linear elasticity with a per-cell modulus E_e ~ lognormal(log 200e3, 0.5) (seeded), nu 0.3,
     b = (0, 0, -1). Mixed and FP64 forms timed; the mixed result against the FP64 one."""
@@ -568,7 +748,6 @@ def config_q2(fg, stream, nel=64, reps=5):
     t1 = time.perf_counter()
     h = dh.handle([host.CellValues(host.HEXAHEDRON, 2, 3)], colptr, rowval)
     t2 = time.perf_counter()
-    del rowval
     E = np.random.default_rng(SEED + 7).lognormal(np.log(E_MOD), 0.5, dh.n_cells)
     scale = torch.as_tensor(E / E_MOD, device="cuda")
     nz = torch.empty(h.nnz, dtype=torch.float64, device="cuda")
@@ -581,7 +760,14 @@ def config_q2(fg, stream, nel=64, reps=5):
     h.sync()
     rel_k = float(torch.linalg.vector_norm(nz_m - nz) / torch.linalg.vector_norm(nz))
     rel_f = float(torch.linalg.vector_norm(f_m - f) / torch.linalg.vector_norm(f))
-    del nz_m, f_m
+    parity = None
+    if oracle:
+        O = _oracle()
+        prob_o = oracle_view(O, dh, colptr, rowval, [3])
+        parity = oracle_parity(O, prob_o, nz_m, f_m, os.cpu_count() or 1, physics=O.LINEAR_ELASTIC, p0=E_MOD, p1=NU,
+                               body=list(BODY), cell_scale=E / E_MOD)
+        del prob_o
+    del nz_m, f_m, rowval
     info = h.info()
     n_nodes = g.nodes.shape[0]
     balg = 8 * h.nnz + 8 * dh.ndofs + 24 * n_nodes + 4 * 27 * dh.n_cells + 8 * dh.n_cells
@@ -590,7 +776,11 @@ def config_q2(fg, stream, nel=64, reps=5):
                      "achieved_GBs": balg / (mixed * 1e-3) / 1e9, "algorithmic_bytes": balg},
            "fp64": {"ms_per_assembly": fp64, "Melem_s": dh.n_cells / (fp64 * 1e-3) / 1e6},
            "speedup_mixed_over_fp64": fp64 / mixed,
-           "mixed_vs_fp64_rel_frobenius": {"K": rel_k, "f": rel_f},
+           "mixed_vs_fp64_rel_frobenius": {"K": rel_k, "f": rel_f}, "oracle_parity": parity,
+           "roofline": {"bound": "hbm", "achieved": balg / (mixed * 1e-3) / 1e9, "peak": hbm_peak_gbs(), "unit": "GB/s",
+                        "frac": balg / (mixed * 1e-3) / 1e9 / hbm_peak_gbs(), "algorithmic_bytes": balg,
+                        "tensor_pipe": read_profile_value(Q2_PROFILE, "tensor_pipe_active_pct"),
+                        "tensor_pipe_source": os.path.relpath(Q2_PROFILE, ROOT)},
            "tiles": info["n_tiles"], "cell_visits_per_cell": info["n_cell_visits"] / dh.n_cells,
            "setup_s": {"host": t1 - t0, "fe_create": t2 - t1},
            "path": "two-phase: element matrices once per cell on the tensor cores (tcgen05 kind::tf32, split-TF32 "
@@ -713,7 +903,7 @@ def config_pattern(fg, stream, nel=128):
     return out
 
 
-def config_mixed_graph(fg, stream, steps=20):
+def config_mixed_graph(fg, stream, steps=20, oracle=True):
     """~2M cells over three x-slabs sharing vertex nodes (Hex Q1 50%, Tet P1 25% as 6 per cube,
     Wedge P1 25% as 2 per cube), compressible Neo-Hooke (mu 1, lambda 10), displacement
     amplitude 0.05 of the cell size h = 0.01 (u = 0.05 h U(-1,1), seeded per step: an absolute
@@ -754,12 +944,40 @@ def config_mixed_graph(fg, stream, steps=20):
     gid = h.graph_capture([dict(u=u, **kw) for u in us], [nz] * steps, [f] * steps, stream)
     replay = _timed(stream, lambda: h.graph_replay(gid, stream, sync=False), 3, warmup=1)
     h.sync()
+    # e2e: a Newton step as a host caller makes it, through fe_assemble with page-locked host
+    # buffers -- u uploaded, K and f read back, every step
+    e2e = None
+    if not os.environ.get("FE_BENCH_SKIP_E2E"):
+        u_h = torch.empty(dh.ndofs, dtype=torch.float64, pin_memory=True)
+        nz_h = torch.empty(h.nnz, dtype=torch.float64, pin_memory=True).numpy()
+        f_h = torch.empty(dh.ndofs, dtype=torch.float64, pin_memory=True).numpy()
+        u_h.copy_(us[0].cpu())
+        u_hn = u_h.numpy()
+        h.assemble(nz_h, f_h, u=u_hn, stream=stream, **kw)
+        ke = 5
+        t = time.perf_counter()
+        for k in range(ke):
+            h.assemble(nz_h, f_h, u=u_hn, stream=stream, **kw)
+        dt = (time.perf_counter() - t) / ke
+        e2e = {"ms_per_step": dt * 1e3, "Melem_s": n_cells / dt / 1e6, "h2d_bytes_per_step": 8 * dh.ndofs,
+               "d2h_bytes_per_step": 8 * h.nnz + 8 * dh.ndofs, "steps": ke,
+               "what": "fe_assemble with u, nzval and f in page-locked host memory (host wall time per call)"}
+        del nz_h, f_h, u_h
     h.assemble(nz, f, u=us[-1], stream=stream, **kw)
     nz_m, f_m = nz.clone(), f.clone()
     h.assemble(nz, f, u=us[-1], stream=stream, precision=fg.PREC_FP64, **kw)
     err = {"K": rel_fro_t(nz_m, nz), "f": rel_fro_t(f_m, f)}
+    parity = None
+    if oracle:
+        O = _oracle()
+        prob_o = oracle_view(O, dh, colptr, rowval, [2, 1, 2])
+        parity = oracle_parity(O, prob_o, nz_m, f_m, os.cpu_count() or 1, physics=O.NEO_HOOKE, p0=1.0, p1=10.0,
+                               body=[0.0, 0.0, 0.0], u=us[-1].cpu().numpy())
+        del prob_o
     del nz_m, f_m
     info = h.info()
+    n_nodes = g.nodes.shape[0]
+    balg = 8 * h.nnz + 16 * dh.ndofs + 24 * n_nodes + 4 * (8 * len(hexes) + 4 * len(tets) + 6 * len(wedges))
     out = {"workload": "mixed_hex_tet_wedge_neo_hooke_2M", "cells": n_cells, "hex": len(hexes), "tet": len(tets),
            "wedge": len(wedges), "ndofs": dh.ndofs, "nnz": h.nnz, "steps_per_graph": steps,
            "graph_replay_ms": replay, "ms_per_assembly_in_graph": replay / steps,
@@ -767,7 +985,13 @@ def config_mixed_graph(fg, stream, steps=20):
            "autotune": {"best_stage_cap": tune["best_stage_cap"],
                         "candidates": [{"stage_cap": c, "ms": ms, "tiles": t} for c, ms, t, _ in tune["candidates"]]},
            "tiles": info["n_tiles"], "cell_visits_per_cell": info["n_cell_visits"] / n_cells,
-           "mixed_vs_fp64_rel_frobenius": err, "u": "0.05 * 0.01 * U(-1,1) per dof (amplitude 0.05 of the cell size)",
+           "mixed_vs_fp64_rel_frobenius": err, "oracle_parity": parity, "e2e": e2e,
+           "roofline": {"bound": "hbm", "achieved": balg / (replay / steps * 1e-3) / 1e9, "peak": hbm_peak_gbs(),
+                        "unit": "GB/s", "frac": balg / (replay / steps * 1e-3) / 1e9 / hbm_peak_gbs(),
+                        "algorithmic_bytes": balg,
+                        "formula": "8 nnz + 8 ndofs (f written) + 8 ndofs (u read) + 24 n_nodes (coordinates) + "
+                                   "4 bytes per node id per cell (8 hex, 4 tet, 6 wedge)"},
+           "u": "0.05 * 0.01 * U(-1,1) per dof (amplitude 0.05 of the cell size)",
            "quadrature": "hex 2x2x2 Gauss, tet 1 point, wedge 5-point order-2 rule"}
     h.close()
     return out
@@ -783,6 +1007,7 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-configs", action="store_true", help="skip the heat / Q2 / adjoint / mixed-graph configurations")
+    ap.add_argument("--skip-oracle", action="store_true", help="skip the full-size FP64 oracle parity legs")
     ap.add_argument("--nel", type=int, default=128, help="cells per axis (128 = the benchmark workload)")
     ap.add_argument("--config", choices=["heat", "q2", "adjoint", "mixed_graph", "elements", "pattern"],
                     help="run only this configuration and print its JSON (profiling runs)")

@@ -1068,6 +1068,307 @@ int or_greedy_coloring(const or_problem* p, int32_t* cell_color, int32_t* n_colo
     return OR_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Node-sharing cell incidence (create_incidence_matrix, coloring.jl:47-103): for each cell,
+// the other cells sharing at least one node with it, ascending and without duplicates.
+struct Incidence {
+    std::vector<int64_t> ptr, adj;  // 0-based cell ids; ptr has n_cells + 1 entries
+};
+Incidence cell_incidence(const or_problem* p) {
+    const int64_t n = p->n_cells;
+    std::vector<int64_t> nptr(p->n_nodes + 1, 0);
+    for (int64_t c = 0; c < n; ++c)
+        for (int64_t k = p->cell_nodes_offset[c]; k < p->cell_nodes_offset[c + 1]; ++k) nptr[p->cell_nodes[k]]++;
+    for (int64_t v = 0; v < p->n_nodes; ++v) nptr[v + 1] += nptr[v];
+    std::vector<int64_t> ncells(nptr[p->n_nodes]);
+    {
+        std::vector<int64_t> cur(nptr.begin(), nptr.end() - 1);
+        for (int64_t c = 0; c < n; ++c)
+            for (int64_t k = p->cell_nodes_offset[c]; k < p->cell_nodes_offset[c + 1]; ++k)
+                ncells[cur[p->cell_nodes[k] - 1]++] = c;
+    }
+    Incidence I;
+    I.ptr.assign(n + 1, 0);
+    std::vector<std::vector<int64_t>> rows(n);
+#pragma omp parallel for schedule(static)
+    for (int64_t c = 0; c < n; ++c) {
+        std::vector<int64_t>& cand = rows[c];
+        for (int64_t k = p->cell_nodes_offset[c]; k < p->cell_nodes_offset[c + 1]; ++k) {
+            const int64_t v = p->cell_nodes[k] - 1;
+            for (int64_t r = nptr[v]; r < nptr[v + 1]; ++r)
+                if (ncells[r] != c) cand.push_back(ncells[r]);
+        }
+        std::sort(cand.begin(), cand.end());
+        cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+    }
+    for (int64_t c = 0; c < n; ++c) I.ptr[c + 1] = I.ptr[c] + (int64_t)rows[c].size();
+    I.adj.resize(I.ptr[n]);
+    for (int64_t c = 0; c < n; ++c) std::copy(rows[c].begin(), rows[c].end(), I.adj.begin() + I.ptr[c]);
+    return I;
+}
+
+// _greedy_coloring! (coloring.jl:108-143) over `cells` in order, neighbours restricted to the
+// cells for which member(c) holds; returns the color classes, cells in visiting order.
+template <class Member>
+std::vector<std::vector<int64_t>> greedy_classes(const Incidence& I, const std::vector<int64_t>& cells,
+                                                 std::vector<int32_t>& cell_colors, Member member) {
+    std::vector<std::vector<int64_t>> classes;
+    std::vector<char> occupied;
+    for (const int64_t c : cells) {
+        std::fill(occupied.begin(), occupied.end(), 0);
+        for (int64_t r = I.ptr[c]; r < I.ptr[c + 1]; ++r) {
+            const int64_t nb = I.adj[r];
+            if (!member(nb)) continue;
+            const int32_t col = cell_colors[nb];
+            if (col) occupied[col - 1] = 1;
+        }
+        int32_t free_color = 0;
+        for (int32_t k = 0; k < (int32_t)classes.size(); ++k)
+            if (!occupied[k]) { free_color = k + 1; break; }
+        if (!free_color) {
+            classes.emplace_back();
+            occupied.push_back(0);
+            free_color = (int32_t)classes.size();
+        }
+        cell_colors[c] = free_color;
+        classes[free_color - 1].push_back(c);
+    }
+    return classes;
+}
+
+// workstream_coloring (coloring.jl:171-264, Turcksin et al. 2016 with greedy zone colorings),
+// Ferrite's default create_coloring algorithm (coloring.jl:308), over all cells:
+//  1. zones = levels of a breadth-first traversal from the lowest unvisited cell;
+//  2. each zone colored greedily among its own cells;
+//  3. the colors of the largest odd zone followed by those of the largest even zone are the
+//     global colors; every other zone's colors, largest first, join the smallest global
+//     color of its parity not yet used by that zone; each color is then sorted.
+std::vector<std::vector<int64_t>> workstream_colors(const or_problem* p, const Incidence& I) {
+    const int64_t n = p->n_cells;
+    std::vector<std::vector<int64_t>> out;
+    if (n == 0) return out;
+    if (n == 1) return {{0}};
+    std::vector<int64_t> zone_of(n, 0);
+    std::vector<std::vector<int64_t>> zones;
+    int64_t visited = 0, seed = 0;
+    while (visited < n) {
+        while (zone_of[seed] != 0) ++seed;
+        zones.push_back({seed});
+        zone_of[seed] = (int64_t)zones.size();
+        ++visited;
+        while (true) {
+            std::vector<int64_t> s;
+            const int64_t Z = (int64_t)zones.size() + 1;
+            for (const int64_t c : zones.back())
+                for (int64_t r = I.ptr[c]; r < I.ptr[c + 1]; ++r) {
+                    const int64_t nb = I.adj[r];
+                    if (zone_of[nb] == 0) {
+                        zone_of[nb] = Z;
+                        s.push_back(nb);
+                    }
+                }
+            if (s.empty()) break;
+            visited += (int64_t)s.size();
+            zones.push_back(std::move(s));
+        }
+    }
+    const int64_t nz = (int64_t)zones.size();
+    std::vector<std::vector<std::vector<int64_t>>> zc(nz);
+    std::vector<int32_t> cell_colors(n, 0);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t zi = 0; zi < nz; ++zi)  // zones touch disjoint parts of cell_colors
+        zc[zi] = greedy_classes(I, zones[zi], cell_colors, [&](int64_t c) { return zone_of[c] == zi + 1; });
+    // findmax over odd / even zone numbers (1-based), first maximum
+    int64_t Nodd = -1, Zodd = -1, Neven = -1, Zeven = -1;
+    for (int64_t z = 1; z <= nz; ++z) {
+        const int64_t len = (int64_t)zc[z - 1].size();
+        if (z & 1) {
+            if (len > Nodd) { Nodd = len; Zodd = z; }
+        } else if (len > Neven) {
+            Neven = len;
+            Zeven = z;
+        }
+    }
+    if (Zeven < 0) Neven = 0;
+    const int64_t N = Nodd + Neven;
+    out = zc[Zodd - 1];
+    if (Zeven > 0) out.insert(out.end(), zc[Zeven - 1].begin(), zc[Zeven - 1].end());
+    std::vector<int64_t> sizes(N);
+    for (int64_t x = 0; x < N; ++x) sizes[x] = (int64_t)out[x].size();
+    std::vector<char> used(N);
+    for (int64_t z = 1; z <= nz; ++z) {
+        if (z == Zodd || z == Zeven) continue;
+        const auto& zcv = zc[z - 1];
+        const bool odd = z & 1;
+        std::fill(used.begin(), used.end(), 0);
+        std::vector<int64_t> order(zcv.size());
+        for (size_t k = 0; k < order.size(); ++k) order[k] = (int64_t)k;
+        std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return zcv[a].size() > zcv[b].size(); });
+        for (const int64_t lc : order) {
+            int64_t best = -1;
+            for (int64_t x = 0; x < N; ++x) {
+                const bool ok = (odd ? x + 1 <= Nodd : x + 1 > Nodd) && !used[x];
+                if (ok && (best < 0 || sizes[x] < sizes[best])) best = x;
+            }
+            used[best] = 1;
+            out[best].insert(out[best].end(), zcv[lc].begin(), zcv[lc].end());
+            sizes[best] = (int64_t)out[best].size();
+        }
+    }
+    for (auto& c : out) std::sort(c.begin(), c.end());
+    return out;
+}
+
+// Greedy colors in cell order (greedy_coloring, coloring.jl:146-160), as classes.
+std::vector<std::vector<int64_t>> greedy_colors(const or_problem* p) {
+    std::vector<int32_t> color(p->n_cells);
+    int32_t ncol = 0;
+    or_greedy_coloring(p, color.data(), &ncol);
+    std::vector<std::vector<int64_t>> colors(ncol);
+    for (int s = 0; s < p->n_sdh; ++s)
+        for (int64_t k = p->sdh_cellset_offset[s]; k < p->sdh_cellset_offset[s + 1]; ++k) {
+            const int64_t c = p->sdh_cellset[k] - 1;
+            colors[color[c] - 1].push_back(c);
+        }
+    return colors;
+}
+
+// One cell of the loop body of threaded_assembly.jl:232-265 / heat_equation.jl:186-206:
+// reinit!, the element routine, then assemble! (f += fe; merge walk into nzval).
+int assemble_cell(const or_problem* p, const Setup& S, const or_physics* ph, int64_t c, CellValues& cv,
+                  std::vector<double>& Ke, std::vector<double>& fe, std::vector<double>& x, std::vector<double>& ue,
+                  std::vector<int64_t>& sorted, std::vector<int>& perm, double* nzval, double* f, or_error& e) {
+    const CSCView K{p->ndofs, p->colptr, p->rowval};
+    const int s = S.cell_sdh[c];
+    const int ld = S.ndpc[s];
+    Ke.resize(ld * ld);
+    fe.resize(ld);
+    int r = element(S, cv, s, c, ph, Ke.data(), fe.data(), x, ue, &e);
+    if (r) return r;
+    const int64_t* dofs = p->cell_dofs + p->cell_dofs_offset[c] - 1;
+    if (f)
+        for (int i = 0; i < ld; ++i) f[dofs[i] - 1] += fe[i];
+    if (!nzval) return OR_OK;
+    int miss_code = OR_OK;
+    merge_walk(K, dofs, ld, sorted, perm,
+               [&](int64_t R, int ker, int kec) {
+                   const double v = Ke[kec * ld + ker];
+                   if (v != 0.0) nzval[R] += v;  // addindex! skips zeros (arrayutils.jl:100-107)
+               },
+               [&](int64_t row, int64_t col, int ker, int kec) {
+                   if (Ke[kec * ld + ker] != 0.0 && miss_code == OR_OK) {
+                       miss_code = OR_ERR_PATTERN_MISSING;
+                       e.code = OR_ERR_PATTERN_MISSING;
+                       e.row = row;
+                       e.col = col;
+                       e.cell = c + 1;
+                   }
+               });
+    return miss_code;
+}
+
+// The colored loop of threaded_assembly.jl:232-265: colors in order, the cells of one color
+// split into equal chunks over the threads (OhMyThreads' DynamicScheduler with ntasks = the
+// thread count), each thread with its own CellValues copy and assembler buffers (ScratchData,
+// created per task, 164-193). The first error by cell id is reported.
+int assemble_colored(const or_problem* p, const Setup& S, const std::vector<std::vector<int64_t>>& colors,
+                     const or_physics* ph, int32_t nthreads, double* nzval, double* f, or_error* err) {
+    int status = OR_OK;
+    or_error first_err{};
+#ifdef _OPENMP
+    omp_set_num_threads(nthreads);
+#endif
+    for (size_t col = 0; col < colors.size() && status == OR_OK; ++col) {
+        const std::vector<int64_t>& cells = colors[col];
+#pragma omp parallel
+        {
+            std::vector<CellValues> cvs = S.cvs;  // task-local CellValues copies
+            std::vector<double> Ke, fe, x, ue;
+            std::vector<int64_t> sorted;
+            std::vector<int> perm;
+            or_error e{};
+#pragma omp for schedule(static)
+            for (int64_t k = 0; k < (int64_t)cells.size(); ++k) {
+                const int64_t c = cells[k];
+                int r = assemble_cell(p, S, ph, c, cvs[S.cell_sdh[c]], Ke, fe, x, ue, sorted, perm, nzval, f, e);
+                if (r) {
+#pragma omp critical
+                    {
+                        if (status == OR_OK || e.cell < first_err.cell) {
+                            status = r;
+                            first_err = e;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    if (status) *err = first_err;
+    return status;
+}
+
+}  // namespace
+
+// A threaded assembly prepared once, as the how-to prepares it before its timed calls: the
+// problem view, the CellValues and the coloring (create_coloring in create_cantilever_grid,
+// threaded_assembly.jl:134-141); each or_threaded_assemble call is one assemble_global!.
+struct or_threaded {
+    or_problem p;
+    Setup S;
+    std::vector<std::vector<int64_t>> colors;
+    int32_t nthreads;
+};
+
+extern "C" {
+
+int or_threaded_create(const or_problem* p, int32_t nthreads, int32_t algorithm, or_threaded** out,
+                       int32_t* n_colors) {
+    if (!p || !out || nthreads <= 0) return OR_ERR_ARG;
+    or_threaded* t = new or_threaded();
+    t->p = *p;
+    t->nthreads = nthreads;
+    int rc = t->S.init(&t->p);
+    if (rc) {
+        delete t;
+        return rc;
+    }
+#ifdef _OPENMP
+    omp_set_num_threads(nthreads);
+#endif
+    if (algorithm == OR_COLORING_WORKSTREAM) {
+        t->colors = workstream_colors(&t->p, cell_incidence(&t->p));
+    } else if (algorithm == OR_COLORING_GREEDY) {
+        t->colors = greedy_colors(&t->p);
+    } else {
+        delete t;
+        return OR_ERR_ARG;
+    }
+    if (n_colors) *n_colors = (int32_t)t->colors.size();
+    *out = t;
+    return OR_OK;
+}
+
+int or_threaded_colors(const or_threaded* t, int32_t* cell_color) {
+    for (size_t k = 0; k < t->colors.size(); ++k)
+        for (const int64_t c : t->colors[k]) cell_color[c] = (int32_t)k + 1;
+    return OR_OK;
+}
+
+int or_threaded_assemble(or_threaded* t, const or_physics* ph, double* nzval, double* f, or_error* err) {
+    err->code = OR_OK;
+    err->cell = 0;
+    const or_problem* p = &t->p;
+    // start_assemble(K, f) zeroes K and f (assembler.jl:287-291, arrayutils.jl:145-148)
+    if (nzval) std::memset(nzval, 0, (p->colptr[p->ndofs] - 1) * sizeof(double));
+    if (f) std::memset(f, 0, p->ndofs * sizeof(double));
+    return assemble_colored(p, t->S, t->colors, ph, t->nthreads, nzval, f, err);
+}
+
+void or_threaded_destroy(or_threaded* t) { delete t; }
+
 // Full assembly: start_assemble (zero K and f), then the cell loop with reinit!, the element
 // routine and assemble!. nthreads == 0: sequential loop over the SubDofHandlers' cells in
 // order (heat_equation.jl:186-206). nthreads > 0: greedy colors, cells of one color in
@@ -1084,90 +1385,17 @@ int or_assemble(const or_problem* p, const or_physics* ph, int32_t nthreads, int
         if (nzval) std::memset(nzval, 0, nnz * sizeof(double));
         if (f) std::memset(f, 0, p->ndofs * sizeof(double));
     }
-    CSCView K{p->ndofs, p->colptr, p->rowval};
-    auto do_cell = [&](int64_t c, CellValues& cv, std::vector<double>& Ke, std::vector<double>& fe,
-                       std::vector<double>& x, std::vector<double>& ue, std::vector<int64_t>& sorted,
-                       std::vector<int>& perm, or_error& e) -> int {
-        const int s = S.cell_sdh[c];
-        const int ld = S.ndpc[s];
-        Ke.resize(ld * ld);
-        fe.resize(ld);
-        int r = element(S, cv, s, c, ph, Ke.data(), fe.data(), x, ue, &e);
-        if (r) return r;
-        const int64_t* dofs = p->cell_dofs + p->cell_dofs_offset[c] - 1;
-        if (f)
-            for (int i = 0; i < ld; ++i) f[dofs[i] - 1] += fe[i];
-        if (!nzval) return OR_OK;
-        int miss_code = OR_OK;
-        merge_walk(K, dofs, ld, sorted, perm,
-                   [&](int64_t R, int ker, int kec) {
-                       const double v = Ke[kec * ld + ker];
-                       if (v != 0.0) nzval[R] += v;  // addindex! skips zeros (arrayutils.jl:100-107)
-                   },
-                   [&](int64_t row, int64_t col, int ker, int kec) {
-                       if (Ke[kec * ld + ker] != 0.0 && miss_code == OR_OK) {
-                           miss_code = OR_ERR_PATTERN_MISSING;
-                           e.code = OR_ERR_PATTERN_MISSING;
-                           e.row = row;
-                           e.col = col;
-                           e.cell = c + 1;
-                       }
-                   });
-        return miss_code;
-    };
-    if (nthreads <= 0) {
-        std::vector<double> Ke, fe, x, ue;
-        std::vector<int64_t> sorted;
-        std::vector<int> perm;
-        for (int s = 0; s < p->n_sdh; ++s)
-            for (int64_t k = p->sdh_cellset_offset[s]; k < p->sdh_cellset_offset[s + 1]; ++k) {
-                const int64_t c = p->sdh_cellset[k] - 1;
-                int r = do_cell(c, S.cvs[s], Ke, fe, x, ue, sorted, perm, *err);
-                if (r) return r;
-            }
-        return OR_OK;
-    }
-    std::vector<int32_t> color(p->n_cells);
-    int32_t ncol = 0;
-    or_greedy_coloring(p, color.data(), &ncol);
-    std::vector<std::vector<int64_t>> colors(ncol);
+    if (nthreads > 0) return assemble_colored(p, S, greedy_colors(p), ph, nthreads, nzval, f, err);
+    std::vector<double> Ke, fe, x, ue;
+    std::vector<int64_t> sorted;
+    std::vector<int> perm;
     for (int s = 0; s < p->n_sdh; ++s)
         for (int64_t k = p->sdh_cellset_offset[s]; k < p->sdh_cellset_offset[s + 1]; ++k) {
             const int64_t c = p->sdh_cellset[k] - 1;
-            colors[color[c] - 1].push_back(c);
+            int r = assemble_cell(p, S, ph, c, S.cvs[s], Ke, fe, x, ue, sorted, perm, nzval, f, *err);
+            if (r) return r;
         }
-    int status = OR_OK;
-    or_error first_err{};
-#ifdef _OPENMP
-    omp_set_num_threads(nthreads);
-#endif
-    for (int col = 0; col < ncol && status == OR_OK; ++col) {
-        const std::vector<int64_t>& cells = colors[col];
-#pragma omp parallel
-        {
-            std::vector<CellValues> cvs = S.cvs;  // task-local CellValues copies
-            std::vector<double> Ke, fe, x, ue;
-            std::vector<int64_t> sorted;
-            std::vector<int> perm;
-            or_error e{};
-#pragma omp for schedule(dynamic, 256)
-            for (int64_t k = 0; k < (int64_t)cells.size(); ++k) {
-                const int64_t c = cells[k];
-                int r = do_cell(c, cvs[S.cell_sdh[c]], Ke, fe, x, ue, sorted, perm, e);
-                if (r) {
-#pragma omp critical
-                    {
-                        if (status == OR_OK || e.cell < first_err.cell) {
-                            status = r;
-                            first_err = e;
-                        }
-                    }
-                }
-            }
-        }
-    }
-    if (status) *err = first_err;
-    return status;
+    return OR_OK;
 }
 
 

@@ -124,6 +124,21 @@ int or_apply(int64_t n, const int64_t* colptr, const int64_t* rowval, double* nz
              int64_t n_prescribed, const int64_t* prescribed, const double* inhomogeneities, int32_t applyzero);
 int or_greedy_coloring(const or_problem* p, int32_t* cell_color, int32_t* n_colors);
 
+/* Threaded colored assembly prepared once (threaded_assembly.jl:134-141, 232-265): the
+ * CellValues and the coloring are built by or_threaded_create, as the how-to builds them
+ * before it assembles; each or_threaded_assemble is one assemble_global! call (start_assemble
+ * zeroes K and f, then the colors in order, each color's cells in equal chunks over nthreads
+ * threads with per-thread CellValues and assembler buffers). The problem's arrays must stay
+ * valid until or_threaded_destroy. algorithm: OR_COLORING_WORKSTREAM (Ferrite's default,
+ * coloring.jl:171-264, 308) or OR_COLORING_GREEDY (coloring.jl:108-160). */
+enum { OR_COLORING_GREEDY = 1, OR_COLORING_WORKSTREAM = 2 };
+typedef struct or_threaded or_threaded;
+int or_threaded_create(const or_problem* p, int32_t nthreads, int32_t algorithm, or_threaded** out,
+                       int32_t* n_colors);
+int or_threaded_colors(const or_threaded* t, int32_t* cell_color);
+int or_threaded_assemble(or_threaded* t, const or_physics* phys, double* nzval, double* f, or_error* err);
+void or_threaded_destroy(or_threaded* t);
+
 /* CSR assembly (ext/FerriteSparseMatrixCSR.jl:9-96, SparseMatrixCSR{1}): as or_assemble (serial,
  * cell order) into a CSR matrix with 1-based rowptr[ndofs+1] / colval[nnz] (columns ascending
  * within a row): K[row, col] += Ke[row_local, col_local]; a pattern miss reports (row, col). */

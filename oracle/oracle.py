@@ -15,6 +15,7 @@ import ctypes
 import os
 import subprocess
 import threading
+import time
 
 import numpy as np
 
@@ -97,6 +98,13 @@ def lib():
                                           f64p, f64p, ctypes.POINTER(_Error)]
             L.or_element_matvec.argtypes = [ctypes.POINTER(_Problem), ctypes.c_int32, ctypes.c_void_p, i64p, f64p,
                                             ctypes.c_int32, f64p]
+            L.or_threaded_create.argtypes = [ctypes.POINTER(_Problem), ctypes.c_int32, ctypes.c_int32,
+                                             ctypes.POINTER(ctypes.c_void_p), i32p]
+            L.or_threaded_colors.argtypes = [ctypes.c_void_p, i32p]
+            L.or_threaded_assemble.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Physics), f64p, f64p,
+                                               ctypes.POINTER(_Error)]
+            L.or_threaded_destroy.argtypes = [ctypes.c_void_p]
+            L.or_threaded_destroy.restype = None
             _lib = L
     return _lib
 
@@ -468,6 +476,59 @@ class Problem:
     def to_scipy(self, nzval):
         import scipy.sparse as sp
         return sp.csc_matrix((nzval, self.rowval - 1, self.colptr - 1), shape=(self.ndofs, self.ndofs))
+
+    def threaded(self, nthreads, algorithm="workstream"):
+        """The threaded colored assembly of threaded_assembly.jl, prepared once (CellValues and
+        coloring at set-up); ``.assemble(...)`` is one assemble_global! call."""
+        return Threaded(self, nthreads, algorithm)
+
+
+class Threaded:
+    """or_threaded_*: set-up (coloring) outside, the colored loop inside each call."""
+
+    ALGORITHMS = {"greedy": 1, "workstream": 2}
+
+    def __init__(self, prob, nthreads, algorithm="workstream"):
+        self.prob, self.nthreads, self.algorithm = prob, int(nthreads), algorithm
+        self._P = prob._struct()
+        self._keep = list(prob._keep)  # the view's arrays live as long as the context
+        ptr, n = ctypes.c_void_p(), ctypes.c_int32()
+        t = time.perf_counter()
+        rc = lib().or_threaded_create(ctypes.byref(self._P), self.nthreads, self.ALGORITHMS[algorithm],
+                                      ctypes.byref(ptr), ctypes.byref(n))
+        self.setup_s = time.perf_counter() - t
+        if rc:
+            raise OracleError(rc, _Error())
+        self._h, self.n_colors = ptr, n.value
+
+    def colors(self):
+        col = np.zeros(self.prob.n_cells, np.int32)
+        lib().or_threaded_colors(self._h, _p(col, i32p))
+        return col
+
+    def assemble(self, physics, p0, p1, body=None, cell_scale=None, u=None, nzval=None, f=None):
+        prob = self.prob
+        if nzval is None:
+            nzval = np.zeros(prob.nnz)
+        if f is None:
+            f = np.zeros(prob.ndofs)
+        ph = prob._physics(physics, p0, p1, body, cell_scale, u)
+        err = _Error()
+        rc = lib().or_threaded_assemble(self._h, ctypes.byref(ph), _p(nzval, f64p), _p(f, f64p), ctypes.byref(err))
+        if rc:
+            raise OracleError(rc, err)
+        return nzval, f
+
+    def close(self):
+        if self._h:
+            lib().or_threaded_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class OracleError(RuntimeError):

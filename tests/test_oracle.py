@@ -339,6 +339,36 @@ def test_colored_threaded_determinism(oracle):
     assert np.allclose(runs[0][1], f0, rtol=1e-13)
 
 
+@pytest.mark.parametrize("ct,nel", [("QUADRILATERAL", (5, 5)), ("TRIANGLE", (5, 5)), ("TETRAHEDRON", (5, 5, 5)),
+                                    ("HEXAHEDRON", (5, 5, 5)), ("HEXAHEDRON", (12, 7, 3))])
+def test_colorings_partition_without_conflicts(oracle, ct, nel):
+    """Both colorings (WorkStream, Ferrite's default, and Greedy) cover every cell once and
+    never give two cells sharing a node the same color (test_grid_dofhandler_vtk.jl:719-740);
+    the threaded assembly prepared with either equals the serial loop up to summation order
+    and is bitwise the same for 1 and 3 threads (threaded_assembly.jl:397-410)."""
+    O = oracle
+    ct = getattr(O, ct)
+    ncomp = O.ref_dim(ct)
+    p = O.box_problem(ct, nel, ip_order=1, ncomp=ncomp, perturb=0.1, seed=4)
+    nz0, f0 = p.assemble(O.LINEAR_ELASTIC, 200e3, 0.3, body=[0.0, -1.0, 0.0][:ncomp] + [0.0] * (3 - ncomp))
+    for alg in ("workstream", "greedy"):
+        runs = []
+        for nt in (1, 3):
+            T = p.threaded(nt, alg)
+            col = T.colors()
+            assert col.min() == 1 and col.max() == T.n_colors
+            for c in range(p.n_cells):  # no neighbour (shared node) has the cell's color
+                nodes = set(p.cells_of(c).tolist())
+                for d in range(c + 1, p.n_cells):
+                    if col[d] == col[c]:
+                        assert not nodes.intersection(p.cells_of(d).tolist()), (alg, c, d)
+            runs.append(T.assemble(O.LINEAR_ELASTIC, 200e3, 0.3, body=[0.0, -1.0, 0.0][:ncomp] + [0.0] * (3 - ncomp)))
+            T.close()
+        assert np.array_equal(runs[0][0], runs[1][0]) and np.array_equal(runs[0][1], runs[1][1])
+        assert np.allclose(runs[0][0], nz0, rtol=1e-13, atol=1e-13 * np.abs(nz0).max())
+        assert np.allclose(runs[0][1], f0, rtol=1e-13, atol=1e-15)
+
+
 def test_index_map_matches_binary_search(oracle):
     O = oracle
     p = O.box_problem(O.HEXAHEDRON, (2, 2, 2), ip_order=2, ncomp=3, qr_order=3)
