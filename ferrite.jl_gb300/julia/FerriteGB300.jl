@@ -8,13 +8,19 @@
 module FerriteGB300
 
 using Ferrite, SparseArrays
+import ChainRulesCore
+using ChainRulesCore: NoTangent, unthunk
 
 const LIB = get(ENV, "FERRITE_GB300_LIB", joinpath(@__DIR__, "..", "lib", "libferrite_gb300.so"))
 
 const FE_HEAT, FE_LINEAR_ELASTIC, FE_NEO_HOOKE = Int32(1), Int32(2), Int32(3)
 const FE_PREC_MIXED, FE_PREC_FP64 = Int32(0), Int32(1)
 const FE_FILLZERO = UInt32(1)
+const FE_ASYNC = UInt32(8)
 const FE_STAGED_OUTPUT = UInt32(512)
+
+# raw address of a host Vector or a device array (CuArray's CuPtr is a 64-bit primitive)
+_ptr(x, ::Type{T}=Float64) where {T} = x === nothing ? Ptr{T}(C_NULL) : reinterpret(Ptr{T}, pointer(x))
 
 struct GridDesc
     dim::Int32
@@ -82,6 +88,9 @@ celltype_code(::Type{Wedge}) = Int32(5)
 mutable struct Handle
     ptr::Ptr{Cvoid}
     keep::Vector{Any}
+    dim::Int
+    n_nodes::Int
+    n_cells::Int
 end
 
 function check(rc, h)
@@ -139,7 +148,7 @@ function Handle(dh::DofHandler, cvs::Vector, colptr::Vector{Int64}, rowval::Vect
         (Ptr{GridDesc}, Int32, Ptr{SubdomainDesc}, Ptr{DofDesc}, Ptr{CscDesc}, Ptr{Ptr{Cvoid}}),
         g, Int32(length(subs)), subs, d, p, out)
     check(rc, C_NULL)
-    h = Handle(out[], keep)
+    h = Handle(out[], keep, Int(Ferrite.getspatialdim(grid)), length(grid.nodes), length(grid.cells))
     finalizer(x -> ccall((:fe_destroy, LIB), Cvoid, (Ptr{Cvoid},), x.ptr), h)
     return h
 end
@@ -351,6 +360,175 @@ function assemble_facet_load!(f, fs::FacetSet; pressure=0.0, traction=(0.0, 0.0,
         fs.ptr, pressure, t, fillzero ? FE_FILLZERO : UInt32(0), pointer(f), C_NULL)
     check(rc, fs.h.ptr)
     return f
+end
+
+# ---------------------------------------------------------------------------------------
+# Adjoint: vector-Jacobian products of Phi = lambda' (K(X, s) u - f(X))
+# ---------------------------------------------------------------------------------------
+struct AdjointParams
+    physics::Int32
+    precision::Int32
+    flags::UInt32
+    p0::Float64
+    p1::Float64
+    body::NTuple{3,Float64}
+    cell_scale::Ptr{Float64}
+    dscale::Ptr{Float64}
+    stream::Ptr{Cvoid}
+end
+
+"""
+    assemble_adjoint!(d_s, d_X, h, u, λ; physics, p0, p1, body, cell_scale, dscale, precision)
+
+fe_assemble_adjoint: `d_s[c] = dscale[c] * λ_c' (∂K_c/∂s_c) u_c` for every cell (the SIMP
+sensitivity of topology_optimization.jl:347-383 with `s = ρ^p`, `dscale = p ρ^(p-1)`; with
+`dscale = nothing` it is ∂Φ/∂s itself), and `d_X = ∂Φ/∂X` for the node coordinates (node-major
+like `grid.nodes`; `d_X = nothing` skips it). Heat and linear elasticity on linear cells.
+Arrays may be host `Vector`s or device arrays.
+"""
+function assemble_adjoint!(d_s, d_X, h::Handle, u, λ; physics=FE_LINEAR_ELASTIC, p0=1.0, p1=0.3,
+                           body=(0.0, 0.0, 0.0), cell_scale=nothing, dscale=nothing, precision=FE_PREC_MIXED)
+    par = Ref(AdjointParams(physics, precision, UInt32(0), p0, p1, Tuple(Float64.(body)),
+                            _ptr(cell_scale), _ptr(dscale), C_NULL))
+    rc = GC.@preserve d_s d_X u λ cell_scale dscale ccall((:fe_assemble_adjoint, LIB), Cint,
+        (Ptr{Cvoid}, Ptr{AdjointParams}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+        h.ptr, par, _ptr(u), _ptr(λ), _ptr(d_s), _ptr(d_X))
+    check(rc, h.ptr)
+    return d_s, d_X
+end
+
+"""
+    coordinate_sensitivity(h, u, λ; kwargs...) -> d_X
+
+`∂Φ/∂X` of `Φ = λ' (K(X, s) u - f(X))` at the handle's node coordinates, as a
+`(dim, n_nodes)` matrix (the layout of `reinterpret(Float64, grid.nodes)`).
+"""
+function coordinate_sensitivity(h::Handle, u::Vector{Float64}, λ::Vector{Float64}; kwargs...)
+    d_s = zeros(h.n_cells)
+    d_X = zeros(h.dim, h.n_nodes)
+    assemble_adjoint!(d_s, d_X, h, u, λ; kwargs...)
+    return d_X
+end
+
+"""
+    residual(h, K, s, u; physics, p0, p1, body, precision) -> r = K(s) u - f
+
+Assembles K and f with the per-cell material factor `s` (`cell_scale`: E_c = s_c p0) into K
+and a fresh f, and returns the residual. Differentiable in `s` and `u` through the
+ChainRulesCore.rrule below, whose pullback for a cotangent `λ` is one adjoint kernel launch,
+`s̄ = λ' ∂(K u - f)/∂s` (geometry recomputed on the device, nothing stored), and
+`ū = K' λ = K λ` (K is symmetric). This replaces differentiating Ferrite's cell loop
+(topology_optimization.jl:347-383): with `s = ρ.^p` the chain rule through `s` gives the SIMP
+sensitivities. For the node coordinates see `coordinate_sensitivity`.
+"""
+function residual(h::Handle, K::SparseMatrixCSC{Float64,Int}, s::Vector{Float64}, u::Vector{Float64};
+                  physics=FE_LINEAR_ELASTIC, p0=1.0, p1=0.3, body=(0.0, 0.0, 0.0), precision=FE_PREC_MIXED)
+    f = zeros(size(K, 1))
+    assemble_csc!(K, f, h; physics=physics, p0=p0, p1=p1, body=body, cell_scale=s, precision=precision)
+    return K * u - f
+end
+
+function ChainRulesCore.rrule(::typeof(residual), h::Handle, K::SparseMatrixCSC{Float64,Int}, s::Vector{Float64},
+                              u::Vector{Float64}; physics=FE_LINEAR_ELASTIC, p0=1.0, p1=0.3, body=(0.0, 0.0, 0.0),
+                              precision=FE_PREC_MIXED)
+    r = residual(h, K, s, u; physics=physics, p0=p0, p1=p1, body=body, precision=precision)
+    # K(s) of this evaluation: the caller may re-assemble into K before the pullback runs
+    Ks = SparseMatrixCSC(size(K, 1), size(K, 2), K.colptr, K.rowval, copy(nonzeros(K)))
+    function residual_pullback(r̄)
+        λ = Vector{Float64}(unthunk(r̄))
+        s̄ = zeros(length(s))
+        assemble_adjoint!(s̄, nothing, h, u, λ; physics=physics, p0=p0, p1=p1, body=body, cell_scale=s,
+                          precision=precision)
+        ū = Ks * λ
+        return NoTangent(), NoTangent(), NoTangent(), s̄, ū
+    end
+    return r, residual_pullback
+end
+
+# ---------------------------------------------------------------------------------------
+# CUDA graphs of repeated assemblies and the plan autotuner
+# ---------------------------------------------------------------------------------------
+mutable struct AssemblyGraph
+    id::Int32
+    h::Handle
+    stream::Ptr{Cvoid}
+    keep::Vector{Any}
+end
+
+"""
+    capture_graph(h, steps, nzvals, fs; stream) -> AssemblyGraph
+
+fe_graph_capture: the assemblies `steps[k]` (NamedTuples with `physics, p0, p1, body, u,
+cell_scale, precision`) into `nzvals[k]`, `fs[k]` (device arrays) recorded as one CUDA graph on
+`stream` (a created stream's handle, e.g. `CUDA.stream().handle`). Replaying re-reads the
+buffers, so a `u` updated in place re-assembles with the new values: the Newton loop of
+hyperelasticity.jl:386-420 without per-step launch overhead.
+"""
+function capture_graph(h::Handle, steps::AbstractVector, nzvals::AbstractVector, fs::AbstractVector; stream::Ptr{Cvoid})
+    params = AssembleParams[]
+    for s in steps
+        push!(params, AssembleParams(Int32(get(s, :physics, FE_LINEAR_ELASTIC)), Int32(get(s, :precision, FE_PREC_MIXED)),
+                                     FE_FILLZERO, Float64(get(s, :p0, 1.0)), Float64(get(s, :p1, 0.3)),
+                                     Tuple(Float64.(get(s, :body, (0.0, 0.0, 0.0)))), _ptr(get(s, :cell_scale, nothing)),
+                                     _ptr(get(s, :u, nothing)), 0.0, stream))
+    end
+    nzp = Ptr{Float64}[_ptr(x) for x in nzvals]
+    fp = Ptr{Float64}[_ptr(x) for x in fs]
+    id = Ref{Int32}(0)
+    rc = GC.@preserve steps nzvals fs params nzp fp ccall((:fe_graph_capture, LIB), Cint,
+        (Ptr{Cvoid}, Ptr{Cvoid}, Int32, Ptr{AssembleParams}, Ptr{Ptr{Float64}}, Ptr{Ptr{Float64}}, Ptr{Int32}),
+        h.ptr, stream, Int32(length(params)), params, nzp, fp, id)
+    check(rc, h.ptr)
+    g = AssemblyGraph(id[], h, stream, Any[steps, nzvals, fs])
+    finalizer(x -> ccall((:fe_graph_destroy, LIB), Cint, (Ptr{Cvoid}, Int32), x.h.ptr, x.id), g)
+    return g
+end
+
+"""
+    replay!(g::AssemblyGraph; async=false)
+
+fe_graph_replay: all captured assemblies, reading the current contents of their buffers.
+"""
+function replay!(g::AssemblyGraph; async::Bool=false)
+    rc = GC.@preserve g ccall((:fe_graph_replay, LIB), Cint, (Ptr{Cvoid}, Int32, Ptr{Cvoid}, UInt32),
+                              g.h.ptr, g.id, g.stream, async ? FE_ASYNC : UInt32(0))
+    check(rc, g.h.ptr)
+    return g
+end
+
+const FE_TUNE_MAX = 16
+struct TuneResult
+    n_candidates::Int32
+    stage_cap::NTuple{FE_TUNE_MAX,Int32}
+    ms::NTuple{FE_TUNE_MAX,Float64}
+    n_tiles::NTuple{FE_TUNE_MAX,Int64}
+    n_cell_visits::NTuple{FE_TUNE_MAX,Int64}
+    best_stage_cap::Int32
+    best_ms::Float64
+end
+
+"""
+    autotune!(h, nzval, f; stage_caps=nothing, reps=3, physics, p0, p1, body, cell_scale, u, precision)
+
+fe_autotune: re-plan the handle for each candidate staging capacity (tile size), time `reps`
+assemblies of these parameters and keep the fastest plan. Returns a NamedTuple with the
+candidates, their times and the chosen capacity.
+"""
+function autotune!(h::Handle, nzval, f; stage_caps=nothing, reps::Integer=3, physics=FE_LINEAR_ELASTIC, p0=1.0,
+                   p1=0.3, body=(0.0, 0.0, 0.0), cell_scale=nothing, u=nothing, precision=FE_PREC_MIXED)
+    par = Ref(AssembleParams(physics, precision, FE_FILLZERO, p0, p1, Tuple(Float64.(body)), _ptr(cell_scale),
+                             _ptr(u), 0.0, C_NULL))
+    caps = stage_caps === nothing ? Int32[] : Vector{Int32}(stage_caps)
+    res = Ref{TuneResult}()
+    rc = GC.@preserve nzval f cell_scale u caps ccall((:fe_autotune, LIB), Cint,
+        (Ptr{Cvoid}, Ptr{AssembleParams}, Ptr{Float64}, Ptr{Float64}, Int32, Ptr{Int32}, Int32, Ptr{TuneResult}),
+        h.ptr, par, _ptr(nzval), _ptr(f), Int32(length(caps)), isempty(caps) ? Ptr{Int32}(C_NULL) : pointer(caps),
+        Int32(reps), res)
+    check(rc, h.ptr)
+    r = res[]
+    n = Int(r.n_candidates)
+    return (stage_caps=collect(r.stage_cap[1:n]), ms=collect(r.ms[1:n]), n_tiles=collect(r.n_tiles[1:n]),
+            best_stage_cap=Int(r.best_stage_cap), best_ms=r.best_ms)
 end
 
 end # module

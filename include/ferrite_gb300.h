@@ -357,8 +357,9 @@ int fe_assemble_noalloc(fe_handle* h, const fe_assemble_params* params, double* 
 
 /* Adjoint of the assembly: vector-Jacobian products of Phi = lambda^T (K(X, s) u - f(X)).
  * No counterpart in the reference (Ferrite has no adjoint); the Julia binding exposes it as the
- * pullback of assemble_csc! (a ChainRulesCore.rrule), replacing differentiation of the cell
- * loop of docs/src/literate-gallery/topology_optimization.jl:347-383 (SIMP: s_e = rho_e^p).
+ * pullback of residual(h, K, s, u) = K(s) u - f (a ChainRulesCore.rrule), replacing
+ * differentiation of the cell loop of docs/src/literate-gallery/topology_optimization.jl:347-383
+ * (SIMP: s_e = rho_e^p).
  *   physics      FE_HEAT (p0 = k, p1 = source) or FE_LINEAR_ELASTIC (p0 = E, p1 = nu, body)
  *   cell_scale   per Ferrite cell material factor s_e (E_e = s_e p0; NULL = 1)
  *   dscale       per Ferrite cell ds_e/drho_e (NULL = 1: d_rho is then dPhi/ds_e)
