@@ -938,7 +938,7 @@ def config_mixed_graph(fg, stream, steps=20, oracle=True):
     nz = torch.empty(h.nnz, dtype=torch.float64, device="cuda")
     f = torch.empty(dh.ndofs, dtype=torch.float64, device="cuda")
     kw = dict(physics=fg.NEO_HOOKE, p0=1.0, p1=10.0, body=(0.0, 0.0, 0.0))
-    tune = h.autotune(nz, f, stage_caps=[8192, 12288, 16384], reps=2, stream=stream, u=us[0], **kw)
+    tune = h.autotune(nz, f, stage_caps=[12288, 16384, 24576], reps=2, stream=stream, u=us[0], **kw)
     single = _timed(stream, lambda: h.assemble(nz, f, u=us[0], stream=stream, sync=False, **kw), 5)
     h.sync()
     gid = h.graph_capture([dict(u=u, **kw) for u in us], [nz] * steps, [f] * steps, stream)
@@ -982,8 +982,10 @@ def config_mixed_graph(fg, stream, steps=20, oracle=True):
            "wedge": len(wedges), "ndofs": dh.ndofs, "nnz": h.nnz, "steps_per_graph": steps,
            "graph_replay_ms": replay, "ms_per_assembly_in_graph": replay / steps,
            "Melem_s_in_graph": n_cells * steps / (replay * 1e-3) / 1e6, "ms_single_assembly": single,
-           "autotune": {"best_stage_cap": tune["best_stage_cap"],
-                        "candidates": [{"stage_cap": c, "ms": ms, "tiles": t} for c, ms, t, _ in tune["candidates"]]},
+           "autotune": {"best_stage_cap": tune["best_stage_cap"], "best_form_mask": tune["best_form_mask"],
+                        "form_mask_bits": "bit 0 hex, bit 1 tet, bit 2 wedge subdomain in the two-phase form",
+                        "candidates": [{"stage_cap": c, "ms": ms, "tiles": t, "form_mask": m}
+                                       for c, ms, t, _, m in tune["candidates"]]},
            "tiles": info["n_tiles"], "cell_visits_per_cell": info["n_cell_visits"] / n_cells,
            "mixed_vs_fp64_rel_frobenius": err, "oracle_parity": parity, "e2e": e2e,
            "roofline": {"bound": "hbm", "achieved": balg / (replay / steps * 1e-3) / 1e9, "peak": hbm_peak_gbs(),

@@ -101,7 +101,8 @@ class TuneResult(ctypes.Structure):
     _fields_ = [("n_candidates", ctypes.c_int32), ("stage_cap", ctypes.c_int32 * TUNE_MAX),
                 ("ms", ctypes.c_double * TUNE_MAX), ("n_tiles", ctypes.c_int64 * TUNE_MAX),
                 ("n_cell_visits", ctypes.c_int64 * TUNE_MAX), ("best_stage_cap", ctypes.c_int32),
-                ("best_ms", ctypes.c_double)]
+                ("best_ms", ctypes.c_double), ("form_mask", ctypes.c_uint32 * TUNE_MAX),
+                ("best_form_mask", ctypes.c_uint32)]
 
 
 class ErrorInfo(ctypes.Structure):
@@ -549,8 +550,10 @@ class Handle:
         return p
 
     def autotune(self, nzval, f, stage_caps=None, reps: int = 3, stream=None, **assemble_kw):
-        """fe_autotune: re-plan with each candidate staging capacity, time it, keep the fastest.
-        Returns {"best_stage_cap", "best_ms", "candidates": [(cap, ms, tiles, visits), ...]}."""
+        """fe_autotune: re-plan with each candidate staging capacity, time every form mask (bit s:
+        subdomain s two-phase) unless ``form`` names one, keep the fastest plan and form.
+        Returns {"best_stage_cap", "best_ms", "best_form_mask", "candidates": [(cap, ms, tiles,
+        visits, form_mask), ...]} (per capacity its fastest form)."""
         if stream is not None and hasattr(stream, "cuda_stream"):
             stream = stream.cuda_stream
         self._check_outputs(nzval, f)
@@ -565,8 +568,10 @@ class Handle:
         rc = lib().fe_autotune(self._h, ctypes.byref(p), _ptr(nzval), _ptr(f), n, caps, int(reps), ctypes.byref(res))
         if rc != FE_OK:
             self._raise(rc)
-        cands = [(res.stage_cap[k], res.ms[k], res.n_tiles[k], res.n_cell_visits[k]) for k in range(res.n_candidates)]
-        return {"best_stage_cap": res.best_stage_cap, "best_ms": res.best_ms, "candidates": cands}
+        cands = [(res.stage_cap[k], res.ms[k], res.n_tiles[k], res.n_cell_visits[k], res.form_mask[k])
+                 for k in range(res.n_candidates)]
+        return {"best_stage_cap": res.best_stage_cap, "best_ms": res.best_ms, "best_form_mask": res.best_form_mask,
+                "candidates": cands}
 
     def graph_capture(self, steps, nzvals, fs, stream):
         """fe_graph_capture: steps = list of dicts of assemble() keywords (physics, p0, p1, body,

@@ -130,6 +130,13 @@ struct fe_handle {
     const void* fitted_fn = nullptr;  // kernel and form (two-phase subdomains) the plan was last fitted to
     unsigned fitted_mask = 0;
     bool plan_pinned = false;         // staging capacity set by the caller or the autotuner
+    // form chosen by fe_autotune (bit s: subdomain s two-phase) for its physics and precision,
+    // used when a call names no form; force_mask overrides everything while the tuner times
+    bool tuned_valid = false;
+    int32_t tuned_phys = 0, tuned_prec = 0;
+    unsigned tuned_mask = 0;
+    bool force_on = false;
+    unsigned force_mask = 0;
     const void* occ_fn = nullptr;    // occupancy of the last launch configuration
     int occ_smem = -1, occ_per_sm = 1;
     int accumulate_status = 0;       // a pending FE_ASYNC assembly's status is still being collected
@@ -909,10 +916,17 @@ static int assemble_common(fe_handle* h, const fe_assemble_params* p, double* nz
     }
     // two-phase form per subdomain: quadratic elements by default (their geometry would be
     // recomputed in every tile that owns one of their ~27 dof entities)
+    // (or the form fe_autotune chose for this physics and precision, when the call names none)
     unsigned ea_mask = 0;
     bool all_ea = true;
+    const bool named = (p->flags & (FE_TWO_PHASE | FE_FUSED)) != 0;
+    const bool tuned = !named && h->tuned_valid && h->tuned_phys == p->physics && h->tuned_prec == p->precision;
     for (int s = 0; s < (int)hp.subs.size() && !eo; ++s) {
-        if (hp.subs[s].n_cells > 0 && ((p->flags & FE_TWO_PHASE) || (!(p->flags & FE_FUSED) && hp.subs[s].nb > 16)))
+        bool two;
+        if (h->force_on) two = (h->force_mask >> s) & 1u;
+        else if (tuned) two = (h->tuned_mask >> s) & 1u;
+        else two = (p->flags & FE_TWO_PHASE) || (!(p->flags & FE_FUSED) && hp.subs[s].nb > 16);
+        if (hp.subs[s].n_cells > 0 && two)
             ea_mask |= 1u << s;
         else if (hp.subs[s].n_cells > 0)
             all_ea = false;
@@ -1348,14 +1362,24 @@ int fe_autotune(fe_handle* h, const fe_assemble_params* p, double* nzval, double
     if (reps < 1) reps = 3;
     *out = fe_tune_result{};
     if (h->pending) fe_sync(h);
+    // forms: the one the call names, else every assignment of the subdomains (cell types) to
+    // the fused or the two-phase form (bit s of a mask: subdomain s two-phase)
+    const int n_sub = (int)h->hp.subs.size();
+    const unsigned all = (1u << n_sub) - 1u;
+    std::vector<unsigned> masks;
+    if (p->flags & FE_TWO_PHASE) masks = {all};
+    else if (p->flags & FE_FUSED) masks = {0u};
+    else
+        for (unsigned m = 0; m <= all; ++m) masks.push_back(m);
     cudaStream_t st = (cudaStream_t)p->stream;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     fe_assemble_params q = *p;
-    q.flags = (q.flags & ~(uint32_t)(FE_PROFILE)) | FE_ASYNC;
+    q.flags = (q.flags & ~(uint32_t)(FE_PROFILE | FE_TWO_PHASE | FE_FUSED)) | FE_ASYNC;
     double best_ms = 1e300;
     int32_t best_cap = h->stage_cap;
+    unsigned best_mask = 0;
     int rc = FE_OK;
     for (int32_t k = 0; k < n_candidates && rc == FE_OK; ++k) {
         out->stage_cap[k] = stage_caps[k];
@@ -1371,32 +1395,42 @@ int fe_autotune(fe_handle* h, const fe_assemble_params* p, double* nzval, double
         h->stage_cap = opt.stage_cap;
         out->n_tiles[k] = h->plan.n_tiles;
         out->n_cell_visits[k] = h->plan.visits;
-        // one warm-up, then reps timed assemblies; a candidate whose tiles do not fit shared
-        // memory is skipped
-        if (fe_assemble(h, &q, nzval, f) != FE_OK || fe_sync(h) != FE_OK) {
-            h->last = fe_error_info{};
-            continue;
+        for (const unsigned m : masks) {
+            h->force_on = true;
+            h->force_mask = m;
+            // one warm-up, then reps timed assemblies; a form whose tiles do not fit shared
+            // memory is skipped
+            if (fe_assemble(h, &q, nzval, f) != FE_OK || fe_sync(h) != FE_OK) {
+                h->last = fe_error_info{};
+                continue;
+            }
+            cudaEventRecord(e0, st);
+            for (int32_t r = 0; r < reps && rc == FE_OK; ++r) rc = fe_assemble(h, &q, nzval, f);
+            cudaEventRecord(e1, st);
+            if (rc != FE_OK) break;
+            rc = fe_sync(h);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            const double per = ms / reps;
+            if (out->ms[k] < 0 || per < out->ms[k]) {
+                out->ms[k] = per;
+                out->form_mask[k] = m;
+            }
+            if (per < best_ms) {
+                best_ms = per;
+                best_cap = stage_caps[k];
+                best_mask = m;
+            }
         }
-        cudaEventRecord(e0, st);
-        for (int32_t r = 0; r < reps && rc == FE_OK; ++r) rc = fe_assemble(h, &q, nzval, f);
-        cudaEventRecord(e1, st);
-        if (rc != FE_OK) break;
-        rc = fe_sync(h);
-        float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
-        out->ms[k] = ms / reps;
-        out->n_candidates = k + 1;
-        if (ms / reps < best_ms) {
-            best_ms = ms / reps;
-            best_cap = stage_caps[k];
-        }
+        h->force_on = false;
     }
+    h->force_on = false;
     out->n_candidates = n_candidates;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc != FE_OK) return rc;
     if (best_ms == 1e300) return set_error(h, FE_ERR_UNSUPPORTED, "autotune: no candidate ran");
-    // keep the fastest plan
+    // keep the fastest plan and form
     if (best_cap != h->stage_cap) {
         PlanOptions opt;
         opt.stage_cap = best_cap;
@@ -1409,8 +1443,13 @@ int fe_autotune(fe_handle* h, const fe_assemble_params* p, double* nzval, double
         if (ce != cudaSuccess) return cuda_fail(h, ce, "autotune: upload plan");
         h->stage_cap = best_cap;
     }
+    h->tuned_valid = true;
+    h->tuned_phys = p->physics;
+    h->tuned_prec = p->precision;
+    h->tuned_mask = best_mask;
     out->best_stage_cap = best_cap;
     out->best_ms = best_ms;
+    out->best_form_mask = best_mask;
     return FE_OK;
 }
 

@@ -55,7 +55,12 @@ static_assert(ElemT<KIND_TRI3>::GS == GROUP_LANES[KIND_TRI3] && ElemT<KIND_QUAD4
               "lane groups agree with the planner");
 
 constexpr int PHYS_HEAT = 1, PHYS_ELASTIC = 2, PHYS_NEO = 3;
-constexpr int NEO_EXTRA = 32;  // per (cell, qp): T = S + c1 C^-1 (9), B = F^-T (9), c1, 2c2, P (9), pad
+constexpr int NEO_POINT = 29;  // neo_hooke_point output: T = S + c1 C^-1 (9), B = F^-T (9), c1, 2c2, P (9)
+// Neo-Hooke cell-table entries per quadrature-point pair (values of the two points
+// interleaved): T's six distinct entries (T is symmetric: S and C^-1 are), c1, 2c2, then
+// s P (9) for the residual
+constexpr int NEO_PAIR = 34;
+constexpr int NEO_T = 0, NEO_C1 = 12, NEO_C2 = 14, NEO_SP = 16;
 constexpr int THREADS = CTA_THREADS;
 
 struct __align__(16) D4 {
@@ -255,6 +260,8 @@ __device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return __
 __device__ __forceinline__ double2 pfma(double2 a, double2 b, double2 c) {
     return make_double2(fma(a.x, b.x, c.x), fma(a.y, b.y, c.y));
 }
+__device__ __forceinline__ float2 pmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ double2 pmul(double2 a, double2 b) { return make_double2(a.x * b.x, a.y * b.y); }
 template <typename P> __device__ __forceinline__ P pzero();
 template <> __device__ __forceinline__ float2 pzero<float2>() { return make_float2(0.f, 0.f); }
 template <> __device__ __forceinline__ double2 pzero<double2>() { return make_double2(0.0, 0.0); }
@@ -285,7 +292,9 @@ __host__ __device__ constexpr ShapeQ shape_q(int nb, int ng, int dim, int real_b
 //   grad[NQP][SP]    : at p*SP + i*6: (gx0, gx1, gy0, gy1, gz0, gz1), g = sqrt(detJ w) gradN
 //   sq[NQP][2]       : sqrt(detJ w) per point
 //   cellp[4]         : per-cell material values
-//   neo[NQ][NEO_EXTRA] (Neo-Hooke only)
+//   Neo-Hooke only:
+//   bgrad[NQP][SP]   : B g per point and base function, laid out as grad (B = F^-T)
+//   pairs[NQP][NEO_PAIR] : per point pair, T (6), c1, 2c2, s P (9), the two points interleaved
 // SP (>= 6 NB) is chosen so that the lanes of a warp (lane = point, GS lanes per group, group
 // tables GS words apart modulo 32) write their values to distinct shared-memory banks.
 __host__ __device__ constexpr int table_sp(int nb, int nqp, int gs) {
@@ -312,7 +321,7 @@ struct CellTable {
     static constexpr int SP = table_sp(NB, NQP, GS);
     static constexpr int GRAD = NQP * SP;
     static constexpr int SQ = NQP * 2;
-    static constexpr int NEO = PHYS == PHYS_NEO ? NQ * NEO_EXTRA : 0;
+    static constexpr int NEO = PHYS == PHYS_NEO ? NQP * SP + NQP * NEO_PAIR : 0;
     static constexpr int USED = GRAD + SQ + 4 + NEO;
     // group stride = GS (mod 32) elements
     static constexpr int REALS = USED + ((GS % 32 - USED % 32) + 32) % 32;
@@ -532,8 +541,35 @@ __device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev
         const Real is = s > Real(0) ? Real(1) / s : Real(0);
         #pragma unroll
         for (int t = 0; t < 9; ++t) H[t] *= is;
-        neo_hooke_point<Real>(pconst<Real>(a.phys.p0, a.phys.p0_f), pconst<Real>(a.phys.p1, a.phys.p1_f), H,
-                              neo + q * NEO_EXTRA);
+        Real nq[NEO_POINT];
+        neo_hooke_point<Real>(pconst<Real>(a.phys.p0, a.phys.p0_f), pconst<Real>(a.phys.p1, a.phys.p1_f), H, nq);
+        // the point's entries of the pair table (a padded partner point gets zeros)
+        if (lead) {
+            Real* pp = neo + CT::GRAD + p * NEO_PAIR;
+            constexpr int TK[6] = {0, 4, 8, 1, 2, 5};  // T00, T11, T22, T01, T02, T12
+            #pragma unroll
+            for (int k = 0; k < 6; ++k) pp[NEO_T + 2 * k + hh] = nq[TK[k]];
+            pp[NEO_C1 + hh] = nq[18];
+            pp[NEO_C2 + hh] = nq[19];
+            #pragma unroll
+            for (int k = 0; k < 9; ++k) pp[NEO_SP + 2 * k + hh] = s * nq[20 + k];
+            if (pad) {
+                #pragma unroll
+                for (int k = 0; k < NEO_PAIR / 2; ++k) pp[2 * k + 1] = Real(0);
+            }
+        }
+        // B g_i of this point for the base functions this group writes (B = F^-T): the
+        // gradients written above are read back by the same lane
+        #pragma unroll
+        for (int i = 0; i < NB; ++i) {
+            if (i < i0 || i >= i1) continue;
+            const Real* gs = grad + p * CT::SP + i * 6 + hh;
+            const Real gx = gs[0], gy = gs[2], gz = gs[4];
+            Real* bd = neo + p * CT::SP + i * 6 + hh;
+            #pragma unroll
+            for (int x = 0; x < 3; ++x) bd[2 * x] = nq[9 + 3 * x] * gx + nq[9 + 3 * x + 1] * gy + nq[9 + 3 * x + 2] * gz;
+            if (pad) { bd[1] = Real(0); bd[3] = Real(0); bd[5] = Real(0); }
+        }
     }
 }
 
@@ -732,7 +768,54 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
         // one item at a time (two interleaved items measured slower: more instructions, same
         // registers)
         for (int it = it0; it < it1; ++it) items_m(std::integral_constant<int, 1>{}, it);
-    } else {  // PHYS_NEO: per item and point, scalar
+    } else {  // PHYS_NEO
+        // K_ab(i, j) = sum_q delta_ab g_i.T g_j + c1 (B g_j)_a (B g_i)_b + 2c2 (B g_i)_a (B g_j)_b
+        // (hyperelasticity.jl:254-276 with dP/dF from 157-176). The row lane keeps, per point
+        // pair, its own B g_i and h_i = T g_i (T symmetric) and computes its residual entry
+        // once; per item it reads the column's g_j and B g_j and runs the point pairs packed.
+        const Real* bgt = neo;               // B g, laid out as grad
+        const Real* pt = neo + CT::GRAD;     // per pair: T, c1, 2c2, s P
+        P bgi[NQP][3], hi[NQP][3];
+        P fr[3] = {pzero<P>(), pzero<P>(), pzero<P>()};
+        #pragma unroll
+        for (int p = 0; p < NQP; ++p) {
+            const Real* pp = pt + p * NEO_PAIR;
+            P g[3], T6[6], sP[9];
+            #pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                g[c] = *(const P*)(grad + p * CT::SP + i * 6 + 2 * c);
+                bgi[p][c] = *(const P*)(bgt + p * CT::SP + i * 6 + 2 * c);
+            }
+            #pragma unroll
+            for (int k = 0; k < 6; ++k) T6[k] = *(const P*)(pp + NEO_T + 2 * k);
+            #pragma unroll
+            for (int k = 0; k < 9; ++k) sP[k] = *(const P*)(pp + NEO_SP + 2 * k);
+            // T rows from its distinct entries (T00, T11, T22, T01, T02, T12)
+            const P Tr[3][3] = {{T6[0], T6[3], T6[4]}, {T6[3], T6[1], T6[5]}, {T6[4], T6[5], T6[2]}};
+            #pragma unroll
+            for (int x = 0; x < 3; ++x) {
+                P h = pzero<P>(), r = fr[x];
+                #pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    h = pfma(Tr[x][c], g[c], h);
+                    r = pfma(sP[x * 3 + c], g[c], r);
+                }
+                hi[p][x] = h;
+                fr[x] = r;
+            }
+        }
+        // residual of the lane's own base function: sum_q s P g_i - s^2 N_i b
+        Real fe_own[3];
+        {
+            Real nw = Real(0);
+            #pragma unroll
+            for (int q = 0; q < NQ; ++q) {
+                const Real s = sq[q];
+                nw += s * s * shp[q * SQL.qs + SQL.n + i];
+            }
+            #pragma unroll
+            for (int x = 0; x < 3; ++x) fe_own[x] = (fr[x].x + fr[x].y) - nw * pconst<Real>(a.phys.body[x], a.phys.body_f[x]);
+        }
         for (int it = it0; it < it1; ++it) {
             int j = it, fslot = 0, slot = 0;
             if constexpr (EA == 0) {
@@ -741,42 +824,37 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
                 fslot = (int)(word >> 16);
                 slot = slot_rows[(it - it0) * NB + i];
             }
-            Real Kb[NC_MAX * NC_MAX];
-            Real fe[NC_MAX];
+            P K[3][3], t = pzero<P>();
             #pragma unroll
-            for (int t = 0; t < NC_MAX * NC_MAX; ++t) Kb[t] = Real(0);
-            #pragma unroll
-            for (int t = 0; t < NC_MAX; ++t) fe[t] = Real(0);
-            #pragma unroll 1
-            for (int q = 0; q < NQ; ++q) {
-                const int p = q >> 1, h = q & 1;
-                const Real* gio = grad + p * CT::SP + i * 6 + h;
-                const Real* gjo = grad + p * CT::SP + j * 6 + h;
-                const Real ai[3] = {gio[0], gio[2], gio[4]}, aj[3] = {gjo[0], gjo[2], gjo[4]};
-                const Real s = sq[q];
-                const Real nj = shp[q * SQL.qs + SQL.n + j] * s;
-                const Real* nq_ = neo + q * NEO_EXTRA;
-                Real Bi[3], Bj[3], tij = 0;
+            for (int x = 0; x < 3; ++x)
                 #pragma unroll
-                for (int x = 0; x < 3; ++x) {
-                    Bi[x] = nq_[9 + x * 3] * ai[0] + nq_[9 + x * 3 + 1] * ai[1] + nq_[9 + x * 3 + 2] * ai[2];
-                    Bj[x] = nq_[9 + x * 3] * aj[0] + nq_[9 + x * 3 + 1] * aj[1] + nq_[9 + x * 3 + 2] * aj[2];
-                    tij += ai[x] * (nq_[x * 3] * aj[0] + nq_[x * 3 + 1] * aj[1] + nq_[x * 3 + 2] * aj[2]);
+                for (int y = 0; y < 3; ++y) K[x][y] = pzero<P>();
+            #pragma unroll
+            for (int p = 0; p < NQP; ++p) {
+                const Real* pp = pt + p * NEO_PAIR;
+                const P c1 = *(const P*)(pp + NEO_C1), c2 = *(const P*)(pp + NEO_C2);
+                P gj[3], c1b[3], c2b[3];
+                #pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    gj[c] = *(const P*)(grad + p * CT::SP + j * 6 + 2 * c);
+                    const P b = *(const P*)(bgt + p * CT::SP + j * 6 + 2 * c);
+                    c1b[c] = pmul(c1, b);
+                    c2b[c] = pmul(c2, b);
                 }
-                const Real c1 = nq_[18], c2x2 = nq_[19];
-                // K_ab += delta_ab giT.T.gj + c1 (B gi)_b (B gj)_a + 2c2 (B gi)_a (B gj)_b
+                #pragma unroll
+                for (int c = 0; c < 3; ++c) t = pfma(hi[p][c], gj[c], t);
                 #pragma unroll
                 for (int x = 0; x < 3; ++x)
                     #pragma unroll
-                    for (int y = 0; y < 3; ++y)
-                        Kb[x * 3 + y] += (x == y ? tij : Real(0)) + c1 * Bi[y] * Bj[x] + c2x2 * Bi[x] * Bj[y];
-                // residual: (gradN_j : P - N_j b) dV
-                #pragma unroll
-                for (int x = 0; x < 3; ++x)
-                    fe[x] += s * (nq_[20 + x * 3] * aj[0] + nq_[20 + x * 3 + 1] * aj[1] + nq_[20 + x * 3 + 2] * aj[2] -
-                                  nj * pconst<Real>(a.phys.body[x], a.phys.body_f[x]));
+                    for (int y = 0; y < 3; ++y) K[x][y] = pfma(bgi[p][x], c2b[y], pfma(c1b[x], bgi[p][y], K[x][y]));
             }
-            store_block(j, fslot, slot, Kb, fe);
+            Real Kb[NC_MAX * NC_MAX];
+            const Real tij = t.x + t.y;
+            #pragma unroll
+            for (int x = 0; x < 3; ++x)
+                #pragma unroll
+                for (int y = 0; y < 3; ++y) Kb[x * 3 + y] = (K[x][y].x + K[x][y].y) + (x == y ? tij : Real(0));
+            store_block(j, fslot, slot, Kb, fe_own);
         }
     }
 }

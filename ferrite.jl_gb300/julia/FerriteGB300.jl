@@ -505,14 +505,17 @@ struct TuneResult
     n_cell_visits::NTuple{FE_TUNE_MAX,Int64}
     best_stage_cap::Int32
     best_ms::Float64
+    form_mask::NTuple{FE_TUNE_MAX,UInt32}
+    best_form_mask::UInt32
 end
 
 """
     autotune!(h, nzval, f; stage_caps=nothing, reps=3, physics, p0, p1, body, cell_scale, u, precision)
 
 fe_autotune: re-plan the handle for each candidate staging capacity (tile size), time `reps`
-assemblies of these parameters and keep the fastest plan. Returns a NamedTuple with the
-candidates, their times and the chosen capacity.
+assemblies of these parameters for every assignment of the SubDofHandlers (cell types) to the
+fused or two-phase form, and keep the fastest plan and form. Returns a NamedTuple with the
+candidates, their times, the chosen capacity and form mask (bit s: SubDofHandler s two-phase).
 """
 function autotune!(h::Handle, nzval, f; stage_caps=nothing, reps::Integer=3, physics=FE_LINEAR_ELASTIC, p0=1.0,
                    p1=0.3, body=(0.0, 0.0, 0.0), cell_scale=nothing, u=nothing, precision=FE_PREC_MIXED)
@@ -528,7 +531,8 @@ function autotune!(h::Handle, nzval, f; stage_caps=nothing, reps::Integer=3, phy
     r = res[]
     n = Int(r.n_candidates)
     return (stage_caps=collect(r.stage_cap[1:n]), ms=collect(r.ms[1:n]), n_tiles=collect(r.n_tiles[1:n]),
-            best_stage_cap=Int(r.best_stage_cap), best_ms=r.best_ms)
+            form_masks=collect(r.form_mask[1:n]), best_stage_cap=Int(r.best_stage_cap), best_ms=r.best_ms,
+            best_form_mask=r.best_form_mask)
 end
 
 end # module

@@ -400,12 +400,16 @@ int fe_graph_capture(fe_handle* h, void* stream, int32_t n_steps, const fe_assem
 int fe_graph_replay(fe_handle* h, int32_t graph, void* stream, uint32_t flags);
 int fe_graph_destroy(fe_handle* h, int32_t graph);
 
-/* Autotuner of the tile plan: for each candidate staging capacity (values per tile, which sets
- * the tile size and hence the cells recomputed at tile borders and the CTAs that fit per SM),
- * re-plan the handle, time `reps` assemblies of `params` (after one warm-up) with CUDA events,
- * and keep the fastest plan for later calls. stage_caps NULL: a built-in candidate list.
- * Candidates whose tiles do not fit shared memory are skipped (ms = -1). nzval and f receive
- * the assembled values. No counterpart in the reference. */
+/* Autotuner of the tile plan and of the assembly form per cell type: for each candidate
+ * staging capacity (values per tile, which sets the tile size and hence the cells recomputed
+ * at tile borders and the CTAs that fit per SM), re-plan the handle and time `reps` assemblies
+ * of `params` (after one warm-up) with CUDA events for each form mask: bit s set = subdomain s
+ * (one SubDofHandler, one cell type) in the two-phase form, clear = fused. If params->flags
+ * names FE_FUSED or FE_TWO_PHASE only that form is timed, else every mask. The fastest plan is
+ * kept, and its form is used by later calls with the same physics and precision that name no
+ * form. stage_caps NULL: a built-in candidate list. Per capacity, ms and form_mask are those
+ * of its fastest form; candidates whose tiles do not fit shared memory are skipped (ms = -1).
+ * nzval and f receive the assembled values. No counterpart in the reference. */
 #define FE_TUNE_MAX 16
 typedef struct {
     int32_t n_candidates;
@@ -415,6 +419,8 @@ typedef struct {
     int64_t n_cell_visits[FE_TUNE_MAX];
     int32_t best_stage_cap;
     double best_ms;
+    uint32_t form_mask[FE_TUNE_MAX];   /* fastest form per capacity (bit s: subdomain s two-phase) */
+    uint32_t best_form_mask;
 } fe_tune_result;
 
 int fe_autotune(fe_handle* h, const fe_assemble_params* params, double* nzval, double* f, int32_t n_candidates,

@@ -86,7 +86,8 @@ def test_autotune_keeps_fastest_plan_and_results(built, oracle, torch_cuda):
     nz0, f0 = nz.clone(), f.clone()
     res = h.autotune(nz, f, stage_caps=[4096, 8192, 12288], reps=2, **kw)
     assert res["best_stage_cap"] in (4096, 8192, 12288)
-    assert all(ms > 0 for _, ms, _, _ in res["candidates"])
+    assert all(c[1] > 0 for c in res["candidates"])
+    assert res["best_form_mask"] in (0, 1)  # one subdomain: fused or two-phase
     assert res["candidates"][0][2] > res["candidates"][2][2]  # smaller tiles, more of them
     nz.zero_()
     f.zero_()
@@ -120,3 +121,35 @@ def test_graph_replay_two_phase_tensor_core(built, oracle, torch_cuda):
     h.assemble(ref2, fr, cell_scale=scales[1], **kw)
     assert torch.equal(nz, ref1) and torch.equal(nz2, ref2) and torch.equal(f, fr)
     h.graph_destroy(gid)
+
+
+def test_autotune_chooses_a_form_per_cell_type(built, oracle, torch_cuda):
+    """On a hexahedron / tetrahedron / wedge grid (three SubDofHandlers) the tuner times every
+    assignment of the cell types to the fused or two-phase form; all of them give the same bits
+    (the element math is the same on the CUDA cores), and later calls without a form use the
+    chosen one."""
+    from test_gpu_parity import mixed_problem
+    torch = torch_cuda
+    fg, O = built, oracle
+    prob = mixed_problem(O, nel=(9, 4, 4), seed=6)
+    h = make_handle(fg, O, prob)
+    rng = np.random.default_rng(3)
+    u = torch.as_tensor(0.02 * rng.uniform(-1, 1, prob.ndofs), device="cuda")
+    nz = torch.zeros(prob.nnz, dtype=torch.float64, device="cuda")
+    f = torch.zeros(prob.ndofs, dtype=torch.float64, device="cuda")
+    kw = dict(physics=fg.NEO_HOOKE, p0=1.0, p1=10.0, u=u)
+    h.assemble(nz, f, form="fused", **kw)
+    ref = (nz.clone(), f.clone())
+    res = h.autotune(nz, f, stage_caps=[8192, 12288], reps=1, **kw)  # all 8 form masks per capacity
+    assert 0 <= res["best_form_mask"] < 8
+    assert res["best_form_mask"] in [c[4] for c in res["candidates"]]
+    assert torch.equal(nz, ref[0]) and torch.equal(f, ref[1])  # the tuner's last assembly
+    nz.zero_()
+    f.zero_()
+    h.assemble(nz, f, **kw)  # the tuned form
+    assert torch.equal(nz, ref[0]) and torch.equal(f, ref[1])
+    for form in ("fused", "two_phase"):
+        nz.zero_()
+        f.zero_()
+        h.assemble(nz, f, form=form, **kw)
+        assert torch.equal(nz, ref[0]) and torch.equal(f, ref[1]), form
