@@ -1089,10 +1089,20 @@ __device__ __forceinline__ void reduce_tile(const KernelArgs& a, const char* R, 
                         #pragma unroll
                         for (int t = 0; t < NP; ++t) acc_add2(hi[t], lo[t], v[t]);
                     }
-                    #pragma unroll
-                    for (int t = 0; t < NP; ++t) {
-                        out[2 * t] = pair_to_double_fast(hi[t].x, lo[t].x);
-                        if (2 * t + 1 < NCC) out[2 * t + 1] = pair_to_double_fast(hi[t].y, lo[t].y);
+                    if (a.fillzero && cnt <= 1) {
+                        // a single contribution is its own exact sum: no low word to round in
+                        // (blocks of equal counts are adjacent, so warps take one branch)
+                        #pragma unroll
+                        for (int t = 0; t < NP; ++t) {
+                            out[2 * t] = float_to_double(hi[t].x);
+                            if (2 * t + 1 < NCC) out[2 * t + 1] = float_to_double(hi[t].y);
+                        }
+                    } else {
+                        #pragma unroll
+                        for (int t = 0; t < NP; ++t) {
+                            out[2 * t] = pair_to_double_fast(hi[t].x, lo[t].x);
+                            if (2 * t + 1 < NCC) out[2 * t + 1] = pair_to_double_fast(hi[t].y, lo[t].y);
+                        }
                     }
                 } else {
                     // packed FP32 sums in cell order, each rounded exactly to FP64
