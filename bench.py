@@ -903,7 +903,7 @@ def config_pattern(fg, stream, nel=128):
     return out
 
 
-def config_mixed_graph(fg, stream, steps=20, oracle=True):
+def config_mixed_graph(fg, stream, steps=20, oracle=True, ny=100, tune=True):
     """~2M cells over three x-slabs sharing vertex nodes (Hex Q1 50%, Tet P1 25% as 6 per cube,
     Wedge P1 25% as 2 per cube), compressible Neo-Hooke (mu 1, lambda 10), displacement
     amplitude 0.05 of the cell size h = 0.01 (u = 0.05 h U(-1,1), seeded per step: an absolute
@@ -911,10 +911,11 @@ def config_mixed_graph(fg, stream, steps=20, oracle=True):
     as one CUDA graph and replayed."""
     import torch
     host = __import__("ferrite_gb300.host", fromlist=["host"])
-    nh, nt, nw, ny, nzc = 100, 8, 25, 100, 100
+    nh, nt, nw, nzc = 100, 8, 25, ny
     nx = nh + nt + nw
-    g = host.generate_grid(host.HEXAHEDRON, (nx, ny, nzc), (0, 0, 0), (nx / 100.0, 1, 1))
-    g = host.perturb_interior(g, (nx, ny, nzc), 0.15, SEED + 5, (0, 0, 0), (nx / 100.0, 1, 1))
+    box = (nx / 100.0, ny / 100.0, nzc / 100.0)  # cubes of side 0.01 (the unit-depth box at ny = 100)
+    g = host.generate_grid(host.HEXAHEDRON, (nx, ny, nzc), (0, 0, 0), box)
+    g = host.perturb_interior(g, (nx, ny, nzc), 0.15, SEED + 5, (0, 0, 0), box)
     cubes = g.cells  # [n, 8], 1-based, x fastest
     ix = np.arange(cubes.shape[0]) % nx
     T = np.array([[1, 2, 4, 8], [1, 5, 2, 8], [2, 3, 4, 8], [2, 7, 3, 8], [2, 5, 6, 8], [2, 6, 7, 8]]) - 1
@@ -938,7 +939,10 @@ def config_mixed_graph(fg, stream, steps=20, oracle=True):
     nz = torch.empty(h.nnz, dtype=torch.float64, device="cuda")
     f = torch.empty(dh.ndofs, dtype=torch.float64, device="cuda")
     kw = dict(physics=fg.NEO_HOOKE, p0=1.0, p1=10.0, body=(0.0, 0.0, 0.0))
-    tune = h.autotune(nz, f, stage_caps=[12288, 16384, 24576], reps=2, stream=stream, u=us[0], **kw)
+    if tune:
+        tune = h.autotune(nz, f, stage_caps=[12288, 16384, 24576], reps=2, stream=stream, u=us[0], **kw)
+    else:  # the form and tile size the tuner picks at full size (profiling runs)
+        tune = h.autotune(nz, f, stage_caps=[24576], reps=1, stream=stream, u=us[0], form="two_phase", **kw)
     single = _timed(stream, lambda: h.assemble(nz, f, u=us[0], stream=stream, sync=False, **kw), 5)
     h.sync()
     gid = h.graph_capture([dict(u=u, **kw) for u in us], [nz] * steps, [f] * steps, stream)
@@ -1014,6 +1018,10 @@ def main():
     ap.add_argument("--config", choices=["heat", "q2", "adjoint", "mixed_graph", "elements", "pattern"],
                     help="run only this configuration and print its JSON (profiling runs)")
     ap.add_argument("--q2-nel", type=int, default=64, help="cells per axis of the Q2 configuration")
+    ap.add_argument("--mixed-ny", type=int, default=100,
+                    help="cells along y and z of the mixed-cell configuration (100 = the 1.98M-cell workload)")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="mixed-cell configuration: skip the autotuner, use its full-size choice (profiling runs)")
     args = ap.parse_args()
     if args.config:
         import torch
@@ -1021,7 +1029,8 @@ def main():
         fg.build()
         stream = torch.cuda.Stream()
         fn = {"heat": config_heat, "q2": lambda g, s: config_q2(g, s, nel=args.q2_nel), "adjoint": config_adjoint,
-              "mixed_graph": config_mixed_graph, "elements": config_elements, "pattern": config_pattern}[args.config]
+              "mixed_graph": lambda g, s: config_mixed_graph(g, s, ny=args.mixed_ny, tune=not args.no_tune),
+              "elements": config_elements, "pattern": config_pattern}[args.config]
         print(json.dumps({"config": args.config, "result": fn(fg, stream)}))
         return
     if args.warmup < 3:

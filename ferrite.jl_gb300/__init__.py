@@ -38,6 +38,7 @@ HEAT, LINEAR_ELASTIC, NEO_HOOKE = 1, 2, 3
 PREC_MIXED, PREC_FP64 = 0, 1
 FILLZERO, NO_K, NO_F, ASYNC, PROFILE, COMPENSATED, TWO_PHASE, FUSED, NO_TENSOR = 1, 2, 4, 8, 16, 32, 64, 128, 256
 STAGED_OUTPUT = 512
+FP32_SUM = 1024
 _FORMS = {None: 0, "two_phase": TWO_PHASE, "fused": FUSED, "two_phase_cuda_cores": TWO_PHASE | NO_TENSOR}
 
 EXPORTED = ["fe_abi_version", "fe_create", "fe_assemble", "fe_sync", "fe_last_error", "fe_get_info",
@@ -395,10 +396,11 @@ class Handle:
 
     def assemble(self, nzval, f, physics: int, p0: float, p1: float, body=(0.0, 0.0, 0.0), cell_scale=None, u=None,
                  precision: int = PREC_MIXED, fillzero: bool = True, stream=None, sync: bool = True,
-                 cond_threshold: float = 0.0, profile: bool = False, compensated: bool = False, form=None,
+                 cond_threshold: float = 0.0, profile: bool = False, compensated: bool = True, form=None,
                  staged_output: bool = False):
         """One fe_assemble call. ``stream`` is a torch.cuda.Stream, a raw handle or None.
-        ``compensated`` (mixed precision): sum each entry as a compensated FP32 pair.
+        ``compensated`` (mixed precision): sum each entry as a compensated FP32 pair (FP64-class, the
+        default); False: one plain FP32 sum per entry (FE_FP32_SUM).
         ``staged_output``: host outputs through a device buffer and the copy engine, also when
         they are page-locked (default there: written by the kernels through the mapping).
         ``form``: None (the engine's choice), "two_phase" (element matrices first; on the tensor
@@ -416,8 +418,8 @@ class Handle:
             flags |= ASYNC
         if profile:
             flags |= PROFILE
-        if compensated:
-            flags |= COMPENSATED
+        if not compensated:
+            flags |= FP32_SUM
         if staged_output:
             flags |= STAGED_OUTPUT
         flags |= _FORMS[form]
@@ -536,10 +538,10 @@ class Handle:
 
     @staticmethod
     def _params(physics, p0, p1, body=(0.0, 0.0, 0.0), cell_scale=None, u=None, precision=PREC_MIXED, fillzero=True,
-                cond_threshold=0.0, compensated=False, stream=None, form=None):
+                cond_threshold=0.0, compensated=True, stream=None, form=None):
         p = AssembleParams()
         p.physics, p.precision = physics, precision
-        p.flags = (FILLZERO if fillzero else 0) | (COMPENSATED if compensated else 0) | _FORMS[form]
+        p.flags = (FILLZERO if fillzero else 0) | (0 if compensated else FP32_SUM) | _FORMS[form]
         p.p0, p.p1 = float(p0), float(p1)
         for k in range(3):
             p.body[k] = float(body[k]) if k < len(body) else 0.0

@@ -989,7 +989,7 @@ static int assemble_common(fe_handle* h, const fe_assemble_params* p, double* nz
     A.do_k = do_k;
     A.do_f = do_f;
     A.fillzero = fill;
-    A.compensated = (p->flags & FE_COMPENSATED) != 0;
+    A.compensated = (p->flags & FE_FP32_SUM) == 0;  // compensated unless plain FP32 sums are asked for
     // element-matrix scratch of the two-phase subdomains
     {
         size_t need = 0;
@@ -2016,7 +2016,7 @@ extern "C" int fe_assemble_noalloc(fe_handle* h, const fe_assemble_params* p, do
     A.do_k = do_k;
     A.do_f = do_f;
     A.fillzero = (p->flags & FE_FILLZERO) != 0;
-    A.compensated = (p->flags & FE_COMPENSATED) != 0;
+    A.compensated = (p->flags & FE_FP32_SUM) == 0;  // compensated unless plain FP32 sums are asked for
     Physics& ph = A.phys;
     ph = Physics{};
     ph.kind = p->physics;

@@ -16,5 +16,10 @@ void register_elastic(std::vector<KernelEntry>& out, std::vector<ElemEntry>& eou
     FE_ONE(KIND_TRI3, 3, PHYS_ELASTIC)
     // Q2 quadrilaterals, ip^2, 3x3 Gauss (fused form: 9 base functions)
     FE_ONE(KIND_QUAD9, 9, PHYS_ELASTIC)
+    // several cell types in one launch: hexahedra / tetrahedra / wedges, quadrilaterals / triangles
+    out.push_back(make_entry<KIND_HEX8, 8, KIND_TET4, 1, KIND_WEDGE6, 5, PHYS_ELASTIC, float>());
+    out.push_back(make_entry<KIND_HEX8, 8, KIND_TET4, 1, KIND_WEDGE6, 5, PHYS_ELASTIC, double>());
+    out.push_back(make_entry<KIND_QUAD4, 4, KIND_TRI3, 1, -1, 0, PHYS_ELASTIC, float>());
+    out.push_back(make_entry<KIND_QUAD4, 4, KIND_TRI3, 1, -1, 0, PHYS_ELASTIC, double>());
 }
 }  // namespace fe

@@ -18,6 +18,7 @@ const FE_PREC_MIXED, FE_PREC_FP64 = Int32(0), Int32(1)
 const FE_FILLZERO = UInt32(1)
 const FE_ASYNC = UInt32(8)
 const FE_STAGED_OUTPUT = UInt32(512)
+const FE_FP32_SUM = UInt32(1024)   # plain FP32 sums per entry instead of the compensated default
 
 # raw address of a host Vector or a device array (CuArray's CuPtr is a 64-bit primitive)
 _ptr(x, ::Type{T}=Float64) where {T} = x === nothing ? Ptr{T}(C_NULL) : reinterpret(Ptr{T}, pointer(x))

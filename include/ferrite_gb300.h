@@ -61,8 +61,9 @@ extern "C" {
 #define FE_NEO_HOOKE 3      /* tangent and residual of hyperelasticity.jl:157-276 (cell part) */
 
 /* precision */
-#define FE_PREC_MIXED 0 /* FP32 element math (FP64 Jacobians for flagged cells), FP32 sums per entry, each entry
-                           rounded exactly to FP64; with FE_COMPENSATED the sums are compensated FP32 pairs */
+#define FE_PREC_MIXED 0 /* FP32 element math (FP64 Jacobians for flagged cells); each entry's contributions summed
+                           as a compensated FP32 pair (FP64-class) and rounded exactly to FP64; with FE_FP32_SUM
+                           one plain FP32 sum per entry instead */
 #define FE_PREC_FP64 1  /* the plain FP64 drop-in: all math and accumulation in FP64 */
 
 /* fe_assemble flags */
@@ -72,7 +73,8 @@ extern "C" {
 #define FE_ASYNC 8u    /* do not wait for the kernels; read the status later with fe_sync() */
 #define FE_PROFILE 16u /* bracket the assembly kernel with CUDA events; read with fe_kernel_time() */
 #define FE_COMPENSATED 32u /* FE_PREC_MIXED: sum each entry's contributions as a compensated FP32 pair
-                              (TwoSum, FP64-class summation error) and round the pair exactly to FP64 */
+                              (TwoSum, FP64-class summation error) and round the pair exactly to FP64.
+                              The default; the flag is accepted and changes nothing */
 #define FE_TWO_PHASE 64u   /* element matrices first: one pass per cell writes Ke and fe to a device scratch
                               held by the handle, then the owner tiles load them instead of recomputing the
                               cell's geometry in every tile that owns one of its dofs. The default for
@@ -85,6 +87,9 @@ extern "C" {
 #define FE_STAGED_OUTPUT 512u /* host nzval / f: assemble into a device buffer held by the handle and copy it back
                                  with the copy engine, also for page-locked memory (which by default the kernels
                                  write through its mapping); pageable memory is always staged */
+#define FE_FP32_SUM 1024u     /* FE_PREC_MIXED: one plain FP32 sum per entry, rounded exactly to FP64, instead of
+                                 the compensated pair (about a tenth faster; the summation error is then FP32's,
+                                 ~1e-7 relative, where the element math's own FP32 rounding is of the same order) */
 
 typedef struct fe_handle fe_handle;
 

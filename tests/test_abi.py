@@ -50,7 +50,7 @@ def test_python_constants_match_header(fg):
     defs = {m.group(1): int(m.group(2)) for m in re.finditer(r"#define\s+(FE_[A-Z0-9_]+)\s+(\d+)u?\b", txt)}
     pairs = {"FE_FILLZERO": fg.FILLZERO, "FE_NO_K": fg.NO_K, "FE_NO_F": fg.NO_F, "FE_ASYNC": fg.ASYNC,
              "FE_PROFILE": fg.PROFILE, "FE_COMPENSATED": fg.COMPENSATED, "FE_TWO_PHASE": fg.TWO_PHASE,
-             "FE_FUSED": fg.FUSED, "FE_NO_TENSOR": fg.NO_TENSOR, "FE_STAGED_OUTPUT": fg.STAGED_OUTPUT,
+             "FE_FUSED": fg.FUSED, "FE_NO_TENSOR": fg.NO_TENSOR, "FE_STAGED_OUTPUT": fg.STAGED_OUTPUT, "FE_FP32_SUM": fg.FP32_SUM,
              "FE_PREC_MIXED": fg.PREC_MIXED, "FE_PREC_FP64": fg.PREC_FP64, "FE_HEAT": fg.HEAT,
              "FE_LINEAR_ELASTIC": fg.LINEAR_ELASTIC, "FE_NEO_HOOKE": fg.NEO_HOOKE, "FE_TRIANGLE": fg.TRIANGLE,
              "FE_QUADRILATERAL": fg.QUADRILATERAL, "FE_TETRAHEDRON": fg.TETRAHEDRON, "FE_HEXAHEDRON": fg.HEXAHEDRON,
@@ -61,6 +61,6 @@ def test_python_constants_match_header(fg):
     for code, name in fg.ERROR_NAMES.items():
         assert defs.get("FE_OK" if name == "OK" else "FE_ERR_" + name) == code, name
     flag_names = ("FE_FILLZERO", "FE_NO_K", "FE_NO_F", "FE_ASYNC", "FE_PROFILE", "FE_COMPENSATED", "FE_TWO_PHASE",
-                  "FE_FUSED", "FE_NO_TENSOR", "FE_STAGED_OUTPUT")
+                  "FE_FUSED", "FE_NO_TENSOR", "FE_STAGED_OUTPUT", "FE_FP32_SUM")
     flags = [defs[k] for k in flag_names]
     assert len(set(flags)) == len(flags) and all(f & (f - 1) == 0 for f in flags)  # distinct single bits

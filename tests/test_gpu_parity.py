@@ -2,7 +2,7 @@
 
 Tolerances (relative Frobenius norm of nzval and f against the FP64 oracle):
   * FE_PREC_FP64 (the plain FP64 drop-in):      <= 1e-12
-  * FE_PREC_MIXED (FP32 element math, FP32 sums per entry rounded exactly to FP64): <= 1e-6
+  * FE_PREC_MIXED (FP32 element math, compensated sums per entry rounded exactly to FP64): <= 1e-6
 Sparsity structure and index maps are bit-exact. Runs are bitwise reproducible.
 """
 import numpy as np
@@ -82,7 +82,7 @@ def test_neo_hooke_single_type(built, oracle, ct, qo):
           dict(physics=O.NEO_HOOKE, p0=1.0, p1=10.0, u=u, body=(0, -0.5, 0)), tol={0: 2e-6})
 
 
-def mixed_problem(O, nel=(6, 3, 3), seed=4):
+def mixed_problem(O, nel=(6, 3, 3), seed=4, ncomp=3):
     """Three x-slabs over one node grid: hexahedra, then tetrahedra (6 per cube), then
     wedges (2 per cube), one SubDofHandler each, dofs shared through the vertex dict."""
     nodes, hexes = O.generate_grid(O.HEXAHEDRON, nel, [0, 0, 0], [2, 1, 1])
@@ -107,9 +107,47 @@ def mixed_problem(O, nel=(6, 3, 3), seed=4):
     flat = np.concatenate(cells).astype(np.int64)
     subs = []
     for ct, qo in [(O.HEXAHEDRON, 2), (O.TETRAHEDRON, 1), (O.WEDGE, 2)]:
-        subs.append(O.Subdomain(np.where(types == ct)[0] + 1, 1, 3, qo))
+        subs.append(O.Subdomain(np.where(types == ct)[0] + 1, 1, ncomp, qo))
     prob = O.Problem(nodes, types, off, flat, subs).close().allocate_matrix()
     return prob
+
+
+def mixed_problem_2d(O, nel=(8, 5), seed=7, ncomp=2):
+    """Two x-halves over one node grid: quadrilaterals, then triangles (2 per square), one
+    SubDofHandler each (quadrilaterals 2x2 Gauss, triangles 1 point)."""
+    nodes, quads = O.generate_grid(O.QUADRILATERAL, nel, [0, 0], [2, 1])
+    nodes = O.perturb_interior(nodes, nel, 0.15, seed, [0, 0], [2, 1])
+    i = np.arange(len(quads)) % nel[0]
+    cells, types = [], []
+    for c in np.where(i < nel[0] // 2)[0]:
+        cells.append(quads[c]); types.append(O.QUADRILATERAL)
+    for c in np.where(i >= nel[0] // 2)[0]:
+        q = quads[c]
+        for t in ([0, 1, 2], [0, 2, 3]):
+            cells.append(q[np.array(t)]); types.append(O.TRIANGLE)
+    types = np.array(types, np.int32)
+    off = np.zeros(len(cells) + 1, np.int64)
+    off[1:] = np.cumsum([len(c) for c in cells])
+    flat = np.concatenate(cells).astype(np.int64)
+    subs = [O.Subdomain(np.where(types == ct)[0] + 1, 1, ncomp, qo) for ct, qo in [(O.QUADRILATERAL, 2), (O.TRIANGLE, 1)]]
+    return O.Problem(nodes, types, off, flat, subs).close().allocate_matrix()
+
+
+@pytest.mark.parametrize("dim", [3, 2])
+def test_heat_and_elastic_mixed_cells(built, oracle, dim):
+    """Heat and linear elasticity over grids with several cell types in one launch: hexahedra /
+    tetrahedra / wedges in 3D, quadrilaterals / triangles in 2D (one SubDofHandler per type,
+    dofs shared across the type boundary)."""
+    fg, O = built, oracle
+    make = mixed_problem if dim == 3 else mixed_problem_2d
+    heat = make(O, ncomp=1)
+    check(fg, O, heat, dict(physics=fg.HEAT, p0=2.0, p1=1.0), dict(physics=O.HEAT, p0=2.0, p1=1.0))
+    el = make(O, ncomp=dim)
+    b = (0.0, -1.0, 0.0)[:dim] + (0.0,) * (3 - dim)
+    rng = np.random.default_rng(8)
+    scale = rng.uniform(0.5, 2.0, el.n_cells)
+    check(fg, O, el, dict(physics=fg.LINEAR_ELASTIC, p0=200e3, p1=0.3, body=b, cell_scale=scale),
+          dict(physics=O.LINEAR_ELASTIC, p0=200e3, p1=0.3, body=list(b), cell_scale=scale))
 
 
 def test_neo_hooke_mixed_cells(built, oracle):
