@@ -861,8 +861,21 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
 
 // ---------------------------------------------------------------------------------------
 // two-phase form, phase B: the items' blocks come from the cell's element matrix in global
-// memory (written by element_kernel); lane i = row base function, coalesced over i
+// memory (written by element_kernel); lane i = row base function, coalesced over i. The
+// scratch keeps a column's values in the staging slot's own order (t = y nc + x), so each value
+// is copied global -> shared with cp.async: every lane issues all its copies without waiting,
+// and the tile waits for them once, before the reduce (rows without a pattern entry are loaded
+// into registers instead and checked for non-zeros).
 // ---------------------------------------------------------------------------------------
+template <typename Real>
+__device__ __forceinline__ void async_copy(Real* dst, const Real* src) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+    if constexpr (sizeof(Real) == 4)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+}
+
 template <int K, int PHYS, typename Real>
 __device__ __forceinline__ void gather_blocks(const KernelArgs& a, const SubDev& sd, const char* R, const uint16_t* slot_rows,
                                               Real* stage, int f_off, const Real* __restrict__ ea, int cell, int i, int it0,
@@ -871,29 +884,34 @@ __device__ __forceinline__ void gather_blocks(const KernelArgs& a, const SubDev&
     constexpr int NB = E::NB, NC_MAX = E::DIM;
     constexpr int nc = PHYS == PHYS_HEAT ? 1 : E::DIM;
     constexpr int JS = ea_col_values(NB, nc);
+    constexpr int BSC = (nc * nc + 1) & ~1;
     const uint32_t* items = (const uint32_t*)(R + ((const RecHead*)R)->off_items);
-    #pragma unroll 2
     for (int it = it0; it < it1; ++it) {
         const uint32_t word = items[it];
         const int j = (int)(word & 0xFF);
-        Real Kb[NC_MAX * NC_MAX], fe[NC_MAX];
-        #pragma unroll
-        for (int t = 0; t < NC_MAX * NC_MAX; ++t) Kb[t] = Real(0);
-        #pragma unroll
-        for (int x = 0; x < NC_MAX; ++x) fe[x] = Real(0);
+        const int slot = slot_rows[(it - it0) * NB + i];
         if (a.do_k) {
-            #pragma unroll
-            for (int y = 0; y < nc; ++y)
+            if (slot != SLOT_MISS) {
+                Real* dst = stage + slot * BSC;
                 #pragma unroll
-                for (int x = 0; x < nc; ++x) Kb[x * NC_MAX + y] = __ldcs(ea + j * JS + (y * nc + x) * NB + i);
+                for (int t = 0; t < nc * nc; ++t) async_copy(dst + t, ea + j * JS + t * NB + i);
+            } else {
+                // no pattern entry: allowed only for exact zeros (assembler.jl:413-417, 459-467)
+                #pragma unroll
+                for (int y = 0; y < nc; ++y)
+                    #pragma unroll
+                    for (int x = 0; x < nc; ++x)
+                        if (__ldcs(ea + j * JS + (y * nc + x) * NB + i) != Real(0))
+                            record_miss(a.status, sd.cellid[cell], i * nc + x, j * nc + y);
+            }
         }
         if (a.do_f && i == j) {
+            Real* dst = stage + f_off + (int)(word >> 16) * nc;
             #pragma unroll
-            for (int x = 0; x < nc; ++x) fe[x] = __ldcs(ea + NB * JS + x * NB + i);
+            for (int x = 0; x < nc; ++x) async_copy(dst + x, ea + NB * JS + x * NB + i);
         }
-        stage_block<NC_MAX, nc, Real>(a, sd, stage, f_off, cell, i, j, (int)(word >> 16), slot_rows[(it - it0) * NB + i], Kb,
-                                      fe);
     }
+    asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
 // ---------------------------------------------------------------------------------------
@@ -1320,6 +1338,7 @@ __global__ void __launch_bounds__(THREADS, EAK ? 3 : 2) tile_kernel(const Kernel
                 }
             }
         }
+        asm volatile("cp.async.wait_all;" ::: "memory");  // this thread's slot copies (two-phase form)
         __syncthreads();  // all staging slots written
         if (a.nc == 3) reduce_tile<3, Real>(a, R, stage, (double*)chunk);
         else if (a.nc == 2) reduce_tile<2, Real>(a, R, stage, (double*)chunk);
@@ -1395,15 +1414,31 @@ __global__ void __launch_bounds__(THREADS, 2) element_kernel(const KernelArgs a,
     __syncthreads();
     const char* src = sizeof(Real) == 4 ? (const char*)a.xf6 : (const char*)a.xd3;
     const int64_t step = (int64_t)gridDim.x * NGRP;
-    for (int64_t c = (int64_t)blockIdx.x * NGRP + grp; c < sd.n_cells; c += step) {
+    // node ids two cells ahead and coordinates one cell ahead, in registers (lanes < NG)
+    const int64_t c0 = (int64_t)blockIdx.x * NGRP + grp;
+    int nd_cur = 0, nd_next = 0;
+    uint2 x_cur[3] = {}, x_next[3] = {};
+    if (lane < NG) {
+        if (c0 < sd.n_cells) {
+            nd_cur = sd.conn[c0 * NG + lane];
+            const uint2* p = (const uint2*)(src + (int64_t)nd_cur * NODE_BYTES);
+            x_cur[0] = p[0]; x_cur[1] = p[1]; x_cur[2] = p[2];
+        }
+        if (c0 + step < sd.n_cells) nd_next = sd.conn[(c0 + step) * NG + lane];
+    }
+    for (int64_t c = c0; c < sd.n_cells; c += step) {
+        int nd_after = 0;
         if (lane < NG) {
-            const int nd = sd.conn[c * NG + lane];
-            nodes[lane] = nd;
-            const uint2* p = (const uint2*)(src + (int64_t)nd * NODE_BYTES);
+            nodes[lane] = nd_cur;
             uint2* d = (uint2*)(xs + lane * NODE_BYTES);
-            d[0] = p[0];
-            d[1] = p[1];
-            d[2] = p[2];
+            d[0] = x_cur[0];
+            d[1] = x_cur[1];
+            d[2] = x_cur[2];
+            if (c + step < sd.n_cells) {
+                const uint2* p = (const uint2*)(src + (int64_t)nd_next * NODE_BYTES);
+                x_next[0] = p[0]; x_next[1] = p[1]; x_next[2] = p[2];
+            }
+            if (c + 2 * step < sd.n_cells) nd_after = sd.conn[(c + 2 * step) * NG + lane];
         }
         __syncwarp(gmask);
         geometry_lanes<K, NQ, PHYS, Real>(a, sd, shape, (int)c, cn, xs, nodes, lane, gmask, gbase, tb);
@@ -1412,6 +1447,10 @@ __global__ void __launch_bounds__(THREADS, 2) element_kernel(const KernelArgs a,
             cell_blocks<K, NQ, PHYS, Real, MODE>(a, sd, nullptr, nullptr, nullptr, 0, tb, shape, (int)c, lane, 0, NB,
                                                  (Real*)eo.ke + c * eo.ks[0], &eo);
         __syncwarp(gmask);  // the next cell overwrites the table and the coordinates
+        nd_cur = nd_next;
+        nd_next = nd_after;
+        #pragma unroll
+        for (int k = 0; k < 3; ++k) x_cur[k] = x_next[k];
     }
 }
 
@@ -1535,16 +1574,34 @@ __global__ void __launch_bounds__(128, 3) element_kernel_tc(const KernelArgs a, 
     const char* src = (const char*)a.xf6;
     bool failed = false;
     int it = 0;
+    // node ids two cells ahead and coordinates one cell ahead, in registers (threads < NG), so
+    // neither global round trip sits on a cell's critical path
+    const int64_t G0 = gridDim.x;
+    int nd_cur = 0, nd_next = 0;
+    uint2 x_cur[3] = {}, x_next[3] = {};
+    if (tid < NG) {
+        if ((int64_t)blockIdx.x < sd.n_cells) {
+            nd_cur = sd.conn[(int64_t)blockIdx.x * NG + tid];
+            const uint2* p = (const uint2*)(src + (int64_t)nd_cur * NODE_BYTES);
+            x_cur[0] = p[0]; x_cur[1] = p[1]; x_cur[2] = p[2];
+        }
+        if ((int64_t)blockIdx.x + G0 < sd.n_cells) nd_next = sd.conn[((int64_t)blockIdx.x + G0) * NG + tid];
+    }
     for (int64_t c = blockIdx.x; c < sd.n_cells; c += gridDim.x, ++it) {
-        // node ids and coordinates
+        // node ids and coordinates of this cell; the loads for the next ones are issued here
+        // and consumed an iteration later
+        int nd_after = 0;
         if (tid < NG) {
-            const int nd = sd.conn[c * NG + tid];
-            nodes[tid] = nd;
-            const uint2* p = (const uint2*)(src + (int64_t)nd * NODE_BYTES);
+            nodes[tid] = nd_cur;
             uint2* d = (uint2*)(xs + tid * NODE_BYTES);
-            d[0] = p[0];
-            d[1] = p[1];
-            d[2] = p[2];
+            d[0] = x_cur[0];
+            d[1] = x_cur[1];
+            d[2] = x_cur[2];
+            if (c + G0 < sd.n_cells) {
+                const uint2* p = (const uint2*)(src + (int64_t)nd_next * NODE_BYTES);
+                x_next[0] = p[0]; x_next[1] = p[1]; x_next[2] = p[2];
+            }
+            if (c + 2 * G0 < sd.n_cells) nd_after = sd.conn[(c + 2 * G0) * NG + tid];
         }
         __syncthreads();
         // geometry: every warp maps the 27 points, warp w writes the gradients of functions
@@ -1654,6 +1711,10 @@ __global__ void __launch_bounds__(128, 3) element_kernel_tc(const KernelArgs a, 
             }
         }
         __syncthreads();  // the next cell overwrites the table, the operands and G
+        nd_cur = nd_next;
+        nd_next = nd_after;
+        #pragma unroll
+        for (int k = 0; k < 3; ++k) x_cur[k] = x_next[k];
     }
     if (failed) {
         // the MMAs of this cell did not report back: record it and wait (bounded) once more
