@@ -39,14 +39,14 @@ __host__ __device__ __forceinline__ double u2d(uint64_t u) {
 #endif
 }
 
-// Round hi + lo to the nearest double (ties to even). After a Fast2Sum the pair (s, e) has
+// Round hi + lo to the nearest double (ties to even). After a TwoSum the pair (s, e) has
 // |e| <= ulp(s)/2; the double of s is exact and e only touches the 29 mantissa bits below
 // s's FP32 precision, so the result is an integer add/subtract on the bit pattern.
 #ifdef __CUDA_ARCH__
 __device__ __noinline__ double pair_to_double(float hi, float lo);
 #endif
-// (kept out of line on the device: the rare paths of pair_to_double_fast call it, and a call
-// cannot be turned into predicated FP64 instructions on the common path)
+// (kept out of line on the device: the kernels call it only for the rare sums that
+// pair2_to_double / pair1_to_double flag)
 #ifdef __CUDA_ARCH__
 __device__ __noinline__
 #else
@@ -54,7 +54,8 @@ __host__ __forceinline__
 #endif
 double pair_to_double(float hi, float lo) {
     const float s = hi + lo;
-    const float e = lo - (s - hi);
+    const float bb = s - hi;
+    const float e = (hi - (s - bb)) + (lo - bb);  // TwoSum: exact for any magnitudes
     if (s == 0.0f) return 0.0;
     const uint32_t bs = f2u(s), be = f2u(e);
     const uint32_t es = (bs >> 23) & 0xFF, ee = (be >> 23) & 0xFF;
@@ -99,26 +100,73 @@ __host__ __device__ __forceinline__ int f2i_rn(float x) {
 #endif
 }
 
-// Same result as pair_to_double, fewer operations: the low word, scaled by a power of two
-// to units of the double's last place, is rounded to an integer (ties to even) and added to
-// the bit pattern of double(s). |e| <= ulp_f(s)/2 keeps that integer within +-2^28.
-__host__ __device__ __forceinline__ double pair_to_double_fast(float hi, float lo) {
-    const float s = hi + lo;
-    const float e = lo - (s - hi);
-    const uint32_t bs = f2u(s);
+// packed FP32 helpers (FADD2 / FFMA2 / FMUL2 on the device)
+#if !defined(__CUDACC__) && !defined(__VECTOR_TYPES_H__)
+struct float2 {
+    float x, y;
+};
+#endif
+__host__ __device__ __forceinline__ float2 f2add(float2 a, float2 b) {
+#ifdef __CUDA_ARCH__
+    return __fadd2_rn(a, b);
+#else
+    return float2{a.x + b.x, a.y + b.y};
+#endif
+}
+__host__ __device__ __forceinline__ float2 f2sub(float2 a, float2 b) {
+#ifdef __CUDA_ARCH__
+    return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+#else
+    return float2{a.x - b.x, a.y - b.y};
+#endif
+}
+__host__ __device__ __forceinline__ float2 f2mul(float2 a, float2 b) {
+#ifdef __CUDA_ARCH__
+    return __fmul2_rn(a, b);
+#else
+    return float2{a.x * b.x, a.y * b.y};
+#endif
+}
+// bit pattern of double(s) plus d units of its last place (|d| < 2^29)
+__host__ __device__ __forceinline__ uint64_t scaled_low_word_add(uint32_t bs, int d) {
     const uint32_t mag = bs & 0x7FFFFFFFu;
-    const uint32_t es = mag >> 23;
-    if (es < 60u || es == 0xFFu) return pair_to_double(hi, lo);  // tiny / subnormal / inf: rare
-    // double(s): same sign, exponent rebased by 1023-127, mantissa shifted up by 29
     const uint32_t dhi = (bs & 0x80000000u) | ((mag >> 3) + (896u << 20));
     const uint32_t dlo = mag << 29;
-    // e in units of ulp(double(s)) = 2^(es-127-52); one more bit if s is a power of two and
-    // e points into the binade below
-    const bool down = ((bs ^ f2u(e)) & 0x80000000u) && (mag & 0x7FFFFFu) == 0u;
-    const uint32_t sc = (uint32_t)(306 - (int)es + (down ? 1 : 0)) << 23;
-    const int d = f2i_rn(e * u2f(sc));
-    const uint64_t D = (((uint64_t)dhi << 32) | dlo) + (uint64_t)(int64_t)((bs & 0x80000000u) ? -d : d);
-    return u2d(D);
+    return (((uint64_t)dhi << 32) | dlo) + (uint64_t)(int64_t)d;
+}
+// s zero or below 2^-67, infinite or NaN, or a power of two
+__host__ __device__ __forceinline__ bool sum_needs_care(uint32_t bs) {
+    const uint32_t mag = bs & 0x7FFFFFFFu;
+    return (mag - (60u << 23)) >= (195u << 23) || (mag & 0x7FFFFFu) == 0u;
+}
+// Two entries at once, without a branch: o0, o1 = hi + lo rounded to the nearest double (ties
+// to even), exactly as pair_to_double, unless an entry's sum s needs care. `rare` is set for
+// those (s zero, below 2^-67, infinite or NaN, or a power of two, whose low word may point into
+// the binade below) and the caller redoes them with pair_to_double. The TwoSum renormalisation
+// runs packed on both entries (any magnitudes of hi and lo); the low word e, scaled by a power
+// of two that carries the sign of s to units of the double's last place, is rounded to an
+// integer (|e| <= ulp_f(s)/2 keeps it within +-2^28) and added to the bit pattern of double(s).
+__host__ __device__ __forceinline__ void pair2_to_double(float2 hi, float2 lo, double& o0, double& o1, bool& rare) {
+    const float2 s = f2add(hi, lo);
+    const float2 bb = f2sub(s, hi);
+    const float2 e = f2add(f2sub(hi, f2sub(s, bb)), f2sub(lo, bb));
+    const uint32_t b0 = f2u(s.x), b1 = f2u(s.y);
+    // 2^(179 - exponent(s)) with the sign of s: (306 << 23) - (sign | exponent field), mod 2^32
+    const float2 sc = float2{u2f((306u << 23) - (b0 & 0xFF800000u)), u2f((306u << 23) - (b1 & 0xFF800000u))};
+    const float2 q = f2mul(e, sc);
+    o0 = u2d(scaled_low_word_add(b0, f2i_rn(q.x)));
+    o1 = u2d(scaled_low_word_add(b1, f2i_rn(q.y)));
+    rare |= sum_needs_care(b0) | sum_needs_care(b1);
+}
+
+// One entry, the same way (scalar TwoSum)
+__host__ __device__ __forceinline__ double pair1_to_double(float hi, float lo, bool& rare) {
+    const float s = hi + lo;
+    const float bb = s - hi;
+    const float e = (hi - (s - bb)) + (lo - bb);
+    const uint32_t b = f2u(s);
+    rare |= sum_needs_care(b);
+    return u2d(scaled_low_word_add(b, f2i_rn(e * u2f((306u << 23) - (b & 0xFF800000u)))));
 }
 
 __host__ __device__ __forceinline__ int clz32(uint32_t x) {  // x != 0

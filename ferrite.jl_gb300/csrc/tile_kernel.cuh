@@ -86,7 +86,11 @@ __device__ __forceinline__ void acc_add(float2& a, float x) {
 }
 __device__ __forceinline__ void acc_add(double& a, double x) { a += x; }
 
-__device__ __forceinline__ double acc_value(float2 a) { return pair_to_double_fast(a.x, a.y); }
+__device__ __forceinline__ double acc_value(float2 a) {
+    bool rare = false;
+    const double v = pair1_to_double(a.x, a.y, rare);
+    return rare ? pair_to_double(a.x, a.y) : v;
+}
 __device__ __forceinline__ double acc_value(double a) { return a; }
 __device__ __forceinline__ void acc_zero(float2& a) { a = make_float2(0.f, 0.f); }
 __device__ __forceinline__ void acc_init(float2& a, float x) { a = make_float2(x, 0.f); }
@@ -1116,10 +1120,18 @@ __device__ __forceinline__ void reduce_tile(const KernelArgs& a, const char* R, 
                             if (2 * t + 1 < NCC) out[2 * t + 1] = float_to_double(hi[t].y);
                         }
                     } else {
+                        // branch-free rounding of every entry; the block's few entries whose sum
+                        // needs care (zero, tiny, a power of two) are redone exactly
+                        bool rare = false;
                         #pragma unroll
-                        for (int t = 0; t < NP; ++t) {
-                            out[2 * t] = pair_to_double_fast(hi[t].x, lo[t].x);
-                            if (2 * t + 1 < NCC) out[2 * t + 1] = pair_to_double_fast(hi[t].y, lo[t].y);
+                        for (int t = 0; t < NCC / 2; ++t) pair2_to_double(hi[t], lo[t], out[2 * t], out[2 * t + 1], rare);
+                        if constexpr (NCC & 1) out[NCC - 1] = pair1_to_double(hi[NP - 1].x, lo[NP - 1].x, rare);
+                        if (rare) {
+                            #pragma unroll
+                            for (int t = 0; t < NP; ++t) {
+                                out[2 * t] = pair_to_double(hi[t].x, lo[t].x);
+                                if (2 * t + 1 < NCC) out[2 * t + 1] = pair_to_double(hi[t].y, lo[t].y);
+                            }
                         }
                     }
                 } else {
