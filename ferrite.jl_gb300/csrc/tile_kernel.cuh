@@ -1065,7 +1065,12 @@ __device__ __forceinline__ void reduce_tile(const KernelArgs& a, const char* R, 
         }
         const int end = P.red_end + (p + 1 == n_pass ? nf : 0);
         int u = P.run_begin;  // run of the current block (positions only grow)
-        for (int pos = P.red_begin + (int)threadIdx.x; pos < end; pos += THREADS) {
+        // snake order: round k takes positions k THREADS + (k odd ? THREADS - 1 - tid : tid), so
+        // a thread's second block (fewer contributions, the order being by count) is the lighter
+        // the heavier its first one was
+        for (int k = 0;; ++k) {
+            const int pos = P.red_begin + k * THREADS + ((k & 1) ? THREADS - 1 - (int)threadIdx.x : (int)threadIdx.x);
+            if (pos >= end) break;
             if (pos >= P.red_end) {
                 f_entry<NC, Real>(a, R, stage, pos - P.red_end);
                 continue;
