@@ -160,8 +160,11 @@ __device__ __forceinline__ void record_miss(DevStatus* st, int32_t cellid, int I
 // X = C - I = H + H^T + H^T H, det C - 1 from the invariants of X, I - C^-1 = C^-1 X.
 // Outputs T = S + c1 C^-1, B = F^-T, c1, 2 c2 and P = F S such that
 // dP/dF_aJbL = delta_ab T_JL + c1 B_aL B_bJ + 2c2 B_aJ B_bL (hyperelasticity.jl:157-176, 254).
+// Returns false when det C is small against the size of the terms it came from,
+// det C <= 0.05 (1 + |X|)^3 (the FP32 det C and C^-1 then carry relative errors above about
+// 1e-6): a near-singular or inverted deformation, whose point the caller recomputes in FP64.
 template <typename R>
-__device__ __forceinline__ void neo_hooke_point(R mu, R lam, const R* H, R* out) {
+__device__ __forceinline__ bool neo_hooke_point(R mu, R lam, const R* H, R* out) {
     R F[9], X[9], C[9], Ci[9];
     #pragma unroll
     for (int a = 0; a < 9; ++a) F[a] = H[a];
@@ -184,6 +187,11 @@ __device__ __forceinline__ void neo_hooke_point(R mu, R lam, const R* H, R* out)
         for (int J = 0; J < 3; ++J) trX2 += X[I * 3 + J] * X[J * 3 + I];
     const R detCm1 = trX + R(0.5) * (trX * trX - trX2) + Mat<R, 3>::det(X);
     const R detC = R(1) + detCm1;
+    R nX = 0;
+    #pragma unroll
+    for (int t = 0; t < 9; ++t) nX += X[t] * X[t];
+    const R sX = R(1) + sqrt(nX);
+    const bool ok = detC > R(0.05) * sX * sX * sX;
     Mat<R, 3>::inv(C, detC, Ci);
     const R Jd = sqrt(detC);
     const R Jm1 = detCm1 / (Jd + R(1));
@@ -222,6 +230,39 @@ __device__ __forceinline__ void neo_hooke_point(R mu, R lam, const R* H, R* out)
             for (int I = 0; I < 3; ++I) p += F[a * 3 + I] * S[I * 3 + J];
             out[20 + a * 3 + J] = p;
         }
+    return ok;
+}
+
+// One quadrature point of a Neo-Hooke cell again in FP64 from the FP64 inputs (coordinates,
+// reference tables, u): Jacobian, gradients, H = grad u, then neo_hooke_point; the outputs in
+// FP32. For the rare points the FP32 form flags (kept out of line).
+template <int K>
+__device__ __forceinline__ void neo_point_fp64(const KernelArgs& a, const SubDev& sd, int cell, const uint16_t* cn,
+                                            const int32_t* nodes, int q, float* out) {
+    constexpr int NG = ElemT<K>::NG, NB = ElemT<K>::NB;
+    double J[9], Ji[9], H[9], x0[3];
+    const int n0 = nodes[cn[0]];
+    for (int x = 0; x < 3; ++x) x0[x] = a.xd[(int64_t)n0 * 3 + x];
+    for (int t = 0; t < 9; ++t) { J[t] = 0.0; H[t] = 0.0; }
+    for (int k = 1; k < NG; ++k) {
+        const int nk = nodes[cn[k]];
+        for (int x = 0; x < 3; ++x) {
+            const double o = a.xd[(int64_t)nk * 3 + x] - x0[x];
+            for (int b = 0; b < 3; ++b) J[x * 3 + b] += o * sd.dM_d[(q * NG + k) * 3 + b];
+        }
+    }
+    Mat<double, 3>::inv(J, Mat<double, 3>::det(J), Ji);
+    for (int i = 0; i < NB; ++i) {
+        double g[3] = {0.0, 0.0, 0.0};
+        for (int b = 0; b < 3; ++b)
+            for (int c = 0; c < 3; ++c) g[b] += sd.dN_d[(q * NB + i) * 3 + c] * Ji[c * 3 + b];
+        const int64_t e3 = (int64_t)sd.ents[(int64_t)cell * NB + i] * 3;
+        for (int c = 0; c < 3; ++c)
+            for (int b = 0; b < 3; ++b) H[c * 3 + b] += a.phys.u_d[e3 + c] * g[b];
+    }
+    double o[NEO_POINT];
+    neo_hooke_point<double>(a.phys.p0, a.phys.p1, H, o);
+    for (int k = 0; k < NEO_POINT; ++k) out[k] = (float)o[k];
 }
 
 // ---------------------------------------------------------------------------------------
@@ -546,33 +587,46 @@ __device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev
         #pragma unroll
         for (int t = 0; t < 9; ++t) H[t] *= is;
         Real nq[NEO_POINT];
-        neo_hooke_point<Real>(pconst<Real>(a.phys.p0, a.phys.p0_f), pconst<Real>(a.phys.p1, a.phys.p1_f), H, nq);
-        // the point's entries of the pair table (a padded partner point gets zeros)
-        if (lead) {
-            Real* pp = neo + CT::GRAD + p * NEO_PAIR;
-            constexpr int TK[6] = {0, 4, 8, 1, 2, 5};  // T00, T11, T22, T01, T02, T12
-            #pragma unroll
-            for (int k = 0; k < 6; ++k) pp[NEO_T + 2 * k + hh] = nq[TK[k]];
-            pp[NEO_C1 + hh] = nq[18];
-            pp[NEO_C2 + hh] = nq[19];
-            #pragma unroll
-            for (int k = 0; k < 9; ++k) pp[NEO_SP + 2 * k + hh] = s * nq[20 + k];
-            if (pad) {
+        const bool ok = neo_hooke_point<Real>(pconst<Real>(a.phys.p0, a.phys.p0_f), pconst<Real>(a.phys.p1, a.phys.p1_f), H, nq);
+        // the point's entries of the pair table (a padded partner point gets zeros) and B g_i
+        // for the base functions this group writes (B = F^-T; the gradients written above are
+        // read back by the same lane)
+        auto write_point = [&](const Real* v) {
+            if (lead) {
+                Real* pp = neo + CT::GRAD + p * NEO_PAIR;
+                constexpr int TK[6] = {0, 4, 8, 1, 2, 5};  // T00, T11, T22, T01, T02, T12
                 #pragma unroll
-                for (int k = 0; k < NEO_PAIR / 2; ++k) pp[2 * k + 1] = Real(0);
+                for (int k = 0; k < 6; ++k) pp[NEO_T + 2 * k + hh] = v[TK[k]];
+                pp[NEO_C1 + hh] = v[18];
+                pp[NEO_C2 + hh] = v[19];
+                #pragma unroll
+                for (int k = 0; k < 9; ++k) pp[NEO_SP + 2 * k + hh] = s * v[20 + k];
+                if (pad) {
+                    #pragma unroll
+                    for (int k = 0; k < NEO_PAIR / 2; ++k) pp[2 * k + 1] = Real(0);
+                }
             }
-        }
-        // B g_i of this point for the base functions this group writes (B = F^-T): the
-        // gradients written above are read back by the same lane
-        #pragma unroll
-        for (int i = 0; i < NB; ++i) {
-            if (i < i0 || i >= i1) continue;
-            const Real* gs = grad + p * CT::SP + i * 6 + hh;
-            const Real gx = gs[0], gy = gs[2], gz = gs[4];
-            Real* bd = neo + p * CT::SP + i * 6 + hh;
             #pragma unroll
-            for (int x = 0; x < 3; ++x) bd[2 * x] = nq[9 + 3 * x] * gx + nq[9 + 3 * x + 1] * gy + nq[9 + 3 * x + 2] * gz;
-            if (pad) { bd[1] = Real(0); bd[3] = Real(0); bd[5] = Real(0); }
+            for (int i = 0; i < NB; ++i) {
+                if (i < i0 || i >= i1) continue;
+                const Real* gs = grad + p * CT::SP + i * 6 + hh;
+                const Real gx = gs[0], gy = gs[2], gz = gs[4];
+                Real* bd = neo + p * CT::SP + i * 6 + hh;
+                #pragma unroll
+                for (int x = 0; x < 3; ++x) bd[2 * x] = v[9 + 3 * x] * gx + v[9 + 3 * x + 1] * gy + v[9 + 3 * x + 2] * gz;
+                if (pad) { bd[1] = Real(0); bd[3] = Real(0); bd[5] = Real(0); }
+            }
+        };
+        write_point(nq);
+        if constexpr (sizeof(Real) == 4) {
+            // a near-singular or inverted deformation: this point again in FP64, its entries
+            // rewritten (rare; last, so that little is live across the call)
+            if (!ok && s > Real(0)) {
+                float nd[NEO_POINT];
+                neo_point_fp64<K>(a, sd, cell, cn, nodes, q, nd);
+                write_point(nd);
+                atomicAdd(&a.status->flagged, 1u);
+            }
         }
     }
 }

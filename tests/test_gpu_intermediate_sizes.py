@@ -7,7 +7,7 @@ kernel form runs many tiles on every SM, checked against the oracle's FP64 assem
   * 12^3 Q2 hexahedra, linear elasticity with a lognormal per-cell modulus, tensor-core and
     CUDA-core element matrices;
   * a 30x10x10 hexahedron / tetrahedron / wedge box (1,000 + 6,000 + 2,000 cells), Neo-Hooke,
-    fused and two-phase;
+    fused and two-phase, with a moderate displacement and with one that inverts some elements;
   * the SIMP adjoint on a (24,12,12) cantilever slab.
 
 Tolerances are those of the unit cases: relative Frobenius error of nzval and f <= 1e-6 for
@@ -78,6 +78,27 @@ def test_neo_hooke_mixed_30x10x10(built, oracle):
     _run(fg, O, prob, dict(physics=fg.NEO_HOOKE, p0=1.0, p1=10.0, u=u, body=(0.0, -0.5, 0.0)),
          dict(physics=O.NEO_HOOKE, p0=1.0, p1=10.0, u=u, body=(0.0, -0.5, 0.0)),
          [dict(), dict(form="fused"), dict(form="two_phase")], 2e-6)
+
+
+def test_neo_hooke_near_singular_points(built, oracle):
+    """A displacement of amplitude 0.05 on the same mix (h = 1/15 along x) drives det F down to
+    -0.64 at about 1.6 % of the hexahedron points (inverted elements; Ferrite's J = sqrt(det C)
+    maps them to |det F|). The FP32 point math flags those points and recomputes them in FP64,
+    so the mixed forms still match the FP64 oracle."""
+    fg, O = built, oracle
+    prob = mixed_problem(O, nel=(30, 10, 10), seed=41)
+    u = 0.05 * np.random.default_rng(42).uniform(-1, 1, prob.ndofs)
+    nz_ref, f_ref = prob.assemble(physics=O.NEO_HOOKE, p0=1.0, p1=10.0, u=u, body=(0.0, -0.5, 0.0))
+    assert np.isfinite(nz_ref).all() and np.isfinite(f_ref).all()
+    h = make_handle(fg, O, prob)
+    for kw in (dict(), dict(form="fused"), dict(form="two_phase")):
+        nz = np.full(prob.nnz, np.nan)
+        f = np.full(prob.ndofs, np.nan)
+        h.assemble(nz, f, precision=0, physics=fg.NEO_HOOKE, p0=1.0, p1=10.0, u=u, body=(0.0, -0.5, 0.0), **kw)
+        assert np.isfinite(nz).all() and np.isfinite(f).all(), kw
+        assert rel_fro(nz, nz_ref) <= 2e-6, (kw, rel_fro(nz, nz_ref))
+        assert rel_fro(f, f_ref) <= 2e-6, (kw, rel_fro(f, f_ref))
+        assert h.info()["flagged_cells"] > 0, kw
 
 
 def test_adjoint_cantilever_24x12x12(built, oracle):
