@@ -923,8 +923,9 @@ def config_mixed_graph(fg, stream, steps=20, oracle=True, ny=100, tune=True):
     """~2M cells over three x-slabs sharing vertex nodes (Hex Q1 50%, Tet P1 25% as 6 per cube,
     Wedge P1 25% as 2 per cube), compressible Neo-Hooke (mu 1, lambda 10), displacement
     amplitude 0.05 of the cell size h = 0.01 (u = 0.05 h U(-1,1), seeded per step: an absolute
-    0.05 is five cells wide and inverts cells, where log J is undefined in any precision); the tile plan autotuned, then `steps` re-assemblies with updated u captured
-    as one CUDA graph and replayed."""
+    0.05 is five cells wide and inverts most cells, a state no Newton iteration of the tutorial
+    visits); the tile plan autotuned, then `steps` re-assemblies with updated u captured as one
+    CUDA graph and replayed."""
     import torch
     host = __import__("ferrite_gb300.host", fromlist=["host"])
     nh, nt, nw, nzc = 100, 8, 25, ny
