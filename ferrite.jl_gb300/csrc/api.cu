@@ -294,7 +294,7 @@ cudaError_t install_plan(fe_handle* h) {
     if (A.rec_off) h->release((void*)A.rec_off);
     A.rec = rec;
     A.rec_off = roff;
-    std::vector<uint8_t>().swap(pl.rec);  // the device copy is the one in use
+    decltype(pl.rec)().swap(pl.rec);  // the device copy is the one in use
     A.n_tiles = (int32_t)pl.n_tiles;
     set_plan_caps(A, pl);
     return cudaSuccess;

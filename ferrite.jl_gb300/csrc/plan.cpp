@@ -125,7 +125,14 @@ int build_problem(const CreateInput& in, HostProblem& hp, Error& err) {
         }
     }
     // The cell_dofs array length is not passed; its extent is implied by the offsets.
-    hp.cell_dofs.assign(d->cell_dofs, d->cell_dofs + maxdof_end);
+    hp.cell_dofs.resize(maxdof_end);
+    {
+        const int64_t chunk = 1 << 20;
+#pragma omp parallel for schedule(static)
+        for (int64_t b = 0; b < (maxdof_end + chunk - 1) / chunk; ++b)
+            std::memcpy(hp.cell_dofs.data() + b * chunk, d->cell_dofs + b * chunk,
+                        (size_t)(std::min(chunk, maxdof_end - b * chunk)) * sizeof(int64_t));
+    }
     const int nc = hp.nc;
     if (hp.ndofs % nc) return fail(err, FE_ERR_UNSUPPORTED, "ndofs not a multiple of n_components");
     hp.n_ent = hp.ndofs / nc;
@@ -215,7 +222,7 @@ int build_problem(const CreateInput& in, HostProblem& hp, Error& err) {
         if (fill_ranks(hs.rank8.data(), 255, 255)) {
             hs.wide_rank = false;
         } else {
-            std::vector<uint8_t>().swap(hs.rank8);
+            decltype(hs.rank8)().swap(hs.rank8);
             hs.rank16.resize((size_t)hs.n_cells * nb * nb);
             fill_ranks(hs.rank16.data(), 0xFFFF, 0xFFFF);
             hs.wide_rank = true;
@@ -732,7 +739,7 @@ int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error&
     for (const HostSub& hs : hp.subs)
         for (size_t t = 0; t < hs.ents.size(); ++t) tstart[tile_of[hs.ents[t]] + 1]++;
     for (int64_t t = 0; t < n_tiles; ++t) tstart[t + 1] += tstart[t];
-    std::vector<uint64_t> trip(tstart[n_tiles]);
+    HostBuf<uint64_t> trip(tstart[n_tiles]);
     {
         std::vector<int64_t> cur(tstart.begin(), tstart.end() - 1);
         for (size_t s = 0; s < hp.subs.size(); ++s) {

@@ -3,13 +3,40 @@
 #pragma once
 #include <stdint.h>
 
+#include <memory>
 #include <string>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "common.h"
 #include "ferrite_gb300.h"
 
 namespace fe {
+
+// Allocator whose value-less construct leaves the element uninitialised: large host buffers that
+// are written in full right after they are sized (in parallel, so the first touch of their pages
+// is spread over the threads) skip the serial zero fill of std::vector::resize.
+template <typename T>
+struct DefaultInitAllocator : std::allocator<T> {
+    template <typename U>
+    struct rebind {
+        using other = DefaultInitAllocator<U>;
+    };
+    DefaultInitAllocator() = default;
+    template <typename U>
+    DefaultInitAllocator(const DefaultInitAllocator<U>&) noexcept {}
+    template <typename U>
+    void construct(U* p) noexcept(std::is_nothrow_default_constructible<U>::value) {
+        ::new ((void*)p) U;
+    }
+    template <typename U, typename... A>
+    void construct(U* p, A&&... a) {
+        ::new ((void*)p) U(std::forward<A>(a)...);
+    }
+};
+template <typename T>
+using HostBuf = std::vector<T, DefaultInitAllocator<T>>;
 
 struct HostSub {
     int32_t cell_type = 0, ip_order = 0, kind = 0;
@@ -18,8 +45,8 @@ struct HostSub {
     std::vector<int32_t> cellid;   // 0-based Ferrite cell ids
     std::vector<int32_t> conn;     // [n][ng] 0-based node ids
     std::vector<int32_t> ents;     // [n][nb] entity ids
-    std::vector<uint8_t> rank8;    // [n][nb][nb] (j-major), 255 = missing
-    std::vector<uint16_t> rank16;  // used when a rank exceeds 254; 65535 = missing
+    HostBuf<uint8_t> rank8;        // [n][nb][nb] (j-major), 255 = missing
+    HostBuf<uint16_t> rank16;      // used when a rank exceeds 254; 65535 = missing
     bool wide_rank = false;
     std::vector<double> w, N, dN, dM;  // reference tables (row-major, as passed)
 };
@@ -35,7 +62,7 @@ struct HostProblem {
     std::vector<int64_t> cell_dofs_off;   // per Ferrite cell: 1-based offset (for index-map queries)
     std::vector<int32_t> cell_sub;        // per Ferrite cell: subdomain or -1
     std::vector<int32_t> cell_local;      // per Ferrite cell: index within its subdomain
-    std::vector<int64_t> cell_dofs;       // copy of dh.cell_dofs (for index-map queries / errors)
+    HostBuf<int64_t> cell_dofs;           // copy of dh.cell_dofs (for index-map queries / errors)
 };
 
 struct PlanOptions {
@@ -51,7 +78,7 @@ struct PlanOptions {
 };
 
 struct Plan {
-    std::vector<uint8_t> rec;       // tile records, concatenated (each 16-byte aligned)
+    HostBuf<uint8_t> rec;           // tile records, concatenated (each 16-byte aligned)
     std::vector<int64_t> rec_off;   // [n_tiles + 1] byte offsets
     int64_t n_tiles = 0;
     int32_t max_rec = 0, max_nodes = 0, max_stage = 0, max_out = 0;
