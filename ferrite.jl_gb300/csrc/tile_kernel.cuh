@@ -1258,9 +1258,24 @@ __device__ __forceinline__ void reduce_tile(const KernelArgs& a, const char* R, 
                 bulk_commit();
             }
         } else {
-            for (int gi = P.rng_begin; gi < P.rng_end; ++gi) {
+            // host memory (pinned, through its mapping) or an nzval that is only 8-byte aligned:
+            // one warp per range, so every warp has stores in flight; 16-byte stores for the
+            // aligned pairs when nzval is 16-byte aligned (the buffer keeps each range's parity)
+            const int warp = (int)threadIdx.x >> 5, ln = (int)threadIdx.x & 31;
+            const bool v2 = ((uintptr_t)a.nzval & 15) == 0;
+            for (int gi = P.rng_begin + warp; gi < P.rng_end; gi += THREADS / 32) {
                 const RecRng g = rngs[gi];
-                for (int k = threadIdx.x; k < g.len; k += THREADS) __stcs(a.nzval + g.nz0 + k, outb[g.buf_off + k]);
+                if (v2) {
+                    const int64_t e = g.nz0 + g.len;
+                    const int64_t a0 = g.nz0 + (g.nz0 & 1), a1 = e & ~(int64_t)1;
+                    if (ln == 0 && (g.nz0 & 1)) __stcs(a.nzval + g.nz0, outb[g.buf_off]);
+                    if (ln == 1 && (e & 1)) __stcs(a.nzval + e - 1, outb[g.buf_off + g.len - 1]);  // never the head element
+                    const double2* src = (const double2*)(outb + g.buf_off + (a0 - g.nz0));
+                    double2* dst = (double2*)(a.nzval + a0);
+                    for (int64_t k = ln; 2 * k < a1 - a0; k += 32) __stcs(dst + k, src[k]);
+                } else {
+                    for (int k = ln; k < g.len; k += 32) __stcs(a.nzval + g.nz0 + k, outb[g.buf_off + k]);
+                }
             }
             if (p + 1 < n_pass) __syncthreads();
         }
