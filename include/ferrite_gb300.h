@@ -61,7 +61,8 @@ extern "C" {
 #define FE_NEO_HOOKE 3      /* tangent and residual of hyperelasticity.jl:157-276 (cell part) */
 
 /* precision */
-#define FE_PREC_MIXED 0 /* FP32 element math (FP64 Jacobians for flagged cells); each entry's contributions summed
+#define FE_PREC_MIXED 0 /* FP32 element math (FP64 Jacobians for flagged cells, FP64 Neo-Hooke points where the
+                           deformation is near-singular or inverted); each entry's contributions summed
                            as a compensated FP32 pair (FP64-class) and rounded exactly to FP64; with FE_FP32_SUM
                            one plain FP32 sum per entry instead */
 #define FE_PREC_FP64 1  /* the plain FP64 drop-in: all math and accumulation in FP64 */
@@ -164,8 +165,9 @@ typedef struct {
     int64_t n_tiles;        /* owner tiles the nzval is partitioned into */
     int64_t n_cell_visits;  /* (cell, tile) pairs: geometry evaluations per assembly */
     int64_t n_items;        /* (cell, owned base function) work items per assembly */
-    int64_t flagged_cells;  /* cell evaluations redone with FP64 Jacobians in the last mixed assembly
-                               (a cell is evaluated once per owner tile it touches) */
+    int64_t flagged_cells;  /* cell evaluations redone with FP64 Jacobians, plus Neo-Hooke quadrature points
+                               redone in FP64, in the last mixed assembly (a cell is evaluated once per owner
+                               tile it touches) */
     int64_t device_bytes;   /* device memory held by the handle */
     double create_seconds;  /* host time spent in fe_create */
     int32_t max_record_bytes;   /* largest tile record (shared-memory ring entry) */
