@@ -335,7 +335,7 @@ __host__ __device__ constexpr ShapeQ shape_q(int nb, int ng, int dim, int real_b
 // Cell table layout (one per lane group), quadrature points taken in pairs (q0 = 2p,
 // q1 = 2p+1; an odd count is padded with a zero-weight point):
 //   grad[NQP][SP]    : at p*SP + i*6: (gx0, gx1, gy0, gy1, gz0, gz1), g = sqrt(detJ w) gradN
-//   sq[NQP][2]       : sqrt(detJ w) per point
+//   sq[NQP][2]       : detJ w per point (s squared)
 //   cellp[4]         : per-cell material values
 //   Neo-Hooke only:
 //   bgrad[NQP][SP]   : B g per point and base function, laid out as grad (B = F^-T)
@@ -532,7 +532,7 @@ __device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev
     const int p = q >> 1, hh = q & 1;
     const bool pad = (NQ & 1) && q == NQ - 1;
     if (lead) {
-        sq[2 * p + hh] = s;
+        sq[2 * p + hh] = s * s;
         if (pad) sq[2 * p + 1] = Real(0);
     }
     Real H[9];
@@ -708,10 +708,7 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
     if constexpr (PHYS != PHYS_NEO) {
         if (a.do_f) {
             #pragma unroll
-            for (int q = 0; q < NQ; ++q) {
-                const Real s = sq[q];
-                Fi += s * s * shp[q * SQL.qs + SQL.n + i];
-            }
+            for (int q = 0; q < NQ; ++q) Fi += sq[q] * shp[q * SQL.qs + SQL.n + i];
         }
     }
     // EA 0: the block goes to the tile's staging slot; EA 1: to the cell's element matrix in
@@ -867,10 +864,7 @@ __device__ __forceinline__ void cell_blocks(const KernelArgs& a, const SubDev& s
         {
             Real nw = Real(0);
             #pragma unroll
-            for (int q = 0; q < NQ; ++q) {
-                const Real s = sq[q];
-                nw += s * s * shp[q * SQL.qs + SQL.n + i];
-            }
+            for (int q = 0; q < NQ; ++q) nw += sq[q] * shp[q * SQL.qs + SQL.n + i];
             #pragma unroll
             for (int x = 0; x < 3; ++x) fe_own[x] = (fr[x].x + fr[x].y) - nw * pconst<Real>(a.phys.body[x], a.phys.body_f[x]);
         }
@@ -1164,6 +1158,14 @@ __device__ __forceinline__ void reduce_tile(const KernelArgs& a, const char* R, 
                         #pragma unroll
                         for (int t = 0; t < NP; ++t) hi[t] = v[t];
                         k = 1;
+                        if (cnt == 2) {
+                            // two contributions: the pair (a, b) itself is rounded below, the
+                            // same double as the TwoSum pair of a + b
+                            const float2* w = (const float2*)(stage + (s0 + ds) * BS);
+                            #pragma unroll
+                            for (int t = 0; t < NP; ++t) lo[t] = w[t];
+                            k = 2;
+                        }
                     }
                     for (; k < cnt; ++k) {
                         const float2* v = (const float2*)(stage + (s0 + k * ds) * BS);
@@ -1792,7 +1794,7 @@ __global__ void __launch_bounds__(128, 3) element_kernel_tc(const KernelArgs a, 
                 const float* sq = tb + CT::GRAD;
                 float Fi = 0.f;
                 #pragma unroll
-                for (int q = 0; q < NQ; ++q) Fi += sq[q] * sq[q] * shape[q * SQL.qs + SQL.n + i];
+                for (int q = 0; q < NQ; ++q) Fi += sq[q] * shape[q * SQL.qs + SQL.n + i];
                 out[NB * JS + aa * NB + i] = Fi * a.phys.body_f[aa];
             }
         }
