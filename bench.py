@@ -914,10 +914,25 @@ def config_pattern(fg, stream, nel=128):
     torch.cuda.synchronize()
     dev_s = time.perf_counter() - t0
     same = bool(np.array_equal(cp_d.cpu().numpy(), cp_h) and np.array_equal(rv_d.cpu().numpy(), rv_h))
+    # fe_create on either pattern: the host one reads rowval on the host; the device one keeps
+    # it on the device (pattern check and rank tables by kernels); the plans must be the same
+    cvs = [host.CellValues(host.HEXAHEDRON, ip_order=1, qr_order=2)]
+    create = {}
+    digests = []
+    for name, (cp, rv) in (("host_pattern", (cp_h, rv_h)), ("device_pattern", (cp_d, rv_d))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        h = dh.handle(cvs, cp, rv)
+        torch.cuda.synchronize()
+        create[name] = time.perf_counter() - t0
+        digests.append(h.info()["plan_checksum"])
+        h.close()
     out = {"workload": f"hex{nel}_q1_vector_pattern", "ndofs": dh.ndofs, "nnz": int(len(rv_h)), "host_s": host_s,
            "host_threads": os.cpu_count(), "device_s": dev_s, "identical": same,
+           "fe_create_s": create, "plan_digests_equal": digests[0] == digests[1],
            "note": "device time includes the host pass over cell_dofs, the uploads and both passes "
-                   "(count, then fill); the two-call protocol of fe_sparsity_pattern"}
+                   "(count, then fill); the two-call protocol of fe_sparsity_pattern. fe_create_s: the handle "
+                   "(validation, index map, owner-tile plan, uploads) from each pattern"}
     del rv_d, cp_d
     torch.cuda.empty_cache()
     return out

@@ -648,15 +648,19 @@ int fe_create(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain
     *out = nullptr;
     const auto t0 = std::chrono::steady_clock::now();
     // A device-resident pattern (fe_sparsity_pattern_device, or a CuSparseMatrixCSC's colPtr /
-    // rowVal) is read on the host, like a host one: copy it first.
+    // rowVal): with both arrays in device memory only colptr comes to the host, and the
+    // pattern check and the rank tables (the element -> nzval index map) are built on the
+    // device; with one of them on the host, both are read on the host.
     std::vector<int64_t> cp_host, rv_host;
     fe_csc_desc pattern_host{};
+    const int64_t *cp_dev = nullptr, *rv_dev = nullptr;
     if (pattern && pattern->n > 0 && pattern->nnz >= 0 && pattern->colptr && pattern->rowval &&
         (is_device_ptr(pattern->colptr) || is_device_ptr(pattern->rowval))) {
+        const bool both = is_device_ptr(pattern->colptr) && is_device_ptr(pattern->rowval);
         cp_host.resize((size_t)pattern->n + 1);
-        rv_host.resize((size_t)pattern->nnz);
+        if (!both) rv_host.resize((size_t)pattern->nnz);
         cudaError_t ce = cudaMemcpy(cp_host.data(), pattern->colptr, cp_host.size() * 8, cudaMemcpyDefault);
-        if (ce == cudaSuccess && pattern->nnz > 0)
+        if (ce == cudaSuccess && pattern->nnz > 0 && !both)
             ce = cudaMemcpy(rv_host.data(), pattern->rowval, rv_host.size() * 8, cudaMemcpyDefault);
         if (ce != cudaSuccess) {
             g_create_error = fe_error_info{};
@@ -665,14 +669,20 @@ int fe_create(const fe_grid_desc* grid, int32_t n_subdomains, const fe_subdomain
                           cudaGetErrorString(ce));
             return FE_ERR_CUDA;
         }
-        pattern_host = fe_csc_desc{pattern->n, pattern->nnz, cp_host.data(), rv_host.data()};
+        if (both) {
+            cp_dev = pattern->colptr;
+            rv_dev = pattern->rowval;
+        }
+        pattern_host = fe_csc_desc{pattern->n, pattern->nnz, cp_host.data(), both ? nullptr : rv_host.data()};
         pattern = &pattern_host;
     }
     fe_handle* h = new (std::nothrow) fe_handle();
     if (!h) return FE_ERR_OOM;
     Error err;
     CreateInput in{grid, n_subdomains, subdomains, dofs, pattern};
+    in.device_pattern = rv_dev != nullptr;
     int rc = build_problem(in, h->hp, err);
+    if (rc == FE_OK && in.device_pattern) rc = device_index_map(h->hp, cp_dev, rv_dev, err);
     if (rc == FE_OK) {
         PlanOptions opt;
         if (const char* s = std::getenv("FE_GB300_STAGE_CAP")) opt.stage_cap = std::atoi(s);

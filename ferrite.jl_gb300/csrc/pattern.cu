@@ -218,6 +218,134 @@ cudaError_t scan(const int32_t* in, int64_t n, int64_t* out, fe::DeviceBuffers& 
 
 }  // namespace
 
+namespace {
+
+// ---------------------------------------------------------------------------------------
+// The index map of a device-resident pattern (the device half of fe_create for a
+// CuSparseMatrixCSC-style pattern; the host form is the end of build_problem in plan.cpp).
+// ---------------------------------------------------------------------------------------
+// Per dof entity n: its nc columns have the same rows, the rows come in entity blocks of nc
+// consecutive dofs starting at a multiple of nc, and the blocks ascend. The smallest failing
+// column (1-based) goes to bad.
+__global__ void pattern_blocked(const int64_t* __restrict__ cp, const int64_t* __restrict__ rv, int64_t ne, int nc,
+                                int64_t ndofs, unsigned long long* __restrict__ bad) {
+    for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < ne; n += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c0 = cp[nc * n] - 1, L = cp[nc * n + 1] - cp[nc * n];
+        bool b = (L % nc) != 0;
+        for (int c = 1; c < nc && !b; ++c) {
+            const int64_t cb = cp[nc * n + c] - 1;
+            if (cp[nc * n + c + 1] - cp[nc * n + c] != L) { b = true; break; }
+            for (int64_t k = 0; k < L; ++k)
+                if (rv[cb + k] != rv[c0 + k]) { b = true; break; }
+        }
+        for (int64_t k = 0; k < L && !b; k += nc) {
+            const int64_t r0 = rv[c0 + k];
+            if (r0 < 1 || r0 > ndofs || (r0 - 1) % nc) { b = true; break; }
+            if (k && rv[c0 + k - nc] >= r0) { b = true; break; }
+            for (int a = 1; a < nc; ++a)
+                if (rv[c0 + k + a] != r0 + a) { b = true; break; }
+        }
+        if (b) atomicMin(bad, (unsigned long long)(n * nc + 1));
+    }
+}
+
+// Per (cell, column function j) of one subdomain, for every row function i: the rank of row
+// entity e_i among column entity e_j's row entities (binary search of the ascending rows; the
+// host's merge walk over the sorted entities finds the same position), miss where the column
+// has no such row, and over set when a rank reaches the table type's limit.
+template <typename RT>
+__global__ void entity_ranks(const int64_t* __restrict__ cp, const int64_t* __restrict__ rv, const int32_t* __restrict__ ents,
+                             int64_t n_cells, int nb, int nc, int64_t miss, int64_t limit, RT* __restrict__ out,
+                             int* __restrict__ over) {
+    const int64_t total = n_cells * nb;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k = q / nb;
+        const int j = (int)(q - k * nb);
+        const int32_t* e = ents + k * nb;
+        const int64_t n = e[j];
+        const int64_t c0 = cp[nc * n] - 1, Le = (cp[nc * n + 1] - cp[nc * n]) / nc;
+        for (int i = 0; i < nb; ++i) {
+            const int64_t want = (int64_t)e[i] * nc + 1;
+            int64_t lo = 0, hi = Le;
+            while (lo < hi) {
+                const int64_t mid = (lo + hi) >> 1;
+                if (rv[c0 + nc * mid] < want) lo = mid + 1;
+                else hi = mid;
+            }
+            int64_t r = miss;
+            if (lo < Le && rv[c0 + nc * lo] == want && lo < 0xFFFF) r = lo;
+            if (r != miss && r >= limit) *over = 1;
+            out[q * nb + i] = (RT)(r >= limit ? miss : r);
+        }
+    }
+}
+
+}  // namespace
+
+namespace fe {
+
+int device_index_map(HostProblem& hp, const int64_t* cp_dev, const int64_t* rv_dev, Error& err) {
+    const int nc = hp.nc;
+    DeviceBuffers B;
+    unsigned long long* d_bad;
+    int* d_over;
+    auto cuda_err = [&](cudaError_t e) {
+        err.code = FE_ERR_CUDA;
+        err.msg = std::string("device index map: ") + cudaGetErrorString(e);
+        return FE_ERR_CUDA;
+    };
+    cudaError_t e;
+    if ((e = B.alloc(&d_bad, 1)) != cudaSuccess || (e = B.alloc(&d_over, 1)) != cudaSuccess) return cuda_err(e);
+    if ((e = cudaMemset(d_bad, 0xFF, sizeof(unsigned long long))) != cudaSuccess) return cuda_err(e);
+    int dev = 0, n_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    const unsigned grid = (unsigned)std::max(1, n_sm * 8);
+    pattern_blocked<<<grid, 256>>>(cp_dev, rv_dev, hp.n_ent, nc, hp.ndofs, d_bad);
+    unsigned long long bad = 0;
+    if ((e = cudaGetLastError()) != cudaSuccess || (e = cudaMemcpy(&bad, d_bad, 8, cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return cuda_err(e);
+    if (bad != ~0ull) {
+        err.col = (int64_t)bad;
+        err.code = FE_ERR_UNSUPPORTED;
+        err.msg = "sparsity pattern is not blocked by dof entity (all components coupled)";
+        return FE_ERR_UNSUPPORTED;
+    }
+    for (HostSub& hs : hp.subs) {
+        const int nb = hs.nb;
+        const size_t n_rank = (size_t)hs.n_cells * nb * nb;
+        int32_t* d_ents;
+        uint8_t* d_r8;
+        if ((e = B.upload(&d_ents, hs.ents.data(), hs.ents.size())) != cudaSuccess || (e = B.alloc(&d_r8, n_rank)) != cudaSuccess ||
+            (e = cudaMemset(d_over, 0, sizeof(int))) != cudaSuccess)
+            return cuda_err(e);
+        entity_ranks<uint8_t><<<grid, 256>>>(cp_dev, rv_dev, d_ents, hs.n_cells, nb, nc, 255, 255, d_r8, d_over);
+        int over = 0;
+        if ((e = cudaGetLastError()) != cudaSuccess || (e = cudaMemcpy(&over, d_over, 4, cudaMemcpyDeviceToHost)) != cudaSuccess)
+            return cuda_err(e);
+        if (!over) {
+            hs.wide_rank = false;
+            hs.rank8.resize(n_rank);
+            if ((e = cudaMemcpy(hs.rank8.data(), d_r8, n_rank, cudaMemcpyDeviceToHost)) != cudaSuccess) return cuda_err(e);
+        } else {
+            B.release(d_r8);
+            uint16_t* d_r16;
+            if ((e = B.alloc(&d_r16, n_rank)) != cudaSuccess) return cuda_err(e);
+            entity_ranks<uint16_t><<<grid, 256>>>(cp_dev, rv_dev, d_ents, hs.n_cells, nb, nc, 0xFFFF, 0xFFFF, d_r16, d_over);
+            hs.wide_rank = true;
+            decltype(hs.rank8)().swap(hs.rank8);
+            hs.rank16.resize(n_rank);
+            if ((e = cudaGetLastError()) != cudaSuccess ||
+                (e = cudaMemcpy(hs.rank16.data(), d_r16, n_rank * 2, cudaMemcpyDeviceToHost)) != cudaSuccess)
+                return cuda_err(e);
+        }
+        B.release(d_ents);
+    }
+    return FE_OK;
+}
+
+}  // namespace fe
+
 extern "C" {
 
 int fe_sparsity_pattern_device(const fe_grid_desc* grid, int32_t n_sub, const fe_subdomain_desc* subs, const fe_dof_desc* dofs,

@@ -63,7 +63,7 @@ int build_problem(const CreateInput& in, HostProblem& hp, Error& err) {
     const fe_csc_desc* P = in.pattern;
     if (!d->cell_dofs || !d->cell_dofs_offset || d->ndofs <= 0) return fail(err, FE_ERR_ARG, "empty DofHandler");
     if (P->n != d->ndofs) return fail(err, FE_ERR_ARG, "K is not ndofs x ndofs");
-    if (!P->colptr || !P->rowval) return fail(err, FE_ERR_ARG, "null colptr/rowval");
+    if (!P->colptr || (!P->rowval && !in.device_pattern)) return fail(err, FE_ERR_ARG, "null colptr/rowval");
     hp.ndofs = d->ndofs;
     hp.nnz = P->nnz;
     if (P->colptr[0] != 1 || P->colptr[P->n] - 1 != P->nnz) return fail(err, FE_ERR_ARG, "colptr inconsistent with nnz");
@@ -153,6 +153,8 @@ int build_problem(const CreateInput& in, HostProblem& hp, Error& err) {
             }
         }
     }
+    // a device-resident pattern is checked and ranked on the device (device_index_map)
+    if (in.device_pattern) return FE_OK;
     // pattern: entity-blocked columns (checked once, O(nnz))
     const int64_t* rv = P->rowval;
     const int64_t* cp = hp.colptr.data();

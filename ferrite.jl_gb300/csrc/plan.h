@@ -101,8 +101,15 @@ struct CreateInput {
     const fe_subdomain_desc* subs;
     const fe_dof_desc* dofs;
     const fe_csc_desc* pattern;
+    // the pattern's rowval stays in device memory (pattern->rowval may be null): build_problem
+    // skips the pattern check and the rank tables, which device_index_map then builds
+    bool device_pattern = false;
 };
 int build_problem(const CreateInput& in, HostProblem& hp, Error& err);
+// The entity-blocked pattern check and the rank tables (the element -> nzval index map) of a
+// device-resident pattern, on the device (pattern.cu): hp holds the host set-up of
+// build_problem (entities, colptr); cp_dev / rv_dev are the pattern's device arrays.
+int device_index_map(HostProblem& hp, const int64_t* cp_dev, const int64_t* rv_dev, Error& err);
 int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error& err);
 int check_plan(const HostProblem& hp, const Plan& plan, Error& err);
 // rank of entity(i) among the row entities of entity(j)'s columns for cell k of sub s, or -1
