@@ -405,13 +405,17 @@ __device__ __forceinline__ void lds16(const Real* p, Real* out) {
 // the lane's reference-table record comes in 16-byte loads. Results go to the q-paired table
 // layout; a padded point (odd NQ) is written as zeros.
 // ---------------------------------------------------------------------------------------
+constexpr int JT_STRIDE = 12;  // floats per point in a table of scaled inverse Jacobians (16-byte rows)
+
 template <int K, int NQ, int PHYS, typename Real>
 __device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev& sd, const Real* shp, int cell,
                                                const uint16_t* cn, const char* xs, const int32_t* nodes, int lane,
                                                unsigned gmask, int gbase, Real* tb, int i0 = 0,
-                                               int i1 = ElemT<K>::NB, bool lead = true) {
+                                               int i1 = ElemT<K>::NB, bool lead = true, Real* jt = nullptr) {
     // [i0, i1): the base functions whose gradients this group writes (groups sharing a cell
-    // split them); lead: the group that also writes the cell's point weights and factors
+    // split them); lead: the group that also writes the cell's point weights and factors;
+    // jt: if given, each point's s J^-1 (row-major, JT_STRIDE apart) for callers that form the
+    // gradients themselves
     using E = ElemT<K>;
     using CT = CellTable<K, NQ, PHYS, Real>;
     constexpr int NB = E::NB, NG = E::NG, DIM = E::DIM;
@@ -524,6 +528,10 @@ __device__ __forceinline__ void geometry_lanes(const KernelArgs& a, const SubDev
         s = Real(0);
         #pragma unroll
         for (int t = 0; t < DIM * DIM; ++t) Ji[t] = Real(0);
+    }
+    if (jt) {
+        #pragma unroll
+        for (int t = 0; t < DIM * DIM; ++t) jt[q * JT_STRIDE + t] = Ji[t];
     }
     // small elements keep the whole dN record in registers; large ones read it per node
     constexpr bool DN_REG = NB * DIM <= 32;
@@ -1553,15 +1561,24 @@ __global__ void __launch_bounds__(THREADS, 2) element_kernel(const KernelArgs a,
 // bits, so A = hi + lo is split and G = hi hi^T + hi lo^T + lo hi^T (the lo lo^T term is
 // below FP32 rounding). Operands live in shared memory in the K-major core-matrix layout
 // without swizzle: (m, k) at (m%8)*16 + (k%4)*4 + (k/4)*128 + (m/8)*1024 bytes.
-// 128 threads: the four warps split the geometry (functions), convert the operands, read
-// back the rows of G (warp a = component a, lane = function i: TMEM lane 32 a + i) and
-// write the element matrix columns [j][t][i] of the two-phase scratch.
+// 128 threads per cell:
+//   - warp 0 maps the 27 points once (lane = point: J, s J^-1, the point weights);
+//   - every warp forms gradients with lane = base function i over its quads of points and
+//     writes them, split into tf32 hi and lo parts, straight into the operand rows 32 a + i
+//     (16-byte stores of four points);
+//   - warps 0-2 read back the rows of G (warp a = component a: TMEM lane 32 a + i) and write
+//     the element matrix columns [j][t][i] of the two-phase scratch; warp 3 the load vector.
+// Only the live rows (a < 3, i < 27) and points are rewritten per cell. The rest of the
+// operands may hold stale values of the G exchange: they enter only rows and columns of the
+// product that are never read.
 // ---------------------------------------------------------------------------------------
 constexpr int TC_OPERAND_BYTES = 128 * 32 * 4;  // one 128 x 32 tf32 operand
 constexpr int TC_GS = 81;                        // row stride (floats) of the G exchange (odd: no bank conflicts)
 
+constexpr int TC_JT_POINTS = 28;                 // 27 points and a zero pad point
+
 struct TcLayout {
-    int shape, tb, xs, nodes, cn, hi, lo, bytes;
+    int shape, tb, xs, nodes, cn, jt, hi, lo, bytes;
 };
 __host__ __device__ inline TcLayout tc_layout(int shape_bytes) {
     using CT = CellTable<KIND_HEX27, 27, PHYS_ELASTIC, float>;
@@ -1572,6 +1589,7 @@ __host__ __device__ inline TcLayout tc_layout(int shape_bytes) {
     L.xs = o; o += 8 * NODE_BYTES;
     L.nodes = o; o += 32;
     L.cn = o; o += 16;
+    L.jt = o; o += TC_JT_POINTS * JT_STRIDE * 4;
     o = (o + 127) & ~127;
     L.hi = o; o += TC_OPERAND_BYTES;
     L.lo = o; o += TC_OPERAND_BYTES;
@@ -1611,6 +1629,31 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, float* r) {
     for (int k = 0; k < 32; ++k) r[k] = __uint_as_float(v[k]);
 }
 
+// The rows of G of component AA (one warp, lane = function i) into the element matrix columns
+// of one cell: Ke[(i,a),(j,b)] = lam G[(i,a),(j,b)] + mu G[(i,b),(j,a)] + mu delta_ab tr, with
+// tr = sum_c G[(i,c),(j,c)]. The warp's own row comes from registers (g: G[(i,AA),(j,b)] at
+// 32 b + j), the other components' rows from the exchange (G: row 32 c + i, TC_GS apart).
+template <int AA, int NB, int JS>
+__device__ __forceinline__ void tc_ke_rows(const float* __restrict__ G, const float* g, float lam, float mu, int i,
+                                           float* __restrict__ out) {
+    const float* Gi[3] = {G + i * TC_GS, G + (32 + i) * TC_GS, G + (64 + i) * TC_GS};
+    #pragma unroll
+    for (int j = 0; j < NB; ++j) {
+        const float d0 = AA == 0 ? g[j] : Gi[0][j];
+        const float d1 = AA == 1 ? g[32 + j] : Gi[1][NB + j];
+        const float d2 = AA == 2 ? g[64 + j] : Gi[2][2 * NB + j];
+        const float tr = d0 + d1 + d2;
+        #pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            const float gab = g[32 * b + j];
+            const float gba = b == AA ? gab : Gi[b][NB * AA + j];  // G[(i,b),(j,a)]
+            float v = lam * gab + mu * gba;
+            if (b == AA) v += mu * tr;
+            out[j * JS + (b * 3 + AA) * NB + i] = v;
+        }
+    }
+}
+
 template <int PHYS>
 __global__ void __launch_bounds__(128, 3) element_kernel_tc(const KernelArgs a, const SubDev sd, const float* __restrict__ shape_g,
                                                              int shape_bytes, const EaOut eo) {
@@ -1619,6 +1662,7 @@ __global__ void __launch_bounds__(128, 3) element_kernel_tc(const KernelArgs a, 
     using CT = CellTable<K, NQ, PHYS_ELASTIC, float>;
     constexpr ShapeQ SQL = shape_q(NB, NG, 3, 4);
     constexpr int JS = ea_col_values(NB, 3);
+    static_assert(NB * 3 <= TC_GS && (NQ + 3) / 4 <= 7, "rows of the exchange; point quads 0-6 live, quad 7 pads");
     extern __shared__ __align__(128) char smem_raw[];
     __shared__ __align__(8) unsigned long long bar;
     __shared__ uint32_t tmem_base;
@@ -1638,9 +1682,13 @@ __global__ void __launch_bounds__(128, 3) element_kernel_tc(const KernelArgs a, 
     char* xs = smem_raw + L.xs;
     int32_t* nodes = (int32_t*)(smem_raw + L.nodes);
     uint16_t* cn = (uint16_t*)(smem_raw + L.cn);
+    float* jt = (float*)(smem_raw + L.jt);
     float* G = (float*)(smem_raw + L.hi);  // the G exchange reuses the operands (96 x 81 floats)
     for (int k = tid; k < shape_bytes / 16; k += 128) ((int4*)shape)[k] = ((const int4*)shape_g)[k];
     if (tid < NG) cn[tid] = (uint16_t)tid;
+    // the pad point's row of the Jacobian table and all of both operands start at zero
+    for (int k = tid; k < TC_JT_POINTS * JT_STRIDE; k += 128) jt[k] = 0.f;
+    for (int k = tid; k < 2 * TC_OPERAND_BYTES / 16; k += 128) ((float4*)(smem_raw + L.hi))[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     const uint32_t barp = (uint32_t)__cvta_generic_to_shared(&bar);
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(barp) : "memory");
@@ -1675,57 +1723,83 @@ __global__ void __launch_bounds__(128, 3) element_kernel_tc(const KernelArgs a, 
         }
         if ((int64_t)blockIdx.x + G0 < sd.n_cells) nd_next = sd.conn[((int64_t)blockIdx.x + G0) * NG + tid];
     }
+    // byte offset of this lane's operand row 32 a + i for a = 0 (a component adds 4096)
+    const int rowb = (lane & 7) * 16 + (lane >> 3) * 1024;
     for (int64_t c = blockIdx.x; c < sd.n_cells; c += gridDim.x, ++it) {
-        // node ids and coordinates of this cell; the loads for the next ones are issued here
-        // and consumed an iteration later
         int nd_after = 0;
-        if (tid < NG) {
-            nodes[tid] = nd_cur;
-            uint2* d = (uint2*)(xs + tid * NODE_BYTES);
-            d[0] = x_cur[0];
-            d[1] = x_cur[1];
-            d[2] = x_cur[2];
-            if (c + G0 < sd.n_cells) {
-                const uint2* p = (const uint2*)(src + (int64_t)nd_next * NODE_BYTES);
-                x_next[0] = p[0]; x_next[1] = p[1]; x_next[2] = p[2];
+        if (warp == 0) {
+            // node ids and coordinates of this cell; the loads for the next ones are issued
+            // here and consumed an iteration later
+            if (tid < NG) {
+                nodes[tid] = nd_cur;
+                uint2* d = (uint2*)(xs + tid * NODE_BYTES);
+                d[0] = x_cur[0];
+                d[1] = x_cur[1];
+                d[2] = x_cur[2];
+                if (c + G0 < sd.n_cells) {
+                    const uint2* p = (const uint2*)(src + (int64_t)nd_next * NODE_BYTES);
+                    x_next[0] = p[0]; x_next[1] = p[1]; x_next[2] = p[2];
+                }
+                if (c + 2 * G0 < sd.n_cells) nd_after = sd.conn[(c + 2 * G0) * NG + tid];
             }
-            if (c + 2 * G0 < sd.n_cells) nd_after = sd.conn[(c + 2 * G0) * NG + tid];
+            __syncwarp();
+            // the 27 points once (lane = point): s J^-1 into jt, point weights and cell factors
+            // into the table
+            geometry_lanes<K, NQ, PHYS_ELASTIC, float>(a, sd, shape, (int)c, cn, xs, nodes, lane, 0xFFFFFFFFu, 0, tb, 0, 0,
+                                                        true, jt);
         }
         __syncthreads();
-        // geometry: every warp maps the 27 points, warp w writes the gradients of functions
-        // [7w, 7w + 7); warp 0 also the point weights and the cell's factors
-        geometry_lanes<K, NQ, PHYS_ELASTIC, float>(a, sd, shape, (int)c, cn, xs, nodes, lane, 0xFFFFFFFFu, 0, tb, 7 * warp,
-                                                    7 * warp + 7, warp == 0);
-        __syncthreads();
-        // operands: (m, k) = (32 a + i, point), zero outside a < 3, i < 27, k < 27
-        for (int e = tid; e < 128 * 8; e += 128) {
-            const int m = e & 127, kq = e >> 7;
-            const int ca = m >> 5, ci = m & 31;
-            float x[4] = {0.f, 0.f, 0.f, 0.f};
-            if (ca < 3 && ci < NB) {
+        // gradients g_i(q) = dN_i(q) s J^-1(q), lane = base function i, into the operands
+        // (m, k) = (32 a + i, point); warp w takes the point quads w and w + 4 (point 27 pads)
+        if (lane < NB) {
+            for (int qq = warp; qq < 7; qq += 4) {
+                float x[3][4];
                 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int pp = 2 * kq + h;  // point pair: points 2 pp, 2 pp + 1 (the pad point is zero)
-                    if (pp < CT::NQP) {
-                        const float2 v = *(const float2*)(tb + pp * CT::SP + ci * 6 + 2 * ca);
-                        x[2 * h] = v.x;
-                        x[2 * h + 1] = v.y;
+                for (int h = 0; h < 4; ++h) {
+                    const int q = 4 * qq + h;
+                    float dN[3] = {0.f, 0.f, 0.f};
+                    if (q < NQ) {
+                        const float* Q = shape + q * SQL.qs + SQL.dn + 3 * lane;
+                        dN[0] = Q[0]; dN[1] = Q[1]; dN[2] = Q[2];
                     }
+                    const float* Jq = jt + q * JT_STRIDE;
+                    const float4 j0 = *(const float4*)Jq, j1 = *(const float4*)(Jq + 4);
+                    const float Ji[9] = {j0.x, j0.y, j0.z, j0.w, j1.x, j1.y, j1.z, j1.w, Jq[8]};
+                    float g[3] = {0.f, 0.f, 0.f};
+                    #pragma unroll
+                    for (int b = 0; b < 3; ++b)
+                        #pragma unroll
+                        for (int cc = 0; cc < 3; ++cc) g[b] += dN[cc] * Ji[cc * 3 + b];
+                    x[0][h] = g[0];
+                    x[1][h] = g[1];
+                    x[2][h] = g[2];
+                }
+                #pragma unroll
+                for (int ca = 0; ca < 3; ++ca) {
+                    float4 hv, lv;
+                    float* hp = &hv.x;
+                    float* lp = &lv.x;
+                    #pragma unroll
+                    for (int r = 0; r < 4; ++r) {
+                        uint32_t hb;
+                        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hb) : "f"(x[ca][r]));
+                        hp[r] = __uint_as_float(hb);
+                        lp[r] = x[ca][r] - hp[r];
+                    }
+                    const int off = rowb + ca * 4096 + qq * 128;
+                    *(float4*)(smem_raw + L.hi + off) = hv;
+                    *(float4*)(smem_raw + L.lo + off) = lv;
                 }
             }
-            float4 hv, lv;
-            float* hp = &hv.x;
-            float* lp = &lv.x;
-            #pragma unroll
-            for (int r = 0; r < 4; ++r) {
-                uint32_t hb;
-                asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hb) : "f"(x[r]));
-                hp[r] = __uint_as_float(hb);
-                lp[r] = x[r] - hp[r];
+            if (warp == 3) {
+                // points 28-31 of the live rows (the exchange of G overwrote them)
+                #pragma unroll
+                for (int ca = 0; ca < 3; ++ca) {
+                    const int off = rowb + ca * 4096 + 7 * 128;
+                    *(float4*)(smem_raw + L.hi + off) = make_float4(0.f, 0.f, 0.f, 0.f);
+                    *(float4*)(smem_raw + L.lo + off) = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
             }
-            const int off = (m & 7) * 16 + kq * 128 + (m >> 3) * 1024;
-            *(float4*)(smem_raw + L.hi + off) = hv;
-            *(float4*)(smem_raw + L.lo + off) = lv;
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // operand writes -> tensor core reads
         __syncthreads();
@@ -1763,42 +1837,31 @@ __global__ void __launch_bounds__(128, 3) element_kernel_tc(const KernelArgs a, 
                 #pragma unroll
                 for (int b = 0; b < 3; ++b)
                     #pragma unroll
-                    for (int j = 0; j < NB; ++j) G[(32 * warp + lane) * TC_GS + 27 * b + j] = g[32 * b + j];
+                    for (int j = 0; j < NB; ++j) G[(32 * warp + lane) * TC_GS + NB * b + j] = g[32 * b + j];
             }
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
-        if (warp < 3 && lane < NB) {
-            const int aa = warp, i = lane;
-            const float lam = tb[CT::GRAD + CT::SQ], mu = tb[CT::GRAD + CT::SQ + 1];
+        if (lane < NB) {
             float* out = (float*)eo.ke + c * eo.ks[0];
-            if (a.do_k) {
-                const float* Gi0 = G + (0 * 32 + i) * TC_GS;
-                const float* Gi1 = G + (1 * 32 + i) * TC_GS;
-                const float* Gi2 = G + (2 * 32 + i) * TC_GS;
-                const float* Gia[3] = {Gi0, Gi1, Gi2};
-                #pragma unroll
-                for (int j = 0; j < NB; ++j) {
-                    const float tr = Gi0[j] + Gi1[27 + j] + Gi2[54 + j];
-                    #pragma unroll
-                    for (int b = 0; b < 3; ++b) {
-                        const float gab = g[32 * b + j];
-                        const float gba = Gia[b][27 * aa + j];  // G[(i,b),(j,a)]
-                        float v = lam * gab + mu * gba;
-                        if (b == aa) v += mu * tr;
-                        out[j * JS + (b * 3 + aa) * NB + i] = v;
-                    }
+            if (warp < 3) {
+                if (a.do_k) {
+                    const float lam = tb[CT::GRAD + CT::SQ], mu = tb[CT::GRAD + CT::SQ + 1];
+                    if (warp == 0) tc_ke_rows<0, NB, JS>(G, g, lam, mu, lane, out);
+                    else if (warp == 1) tc_ke_rows<1, NB, JS>(G, g, lam, mu, lane, out);
+                    else tc_ke_rows<2, NB, JS>(G, g, lam, mu, lane, out);
                 }
-            }
-            if (a.do_f) {
+            } else if (a.do_f) {
+                // the load vector, fe[(i,a)] = b_a sum_q N_i(q) detJ w
                 const float* sq = tb + CT::GRAD;
                 float Fi = 0.f;
                 #pragma unroll
-                for (int q = 0; q < NQ; ++q) Fi += sq[q] * shape[q * SQL.qs + SQL.n + i];
-                out[NB * JS + aa * NB + i] = Fi * a.phys.body_f[aa];
+                for (int q = 0; q < NQ; ++q) Fi += sq[q] * shape[q * SQL.qs + SQL.n + lane];
+                #pragma unroll
+                for (int aa = 0; aa < 3; ++aa) out[NB * JS + aa * NB + lane] = Fi * a.phys.body_f[aa];
             }
         }
-        __syncthreads();  // the next cell overwrites the table, the operands and G
+        __syncthreads();  // the next cell overwrites the tables, the operands and G
         nd_cur = nd_next;
         nd_next = nd_after;
         #pragma unroll
