@@ -976,9 +976,9 @@ def config_mixed_graph(fg, stream, steps=20, oracle=True, ny=100, tune=True):
     f = torch.empty(dh.ndofs, dtype=torch.float64, device="cuda")
     kw = dict(physics=fg.NEO_HOOKE, p0=1.0, p1=10.0, body=(0.0, 0.0, 0.0))
     if tune:
-        tune = h.autotune(nz, f, stage_caps=[12288, 14336, 16384, 18432, 20480, 24576], reps=2, stream=stream, u=us[0], **kw)
+        tune = h.autotune(nz, f, stage_caps=[6144, 7168, 8192, 9216, 10240, 12288], reps=2, stream=stream, u=us[0], **kw)
     else:  # the form and tile size the tuner picks at full size (profiling runs)
-        tune = h.autotune(nz, f, stage_caps=[24576], reps=1, stream=stream, u=us[0], form="two_phase", **kw)
+        tune = h.autotune(nz, f, stage_caps=[9216], reps=1, stream=stream, u=us[0], form="two_phase", **kw)
     single = _timed(stream, lambda: h.assemble(nz, f, u=us[0], stream=stream, sync=False, **kw), 5)
     h.sync()
     gid = h.graph_capture([dict(u=u, **kw) for u in us], [nz] * steps, [f] * steps, stream)

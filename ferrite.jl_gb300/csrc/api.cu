@@ -357,7 +357,7 @@ int fit_plan(fe_handle* h, const KernelEntry* ke, cudaStream_t st, unsigned ea_m
     if (over <= 0 || over > smem / 10) return FE_OK;
     int cap = h->stage_cap;
     for (int k = 0; k < 3; ++k) {
-        cap = std::min(cap - 256, (int)(cap * (1.0 - 2.0 * over / cur)) & ~255);
+        cap = std::min(cap - 256, (int)(cap * (1.0 - (double)over / cur)) & ~255);
         if (cap < 2048) return FE_OK;
         PlanOptions opt;
         opt.stage_cap = cap;

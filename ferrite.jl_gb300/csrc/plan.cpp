@@ -606,19 +606,30 @@ int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error&
         if (stage_of(n) > opt.stage_cap || nnb_of(n) > opt.red_cap || out_of(n) > out_cap)
             return fail(err, FE_ERR_UNSUPPORTED, "a dof entity's contributions exceed the tile capacity");
     // sized for the heaviest entities (the interior ones), so interior tiles fit without splits
-    double max_stage = 1, max_nnb = 1, max_out = 1;
+    double max_stage = 1, max_nnb = 1, max_out = 1, sum_stage = 0, sum_nnb = 0, sum_out = 0, n_act = 0;
     for (int64_t n = 0; n < n_ent; ++n) {
         max_stage = std::max(max_stage, (double)stage_of(n));
         max_nnb = std::max(max_nnb, (double)nnb_of(n));
         max_out = std::max(max_out, (double)out_of(n));
+        if (!kcount[n]) continue;
+        sum_stage += (double)stage_of(n);
+        sum_nnb += (double)nnb_of(n);
+        sum_out += (double)out_of(n);
+        n_act += 1;
     }
     // Tiles by recursive coordinate bisection: the entities are split along the longest extent
     // into as many equal parts as an average tile size allows, so tiles are compact, of nearly
     // equal size and all fit the capacities (a part that does not is split again). Within a
     // tile entities are ordered by id, so its nzval is a few contiguous ranges.
+    const double lim = std::min((double)opt.ent_cap, (double)MAX_TILE_ENTS);
     const double target = std::max(1.0, std::min({std::floor(opt.stage_cap / max_stage), std::floor(opt.red_cap / max_nnb),
-                                                  std::floor(out_cap / max_out), (double)opt.ent_cap,
-                                                  (double)MAX_TILE_ENTS}));
+                                                  std::floor(out_cap / max_out), lim}));
+    // Entities of unequal loads (on Q2 meshes a vertex node sits in 8 cells, edge, face and
+    // interior nodes in 4, 2 and 1; mixed cell types): tiles sized for the heaviest would hold
+    // half as many entities as fit. Each part of the bisection is then cut into as many pieces
+    // as its own summed load needs, so tiles are full where entities are light or heavy alike.
+    const bool uneven = n_act > 0 && (max_stage > 1.25 * sum_stage / n_act || max_nnb > 1.25 * sum_nnb / n_act ||
+                                      max_out > 1.25 * sum_out / n_act);
     // The entities with their positions, permuted together, so the selections and bounding
     // boxes below read memory in order.
     struct EntPos {
@@ -645,9 +656,22 @@ int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error&
     // leaves in depth-first (left first) order are the leaves by ascending start; large parts
     // are split in parallel and the leaves sorted afterwards.
     std::vector<std::pair<int64_t, int64_t>> leaves;
+    // pieces of ep[lo, hi) by its load relative to the capacities (leaves average 88 % of it)
+    auto pieces = [&](int64_t lo, int64_t hi) {
+        double st = 0, rd = 0, ot = 0;
+        for (int64_t q = lo; q < hi; ++q) {
+            const int64_t id = ep[q].id;
+            st += (double)stage_of(id);
+            rd += (double)nnb_of(id);
+            ot += (double)out_of(id);
+        }
+        const double load = std::max({st / opt.stage_cap, rd / opt.red_cap, ot / out_cap, (double)(hi - lo) / lim});
+        return std::max<int64_t>(1, (int64_t)std::ceil(load / 0.88));
+    };
     std::function<void(int64_t, int64_t, int64_t)> split = [&](int64_t lo, int64_t hi, int64_t k) {
         const int64_t n = hi - lo;
         if (n == 0) return;
+        if (uneven) k = pieces(lo, hi);
         k = std::min(k, n);
         if (k == 1) {
             if (fits(lo, hi) || n == 1) {
