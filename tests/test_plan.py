@@ -65,7 +65,7 @@ import conftest
 fg = conftest.load_package()
 import oracle as O
 from helpers import subdomain_specs
-for ct, nel, ip, nc in [(4, (40, 40, 42), 1, 1), (4, (12, 10, 9), 1, 3), (4, (5, 4, 4), 2, 3)]:
+for ct, nel, ip, nc in [(4, (40, 40, 42), 1, 1), (4, (12, 10, 9), 1, 3), (4, (5, 4, 4), 2, 3), (4, (200, 200, 2), 1, 1)]:
     p = O.box_problem(ct, nel, ip_order=ip, ncomp=nc, qr_order=3 if ip == 2 else 2, perturb=0.1, seed=2)
     info = fg.plan_dry_run(p.nodes, subdomain_specs(fg, O, p), p.cell_dofs, p.cell_dofs_offset, p.ndofs, p.colptr,
                            p.rowval, p.n_cells)
@@ -76,7 +76,8 @@ for ct, nel, ip, nc in [(4, (40, 40, 42), 1, 1), (4, (12, 10, 9), 1, 3), (4, (5,
 def test_plan_independent_of_thread_count(fg, oracle):
     """The planner splits large bisection parts as OpenMP tasks and builds records in parallel;
     the plan (its record digest) is the same with 1 and 4 host threads, including a problem
-    large enough (70k entities) for the parallel bisection."""
+    large enough (70k entities) for the parallel bisection and a thin slab (121k nodes, most of
+    them on its faces) whose uneven entity loads cut every part by its own summed load."""
     import os
     import subprocess
     import sys
@@ -89,5 +90,5 @@ def test_plan_independent_of_thread_count(fg, oracle):
         r = subprocess.run([sys.executable, "-c", script], env=env, capture_output=True, text=True, timeout=600)
         assert r.returncode == 0, r.stderr[-2000:]
         outs.append(r.stdout.split())
-    assert outs[0] == outs[1] and len(outs[0]) == 6
+    assert outs[0] == outs[1] and len(outs[0]) == 8
     assert all(int(x) != 0 for x in outs[0][1::2])
