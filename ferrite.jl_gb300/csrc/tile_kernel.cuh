@@ -1398,13 +1398,20 @@ __global__ void __launch_bounds__(THREADS, EAK ? 3 : 2) tile_kernel(const Kernel
     }
     if (!failed && !mbar_wait(bar0, 0, WAIT_LIMIT)) failed = true;
     int it = 0;
+    // The gather-only form needs no barrier at the top of a tile after the first: its staging
+    // slots and output buffer are separate, the reduce's barrier before the bulk stores follows
+    // its last read of the slots, and a record that did not arrive is caught at the barrier
+    // after the copies. Warps that finish a tile early start the next tile's copies.
     for (; t < a.n_tiles; ++it, t += G) {
-        asm volatile("cp.async.wait_all;" ::: "memory");
-        if (__syncthreads_or(failed)) break;  // this tile's record and coordinates are in place
+        if (!EAK || it == 0) {
+            asm volatile("cp.async.wait_all;" ::: "memory");
+            if (__syncthreads_or(failed)) break;  // this tile's record and coordinates are in place
+        }
         const char* R = rec_ring + (it % REC_RING) * rec_stride;
         const char* xs = xs_ring + (it & 1) * xs_stride;
-        // keep the pipeline full: record of t + 2G, coordinates of t + G
-        if (tid == 0 && t + 2 * G < a.n_tiles) {
+        // keep the pipeline full: record of t + 2G (the gather-only form issues it after the
+        // copies, once every thread is past the previous tile), coordinates of t + G
+        if (!EAK && tid == 0 && t + 2 * G < a.n_tiles) {
             issue_record(pf0, pf1, (it + 2) % REC_RING);
             if (t + 3 * G < a.n_tiles) { pf0 = a.rec_off[t + 3 * G]; pf1 = a.rec_off[t + 3 * G + 1]; }
         }
@@ -1435,10 +1442,20 @@ __global__ void __launch_bounds__(THREADS, EAK ? 3 : 2) tile_kernel(const Kernel
             }
         }
         asm volatile("cp.async.wait_all;" ::: "memory");  // this thread's slot copies (two-phase form)
-        __syncthreads();  // all staging slots written
+        if constexpr (EAK) {
+            if (__syncthreads_or(failed)) break;  // all staging slots written; the next record arrived
+            if (tid == 0 && t + 2 * G < a.n_tiles) {
+                issue_record(pf0, pf1, (it + 2) % REC_RING);
+                if (t + 3 * G < a.n_tiles) { pf0 = a.rec_off[t + 3 * G]; pf1 = a.rec_off[t + 3 * G + 1]; }
+            }
+        } else {
+            __syncthreads();  // all staging slots written
+        }
         if (a.nc == 3) reduce_tile<3, Real>(a, R, stage, (double*)chunk);
         else if (a.nc == 2) reduce_tile<2, Real>(a, R, stage, (double*)chunk);
         else reduce_tile<1, Real>(a, R, stage, (double*)chunk);
+        if constexpr (EAK)
+            if (!a.do_k) __syncthreads();  // the f entries have read the staging slots
     }
     bulk_wait_all();  // this CTA's output stores have completed
     if (t < a.n_tiles) {
