@@ -1579,7 +1579,8 @@ __global__ void __launch_bounds__(THREADS, 2) element_kernel(const KernelArgs a,
 // below FP32 rounding). Operands live in shared memory in the K-major core-matrix layout
 // without swizzle: (m, k) at (m%8)*16 + (k%4)*4 + (k/4)*128 + (m/8)*1024 bytes.
 // 128 threads per cell:
-//   - warp 0 maps the 27 points once (lane = point: J, s J^-1, the point weights);
+//   - warp 3 maps the 27 points once (lane = point: J, s J^-1, the point weights), the next
+//     cell's while warps 0-2 write this cell's element matrix (two point-weight tables);
 //   - every warp forms gradients with lane = base function i over its quads of points and
 //     writes them, split into tf32 hi and lo parts, straight into the operand rows 32 a + i
 //     (16-byte stores of four points);
@@ -1595,14 +1596,19 @@ constexpr int TC_GS = 81;                        // row stride (floats) of the G
 constexpr int TC_JT_POINTS = 28;                 // 27 points and a zero pad point
 
 struct TcLayout {
-    int shape, tb, xs, nodes, cn, jt, hi, lo, bytes;
+    int shape, tb0, tb1, xs, nodes, cn, jt, hi, lo, bytes;
 };
 __host__ __device__ inline TcLayout tc_layout(int shape_bytes) {
     using CT = CellTable<KIND_HEX27, 27, PHYS_ELASTIC, float>;
     TcLayout L;
     int o = 0;
     L.shape = o; o += pad16i(shape_bytes);
-    L.tb = o; o += CT::BYTES;
+    // two cell tables (this cell's, the next cell's) of which only the point weights and the
+    // cell factors are written, the gradients going to the operands: each table's base sits
+    // CT::GRAD floats before those, over the shape tables
+    if (o < CT::GRAD * 4) o = CT::GRAD * 4;
+    L.tb0 = o - CT::GRAD * 4; o += pad16i((CT::SQ + 4) * 4);
+    L.tb1 = o - CT::GRAD * 4; o += pad16i((CT::SQ + 4) * 4);
     L.xs = o; o += 8 * NODE_BYTES;
     L.nodes = o; o += 32;
     L.cn = o; o += 16;
@@ -1695,7 +1701,8 @@ __global__ void __launch_bounds__(128, 3) element_kernel_tc(const KernelArgs a, 
         }
     }
     float* shape = (float*)(smem_raw + L.shape);
-    float* tb = (float*)(smem_raw + L.tb);
+    float* const tb0 = (float*)(smem_raw + L.tb0);
+    float* const tb1 = (float*)(smem_raw + L.tb1);
     char* xs = smem_raw + L.xs;
     int32_t* nodes = (int32_t*)(smem_raw + L.nodes);
     uint16_t* cn = (uint16_t*)(smem_raw + L.cn);
@@ -1727,45 +1734,53 @@ __global__ void __launch_bounds__(128, 3) element_kernel_tc(const KernelArgs a, 
     const char* src = (const char*)a.xf6;
     bool failed = false;
     int it = 0;
-    // node ids two cells ahead and coordinates one cell ahead, in registers (threads < NG), so
-    // neither global round trip sits on a cell's critical path
+    // Warp 3 maps the cells' points: the first cell's before the loop, every next one after
+    // this cell's load vector, while warps 0-2 write this cell's element matrix. Its lanes < NG
+    // hold node ids two cells ahead and coordinates one cell ahead in registers, so neither
+    // global round trip sits on the critical path.
     const int64_t G0 = gridDim.x;
+    const bool nl = warp == 3 && lane < NG;
     int nd_cur = 0, nd_next = 0;
     uint2 x_cur[3] = {}, x_next[3] = {};
-    if (tid < NG) {
+    if (nl) {
         if ((int64_t)blockIdx.x < sd.n_cells) {
-            nd_cur = sd.conn[(int64_t)blockIdx.x * NG + tid];
+            nd_cur = sd.conn[(int64_t)blockIdx.x * NG + lane];
             const uint2* p = (const uint2*)(src + (int64_t)nd_cur * NODE_BYTES);
             x_cur[0] = p[0]; x_cur[1] = p[1]; x_cur[2] = p[2];
         }
-        if ((int64_t)blockIdx.x + G0 < sd.n_cells) nd_next = sd.conn[((int64_t)blockIdx.x + G0) * NG + tid];
+        if ((int64_t)blockIdx.x + G0 < sd.n_cells) nd_next = sd.conn[((int64_t)blockIdx.x + G0) * NG + lane];
     }
+    // cell cc's nodes into shared memory, then its 27 points (lane = point): s J^-1 into jt,
+    // point weights and cell factors into table tbc (warp 3 only)
+    auto map_cell = [&](int64_t cc, float* tbc) {
+        int nd_after = 0;
+        __syncwarp();  // the previous cell's geometry has read the node data
+        if (nl) {
+            nodes[lane] = nd_cur;
+            uint2* d = (uint2*)(xs + lane * NODE_BYTES);
+            d[0] = x_cur[0];
+            d[1] = x_cur[1];
+            d[2] = x_cur[2];
+            if (cc + G0 < sd.n_cells) {
+                const uint2* p = (const uint2*)(src + (int64_t)nd_next * NODE_BYTES);
+                x_next[0] = p[0]; x_next[1] = p[1]; x_next[2] = p[2];
+            }
+            if (cc + 2 * G0 < sd.n_cells) nd_after = sd.conn[(cc + 2 * G0) * NG + lane];
+        }
+        __syncwarp();
+        geometry_lanes<K, NQ, PHYS_ELASTIC, float>(a, sd, shape, (int)cc, cn, xs, nodes, lane, 0xFFFFFFFFu, 0, tbc, 0, 0, true,
+                                                    jt);
+        nd_cur = nd_next;
+        nd_next = nd_after;
+        #pragma unroll
+        for (int k = 0; k < 3; ++k) x_cur[k] = x_next[k];
+    };
+    if (warp == 3 && (int64_t)blockIdx.x < sd.n_cells) map_cell(blockIdx.x, tb0);
+    __syncthreads();
     // byte offset of this lane's operand row 32 a + i for a = 0 (a component adds 4096)
     const int rowb = (lane & 7) * 16 + (lane >> 3) * 1024;
     for (int64_t c = blockIdx.x; c < sd.n_cells; c += gridDim.x, ++it) {
-        int nd_after = 0;
-        if (warp == 0) {
-            // node ids and coordinates of this cell; the loads for the next ones are issued
-            // here and consumed an iteration later
-            if (tid < NG) {
-                nodes[tid] = nd_cur;
-                uint2* d = (uint2*)(xs + tid * NODE_BYTES);
-                d[0] = x_cur[0];
-                d[1] = x_cur[1];
-                d[2] = x_cur[2];
-                if (c + G0 < sd.n_cells) {
-                    const uint2* p = (const uint2*)(src + (int64_t)nd_next * NODE_BYTES);
-                    x_next[0] = p[0]; x_next[1] = p[1]; x_next[2] = p[2];
-                }
-                if (c + 2 * G0 < sd.n_cells) nd_after = sd.conn[(c + 2 * G0) * NG + tid];
-            }
-            __syncwarp();
-            // the 27 points once (lane = point): s J^-1 into jt, point weights and cell factors
-            // into the table
-            geometry_lanes<K, NQ, PHYS_ELASTIC, float>(a, sd, shape, (int)c, cn, xs, nodes, lane, 0xFFFFFFFFu, 0, tb, 0, 0,
-                                                        true, jt);
-        }
-        __syncthreads();
+        const float* tbc = (it & 1) ? tb1 : tb0;
         // gradients g_i(q) = dN_i(q) s J^-1(q), lane = base function i, into the operands
         // (m, k) = (32 a + i, point); warp w takes the point quads w and w + 4 (point 27 pads)
         if (lane < NB) {
@@ -1838,6 +1853,7 @@ __global__ void __launch_bounds__(128, 3) element_kernel_tc(const KernelArgs a, 
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(barp) : "memory");
         }
+        float* out = (float*)eo.ke + c * eo.ks[0];
         const bool ok = tc_wait(barp, (uint32_t)(it & 1), WAIT_LIMIT);
         if (__syncthreads_or(!ok)) {  // the whole CTA leaves together
             failed = true;
@@ -1859,30 +1875,27 @@ __global__ void __launch_bounds__(128, 3) element_kernel_tc(const KernelArgs a, 
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
-        if (lane < NB) {
-            float* out = (float*)eo.ke + c * eo.ks[0];
-            if (warp < 3) {
-                if (a.do_k) {
-                    const float lam = tb[CT::GRAD + CT::SQ], mu = tb[CT::GRAD + CT::SQ + 1];
-                    if (warp == 0) tc_ke_rows<0, NB, JS>(G, g, lam, mu, lane, out);
-                    else if (warp == 1) tc_ke_rows<1, NB, JS>(G, g, lam, mu, lane, out);
-                    else tc_ke_rows<2, NB, JS>(G, g, lam, mu, lane, out);
-                }
-            } else if (a.do_f) {
-                // the load vector, fe[(i,a)] = b_a sum_q N_i(q) detJ w
-                const float* sq = tb + CT::GRAD;
+        if (warp < 3) {
+            if (lane < NB && a.do_k) {
+                const float lam = tbc[CT::GRAD + CT::SQ], mu = tbc[CT::GRAD + CT::SQ + 1];
+                if (warp == 0) tc_ke_rows<0, NB, JS>(G, g, lam, mu, lane, out);
+                else if (warp == 1) tc_ke_rows<1, NB, JS>(G, g, lam, mu, lane, out);
+                else tc_ke_rows<2, NB, JS>(G, g, lam, mu, lane, out);
+            }
+        } else {
+            // the load vector, fe[(i,a)] = b_a sum_q N_i(q) detJ w, then the next cell's points
+            // (jt, the node data and the other table are free) while warps 0-2 write this cell
+            if (a.do_f && lane < NB) {
+                const float* sq = tbc + CT::GRAD;
                 float Fi = 0.f;
                 #pragma unroll
                 for (int q = 0; q < NQ; ++q) Fi += sq[q] * shape[q * SQL.qs + SQL.n + lane];
                 #pragma unroll
                 for (int aa = 0; aa < 3; ++aa) out[NB * JS + aa * NB + lane] = Fi * a.phys.body_f[aa];
             }
+            if (c + G0 < sd.n_cells) map_cell(c + G0, (it & 1) ? tb0 : tb1);
         }
-        __syncthreads();  // the next cell overwrites the tables, the operands and G
-        nd_cur = nd_next;
-        nd_next = nd_after;
-        #pragma unroll
-        for (int k = 0; k < 3; ++k) x_cur[k] = x_next[k];
+        __syncthreads();  // the next cell overwrites the operands and G
     }
     if (failed) {
         // the MMAs of this cell did not report back: record it and wait (bounded) once more
