@@ -255,6 +255,26 @@ struct TileItem {
     int32_t cell;  // tile cell index (before the per-segment reorder)
     int32_t j, te, k;
 };
+struct TileSeg { int32_t sub, cell_begin, cell_end, item_begin, item_end; };
+struct TileTask { int32_t cell, i0, i1, cost; };
+
+// Working arrays of build_record, one set per thread and reused from tile to tile: the planner
+// builds ~10^5 records in parallel, and allocating them per tile costs more than filling them.
+struct RecScratch {
+    std::vector<TileSeg> segs;
+    std::vector<int32_t> cells, cell_item0, kc, z, cnt, item_nb, row_block, row_ord, ord, base, stride, fbase, nodes, pieces,
+        bucket;
+    std::vector<int64_t> item_row0, load;
+    std::vector<TileItem> items;
+    std::vector<RecEnt> rent;
+    std::vector<RecPass> passes;
+    std::vector<RecRng> rngs;
+    std::vector<RecRun> runs;
+    std::vector<uint32_t> red, red_sorted;
+    std::vector<RecSeg> rsegs;
+    std::vector<TileTask> tasks;
+    std::vector<std::vector<std::vector<TileTask>>> seg_tasks;
+};
 
 // Build the record of one tile. ents: owned global entity ids; trip: the tile's (sub, cell,
 // j) triples in (sub, cell, j) order. Returns 0 or an error code (internal inconsistency).
@@ -265,13 +285,18 @@ int build_record(const HostProblem& hp, const std::vector<int32_t>& kcount, cons
     const int nc = hp.nc;
     const int bs = (nc * nc + 1) & ~1;
     const int64_t* cp = hp.colptr.data();
+    thread_local RecScratch S;
     // segments, cells, items (cell order)
-    struct Seg { int32_t sub, cell_begin, cell_end, item_begin, item_end; };
-    std::vector<Seg> segs;
-    std::vector<int32_t> cells;       // sub-local cell index
-    std::vector<int32_t> cell_item0;  // first item of each cell
-    std::vector<TileItem> items;
-    std::vector<int32_t> kc(n_ent, 0);
+    auto& segs = S.segs;
+    auto& cells = S.cells;            // sub-local cell index
+    auto& cell_item0 = S.cell_item0;  // first item of each cell
+    auto& items = S.items;
+    auto& kc = S.kc;
+    segs.clear();
+    cells.clear();
+    cell_item0.clear();
+    items.clear();
+    kc.assign(n_ent, 0);
     for (int64_t q = 0; q < n_trip; ++q) {
         const int s = (int)(trip[q] >> 40);
         const int32_t cell = (int32_t)((trip[q] >> 8) & 0xFFFFFFFFull);
@@ -280,7 +305,7 @@ int build_record(const HostProblem& hp, const std::vector<int32_t>& kcount, cons
         if (new_cell) {
             if (segs.empty() || segs.back().sub != s) {
                 if (!segs.empty()) { segs.back().cell_end = (int32_t)cells.size(); segs.back().item_end = (int32_t)items.size(); }
-                segs.push_back(Seg{s, (int32_t)cells.size(), 0, (int32_t)items.size(), 0});
+                segs.push_back(TileSeg{s, (int32_t)cells.size(), 0, (int32_t)items.size(), 0});
             }
             cells.push_back(cell);
             cell_item0.push_back((int32_t)items.size());
@@ -293,21 +318,25 @@ int build_record(const HostProblem& hp, const std::vector<int32_t>& kcount, cons
     for (int32_t te = 0; te < n_ent; ++te)
         if (kc[te] != kcount[ents[te]]) return 1;
     // owned blocks: z[te] + r
-    std::vector<int32_t> z(n_ent + 1, 0);
+    auto& z = S.z;
+    z.assign(n_ent + 1, 0);
     for (int32_t te = 0; te < n_ent; ++te) {
         const int64_t n = ents[te];
         z[te + 1] = z[te] + (int32_t)((cp[nc * n + 1] - cp[nc * n]) / nc);
     }
     const int32_t n_red = z[n_ent];
-    std::vector<int32_t> cnt(n_red, 0);
+    auto& cnt = S.cnt;
+    cnt.assign(n_red, 0);
     // per (item, i): block index or -1
     auto cell_sub = [&](int32_t c) {
         int s = 0;
         while (s + 1 < (int)segs.size() && c >= segs[s].cell_end) ++s;
         return s;
     };
-    std::vector<int32_t> item_nb(items.size());
-    std::vector<int64_t> item_row0(items.size() + 1, 0);
+    auto& item_nb = S.item_nb;
+    auto& item_row0 = S.item_row0;
+    item_nb.resize(items.size());
+    item_row0.assign(items.size() + 1, 0);
     {
         int sg = 0;
         for (size_t it = 0; it < items.size(); ++it) {
@@ -316,8 +345,10 @@ int build_record(const HostProblem& hp, const std::vector<int32_t>& kcount, cons
             item_row0[it + 1] = item_row0[it] + item_nb[it];
         }
     }
-    std::vector<int32_t> row_block(item_row0.back());
-    std::vector<int32_t> row_ord(item_row0.back());  // position among the block's contributions
+    auto& row_block = S.row_block;
+    auto& row_ord = S.row_ord;  // position among the block's contributions
+    row_block.resize(item_row0.back());
+    row_ord.resize(item_row0.back());
     for (size_t it = 0; it < items.size(); ++it) {
         const TileItem& I = items[it];
         const int sg = cell_sub(I.cell);
@@ -338,9 +369,12 @@ int build_record(const HostProblem& hp, const std::vector<int32_t>& kcount, cons
     // reduce passes: consecutive owned entities whose columns fit the output buffer; within a
     // pass, contiguous nzval ranges, each placed in the buffer with the parity of its start so
     // the 16-byte aligned middle can be stored with one bulk copy
-    std::vector<RecEnt> rent(n_ent);
-    std::vector<RecPass> passes;
-    std::vector<RecRng> rngs;
+    auto& rent = S.rent;
+    auto& passes = S.passes;
+    auto& rngs = S.rngs;
+    rent.assign(n_ent, RecEnt{});
+    passes.clear();
+    rngs.clear();
     {
         int32_t e = 0;
         while (e < n_ent) {
@@ -376,12 +410,22 @@ int build_record(const HostProblem& hp, const std::vector<int32_t>& kcount, cons
     }
     // reduce order within each pass: most contributions first (stable in (entity, rank)); the
     // slots of a run are k-major so the lanes of a warp read consecutive slots
-    std::vector<int32_t> ord(n_red);
-    for (int32_t b = 0; b < n_red; ++b) ord[b] = b;
-    for (const RecPass& P : passes)
-        std::stable_sort(ord.begin() + P.red_begin, ord.begin() + P.red_end, [&](int32_t x, int32_t y) { return cnt[x] > cnt[y]; });
-    std::vector<int32_t> base(n_red), stride(n_red);
-    std::vector<RecRun> runs;
+    auto& ord = S.ord;
+    auto& bucket = S.bucket;
+    ord.resize(n_red);
+    for (const RecPass& P : passes) {
+        // a stable counting sort by contribution count (at most MAX_ENT_CELLS), most first
+        bucket.assign(MAX_ENT_CELLS + 2, 0);
+        for (int32_t b = P.red_begin; b < P.red_end; ++b) ++bucket[MAX_ENT_CELLS - cnt[b] + 1];
+        for (int v = 1; v <= MAX_ENT_CELLS + 1; ++v) bucket[v] += bucket[v - 1];
+        for (int32_t b = P.red_begin; b < P.red_end; ++b) ord[P.red_begin + bucket[MAX_ENT_CELLS - cnt[b]]++] = b;
+    }
+    auto& base = S.base;
+    auto& stride = S.stride;
+    auto& runs = S.runs;
+    base.resize(n_red);
+    stride.resize(n_red);
+    runs.clear();
     int32_t n_slots = 0;
     for (RecPass& P : passes) {
         P.run_begin = (int32_t)runs.size();
@@ -402,21 +446,24 @@ int build_record(const HostProblem& hp, const std::vector<int32_t>& kcount, cons
         P.run_end = (int32_t)runs.size();
     }
     const int32_t n_runs = (int32_t)runs.size(), n_pass = (int32_t)passes.size(), n_rng = (int32_t)rngs.size();
-    std::vector<uint32_t> red(n_red);
+    auto& red = S.red;
+    auto& red_sorted = S.red_sorted;
+    red.resize(n_red);
+    red_sorted.resize(n_red);
     for (int32_t te = 0; te < n_ent; ++te)
         for (int32_t r = 0; r < z[te + 1] - z[te]; ++r) red[z[te] + r] = ((uint32_t)te << RED_RANK_BITS) | (uint32_t)r;
-    std::vector<uint32_t> red_sorted(n_red);
     for (int32_t q = 0; q < n_red; ++q) red_sorted[q] = red[ord[q]];
     // f slots: per owned entity, one per cell in k order
-    std::vector<int32_t> fbase(n_ent + 1, 0);
+    auto& fbase = S.fbase;
+    fbase.assign(n_ent + 1, 0);
     for (int32_t te = 0; te < n_ent; ++te) fbase[te + 1] = fbase[te] + kc[te];
     const int32_t n_fslots = fbase[n_ent];
     if (n_fslots > 0xFFFF) return 3;
     // work of the lane groups: per segment, (cell, item range) tasks scheduled longest first
     // onto the least loaded of the planned groups; a cell whose geometry plus blocks would
     // exceed the even share is split into pieces that each redo the geometry
-    struct Task { int32_t cell, i0, i1, cost; };
-    std::vector<std::vector<std::vector<Task>>> seg_tasks(segs.size());
+    auto& seg_tasks = S.seg_tasks;  // entries past segs.size() are stale
+    if (seg_tasks.size() < segs.size()) seg_tasks.resize(segs.size());
     for (size_t g = 0; g < segs.size(); ++g) {
         const HostSub& hs = hp.subs[segs[g].sub];
         const int G = CTA_THREADS / GROUP_LANES[hs.kind];
@@ -424,7 +471,8 @@ int build_record(const HostProblem& hp, const std::vector<int32_t>& kcount, cons
         auto n_items_of = [&](int32_t c) {
             return (c + 1 < (int32_t)cells.size() ? cell_item0[c + 1] : (int32_t)items.size()) - cell_item0[c];
         };
-        std::vector<int32_t> pieces(c1 - c0, 1);
+        auto& pieces = S.pieces;
+        pieces.assign(c1 - c0, 1);
         for (int pass = 0; pass < 3; ++pass) {
             int64_t total = 0;
             for (int32_t c = c0; c < c1; ++c)
@@ -437,27 +485,31 @@ int build_record(const HostProblem& hp, const std::vector<int32_t>& kcount, cons
                 pieces[c - c0] = m;
             }
         }
-        std::vector<Task> tasks;
+        auto& tasks = S.tasks;
+        tasks.clear();
         for (int32_t c = c0; c < c1; ++c) {
             const int32_t n = n_items_of(c), m = pieces[c - c0];
             int32_t i = cell_item0[c];
             for (int32_t q = 0; q < m; ++q) {
                 const int32_t len = n / m + (q < n % m ? 1 : 0);
-                tasks.push_back(Task{c, i, i + len, (int32_t)(TASK_GEO_COST + len * TASK_ITEM_COST)});
+                tasks.push_back(TileTask{c, i, i + len, (int32_t)(TASK_GEO_COST + len * TASK_ITEM_COST)});
                 i += len;
             }
         }
-        std::stable_sort(tasks.begin(), tasks.end(), [](const Task& x, const Task& y) { return x.cost > y.cost; });
-        std::vector<int64_t> load(G, 0);
-        seg_tasks[g].assign(G, {});
-        for (const Task& T : tasks) {
+        std::stable_sort(tasks.begin(), tasks.end(), [](const TileTask& x, const TileTask& y) { return x.cost > y.cost; });
+        auto& load = S.load;
+        load.assign(G, 0);
+        seg_tasks[g].resize(G);
+        for (auto& gl : seg_tasks[g]) gl.clear();
+        for (const TileTask& T : tasks) {
             const int w = (int)(std::min_element(load.begin(), load.end()) - load.begin());
             load[w] += T.cost;
             seg_tasks[g][w].push_back(T);
         }
     }
     // nodes of the tile, ascending
-    std::vector<int32_t> nodes;
+    auto& nodes = S.nodes;
+    nodes.clear();
     for (size_t c = 0; c < cells.size(); ++c) {
         const HostSub& hs = hp.subs[segs[cell_sub((int32_t)c)].sub];
         for (int a = 0; a < hs.ng; ++a) nodes.push_back(hs.conn[(int64_t)cells[c] * hs.ng + a]);
@@ -482,7 +534,8 @@ int build_record(const HostProblem& hp, const std::vector<int32_t>& kcount, cons
     H.off_rng = pad16(o); o = H.off_rng + (int64_t)n_rng * 16;
     H.off_items = pad16(o); o = H.off_items + (int64_t)n_items * 4;
     H.off_cells = pad16(o); o = H.off_cells + (int64_t)n_cells * 4;
-    std::vector<RecSeg> rsegs(n_seg);
+    auto& rsegs = S.rsegs;
+    rsegs.assign(n_seg, RecSeg{});
     for (int32_t g = 0; g < n_seg; ++g) {
         const HostSub& hs = hp.subs[segs[g].sub];
         RecSeg& R = rsegs[g];
@@ -496,8 +549,8 @@ int build_record(const HostProblem& hp, const std::vector<int32_t>& kcount, cons
         R.pad[0] = R.pad[1] = R.pad[2] = 0;
     }
     int32_t n_tasks = 0;
-    for (const auto& st : seg_tasks)
-        for (const auto& gl : st) n_tasks += (int32_t)gl.size();
+    for (int32_t g = 0; g < n_seg; ++g)
+        for (const auto& gl : seg_tasks[g]) n_tasks += (int32_t)gl.size();
     if (n_tasks > 0xFFFF) return 3;
     H.n_tasks = n_tasks;
     H.off_tasks = pad16(o); o = H.off_tasks + (int64_t)n_tasks * 8;
@@ -546,7 +599,7 @@ int build_record(const HostProblem& hp, const std::vector<int32_t>& kcount, cons
             uint16_t* gt = (uint16_t*)(B + rsegs[g].gt_off);
             for (int32_t w = 0; w < rsegs[g].n_grp; ++w) {
                 gt[w] = (uint16_t)tn;
-                for (const Task& T : seg_tasks[g][w]) {
+                for (const TileTask& T : seg_tasks[g][w]) {
                     RecTask rt{(uint16_t)T.cell, (uint16_t)T.i0, (uint16_t)T.i1, 0};
                     std::memcpy(B + H.off_tasks + (int64_t)tn * 8, &rt, 8);
                     ++tn;
