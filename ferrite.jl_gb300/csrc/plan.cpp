@@ -871,12 +871,22 @@ int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error&
 // arrays) and that the slots are a bijection onto the owned blocks' contributions with
 // the right destinations. Run once per fe_create.
 // ---------------------------------------------------------------------------------------
+namespace {
+// Working arrays of check_plan, one set per thread and reused from tile to tile
+struct CheckScratch {
+    std::vector<int32_t> slot_block, blk_pass, slot_writes, fslot_writes, item_cover;
+    std::vector<int64_t> slot_cell;
+    std::vector<std::vector<int32_t>> writes, cover, owner;  // per pass; entries past n_pass are stale
+};
+}  // namespace
+
 int check_plan(const HostProblem& hp, const Plan& pl, Error& err) {
     const int nc = hp.nc;
     const int64_t* cp = hp.colptr.data();
     int bad = 0;
 #pragma omp parallel for schedule(dynamic, 64) reduction(| : bad)
     for (int64_t t = 0; t < pl.n_tiles; ++t) {
+        thread_local CheckScratch CS;
         const int64_t off = pl.rec_off[t], len = pl.rec_off[t + 1] - off;
         if ((off & 15) || len < (int64_t)sizeof(RecHead) || len > pl.max_rec) { bad = 1; continue; }
         const uint8_t* B = pl.rec.data() + off;
@@ -917,7 +927,10 @@ int check_plan(const HostProblem& hp, const Plan& pl, Error& err) {
         }
         // passes partition the blocks, runs and ranges in order; within a pass the runs cover
         // its blocks and hand out k-major slot ranges, consecutive over the whole tile
-        std::vector<int32_t> slot_block(H.n_slots, -1), blk_pass(H.n_red, -1);
+        auto& slot_block = CS.slot_block;
+        auto& blk_pass = CS.blk_pass;
+        slot_block.assign(H.n_slots, -1);
+        blk_pass.assign(H.n_red, -1);
         {
             int32_t red_next = 0, run_next = 0, rng_next = 0, slot_next = 0;
             for (int32_t p = 0; p < H.n_pass && !bad; ++p) {
@@ -957,9 +970,15 @@ int check_plan(const HostProblem& hp, const Plan& pl, Error& err) {
         // blocks: ranks inside the column; every output entry lands in a buffer position of its
         // pass that one range maps to that entry's nzval index, and every range position is written once
         {
-            std::vector<std::vector<int32_t>> writes(H.n_pass);
+            auto& writes = CS.writes;
             // per pass and buffer position: how many ranges cover it, and the last one that does
-            std::vector<std::vector<int32_t>> cover(H.n_pass), owner(H.n_pass);
+            auto& cover = CS.cover;
+            auto& owner = CS.owner;
+            if ((int32_t)writes.size() < H.n_pass) {
+                writes.resize(H.n_pass);
+                cover.resize(H.n_pass);
+                owner.resize(H.n_pass);
+            }
             for (int32_t p = 0; p < H.n_pass; ++p) {
                 writes[p].assign(PS[p].out_len, 0);
                 cover[p].assign(PS[p].out_len, 0);
@@ -995,8 +1014,12 @@ int check_plan(const HostProblem& hp, const Plan& pl, Error& err) {
         for (int32_t e = 0; e < H.n_nodes && !bad; ++e)
             if (ND[e] < 0 || ND[e] >= hp.n_nodes) bad = 1;
         // segments, cells, items, slots
-        std::vector<int32_t> slot_writes(H.n_slots, 0), fslot_writes(H.n_fslots, 0);
-        std::vector<int64_t> slot_cell(H.n_slots, -1);  // (sub, cell) of each slot's contribution
+        auto& slot_writes = CS.slot_writes;
+        auto& fslot_writes = CS.fslot_writes;
+        auto& slot_cell = CS.slot_cell;  // (sub, cell) of each slot's contribution
+        slot_writes.assign(H.n_slots, 0);
+        fslot_writes.assign(H.n_fslots, 0);
+        slot_cell.assign(H.n_slots, -1);
         int32_t cell_next = 0, item_next = 0, task_next = 0;
         for (int32_t g = 0; g < H.n_seg && !bad; ++g) {
             const RecSeg& G = S[g];
@@ -1026,7 +1049,8 @@ int check_plan(const HostProblem& hp, const Plan& pl, Error& err) {
             const uint16_t* GT = (const uint16_t*)(B + G.gt_off);
             const RecTask* TK = (const RecTask*)(B + H.off_tasks);
             if (GT[0] != task_next || GT[G.n_grp] > H.n_tasks) { bad = 1; break; }
-            std::vector<int32_t> cover(G.item_end - G.item_begin, 0);
+            auto& cover = CS.item_cover;
+            cover.assign(G.item_end - G.item_begin, 0);
             for (int32_t w = 0; w < G.n_grp && !bad; ++w) {
                 if (GT[w + 1] < GT[w]) { bad = 1; break; }
                 for (int32_t q = GT[w]; q < GT[w + 1] && !bad; ++q) {
