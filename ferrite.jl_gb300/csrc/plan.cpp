@@ -755,30 +755,25 @@ int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error&
             return x.id < y.id;
         };
         const int64_t slack = std::max<int64_t>(1, (int64_t)(0.15 * (double)nl));
-        // Only the ranks around the cut need their order: place ranks [w0, w1) sorted with every
-        // smaller rank before them and every larger one after (two selections and a short sort).
-        // `less` is a strict total order, so the parts hold the same entities as after a full
-        // sort, and each part is ordered again before it is split or emitted.
-        {
-            const int64_t w0 = std::max<int64_t>(0, nl - slack - 1), w1 = std::min<int64_t>(n, nl + slack + 1);
-            auto b = ep.begin() + lo;
-            std::nth_element(b, b + w0, b + n, less);
-            if (w1 < n) std::nth_element(b + w0 + 1, b + w1, b + n, less);
-            std::sort(b + w0 + 1, b + w1, less);
+        // In axis order the axis coordinate changes only at layer boundaries, so the nearest
+        // change to rank nl is the start c1 or the end c2 of the layer of the entity of rank nl:
+        // one selection finds that entity, one counting pass the layer's ranks, and a second
+        // selection (if the cut moves) puts the `best` smallest entities first. `less` is a
+        // strict total order, so the parts hold the same entities as after a full sort, and each
+        // part is ordered again before it is split or emitted.
+        auto b = ep.begin() + lo;
+        std::nth_element(b, b + nl, b + n, less);
+        const double v = b[nl].p[ax];
+        int64_t c1 = 0, c2 = 0;
+        for (int64_t q = 0; q < n; ++q) {
+            c1 += b[q].p[ax] < v;
+            c2 += b[q].p[ax] <= v;
         }
-        int64_t best = nl;
-        for (int64_t d = 0; d <= slack; ++d) {
-            bool hit = false;
-            for (const int64_t c : {nl - d, nl + d}) {
-                if (c <= 0 || c >= n) continue;
-                if (ep[lo + c - 1].p[ax] != ep[lo + c].p[ax]) {
-                    best = c;
-                    hit = true;
-                    break;
-                }
-            }
-            if (hit) break;
-        }
+        int64_t best = nl;  // the nearer of c1 and c2 within the slack, c1 on a tie
+        const bool ok1 = c1 > 0 && nl - c1 <= slack, ok2 = c2 < n && c2 - nl <= slack;
+        if (ok1 && (!ok2 || nl - c1 <= c2 - nl)) best = c1;
+        else if (ok2) best = c2;
+        if (best != nl) std::nth_element(b, b + best, b + n, less);
         nl = best;
         if (n >= (1 << 16)) {
 #pragma omp task default(shared) firstprivate(lo, nl, kl)
