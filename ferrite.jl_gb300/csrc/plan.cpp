@@ -631,17 +631,21 @@ int build_plan(const HostProblem& hp, const PlanOptions& opt, Plan& plan, Error&
     std::vector<double> pos(n_ent * 3, 0.0);
     std::vector<int32_t> kcount(n_ent, 0);
     for (const HostSub& hs : hp.subs) {
+        // cell centroids in parallel, then the sums per entity in cell order (the same bits)
+        HostBuf<double> cens((size_t)hs.n_cells * 3);
+#pragma omp parallel for schedule(static)
         for (int64_t k = 0; k < hs.n_cells; ++k) {
             double cen[3] = {0, 0, 0};
             for (int a = 0; a < hs.ng; ++a)
                 for (int x = 0; x < dim; ++x) cen[x] += hp.nodes[(int64_t)hs.conn[k * hs.ng + a] * dim + x];
-            for (int x = 0; x < dim; ++x) cen[x] /= hs.ng;
+            for (int x = 0; x < 3; ++x) cens[k * 3 + x] = x < dim ? cen[x] / hs.ng : 0.0;
+        }
+        for (int64_t k = 0; k < hs.n_cells; ++k)
             for (int i = 0; i < hs.nb; ++i) {
                 const int64_t n = hs.ents[k * hs.nb + i];
-                for (int x = 0; x < dim; ++x) pos[n * 3 + x] += cen[x];
+                for (int x = 0; x < dim; ++x) pos[n * 3 + x] += cens[k * 3 + x];
                 kcount[n]++;
             }
-        }
     }
     for (int64_t n = 0; n < n_ent; ++n) {
         if (kcount[n] > MAX_ENT_CELLS) return fail(err, FE_ERR_UNSUPPORTED, "a dof entity belongs to more than 255 cells");
