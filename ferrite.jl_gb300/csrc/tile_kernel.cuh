@@ -1580,7 +1580,9 @@ __global__ void __launch_bounds__(THREADS, 2) element_kernel(const KernelArgs a,
 // without swizzle: (m, k) at (m%8)*16 + (k%4)*4 + (k/4)*128 + (m/8)*1024 bytes.
 // 128 threads per cell:
 //   - warp 3 maps the 27 points once (lane = point: J, s J^-1, the point weights), the next
-//     cell's while warps 0-2 write this cell's element matrix (two point-weight tables);
+//     cell's while the products run and warps 0-2 write this cell's element matrix (two
+//     point-weight tables; warps 0-2 alone wait for the products and meet at a 96-thread
+//     barrier);
 //   - every warp forms gradients with lane = base function i over its quads of points and
 //     writes them, split into tf32 hi and lo parts, straight into the operand rows 32 a + i
 //     (16-byte stores of four points);
@@ -1735,7 +1737,8 @@ __global__ void __launch_bounds__(128, 3) element_kernel_tc(const KernelArgs a, 
     bool failed = false;
     int it = 0;
     // Warp 3 maps the cells' points: the first cell's before the loop, every next one after
-    // this cell's load vector, while warps 0-2 write this cell's element matrix. Its lanes < NG
+    // this cell's load vector, while the products run and warps 0-2 write this cell's element
+    // matrix. Its lanes < NG
     // hold node ids two cells ahead and coordinates one cell ahead in registers, so neither
     // global round trip sits on the critical path.
     const int64_t G0 = gridDim.x;
@@ -1854,29 +1857,29 @@ __global__ void __launch_bounds__(128, 3) element_kernel_tc(const KernelArgs a, 
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(barp) : "memory");
         }
         float* out = (float*)eo.ke + c * eo.ks[0];
-        const bool ok = tc_wait(barp, (uint32_t)(it & 1), WAIT_LIMIT);
-        if (__syncthreads_or(!ok)) {  // the whole CTA leaves together
-            failed = true;
-            break;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        // rows of G: warp a reads TMEM lanes 32 a .. 32 a + 31 (lane = function i)
+        // warps 0-2 wait for the products and read TMEM; warp 3 reads none and goes on with the
+        // load vector and the next cell's points (jt, the node data and the other table are
+        // free once the operands are written)
+        bool ok = true;
         float g[96];
         if (warp < 3) {
-            #pragma unroll
-            for (int c0 = 0; c0 < 3; ++c0) tc_ld32(tm + ((uint32_t)(32 * warp) << 16) + (uint32_t)(32 * c0), g + 32 * c0);
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (lane < NB) {
+            ok = __all_sync(0xFFFFFFFFu, tc_wait(barp, (uint32_t)(it & 1), WAIT_LIMIT));
+            if (ok) {
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                // rows of G: warp a reads TMEM lanes 32 a .. 32 a + 31 (lane = function i)
                 #pragma unroll
-                for (int b = 0; b < 3; ++b)
+                for (int c0 = 0; c0 < 3; ++c0) tc_ld32(tm + ((uint32_t)(32 * warp) << 16) + (uint32_t)(32 * c0), g + 32 * c0);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (lane < NB) {
                     #pragma unroll
-                    for (int j = 0; j < NB; ++j) G[(32 * warp + lane) * TC_GS + NB * b + j] = g[32 * b + j];
+                    for (int b = 0; b < 3; ++b)
+                        #pragma unroll
+                        for (int j = 0; j < NB; ++j) G[(32 * warp + lane) * TC_GS + NB * b + j] = g[32 * b + j];
+                }
             }
-        }
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
-        if (warp < 3) {
-            if (lane < NB && a.do_k) {
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            asm volatile("bar.sync 1, 96;" ::: "memory");  // warps 0-2: the rows of G exchanged
+            if (ok && lane < NB && a.do_k) {
                 const float lam = tbc[CT::GRAD + CT::SQ], mu = tbc[CT::GRAD + CT::SQ + 1];
                 if (warp == 0) tc_ke_rows<0, NB, JS>(G, g, lam, mu, lane, out);
                 else if (warp == 1) tc_ke_rows<1, NB, JS>(G, g, lam, mu, lane, out);
@@ -1884,7 +1887,6 @@ __global__ void __launch_bounds__(128, 3) element_kernel_tc(const KernelArgs a, 
             }
         } else {
             // the load vector, fe[(i,a)] = b_a sum_q N_i(q) detJ w, then the next cell's points
-            // (jt, the node data and the other table are free) while warps 0-2 write this cell
             if (a.do_f && lane < NB) {
                 const float* sq = tbc + CT::GRAD;
                 float Fi = 0.f;
@@ -1895,7 +1897,10 @@ __global__ void __launch_bounds__(128, 3) element_kernel_tc(const KernelArgs a, 
             }
             if (c + G0 < sd.n_cells) map_cell(c + G0, (it & 1) ? tb0 : tb1);
         }
-        __syncthreads();  // the next cell overwrites the operands and G
+        if (__syncthreads_or(!ok)) {  // the next cell overwrites the operands and G; a lost MMA: all leave
+            failed = true;
+            break;
+        }
     }
     if (failed) {
         // the MMAs of this cell did not report back: record it and wait (bounded) once more
