@@ -875,7 +875,7 @@ namespace {
 struct CheckScratch {
     std::vector<int32_t> slot_block, blk_pass, slot_writes, fslot_writes, item_cover;
     std::vector<int64_t> slot_cell;
-    std::vector<std::vector<int32_t>> writes, cover, owner;  // per pass; entries past n_pass are stale
+    std::vector<std::vector<int32_t>> owner;  // per pass; entries past n_pass are stale
 };
 }  // namespace
 
@@ -969,23 +969,16 @@ int check_plan(const HostProblem& hp, const Plan& pl, Error& err) {
         // blocks: ranks inside the column; every output entry lands in a buffer position of its
         // pass that one range maps to that entry's nzval index, and every range position is written once
         {
-            auto& writes = CS.writes;
-            // per pass and buffer position: how many ranges cover it, and the last one that does
-            auto& cover = CS.cover;
-            auto& owner = CS.owner;
-            if ((int32_t)writes.size() < H.n_pass) {
-                writes.resize(H.n_pass);
-                cover.resize(H.n_pass);
-                owner.resize(H.n_pass);
-            }
-            for (int32_t p = 0; p < H.n_pass; ++p) {
-                writes[p].assign(PS[p].out_len, 0);
-                cover[p].assign(PS[p].out_len, 0);
-                owner[p].assign(PS[p].out_len, -1);
-                for (int32_t g = PS[p].rng_begin; g < PS[p].rng_end; ++g)
+            // per pass and buffer position: -1 no range, g the one range covering it (a second
+            // range is an error), -2 - g once a block entry has been written there
+            auto& own = CS.owner;
+            if ((int32_t)own.size() < H.n_pass) own.resize(H.n_pass);
+            for (int32_t p = 0; p < H.n_pass && !bad; ++p) {
+                own[p].assign(PS[p].out_len, -1);
+                for (int32_t g = PS[p].rng_begin; g < PS[p].rng_end && !bad; ++g)
                     for (int32_t i = RG[g].buf_off; i < RG[g].buf_off + RG[g].len; ++i) {
-                        ++cover[p][i];
-                        owner[p][i] = g;
+                        if (own[p][i] != -1) { bad = 1; break; }
+                        own[p][i] = g;
                     }
             }
             for (int32_t q = 0; q < H.n_red && !bad; ++q) {
@@ -998,16 +991,18 @@ int check_plan(const HostProblem& hp, const Plan& pl, Error& err) {
                         const int64_t i = (int64_t)E[e].out_off + (int64_t)b * E[e].L + (int64_t)nc * r + x;
                         if (E[e].out_off < 0 || i >= P.out_len) { bad = 1; break; }
                         const int64_t want = E[e].colbase + (int64_t)b * E[e].L + (int64_t)nc * r + x;
-                        // exactly one range covers i, and it maps i to this entry's nzval index
-                        const int32_t g = owner[p][i];
-                        if (cover[p][i] != 1 || RG[g].nz0 + (i - RG[g].buf_off) != want) bad = 1;
-                        writes[p][i]++;
+                        // one range covers i, it maps i to this entry's nzval index, and no other
+                        // entry was written there
+                        const int32_t g = own[p][i];
+                        if (g < 0 || RG[g].nz0 + (i - RG[g].buf_off) != want) { bad = 1; break; }
+                        own[p][i] = -2 - g;
                     }
             }
+            // every range position written
             for (int32_t p = 0; p < H.n_pass && !bad; ++p)
                 for (int32_t g = PS[p].rng_begin; g < PS[p].rng_end && !bad; ++g)
                     for (int32_t i = RG[g].buf_off; i < RG[g].buf_off + RG[g].len; ++i)
-                        if (writes[p][i] != 1) { bad = 1; break; }
+                        if (own[p][i] >= -1) { bad = 1; break; }
         }
         if (bad) continue;
         for (int32_t e = 0; e < H.n_nodes && !bad; ++e)
