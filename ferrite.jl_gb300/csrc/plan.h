@@ -66,7 +66,10 @@ struct HostProblem {
 };
 
 struct PlanOptions {
-    int32_t stage_cap = 12288;  // staging values per tile (4 bytes each in mixed precision)
+    // staging values per tile (4 bytes each in mixed precision). 13056 is the largest capacity
+    // whose 128^3 Q1 hexahedron tiles keep two CTAs per SM; a plan whose CTA lands just past
+    // its occupancy line is re-planned smaller at its first assembly
+    int32_t stage_cap = 13056;
     int32_t ent_cap = 1024;     // owned entities per tile
     int32_t red_cap = 2048;     // owned blocks (reduce lanes) per tile
     int32_t out_cap = 0;        // output-buffer doubles of one reduce pass; 0: 37.5 % of stage_cap
