@@ -1426,7 +1426,7 @@ __global__ void __launch_bounds__(THREADS, EAK ? 3 : 2) tile_kernel(const Kernel
         const RecHead* H = (const RecHead*)R;
         const int n_seg = H->n_seg;
         for (int gi = 0; gi < n_seg; ++gi) {
-            if (gi) __syncthreads();  // table buffers are laid out per element kind
+            if (!EAK && gi) __syncthreads();  // table buffers are laid out per element kind (none in the gather-only form)
             const RecSeg g = ((const RecSeg*)(R + sizeof(RecHead)))[gi];
             static_assert(sizeof(RecSeg) % 16 == 0, "segment entries are 16-byte multiples");
             if (g.sub == 0) {
